@@ -1,0 +1,80 @@
+/*
+ * amca_oracle — plain-C restatement of AMCA3D's 3-D cellular-automaton
+ * timestep, used ONLY as the test oracle (and the timed CPU baseline of the
+ * benchmark). It is never linked into, or called by, the product library.
+ *
+ * It follows the reference's sequential algorithm step for step, in the same
+ * floating-point operation order (build with -ffp-contract=off), and draws
+ * from the same random streams (glibc rand() for sites and orientations, a
+ * restated libstdc++ minstd_rand0 + normal_distribution for critical
+ * undercoolings). Every function cites the reference file:line it follows.
+ */
+#ifndef AMCA_ORACLE_H
+#define AMCA_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Parameters of the plain (uniform-cooling) CA realm, as the reference reads
+ * them from its YAML deck (CellularAutomataManager_3D.cpp:71-361,
+ * ProblemPhysics.cpp:58-102, CellularAutomataSolver.cpp:99-128). */
+typedef struct {
+  int nx, ny, nz;            /* interior cells per axis */
+  double x0, y0, z0;         /* domain origin */
+  double h;                  /* cell size */
+  double ns, mu_s, sigma_s;  /* surface sites: density (per area), mean, std of dTc */
+  double nv, mu_v, sigma_v;  /* bulk sites: density (per volume), mean, std of dTc */
+  unsigned seed;             /* glibc srand() seed (reference: procID*10000 at np=1 -> 0) */
+  double T0, Tm, Tdot;       /* uniform temperature T(t) = T0 + Tdot*t; melting temperature */
+  double a1, a2, a3;         /* KGT polynomial v = a1*dT + a2*dT^2 + a3*dT^3 */
+  double max_dt;             /* time_step */
+  double final_time;         /* termination_time */
+  double time_step_factor;   /* time_step_factor_ca (default 0.2) */
+  double trunc_coeff;        /* Octahedron truncation coefficient (default (double)sqrtf(3.0f)) */
+} amca_oracle_plain_params;
+
+typedef struct {
+  int steps;             /* CA steps taken */
+  double time;           /* simulation time reached */
+  double last_dt;        /* dt of the last step */
+  int64_t num_grains;    /* envelopes created (grainVector_ size) */
+  int64_t num_orient;    /* orientations created */
+  int64_t liquid_cells;  /* interior liquid cells left */
+  int64_t active_grains; /* active envelopes left */
+  int64_t tests;         /* octahedron containment tests performed */
+  int64_t num_sites;     /* distinct nucleation sites */
+} amca_oracle_result;
+
+/* Run the plain CA until solid / final_time / max_steps (max_steps < 0: no
+ * limit). Outputs are over the ghost-inclusive grid (nx+2)(ny+2)(nz+2) in the
+ * reference's index order k*(nx+2)(ny+2) + j*(nx+2) + i:
+ *   orient_out: cellOrientationID_ (-1 liquid, 0 on the ghost layer)
+ *   grain_out:  cellGrainID_       (envelope index owning the cell)
+ *   site_dtc_out: cellNucleationDT_ (-1 no site, 0 consumed site, else dTc)
+ * Any output pointer may be NULL. euler_out (3 doubles per orientation, up to
+ * euler_cap orientations) receives the orientation Euler angles.
+ * Returns 0 on success, <0 on allocation failure / bad parameters. */
+int amca_oracle_run_plain(const amca_oracle_plain_params *p, int max_steps, int32_t *orient_out, int32_t *grain_out,
+                          double *site_dtc_out, double *euler_out, int64_t euler_cap, amca_oracle_result *res);
+
+/* Building blocks exposed for known-answer tests. */
+/* libstdc++ std::normal_distribution<double>(mean, sigma) driven by a
+ * default-constructed std::default_random_engine (minstd_rand0, seed 1):
+ * writes the first n draws. */
+void amca_oracle_normal_draws(double mean, double sigma, int n, double *out);
+/* Orientation angles + local->global rotation matrix, from three glibc
+ * rand() values (CellularAutomataManager_3D.cpp:839-850, Octahedron.cpp:282-310). */
+void amca_oracle_orientation(int r0, int r1, int r2, double euler[3], double l2g[9]);
+/* Octahedron containment test and decentred capture for one (envelope, cell)
+ * pair (Octahedron.cpp:99-128, 134-275). l2g is the local->global matrix. */
+int amca_oracle_is_captured(const double l2g[9], const double gc[3], double length);
+void amca_oracle_capture(const double l2g[9], const double gc[3], double length, double h, double trunc_coeff,
+                         double new_info[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
