@@ -1,0 +1,201 @@
+"""GB300 CA timestep of AMCA3D behind the reference's own input surface.
+
+Python binding (ctypes) of the C ABI in ``include/amca3d.h``. The compute
+path is the in-tree ``libamca3d.so`` (hand-written sm_103a CUDA); there is no
+CPU fallback — importing works anywhere, but every call that needs the GPU
+fails loudly if the library or the device is missing.
+
+    realm = CellularAutomataRealm(deck_text, seed=0)
+    realm.initialize()
+    realm.run()                       # until solid / termination_time
+    grain_id = realm.field("orientation_id")
+
+The method names follow the reference's ``CellularAutomataManager`` interface
+(CA/include/CellularAutomataManager.h:20-246): ``initialize``,
+``single_integration_step`` (one ``calculate_time_step`` +
+``single_integration_step``), ``time_integration``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libamca3d.so")
+
+AMCA_OK = 0
+FIELD_IDS = {"orientation_id": 0, "grain_id": 1, "site_undercooling": 2}
+_ERRORS = {-1: "bad argument", -2: "deck parse error", -3: "CUDA error", -4: "call out of order",
+           -5: "device-side error", -6: "output error"}
+
+
+class AmcaError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_ERRORS.get(code, code)}: {message}")
+        self.code = code
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("seed", ctypes.c_uint), ("write_outputs", ctypes.c_int),
+                ("workdir", ctypes.c_char_p)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_int64), ("time", ctypes.c_double), ("dt", ctypes.c_double),
+                ("liquid_cells", ctypes.c_int64), ("grains", ctypes.c_int64), ("orientations", ctypes.c_int64),
+                ("active", ctypes.c_int64), ("sites", ctypes.c_int64), ("cells", ctypes.c_int64),
+                ("tests", ctypes.c_int64), ("tests_fp64", ctypes.c_int64), ("generations", ctypes.c_int64),
+                ("done", ctypes.c_int32), ("final_grain_count", ctypes.c_int32), ("kernel_ms", ctypes.c_double),
+                ("launches", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# every entry point declared in include/amca3d.h
+EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
+           "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
+           "amca_last_error", "amca_destroy")
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None) -> ctypes.CDLL:
+    """Load libamca3d.so (built by ``amca3d_gb300.build``). Raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} is missing: build it with `python -m amca3d_gb300.build` "
+                                f"(no CPU fallback exists)")
+    lib = ctypes.CDLL(p)
+    vp, cp, i, i64 = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int64
+    lib.amca_create.argtypes = [cp, ctypes.POINTER(_Opts), ctypes.POINTER(vp)]
+    lib.amca_get_grid.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(ctypes.c_double)]
+    lib.amca_prepare.argtypes = [vp]
+    lib.amca_get_sites.argtypes = [vp, vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    lib.amca_initialize.argtypes = [vp]
+    lib.amca_step.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    lib.amca_run.argtypes = [vp, i]
+    lib.amca_get_field.argtypes = [vp, i, vp, ctypes.c_size_t]
+    lib.amca_get_orientations.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_size_t), i]
+    lib.amca_write_outputs.argtypes = [vp]
+    lib.amca_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.amca_last_error.argtypes = [vp]
+    lib.amca_last_error.restype = cp
+    lib.amca_destroy.argtypes = [vp]
+    lib.amca_destroy.restype = None
+    for name in ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
+                 "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats"):
+        getattr(lib, name).restype = i
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class CellularAutomataRealm:
+    """One AMCA3D CA realm on one GPU, read from a YAML deck."""
+
+    def __init__(self, deck: str, seed: int = 0, device: int = 0, write_outputs: bool = False,
+                 workdir: Optional[str] = None):
+        self._lib = load_library()
+        self._h = ctypes.c_void_p()
+        self._workdir = workdir.encode() if workdir else None
+        opts = _Opts(device, seed, 1 if write_outputs else 0, self._workdir)
+        rc = self._lib.amca_create(deck.encode(), ctypes.byref(opts), ctypes.byref(self._h))
+        if rc != AMCA_OK:
+            raise AmcaError(rc, self._lib.amca_last_error(None).decode())
+        cells = (ctypes.c_int32 * 3)()
+        origin = (ctypes.c_double * 3)()
+        h = ctypes.c_double()
+        self._check(self._lib.amca_get_grid(self._h, cells, origin, ctypes.byref(h)))
+        self.cells = tuple(int(c) for c in cells)
+        self.origin = tuple(float(o) for o in origin)
+        self.cell_size = h.value
+        self._ghost_cells = (self.cells[0] + 2) * (self.cells[1] + 2) * (self.cells[2] + 2)
+
+    def _check(self, rc: int) -> None:
+        if rc != AMCA_OK:
+            raise AmcaError(rc, self._lib.amca_last_error(self._h).decode())
+
+    def prepare(self) -> None:
+        """Host half of initialize (sites, orientation stream); needs no GPU."""
+        self._check(self._lib.amca_prepare(self._h))
+
+    def sites(self):
+        """(cell ids, critical undercoolings) of the nucleation sites after prepare()."""
+        n = ctypes.c_size_t()
+        self._check(self._lib.amca_get_sites(self._h, None, None, 0, ctypes.byref(n)))
+        cells = np.empty(n.value, np.int32)
+        dtc = np.empty(n.value, np.float64)
+        self._check(self._lib.amca_get_sites(self._h, cells.ctypes.data_as(ctypes.c_void_p),
+                                             dtc.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n)))
+        return cells, dtc
+
+    def initialize(self) -> None:
+        self._check(self._lib.amca_initialize(self._h))
+
+    def single_integration_step(self) -> float:
+        dt = ctypes.c_double()
+        self._check(self._lib.amca_step(self._h, ctypes.byref(dt)))
+        return dt.value
+
+    def run(self, max_steps: int = -1) -> None:
+        self._check(self._lib.amca_run(self._h, int(max_steps)))
+
+    time_integration = run
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self._lib.amca_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def field(self, name: str = "orientation_id", out: Optional[np.ndarray] = None) -> np.ndarray:
+        fid = FIELD_IDS[name]
+        n = self.cells_with_ghosts
+        dtype = np.float64 if name == "site_undercooling" else np.int32
+        if out is None:
+            out = np.empty(n, dtype=dtype)
+        assert out.dtype == dtype and out.size == n and out.flags.c_contiguous
+        self._check(self._lib.amca_get_field(self._h, fid, out.ctypes.data_as(ctypes.c_void_p), out.nbytes))
+        return out
+
+    def orientations(self, all: bool = False) -> np.ndarray:
+        """Euler angles of the orientations created so far (all=True: the whole
+        pre-drawn stream, one per site)."""
+        n = ctypes.c_size_t()
+        self._check(self._lib.amca_get_orientations(self._h, None, 0, ctypes.byref(n), int(all)))
+        e = np.empty((n.value, 3), np.float64)
+        self._check(self._lib.amca_get_orientations(self._h, e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                    n.value, ctypes.byref(n), int(all)))
+        return e
+
+    def write_outputs(self) -> None:
+        self._check(self._lib.amca_write_outputs(self._h))
+
+    @property
+    def cells_with_ghosts(self) -> int:
+        return self._ghost_cells
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.amca_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

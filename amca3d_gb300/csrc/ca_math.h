@@ -1,0 +1,248 @@
+// ca_math.h — envelope arithmetic of the CA step, shared by the CUDA kernels
+// and the host engine.
+//
+// The FP64 routines reproduce AMCA3D's octahedron arithmetic bit for bit:
+// the same operations in the same order, no fused multiply-add (device code
+// is built with -fmad=false, host code with -ffp-contract=off), float square
+// roots where the reference calls sqrtf on doubles.
+//
+//   cell centre        CA/src/CellularAutomataManager_3D.cpp:877-888
+//   containment test   CA/src/Octahedron.cpp:99-128
+//   decentred capture  CA/src/Octahedron.cpp:134-275, CA/src/CellularAutomataManager_3D.cpp:677-707
+//   KGT velocity       CA/src/ProblemPhysics.cpp:118-135
+//
+// The FP32 containment pre-test decides a (cell, envelope) pair only when its
+// rounding-error bound keeps it on one side of the FP64 boundary; otherwise
+// the caller runs the FP64 test. Decisions therefore equal the FP64 ones.
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define AMCA_HD __host__ __device__ __forceinline__
+#else
+#define AMCA_HD inline
+#endif
+
+#include <math.h>
+
+namespace amca {
+
+constexpr double kTheodorus = 1.732050807568877;  // CA/src/Octahedron.cpp:13
+
+// Liquid cells hold -1 in the orientation field; during one generation of
+// the capture sweep a liquid cell may instead hold a claim
+// 0x80000000 | parity << 30 | rank (rank = position of the claiming envelope
+// in the generation, which is ascending envelope id). Solid cells and the
+// ghost layer hold an orientation id >= 0.
+constexpr uint32_t kLiquid = 0xFFFFFFFFu;
+constexpr uint32_t kClaimBit = 0x80000000u;
+constexpr uint32_t kParityBit = 0x40000000u;
+constexpr uint32_t kRankMask = 0x3FFFFFFFu;
+
+AMCA_HD uint32_t claim_word(uint32_t parity, uint32_t rank) { return kClaimBit | (parity ? kParityBit : 0u) | rank; }
+// liquid at the start of the current generation: -1, or a claim made in it
+AMCA_HD bool is_liquid_now(uint32_t s, uint32_t parity) {
+  return s == kLiquid || ((s & kClaimBit) && (((s & kParityBit) != 0) == (parity != 0)));
+}
+
+struct Grid {
+  int nx, ny, nz;     // interior cells
+  int nxg, nyg, nzg;  // with the ghost layer
+  int nxyg;
+  double x0, y0, z0, h;
+};
+
+// get_cell_center: x0 + h*(I - 0.5) with the ghost-inclusive index I.
+AMCA_HD double centre_coord(double o, double h, int I) { return o + h * (I - 0.5); }
+
+AMCA_HD void cell_ijk(const Grid &g, int64_t id, int &I, int &J, int &K) {
+  K = (int)(id / g.nxyg);
+  int r = (int)(id - (int64_t)K * g.nxyg);
+  J = r / g.nxg;
+  I = r - J * g.nxg;
+}
+
+// Neighbour n in 0..25 in the reference's k, j, i loop order
+// (CA/src/CellularAutomataManager_3D.cpp:913-925).
+AMCA_HD void nbr_offset(int n, int &di, int &dj, int &dk) {
+  int m = n < 13 ? n : n + 1;  // skip the centre (index 13 of 27)
+  dk = m / 9 - 1;
+  dj = (m / 3) % 3 - 1;
+  di = m % 3 - 1;
+}
+
+// cell_is_captured in FP64. l2g is transMatrixLocal2Global (row-major);
+// the global->local matrix is its transpose, summed from 0 in component order.
+AMCA_HD bool is_captured_f64(const double *l2g, double gcx, double gcy, double gcz, double length) {
+  if (length == 0) return false;
+  double cx = 0, cy = 0, cz = 0;
+  cx += gcx * l2g[0];
+  cy += gcx * l2g[1];
+  cz += gcx * l2g[2];
+  cx += gcy * l2g[3];
+  cy += gcy * l2g[4];
+  cz += gcy * l2g[5];
+  cx += gcz * l2g[6];
+  cy += gcz * l2g[7];
+  cz += gcz * l2g[8];
+  return fabs(cx) + fabs(cy) + fabs(cz) <= 1.0 * length;
+}
+
+// FP32 pre-test. Returns +1 (captured), 0 (not captured) or -1 (too close to
+// the boundary for FP32: use is_captured_f64). gc* are the cell-centre offsets
+// from the envelope centre in FP32; err is an absolute bound on their error
+// per component; m32 is l2g rounded to float.
+//
+// Bound: |m_ij| <= 1, so each local coordinate is a 3-term dot product whose
+// FP32 evaluation errs by at most 3*u*(|gx|+|gy|+|gz|) + 3*err (u = 2^-24),
+// and the final sum of three absolute values adds 2*u*(its magnitude). The
+// margin used is 2^-14 relative plus 8*err per component — orders of
+// magnitude above that bound and the FP64 evaluation's own error.
+AMCA_HD int captured_f32(const float *m32, float gx, float gy, float gz, float err, float length) {
+  float cx = gx * m32[0] + gy * m32[3] + gz * m32[6];
+  float cy = gx * m32[1] + gy * m32[4] + gz * m32[7];
+  float cz = gx * m32[2] + gy * m32[5] + gz * m32[8];
+  float s = fabsf(cx) + fabsf(cy) + fabsf(cz);
+  float scale = fabsf(gx) + fabsf(gy) + fabsf(gz);
+  float margin = 6.103515625e-05f * (3.0f * scale + length) + 24.0f * err;  // 2^-14
+  if (s < length - margin) return 1;
+  if (s > length + margin) return 0;
+  return -1;
+}
+
+// CA/src/Octahedron.cpp:27-84 tables
+AMCA_HD double face_normal(int q, int i) {
+  // normalVector[8][3]: (+x +y +z), (-x +y +z), (-x -y +z), (+x -y +z), then z negated
+  const int sx = (q == 1 || q == 2 || q == 5 || q == 6) ? -1 : 1;
+  const int sy = (q == 2 || q == 3 || q == 6 || q == 7) ? -1 : 1;
+  const int sz = q >= 4 ? -1 : 1;
+  return (double)(i == 0 ? sx : (i == 1 ? sy : sz));
+}
+AMCA_HD int face_corner(int q, int i) {
+  // surfaceCorner[8][3] = {0,1,4},{1,2,4},{2,3,4},{3,0,4},{0,1,5},{1,2,5},{2,3,5},{3,0,5}
+  const int f = q & 3;
+  if (i == 2) return q < 4 ? 4 : 5;
+  return (f + i) & 3;
+}
+AMCA_HD double corner_unit(int c, int j) {
+  // cornerCoord[6][3] = +x, +y, -x, -y, +z, -z
+  switch (c) {
+    case 0: return j == 0 ? 1.0 : 0.0;
+    case 1: return j == 1 ? 1.0 : 0.0;
+    case 2: return j == 0 ? -1.0 : 0.0;
+    case 3: return j == 1 ? -1.0 : 0.0;
+    case 4: return j == 2 ? 1.0 : 0.0;
+    default: return j == 2 ? -1.0 : 0.0;
+  }
+}
+AMCA_HD double dmin_ref(double a, double b) { return (b < a) ? b : a; }  // std::min
+AMCA_HD double dmax_ref(double a, double b) { return (a < b) ? b : a; }  // std::max
+
+// Octahedron::capture_cell: the new, decentred envelope for a captured cell.
+// gc = cell centre - parent centre (FP64). Writes the new centre offset
+// (global frame) into out[0..2] and the new half-diagonal into out[3].
+AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, double length, double h,
+                         double trunc_coeff, double out[4]) {
+  double cx = 0, cy = 0, cz = 0;
+  cx += gcx * l2g[0];
+  cy += gcx * l2g[1];
+  cz += gcx * l2g[2];
+  cx += gcy * l2g[3];
+  cy += gcy * l2g[4];
+  cz += gcy * l2g[5];
+  cx += gcz * l2g[6];
+  cy += gcz * l2g[7];
+  cz += gcz * l2g[8];
+  const double interception = fabs(cx) + fabs(cy) + fabs(cz);
+  int quad = 0;
+  if (cz >= 0) {
+    if (cx >= 0 && cy >= 0) quad = 0;
+    else if (cx >= 0 && cy < 0) quad = 3;
+    else if (cx < 0 && cy >= 0) quad = 1;
+    else quad = 2;
+  } else {
+    if (cx >= 0 && cy >= 0) quad = 4;
+    else if (cx >= 0 && cy < 0) quad = 7;
+    else if (cx < 0 && cy >= 0) quad = 5;
+    else quad = 6;
+  }
+  const double pC[3] = {cx, cy, cz};
+  const double perp = length - interception;
+  double pA[3];
+  for (int i = 0; i < 3; i++) pA[i] = pC[i] + perp * face_normal(quad, i) / 3;
+  double dist[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < 3; i++) {
+    const int id = face_corner(quad, i);
+    for (int j = 0; j < 3; j++) {
+      const double d = pA[j] - corner_unit(id, j) * length;
+      dist[i] += d * d;
+    }
+  }
+  int cid0 = face_corner(quad, 0), cid1, cid2;
+  double mind = dist[0];
+  // i = 1
+  if (mind > dist[1]) {
+    mind = dist[1];
+    cid1 = cid0;
+    cid0 = face_corner(quad, 1);
+  } else {
+    cid1 = face_corner(quad, 1);
+  }
+  // i = 2
+  if (mind > dist[2]) {
+    mind = dist[2];
+    cid2 = cid0;
+    cid0 = face_corner(quad, 2);
+  } else {
+    cid2 = face_corner(quad, 2);
+  }
+  double n12 = 0.0, n13 = 0.0, d12 = 0.0, d13 = 0.0;
+  for (int i = 0; i < 3; i++) {
+    const double c1 = corner_unit(cid0, i) * length;
+    const double s1a = pA[i] - c1;
+    const double s1s2 = corner_unit(cid1, i) * length - c1;
+    n12 += s1s2 * s1s2;
+    d12 += s1a * s1s2;
+    const double s1s3 = corner_unit(cid2, i) * length - c1;
+    n13 += s1s3 * s1s3;
+    d13 += s1a * s1s3;
+  }
+  n12 = (double)sqrtf((float)n12);
+  n13 = (double)sqrtf((float)n13);
+  double I0 = d12 / n12, I1 = n12 - I0;
+  const double J0 = d13 / n13, J1 = n13 - J0;
+  const double tv = trunc_coeff * h;
+  if (I0 < tv && I1 < tv) {
+    I0 = n12 / 2;
+    I1 = n13 / 2;
+  }
+  const double L1 = 0.5 * (dmin_ref(I0, tv) + dmin_ref(I1, tv));
+  const double L2 = 0.5 * (dmin_ref(J0, tv) + dmin_ref(J1, tv));
+  const double Lnew = (double)sqrtf(2.0f) * (dmax_ref(L1, L2));
+  const double mag = (length - Lnew);
+  double o0 = 0.0, o1 = 0.0, o2 = 0.0;
+  for (int i = 0; i < 3; i++) {
+    const double comp = mag * (corner_unit(cid0, i) * length) / (length * kTheodorus);
+    o0 += comp * l2g[i + 0];
+    o1 += comp * l2g[i + 3];
+    o2 += comp * l2g[i + 6];
+  }
+  out[0] = o0;
+  out[1] = o1;
+  out[2] = o2;
+  out[3] = Lnew;
+}
+
+// ProblemPhysics_RappazGandin1993::compute_growth_velocity for a uniform field
+AMCA_HD double kgt_velocity(double Tm, double T, double a1, double a2, double a3) {
+  const double dT = Tm - T;
+  double v = 0.0;
+  if (dT > 0) {
+    v = a1 * dT + a2 * dT * dT + a3 * dT * dT * dT;
+    if (v < 0.0) v = 0.0;
+  }
+  return v;
+}
+
+}  // namespace amca

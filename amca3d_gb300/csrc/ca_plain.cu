@@ -1,0 +1,508 @@
+// ca_plain.cu — the plain (uniform-cooling) CA step as one persistent,
+// cooperative CUDA kernel for sm_103a.
+//
+// Reference semantics (CA/src/CellularAutomataManager_3D.cpp:441-669):
+//   nucleate sites in ascending cell id, compute dt, grow every active
+//   envelope, then walk the active list in ascending envelope id; each
+//   envelope tests its 26 neighbours and captures every liquid one inside
+//   its octahedron, appending the new envelope to the list it is walking.
+//
+// Parallel equivalent, per step:
+//   generation 0 = the active list after nucleation; generation g+1 = the
+//   envelopes created while walking generation g (a contiguous id range,
+//   because ids are handed out in walk order).
+//   claim   : every envelope of the generation tests its liquid neighbours
+//             (FP32 pre-test with a proven error margin, exact FP64 when the
+//             margin is not enough) and atomicMin's a claim word
+//             0x80000000 | parity<<30 | rank into each cell it contains.
+//             rank order == walk order, so the smallest claim is the envelope
+//             that reaches the cell first in the reference.
+//   resolve : an envelope captures the cells whose final claim is its own;
+//             it stays active iff some neighbour was liquid at its turn and
+//             not captured by it (unclaimed, or claimed by a later rank).
+//             A decoupled look-back scan over (captures, survives) gives the
+//             new envelope ids (walk order) and the order-preserving
+//             compaction of survivors into the next active list.
+//   The claim words left in the field are overwritten with the orientation
+//   id by the new envelopes themselves in the next generation's claim phase
+//   (the opposite parity marks them solid meanwhile).
+// Every phase boundary is a grid barrier whose waits are bounded in time.
+#include <cooperative_groups.h>
+
+#include "ca_plain.h"
+
+namespace amca {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr unsigned long long kWaitNs = 5000000000ull;  // 5 s bound on any spin
+constexpr unsigned long long kFlagAgg = 1ull << 62;
+constexpr unsigned long long kFlagPrefix = 2ull << 62;
+constexpr unsigned long long kPayload = (1ull << 62) - 1;
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T ld_volatile(const T *p) {
+  return *(const volatile T *)p;
+}
+
+// Sense-counting grid barrier. Returns false (with ctrl->error set) when a
+// wait ran out or another block reported an error.
+__device__ bool grid_barrier(PlainCtrl *c) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned gen = ld_acquire(&c->bar_gen);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&c->bar_count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = now_ns();
+      while (ld_acquire(&c->bar_gen) == gen) {
+        if (ld_volatile(&c->error) != 0) break;
+        if (now_ns() - t0 > kWaitNs) {
+          atomicCAS(&c->error, 0, kErrBarrier);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ld_volatile(&c->error) == 0;
+}
+
+// Exclusive scan of one u64 per thread over the block; *total = block sum.
+__device__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long *smem,
+                                                   unsigned long long *total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < kWarps ? smem[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < kWarps; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kWarps) smem[lane] = w;
+  }
+  __syncthreads();
+  const unsigned long long before = warp > 0 ? smem[warp - 1] : 0ull;
+  *total = smem[kWarps - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// (a<<32 | b) <-> 62-bit payload (a<<31 | b); a, b < 2^31.
+__device__ __forceinline__ unsigned long long to_payload(unsigned long long v) {
+  return ((v >> 32) << 31) | (v & 0xffffffffull);
+}
+__device__ __forceinline__ unsigned long long from_payload(unsigned long long p) {
+  return ((p >> 31) << 32) | (p & 0x7fffffffull);
+}
+
+// Decoupled look-back (single thread). Publishes tile t's aggregate, walks
+// back to the nearest inclusive prefix, publishes its own. Returns false on
+// a timed-out wait.
+__device__ bool look_back(unsigned long long *status, long long t, unsigned long long agg, unsigned long long *excl,
+                          PlainCtrl *c) {
+  if (t == 0) {
+    atomicExch(status, kFlagPrefix | to_payload(agg));
+    *excl = 0;
+    return true;
+  }
+  atomicExch(status + t, kFlagAgg | to_payload(agg));
+  unsigned long long sum = 0;
+  long long p = t - 1;
+  const unsigned long long t0 = now_ns();
+  for (;;) {
+    const unsigned long long s = ld_acquire(status + p);
+    const unsigned long long flag = s & ~kPayload;
+    if (flag == 0) {
+      if (now_ns() - t0 > kWaitNs || ld_volatile(&c->error) != 0) {
+        atomicCAS(&c->error, 0, kErrLookback);
+        return false;
+      }
+      continue;
+    }
+    sum += from_payload(s & kPayload);
+    if (flag == kFlagPrefix) break;
+    --p;
+  }
+  atomicExch(status + t, kFlagPrefix | to_payload(sum + agg));
+  *excl = sum;
+  return true;
+}
+
+__device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj, int &dk) {
+  nbr_offset(n, di, dj, dk);
+  return dk * g.nxyg + dj * g.nxg + di;
+}
+
+// ---------------------------------------------------------------------------
+// Nucleation (CellularAutomataManager.cpp:219-297) in site order.
+// ---------------------------------------------------------------------------
+__device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned long long *smem) {
+  PlainCtrl *c = d.ctrl;
+  const long long nsites = d.nsites;
+  const long long ntiles = (nsites + kBlock - 1) / kBlock;
+  const long long base_orient = ld_volatile(&c->n_orient);
+  const long long base_grain = ld_volatile(&c->next_grain);
+  const long long base_act = ld_volatile(&c->n_active);
+  int32_t *act = ld_volatile(&c->cur_list) ? d.act1 : d.act0;
+  const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
+  const double dTu = d.Tm - T;
+  __threadfence();
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long i = t * kBlock + threadIdx.x;
+    int cell = -1;
+    unsigned nuc = 0;
+    if (i < nsites && d.site_live[i]) {
+      cell = d.site_cell[i];
+      const bool liquid = __ldcg(d.orient + cell) == kLiquid;
+      if (liquid && dTu > d.site_dtc[i]) nuc = 1;
+      if (!liquid || nuc) d.site_live[i] = 0;
+    }
+    unsigned long long agg;
+    const unsigned long long ex = block_exclusive_scan(nuc, smem, &agg);
+    if (threadIdx.x == 0) {
+      unsigned long long pre;
+      smem[kWarps] = look_back(d.scanA, t, agg, &pre, c) ? pre : ~0ull;
+    }
+    __syncthreads();
+    const unsigned long long pre = smem[kWarps];
+    __syncthreads();
+    if (pre == ~0ull) return false;
+    if (nuc) {
+      const long long r = (long long)(pre + ex);
+      const int oid = (int)(base_orient + r);
+      const long long gid = base_grain + r;
+      int I, J, K;
+      cell_ijk(d.grid, cell, I, J, K);
+      d.orient[cell] = (uint32_t)oid;
+      d.gx[gid] = centre_coord(d.grid.x0, d.grid.h, I);
+      d.gy[gid] = centre_coord(d.grid.y0, d.grid.h, J);
+      d.gz[gid] = centre_coord(d.grid.z0, d.grid.h, K);
+      d.glen[gid] = 0.0;
+      d.gdx[gid] = 0.f;
+      d.gdy[gid] = 0.f;
+      d.gdz[gid] = 0.f;
+      d.gori[gid] = oid;
+      d.gcell[gid] = cell;
+      act[base_act + r] = (int32_t)gid;
+    }
+    if (t == ntiles - 1 && threadIdx.x == 0) {
+      const long long total = (long long)(pre + agg);
+      c->n_orient = base_orient + total;
+      c->next_grain = base_grain + total;
+      c->n_active = base_act + total;
+      c->liquid -= total;
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Claim: growth (generation 0), neighbour tests, atomicMin claims.
+// ---------------------------------------------------------------------------
+__device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par, bool grow,
+                            double dt, double vel, const int32_t *act, unsigned long long *stat_tests,
+                            unsigned long long *stat_tests64) {
+  const Grid &g = d.grid;
+  const long long stride = (long long)gridDim.x * kBlock;
+  // the resolve phase's look-back words for this generation start cleared
+  const long long ntiles = (n + kBlock - 1) / kBlock;
+  for (long long t = (long long)blockIdx.x * kBlock + threadIdx.x; t < ntiles; t += stride) d.scanB[t] = 0ull;
+  unsigned long long tests = 0, tests64 = 0;
+  for (long long r = (long long)blockIdx.x * kBlock + threadIdx.x; r < n; r += stride) {
+    const int id = kind == 0 ? __ldcg(act + r) : (int)(lo + r);
+    const int cell = __ldcg(d.gcell + id);
+    const int ori = __ldcg(d.gori + id);
+    if (kind != 0) d.orient[cell] = (uint32_t)ori;  // finalize the cell captured last generation
+    double L = __ldcg(d.glen + id);
+    if (grow) {
+      L += dt * vel;  // Grain::grow (Grain.h:27)
+      d.glen[id] = L;
+    }
+    int I, J, K;
+    cell_ijk(g, cell, I, J, K);
+    const float dxf = __ldcg(d.gdx + id), dyf = __ldcg(d.gdy + id), dzf = __ldcg(d.gdz + id);
+    const float errg = 4.76837158203125e-07f * (d.h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + d.coord_err;
+    const float L32 = (float)L;
+    float m32[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m32[q] = __ldg(d.omat32 + 9 * ori + q);
+    uint32_t liq = 0, con = 0;
+    const uint32_t mine = claim_word(par, (uint32_t)r);
+    for (int nb = 0; nb < 26; ++nb) {
+      int di, dj, dk;
+      const int nc = cell + nbr_delta(g, nb, di, dj, dk);
+      const uint32_t s = __ldcg(d.orient + nc);
+      if (!is_liquid_now(s, par)) continue;
+      liq |= 1u << nb;
+      if (L == 0) continue;
+      ++tests;
+      int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg, L32);
+      if (f < 0) {
+        ++tests64;
+        const double ccx = centre_coord(g.x0, g.h, I + di);
+        const double ccy = centre_coord(g.y0, g.h, J + dj);
+        const double ccz = centre_coord(g.z0, g.h, K + dk);
+        const double gcx = ccx - __ldcg(d.gx + id), gcy = ccy - __ldcg(d.gy + id), gcz = ccz - __ldcg(d.gz + id);
+        f = is_captured_f64(d.omat + 9 * ori, gcx, gcy, gcz, L) ? 1 : 0;
+      }
+      if (f) {
+        con |= 1u << nb;
+        atomicMin(d.orient + nc, mine);
+      }
+    }
+    d.liq[r] = liq;
+    d.con[r] = con;
+  }
+  *stat_tests += tests;
+  *stat_tests64 += tests64;
+}
+
+// ---------------------------------------------------------------------------
+// Resolve: captures, deactivation, new envelopes, survivor compaction.
+// ---------------------------------------------------------------------------
+__device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par,
+                              const int32_t *act, int32_t *next_act, unsigned long long *smem) {
+  PlainCtrl *c = d.ctrl;
+  const Grid &g = d.grid;
+  const long long base_grain = ld_volatile(&c->next_grain);
+  const long long base_next = ld_volatile(&c->n_active_next);
+  __threadfence();
+  const long long ntiles = (n + kBlock - 1) / kBlock;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long r = t * kBlock + threadIdx.x;
+    uint32_t cap = 0;
+    unsigned surv = 0;
+    int id = -1, cell = 0;
+    if (r < n) {
+      const uint32_t lm = __ldcg(d.liq + r), cm = __ldcg(d.con + r);
+      id = kind == 0 ? __ldcg(act + r) : (int)(lo + r);
+      cell = __ldcg(d.gcell + id);
+      const uint32_t mine = claim_word(par, (uint32_t)r);
+      uint32_t bits = lm;
+      while (bits) {
+        const int nb = __ffs(bits) - 1;
+        bits &= bits - 1;
+        int di, dj, dk;
+        const int nc = cell + nbr_delta(g, nb, di, dj, dk);
+        const uint32_t s = __ldcg(d.orient + nc);
+        if ((cm >> nb) & 1u) {
+          if (s == mine) cap |= 1u << nb;
+        } else if (s == kLiquid || (s & kRankMask) > (uint32_t)r) {
+          surv = 1;
+        }
+      }
+    }
+    const unsigned long long v = ((unsigned long long)__popc(cap) << 32) | surv;
+    unsigned long long agg;
+    const unsigned long long ex = block_exclusive_scan(v, smem, &agg);
+    if (threadIdx.x == 0) {
+      unsigned long long pre;
+      smem[kWarps] = look_back(d.scanB, t, agg, &pre, c) ? pre : ~0ull;
+    }
+    __syncthreads();
+    const unsigned long long pre = smem[kWarps];
+    __syncthreads();
+    if (pre == ~0ull) return false;
+    if (r < n) {
+      const unsigned long long off = pre + ex;
+      if (surv) next_act[base_next + (long long)(off & 0xffffffffull)] = id;
+      if (cap) {
+        long long nid = base_grain + (long long)(off >> 32);
+        const int ori = __ldcg(d.gori + id);
+        const double L = __ldcg(d.glen + id);
+        const double px = __ldcg(d.gx + id), py = __ldcg(d.gy + id), pz = __ldcg(d.gz + id);
+        const double *m = d.omat + 9 * ori;
+        int I, J, K;
+        cell_ijk(g, cell, I, J, K);
+        uint32_t bits = cap;
+        while (bits) {
+          const int nb = __ffs(bits) - 1;
+          bits &= bits - 1;
+          int di, dj, dk;
+          const int nc = cell + nbr_delta(g, nb, di, dj, dk);
+          const double ccx = centre_coord(g.x0, g.h, I + di);
+          const double ccy = centre_coord(g.y0, g.h, J + dj);
+          const double ccz = centre_coord(g.z0, g.h, K + dk);
+          double out[4];
+          capture_f64(m, ccx - px, ccy - py, ccz - pz, L, g.h, d.trunc, out);
+          const double nx = out[0] + px, ny = out[1] + py, nz = out[2] + pz;
+          d.gx[nid] = nx;
+          d.gy[nid] = ny;
+          d.gz[nid] = nz;
+          d.glen[nid] = out[3];
+          d.gdx[nid] = (float)(nx - ccx);
+          d.gdy[nid] = (float)(ny - ccy);
+          d.gdz[nid] = (float)(nz - ccz);
+          d.gori[nid] = ori;
+          d.gcell[nid] = nc;
+          ++nid;
+        }
+      }
+    }
+    if (t == ntiles - 1 && threadIdx.x == 0) {
+      const unsigned long long total = pre + agg;
+      const long long caps = (long long)(total >> 32), survs = (long long)(total & 0xffffffffull);
+      c->gen_lo = base_grain;
+      c->gen_n = caps;
+      c->next_grain = base_grain + caps;
+      c->n_active_next = base_next + survs;
+      c->liquid -= caps;
+      c->captures += (unsigned long long)caps;
+    }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d, long long step_limit) {
+  __shared__ unsigned long long smem[kWarps + 2];
+  PlainCtrl *c = d.ctrl;
+  unsigned long long tests = 0, tests64 = 0;
+  for (;;) {
+    const long long step = ld_volatile(&c->step);
+    const double time = ld_volatile(&c->time);
+    if (ld_volatile(&c->done) || !(time < d.final_time) || step >= step_limit) break;
+
+    // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
+    if (!nucleation_phase(d, time, smem)) break;
+    if (!grid_barrier(c)) break;
+    const long long nA = ld_volatile(&c->n_active);
+    const int cur = ld_volatile(&c->cur_list);
+    const double vel = kgt_velocity(d.Tm, d.T0 + d.Tdot * time, d.a1, d.a2, d.a3);
+    double maxV = 1e-10;
+    if (nA > 0 && vel > maxV) maxV = vel;
+    const double cand = d.tsf * d.grid.h / maxV;
+    const double dt = (d.max_dt < cand) ? d.max_dt : cand;  // std::min (:507)
+
+    // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
+    const int32_t *act = cur ? d.act1 : d.act0;
+    int32_t *next_act = cur ? d.act0 : d.act1;
+    long long n = nA, lo = 0;
+    int kind = 0;
+    unsigned gen = 0;
+    bool ok = true;
+    while (n > 0) {
+      claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dt, vel, act, &tests, &tests64);
+      if (!(ok = grid_barrier(c))) break;
+      if (!(ok = resolve_phase(d, kind, lo, n, gen & 1u, act, next_act, smem))) break;
+      if (!(ok = grid_barrier(c))) break;
+      n = ld_volatile(&c->gen_n);
+      lo = ld_volatile(&c->gen_lo);
+      kind = 1;
+      ++gen;
+    }
+    if (!ok) break;
+    // step end: swap lists, advance time (CellularAutomataManager_3D.cpp:653-659)
+    {
+      const long long ntA = (d.nsites + kBlock - 1) / kBlock;
+      for (long long t = (long long)blockIdx.x * kBlock + threadIdx.x; t < ntA; t += (long long)gridDim.x * kBlock)
+        d.scanA[t] = 0ull;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      c->n_active = c->n_active_next;
+      c->n_active_next = 0;
+      c->cur_list = cur ^ 1;
+      c->time = time + dt;
+      c->dt = dt;
+      c->vel = vel;
+      c->step = step + 1;
+      c->done = c->liquid == 0;
+      c->gens += gen;
+    }
+    if (!grid_barrier(c)) break;
+  }
+  // statistics: one atomic per warp
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    tests += __shfl_down_sync(0xffffffffu, tests, o);
+    tests64 += __shfl_down_sync(0xffffffffu, tests64, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (tests) atomicAdd(&c->tests, tests);
+    if (tests64) atomicAdd(&c->tests64, tests64);
+  }
+}
+
+__global__ void init_field_kernel(uint32_t *orient, Grid g, long long ncells) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < ncells; i += (long long)gridDim.x * blockDim.x) {
+    int I, J, K;
+    cell_ijk(g, i, I, J, K);
+    const bool ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
+    orient[i] = ghost ? 0u : kLiquid;
+  }
+}
+
+__global__ void grain_field_init_kernel(int32_t *out, const uint32_t *orient, Grid g, long long ncells) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < ncells; i += (long long)gridDim.x * blockDim.x) {
+    int I, J, K;
+    cell_ijk(g, i, I, J, K);
+    const bool ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
+    out[i] = ghost ? 0 : -1;
+  }
+}
+
+__global__ void grain_field_scatter_kernel(int32_t *out, const int32_t *gcell, long long ngrains) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < ngrains; i += (long long)gridDim.x * blockDim.x)
+    out[gcell[i]] = (int32_t)i;
+}
+
+}  // namespace
+
+cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s) {
+  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.grid, d.ncells);
+  return cudaGetLastError();
+}
+
+int plain_persistent_grid(int device) {
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plain_persistent_kernel, kBlock, 0) != cudaSuccess)
+    return 0;
+  return sms * per_sm;
+}
+
+cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid_blocks, cudaStream_t s) {
+  PlainDevice dd = d;
+  void *args[] = {(void *)&dd, (void *)&step_limit};
+  return cudaLaunchCooperativeKernel((const void *)plain_persistent_kernel, dim3(grid_blocks), dim3(kBlock), args, 0,
+                                     s);
+}
+
+cudaError_t plain_grain_field(const PlainDevice &d, int32_t *out, long long ngrains, cudaStream_t s) {
+  grain_field_init_kernel<<<1024, 256, 0, s>>>(out, d.orient, d.grid, d.ncells);
+  if (ngrains > 0) grain_field_scatter_kernel<<<1024, 256, 0, s>>>(out, d.gcell, ngrains);
+  return cudaGetLastError();
+}
+
+}  // namespace amca

@@ -1,0 +1,91 @@
+// ca_plain.h — device state and launch API of the plain (uniform-cooling)
+// CA step on one GPU.
+//
+// HBM layout (one realm):
+//   orient      u32[(nx+2)(ny+2)(nz+2)]  cellOrientationID_, ghost-inclusive, reference index order
+//   site_*      nucleation sites sorted by cell id: cell i32, dTc f64, live u8
+//   omat/omat32 per orientation: local->global matrix, 9 x f64 and 9 x f32
+//   g*          envelope table (capacity = interior cells), structure of arrays:
+//               centre f64 x3, half-diagonal f64, centre minus own-cell centre f32 x3,
+//               orientation i32, cell i32
+//   act[2]      active-envelope lists (ascending id), double-buffered per step
+//   liq/con     per-rank neighbour masks of the generation being processed
+//   scanA/scanB decoupled look-back tile status words (nucleation / capture)
+//   ctrl        control block: counters, time, barrier words, error flag
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ca_math.h"
+
+namespace amca {
+
+struct PlainCtrl {
+  unsigned bar_count;
+  unsigned bar_gen;
+  int error;        // 0, or where a bounded wait ran out (see kErr*)
+  int cur_list;     // which act[] holds the current active list
+  long long n_orient;
+  long long next_grain;
+  long long n_active;
+  long long n_active_next;
+  long long liquid;
+  long long gen_lo;
+  long long gen_n;
+  long long step;
+  double time;
+  double dt;
+  double vel;
+  int done;
+  int pad;
+  unsigned long long tests;
+  unsigned long long tests64;
+  unsigned long long gens;
+  unsigned long long captures;
+};
+
+enum { kErrBarrier = 1, kErrLookback = 2 };
+
+struct PlainDevice {
+  Grid grid;
+  // physics
+  double T0, Tm, Tdot, a1, a2, a3;
+  double max_dt, final_time, tsf, trunc;
+  float h32;
+  float coord_err;  // bound on FP64 cell-centre rounding, per component
+  // arrays
+  uint32_t *orient;
+  int64_t ncells;
+  const int32_t *site_cell;
+  const double *site_dtc;
+  uint8_t *site_live;
+  int64_t nsites;
+  const double *omat;
+  const float *omat32;
+  double *gx, *gy, *gz, *glen;
+  float *gdx, *gdy, *gdz;
+  int32_t *gori, *gcell;
+  int64_t gcap;
+  int32_t *act0, *act1;
+  uint32_t *liq, *con;
+  unsigned long long *scanA, *scanB;
+  PlainCtrl *ctrl;
+};
+
+// Fill the orientation field: -1 interior, 0 on the ghost layer
+// (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833).
+cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s);
+
+// Blocks of the persistent kernel that fit on the device at once.
+int plain_persistent_grid(int device);
+
+// Run CA steps until solid, final_time, or ctrl->step reaches step_limit.
+// One cooperative launch; every phase boundary is a bounded grid barrier.
+cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid_blocks, cudaStream_t s);
+
+// cellGrainID_ from the envelope table: -1 liquid, 0 ghost layer, else the
+// id of the envelope created for the cell.
+cudaError_t plain_grain_field(const PlainDevice &d, int32_t *out, long long ngrains, cudaStream_t s);
+
+}  // namespace amca

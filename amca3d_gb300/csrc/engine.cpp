@@ -1,0 +1,530 @@
+// engine.cpp — the C ABI (include/amca3d.h) over the plain CA realm.
+//
+// Host side of CellularAutomataSolver / CellularAutomataManager_3D
+// (CA/src/CellularAutomataSolver.cpp:40-201, CA/src/CellularAutomataManager_3D.cpp:366-379):
+// parse the deck, draw sites and the orientation stream with the reference's
+// libraries, move tables to HBM, run the persistent step kernel, write outputs.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/amca3d.h"
+#include "ca_plain.h"
+#include "deck.h"
+#include "host_init.h"
+#include "writers.h"
+
+using namespace amca;
+
+namespace {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string &m) : std::runtime_error(m) {}
+};
+struct DeviceError : std::runtime_error {
+  explicit DeviceError(const std::string &m) : std::runtime_error(m) {}
+};
+struct StateError : std::runtime_error {
+  explicit StateError(const std::string &m) : std::runtime_error(m) {}
+};
+
+#define CK(call)                                                                                      \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess) throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct amca_t {
+  std::string err;
+  amca_opts opts{};
+  std::string workdir;
+  PlainConfig cfg;
+  bool initialized = false;
+  // host tables
+  SiteSet sites;
+  OrientationTable otab;
+  std::vector<int32_t> mapped_vtr;
+  int64_t rand_draws_before_orient = 0;
+  // device
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int grid_blocks = 0;
+  PlainDevice dev{};
+  std::vector<void *> allocs;
+  int32_t *scratch_field = nullptr;
+  PlainCtrl ctrl{};  // host copy after the last segment
+  VtrSeries vtr;
+  double kernel_ms = 0.0;
+  int64_t launches = 0;
+
+  ~amca_t() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void *p : allocs) cudaFree(p);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  T *alloc(size_t n) {
+    void *p = nullptr;
+    CK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+    allocs.push_back(p);
+    return (T *)p;
+  }
+
+  std::string path(const std::string &p) const {
+    if (p.empty() || p[0] == '/' || workdir.empty()) return p;
+    return workdir + "/" + p;
+  }
+
+  void sync_ctrl() {
+    CK(cudaMemcpyAsync(&ctrl, dev.ctrl, sizeof(PlainCtrl), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (ctrl.error) {
+      throw DeviceError(std::string("CA kernel stopped: ") +
+                        (ctrl.error == kErrBarrier ? "grid barrier wait timed out" : "scan look-back wait timed out"));
+    }
+  }
+
+  bool prepared = false;
+
+  // Host half: sites, mapped ids, orientation stream (one glibc rand() stream).
+  void prepare() {
+    if (prepared) return;
+    GlibcRand rng(opts.seed);
+    sites = make_sites(cfg, rng);
+    mapped_vtr = make_mapped_ids(sites.surface_sites + sites.bulk_sites, cfg.shuffle_vtr, rng);
+    rand_draws_before_orient = rng.draws();
+    otab = make_orientations((int64_t)sites.cell.size(), rng);
+    prepared = true;
+  }
+
+  void initialize() {
+    const PlainConfig &c = cfg;
+    prepare();
+    CK(cudaSetDevice(device));
+    const int64_t nsites = (int64_t)sites.cell.size();
+    // --- device ---
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    Grid g{};
+    g.nx = c.nx;
+    g.ny = c.ny;
+    g.nz = c.nz;
+    g.nxg = c.nx + 2;
+    g.nyg = c.ny + 2;
+    g.nzg = c.nz + 2;
+    g.nxyg = g.nxg * g.nyg;
+    g.x0 = c.x0;
+    g.y0 = c.y0;
+    g.z0 = c.z0;
+    g.h = c.h;
+    PlainDevice &d = dev;
+    d.grid = g;
+    d.T0 = c.T0;
+    d.Tm = c.Tm;
+    d.Tdot = c.Tdot;
+    d.a1 = c.a1;
+    d.a2 = c.a2;
+    d.a3 = c.a3;
+    d.max_dt = c.max_dt;
+    d.final_time = c.final_time;
+    d.tsf = c.time_step_factor;
+    d.trunc = c.trunc_coeff;
+    d.h32 = (float)c.h;
+    double cmax = 0;
+    const double o[3] = {c.x0, c.y0, c.z0};
+    const int nn[3] = {g.nxg, g.nyg, g.nzg};
+    for (int a = 0; a < 3; ++a) cmax = std::max(cmax, std::fabs(o[a]) + (nn[a] + 1) * c.h);
+    d.coord_err = (float)(std::ldexp(cmax, -49) + 1e-30);
+    d.ncells = (int64_t)g.nxyg * g.nzg;
+    d.nsites = nsites;
+    d.gcap = (int64_t)c.nx * c.ny * c.nz;
+    d.orient = alloc<uint32_t>(d.ncells);
+    int32_t *site_cell = alloc<int32_t>(nsites);
+    double *site_dtc = alloc<double>(nsites);
+    d.site_live = alloc<uint8_t>(nsites);
+    double *omat = alloc<double>(nsites * 9);
+    float *omat32 = alloc<float>(nsites * 9);
+    d.site_cell = site_cell;
+    d.site_dtc = site_dtc;
+    d.omat = omat;
+    d.omat32 = omat32;
+    d.gx = alloc<double>(d.gcap);
+    d.gy = alloc<double>(d.gcap);
+    d.gz = alloc<double>(d.gcap);
+    d.glen = alloc<double>(d.gcap);
+    d.gdx = alloc<float>(d.gcap);
+    d.gdy = alloc<float>(d.gcap);
+    d.gdz = alloc<float>(d.gcap);
+    d.gori = alloc<int32_t>(d.gcap);
+    d.gcell = alloc<int32_t>(d.gcap);
+    d.act0 = alloc<int32_t>(d.gcap);
+    d.act1 = alloc<int32_t>(d.gcap);
+    d.liq = alloc<uint32_t>(d.gcap);
+    d.con = alloc<uint32_t>(d.gcap);
+    const int64_t ntA = (nsites + 255) / 256 + 1, ntB = (d.gcap + 255) / 256 + 1;
+    d.scanA = alloc<unsigned long long>(ntA);
+    d.scanB = alloc<unsigned long long>(ntB);
+    d.ctrl = alloc<PlainCtrl>(1);
+    if (nsites) {
+      CK(cudaMemcpyAsync(site_cell, sites.cell.data(), nsites * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+      CK(cudaMemcpyAsync(site_dtc, sites.dtc.data(), nsites * sizeof(double), cudaMemcpyHostToDevice, stream));
+      CK(cudaMemsetAsync(d.site_live, 1, nsites, stream));
+      CK(cudaMemcpyAsync(omat, otab.l2g.data(), nsites * 9 * sizeof(double), cudaMemcpyHostToDevice, stream));
+      CK(cudaMemcpyAsync(omat32, otab.l2g32.data(), nsites * 9 * sizeof(float), cudaMemcpyHostToDevice, stream));
+    }
+    CK(cudaMemsetAsync(d.scanA, 0, ntA * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(d.scanB, 0, ntB * sizeof(unsigned long long), stream));
+    PlainCtrl c0{};
+    c0.liquid = (long long)c.nx * c.ny * c.nz;
+    CK(cudaMemcpyAsync(d.ctrl, &c0, sizeof c0, cudaMemcpyHostToDevice, stream));
+    CK(plain_init_field(d, stream));
+    ctrl = c0;
+    grid_blocks = plain_persistent_grid(device);
+    if (grid_blocks <= 0) throw CudaError("no co-resident blocks for the persistent CA kernel");
+    CK(cudaStreamSynchronize(stream));
+    // VtrManager::initialize
+    vtr.configure(c.output, workdir);
+    if (opts.write_outputs) vtr.make_dirs();
+    initialized = true;
+  }
+
+  bool finished() const { return ctrl.done || !(ctrl.time < cfg.final_time); }
+
+  // Run up to `limit` (absolute step count) in one launch.
+  void segment(long long limit) {
+    CK(cudaEventRecord(ev0, stream));
+    CK(plain_run_steps(dev, limit, grid_blocks, stream));
+    CK(cudaEventRecord(ev1, stream));
+    ++launches;
+    sync_ctrl();
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    kernel_ms += ms;
+  }
+
+  void run(long long max_steps) {
+    if (!initialized) throw StateError("amca_run before amca_initialize");
+    const long long target = max_steps < 0 ? (1ll << 60) : ctrl.step + max_steps;
+    while (!finished() && ctrl.step < target) {
+      long long limit = target;
+      if (opts.write_outputs) {
+        if (cfg.output.frequency >= 1) {
+          const long long f = cfg.output.frequency;
+          limit = std::min(limit, (ctrl.step / f + 1) * f);  // stop at the next output step
+        } else if (cfg.output.time_interval_set && cfg.output.time_interval > 0) {
+          limit = std::min(limit, ctrl.step + 1);  // time-based outputs are checked every step
+        }
+      }
+      const long long before = ctrl.step;
+      segment(limit);
+      if (ctrl.step == before) break;
+      if (opts.write_outputs && vtr.due((int)ctrl.step, ctrl.time)) write_snapshot();
+    }
+  }
+
+  std::vector<int32_t> orient_field() {
+    std::vector<int32_t> h((size_t)dev.ncells);
+    CK(cudaMemcpyAsync(h.data(), dev.orient, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return h;
+  }
+  std::vector<int32_t> grain_field() {
+    if (!scratch_field) scratch_field = alloc<int32_t>(dev.ncells);
+    CK(plain_grain_field(dev, scratch_field, ctrl.next_grain, stream));
+    std::vector<int32_t> h((size_t)dev.ncells);
+    CK(cudaMemcpyAsync(h.data(), scratch_field, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return h;
+  }
+  std::vector<double> site_field() {
+    std::vector<uint8_t> live(sites.cell.size());
+    if (!live.empty()) {
+      CK(cudaMemcpyAsync(live.data(), dev.site_live, live.size(), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+    }
+    std::vector<double> f((size_t)dev.ncells, -1.0);
+    for (size_t i = 0; i < live.size(); ++i) f[sites.cell[i]] = live[i] ? sites.dtc[i] : 0.0;
+    return f;
+  }
+
+  OutputView view(const std::vector<int32_t> &orient) const {
+    OutputView v{};
+    v.nx = cfg.nx;
+    v.ny = cfg.ny;
+    v.nz = cfg.nz;
+    v.x0 = cfg.x0;
+    v.y0 = cfg.y0;
+    v.z0 = cfg.z0;
+    v.h = cfg.h;
+    v.orient = orient.data();
+    v.euler = otab.euler.data();
+    v.n_orient = ctrl.n_orient;
+    v.mapped_vtr = cfg.shuffle_vtr ? &mapped_vtr : nullptr;
+    v.shuffle_vtk = cfg.shuffle_vtk;
+    v.expected_grains = sites.surface_sites + sites.bulk_sites;
+    return v;
+  }
+
+  void write_snapshot() {
+    std::vector<int32_t> o = orient_field();
+    OutputView v = view(o);
+    vtr.write(v, ctrl.time);
+  }
+
+  int final_grain_count(const std::vector<int32_t> &o) const {
+    // get_amount_of_final_orientations: orientation ids present anywhere,
+    // the ghost layer (id 0) included (CA/src/CellularAutomataManager_3D.cpp:2000-2034)
+    const int64_t n = ctrl.n_orient;
+    if (n <= 0) return 0;
+    std::vector<char> seen((size_t)n, 0);
+    for (int32_t v : o)
+      if (v > -1 && v < n) seen[v] = 1;
+    return (int)std::count(seen.begin(), seen.end(), 1);
+  }
+
+  void write_outputs() {
+    if (!initialized) throw StateError("amca_write_outputs before amca_initialize");
+    std::vector<int32_t> o = orient_field();
+    OutputView v = view(o);
+    std::vector<int32_t> grain;
+    std::vector<double> dtc, gx, gy, gz;
+    std::vector<int32_t> gori, gcell;
+    // output_microstructure_information (after the time loop)
+    if (cfg.micro_out) {
+      grain = grain_field();
+      dtc = site_field();
+      const int64_t ng = ctrl.next_grain;
+      gx.resize(ng);
+      gy.resize(ng);
+      gz.resize(ng);
+      gori.resize(ng);
+      gcell.resize(ng);
+      if (ng) {
+        CK(cudaMemcpyAsync(gx.data(), dev.gx, ng * 8, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(gy.data(), dev.gy, ng * 8, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(gz.data(), dev.gz, ng * 8, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(gori.data(), dev.gori, ng * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(gcell.data(), dev.gcell, ng * 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+      }
+      v.grain = grain.data();
+      v.site_dtc = dtc.data();
+      v.n_grains = ng;
+      v.gx = gx.data();
+      v.gy = gy.data();
+      v.gz = gz.data();
+      v.gori = gori.data();
+      v.gcell = gcell.data();
+      write_grain_info(v, path(cfg.micro_out_file));
+    }
+    // CellularAutomataSolver::finalize: last VTR snapshot (step 0), finalGrains.vtk
+    std::vector<int32_t> mapped_vtk;
+    if (cfg.shuffle_vtk) {
+      int maxVal = -1;
+      for (int k = 1; k <= cfg.nz; ++k)
+        for (int j = 1; j <= cfg.ny; ++j)
+          for (int i = 1; i <= cfg.nx; ++i)
+            maxVal = std::max(maxVal, (int)o[((int64_t)k * (cfg.ny + 2) + j) * (cfg.nx + 2) + i]);
+      // replay the glibc stream to where the reference's writeToFile shuffles
+      GlibcRand rng(opts.seed);
+      const int64_t skip = rand_draws_before_orient + 3 * ctrl.n_orient;
+      for (int64_t i = 0; i < skip; ++i) rng.next();
+      mapped_vtk = make_mapped_ids(maxVal + 1, true, rng);
+      v.mapped_vtk = &mapped_vtk;
+    }
+    if (vtr.due(0, ctrl.time)) {
+      vtr.make_dirs();
+      vtr.write(v, ctrl.time);
+    }
+    write_final_grains(v, path("finalGrains.vtk"), vtr.pvd_path());
+  }
+};
+
+namespace {
+
+template <typename F>
+int guarded(amca_t *h, F &&f) {
+  try {
+    f();
+    if (h) h->err.clear();
+    return AMCA_OK;
+  } catch (const CudaError &e) {
+    if (h) h->err = e.what();
+    return AMCA_ERR_CUDA;
+  } catch (const DeviceError &e) {
+    if (h) h->err = e.what();
+    return AMCA_ERR_DEVICE;
+  } catch (const StateError &e) {
+    if (h) h->err = e.what();
+    return AMCA_ERR_STATE;
+  } catch (const std::exception &e) {
+    if (h) h->err = e.what();
+    return AMCA_ERR_ARG;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int amca_create(const char *yaml_text, const amca_opts *opts, amca_t **out) {
+  if (!out || !yaml_text) {
+    g_create_error = "amca_create: null argument";
+    return AMCA_ERR_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<amca_t> h(new amca_t);
+  if (opts) h->opts = *opts;
+  h->device = h->opts.device;
+  if (h->opts.workdir) h->workdir = h->opts.workdir;
+  try {
+    h->cfg = parse_plain_deck(yaml_text);
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    return AMCA_ERR_PARSE;
+  }
+  *out = h.release();
+  return AMCA_OK;
+}
+
+int amca_get_grid(const amca_t *h, int32_t cells[3], double origin[3], double *cell_size) {
+  if (!h) return AMCA_ERR_ARG;
+  if (cells) {
+    cells[0] = h->cfg.nx;
+    cells[1] = h->cfg.ny;
+    cells[2] = h->cfg.nz;
+  }
+  if (origin) {
+    origin[0] = h->cfg.x0;
+    origin[1] = h->cfg.y0;
+    origin[2] = h->cfg.z0;
+  }
+  if (cell_size) *cell_size = h->cfg.h;
+  return AMCA_OK;
+}
+
+int amca_prepare(amca_t *h) {
+  if (!h) return AMCA_ERR_ARG;
+  return guarded(h, [&] { h->prepare(); });
+}
+
+int amca_get_sites(const amca_t *h, int32_t *cells, double *dtc, size_t cap, size_t *n_out) {
+  if (!h) return AMCA_ERR_ARG;
+  if (!h->prepared) return AMCA_ERR_STATE;
+  const size_t n = h->sites.cell.size();
+  if (n_out) *n_out = n;
+  const size_t m = std::min(n, cap);
+  if (cells && m) memcpy(cells, h->sites.cell.data(), m * sizeof(int32_t));
+  if (dtc && m) memcpy(dtc, h->sites.dtc.data(), m * sizeof(double));
+  return AMCA_OK;
+}
+
+int amca_initialize(amca_t *h) {
+  if (!h) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (h->initialized) throw StateError("amca_initialize called twice");
+    h->initialize();
+  });
+}
+
+int amca_step(amca_t *h, double *dt_out) {
+  if (!h) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    h->run(1);
+    if (dt_out) *dt_out = h->ctrl.dt;
+  });
+}
+
+int amca_run(amca_t *h, int max_steps) {
+  if (!h) return AMCA_ERR_ARG;
+  return guarded(h, [&] { h->run(max_steps); });
+}
+
+int amca_get_field(amca_t *h, int field, void *dst, size_t bytes) {
+  if (!h || !dst) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->initialized) throw StateError("amca_get_field before amca_initialize");
+    const size_t n = (size_t)h->dev.ncells;
+    if (field == AMCA_FIELD_ORIENTATION_ID || field == AMCA_FIELD_GRAIN_ID) {
+      if (bytes != n * 4) throw std::invalid_argument("amca_get_field: bytes must be cells*4");
+      if (field == AMCA_FIELD_ORIENTATION_ID) {
+        CK(cudaMemcpyAsync(dst, h->dev.orient, n * 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+      } else {
+        std::vector<int32_t> g = h->grain_field();
+        memcpy(dst, g.data(), n * 4);
+      }
+    } else if (field == AMCA_FIELD_SITE_UNDERCOOLING) {
+      if (bytes != n * 8) throw std::invalid_argument("amca_get_field: bytes must be cells*8");
+      std::vector<double> f = h->site_field();
+      memcpy(dst, f.data(), n * 8);
+    } else {
+      throw std::invalid_argument("amca_get_field: unknown field");
+    }
+  });
+}
+
+int amca_get_orientations(amca_t *h, double *euler, size_t cap, size_t *n_out, int all) {
+  if (!h) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (all && !h->prepared) throw StateError("amca_get_orientations(all=1) before amca_prepare");
+    const size_t n = all ? h->otab.euler.size() / 3 : (size_t)std::max<long long>(0, h->ctrl.n_orient);
+    if (n_out) *n_out = n;
+    if (euler) memcpy(euler, h->otab.euler.data(), std::min(n, cap) * 3 * sizeof(double));
+  });
+}
+
+int amca_write_outputs(amca_t *h) {
+  if (!h) return AMCA_ERR_ARG;
+  int rc = guarded(h, [&] { h->write_outputs(); });
+  if (rc == AMCA_ERR_ARG) rc = AMCA_ERR_IO;
+  return rc;
+}
+
+int amca_get_stats(amca_t *h, amca_stats *s) {
+  if (!h || !s) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    memset(s, 0, sizeof *s);
+    const PlainCtrl &c = h->ctrl;
+    s->step = c.step;
+    s->time = c.time;
+    s->dt = c.dt;
+    s->liquid_cells = c.liquid;
+    s->grains = c.next_grain;
+    s->orientations = c.n_orient;
+    s->active = c.n_active;
+    s->sites = (int64_t)h->sites.cell.size();
+    s->cells = (int64_t)h->cfg.nx * h->cfg.ny * h->cfg.nz;
+    s->tests = (int64_t)c.tests;
+    s->tests_fp64 = (int64_t)c.tests64;
+    s->generations = (int64_t)c.gens;
+    s->done = c.done;
+    s->kernel_ms = h->kernel_ms;
+    s->launches = h->launches;
+    if (h->initialized) s->final_grain_count = h->final_grain_count(h->orient_field());
+  });
+}
+
+const char *amca_last_error(const amca_t *h) {
+  if (!h) return g_create_error.c_str();
+  return h->err.c_str();
+}
+
+void amca_destroy(amca_t *h) { delete h; }
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+/*
+ * amca3d.h — C ABI of the GB300 CA-timestep library (libamca3d.so).
+ *
+ * One handle runs one AMCA3D cellular-automaton realm on one GPU, read from
+ * the reference's own YAML input deck. Every call returns an int status
+ * (AMCA_OK == 0) and never throws; amca_last_error() gives the message of the
+ * last failure on a handle. The library owns all device memory; callers own
+ * host buffers. A handle is used by one host thread at a time and has its own
+ * CUDA stream.
+ *
+ * Each entry point cites the reference interface it replaces.
+ */
+#ifndef AMCA3D_H
+#define AMCA3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  AMCA_OK = 0,
+  AMCA_ERR_ARG = -1,      /* bad argument / unsupported deck content */
+  AMCA_ERR_PARSE = -2,    /* YAML syntax or a missing required key */
+  AMCA_ERR_CUDA = -3,     /* a CUDA call failed (no GPU, no memory, ...) */
+  AMCA_ERR_STATE = -4,    /* call out of order (e.g. step before initialize) */
+  AMCA_ERR_DEVICE = -5,   /* a kernel reported an internal error (bounded wait ran out) */
+  AMCA_ERR_IO = -6        /* output file could not be written */
+};
+
+typedef struct amca_t amca_t;
+
+/* Options the reference takes from its environment rather than the deck. */
+typedef struct {
+  int device;           /* CUDA device ordinal */
+  unsigned seed;        /* glibc srand() seed offset: the reference seeds srand(procID*10000), i.e. 0 at np=1 */
+  int write_outputs;    /* 1: write VTR/PVTR/PVD snapshots every output_frequency steps, like VtrManager::execute */
+  const char *workdir;  /* directory that relative output paths in the deck are resolved against (NULL: cwd) */
+} amca_opts;
+
+/* Parse a deck and select the realm.
+ * Replaces Simulation::load -> CellularAutomataSolver::load ->
+ * CellularAutomataManager_3D::load / ProblemPhysics_RappazGandin1993::load
+ * (CA/src/CellularAutomataSolver.cpp:40-130, CA/src/CellularAutomataManager_3D.cpp:71-361,
+ * CA/src/ProblemPhysics.cpp:58-102). opts may be NULL (device 0, seed 0, no outputs). */
+int amca_create(const char *yaml_text, const amca_opts *opts, amca_t **out);
+
+/* Grid of the realm: interior cells per axis, origin and cell size (the
+ * values CellularAutomataManager_3D::load derives, CA/src/CellularAutomataManager_3D.cpp:155-190).
+ * Needs no GPU. Any pointer may be NULL. */
+int amca_get_grid(const amca_t *h, int32_t cells[3], double origin[3], double *cell_size);
+
+/* Host half of initialize: draw the nucleation sites and the orientation
+ * stream (glibc rand(), libstdc++ normal_distribution, glibc libm), as
+ * CellularAutomataManager_3D::initialize does (CA/src/CellularAutomataManager_3D.cpp:366-379,
+ * CA/src/CellularAutomataManager.cpp:153-213,471-518). Needs no GPU;
+ * amca_initialize calls it when it has not run yet. */
+int amca_prepare(amca_t *h);
+
+/* Nucleation sites after amca_prepare: ghost-inclusive cell ids in ascending
+ * order and their critical undercoolings (nucleationCellIDList_ /
+ * cellNucleationDT_, CA/src/CellularAutomataManager.cpp:153-213). Either
+ * array may be NULL; *n_out receives the site count. */
+int amca_get_sites(const amca_t *h, int32_t *cells, double *dtc, size_t cap, size_t *n_out);
+
+/* Move the prepared tables to the GPU and build the cell field.
+ * Replaces CellularAutomataManager_3D::initialize (CA/src/CellularAutomataManager_3D.cpp:366-379). */
+int amca_initialize(amca_t *h);
+
+/* One CA step: nucleation, dt, growth and the capture sweep.
+ * Replaces CellularAutomataManager_3D::calculate_time_step + single_integration_step
+ * (CA/src/CellularAutomataManager_3D.cpp:441-669). dt_out may be NULL. */
+int amca_step(amca_t *h, double *dt_out);
+
+/* Steps until the domain is solid, the deck's termination_time is reached,
+ * or max_steps steps were taken (max_steps < 0: no step limit).
+ * Replaces CellularAutomataManager::time_integration (CA/src/CellularAutomataManager.cpp:134-147). */
+int amca_run(amca_t *h, int max_steps);
+
+enum {
+  AMCA_FIELD_ORIENTATION_ID = 0, /* int32, ghost-inclusive grid: cellOrientationID_ (the output "grain_id") */
+  AMCA_FIELD_GRAIN_ID = 1,       /* int32, ghost-inclusive grid: cellGrainID_ (envelope index per cell) */
+  AMCA_FIELD_SITE_UNDERCOOLING = 2 /* float64, ghost-inclusive grid: cellNucleationDT_ */
+};
+/* Copy a whole field to host memory. bytes must equal cells * element size,
+ * cells = (nx+2)(ny+2)(nz+2), in the reference's index order
+ * k*(nx+2)(ny+2) + j*(nx+2) + i.
+ * Replaces reading cellOrientationID_ / cellGrainID_ / cellNucleationDT_
+ * (CA/include/CellularAutomataManager.h:20-246). */
+int amca_get_field(amca_t *h, int field, void *host_dst, size_t bytes);
+
+/* Euler angles (3 doubles per orientation, in orientation-id order) of the
+ * orientations created so far; with all=1, of the whole pre-drawn stream
+ * (one per site, available after amca_prepare).
+ * Replaces orientationVector_ (CA/src/CellularAutomataManager_3D.cpp:1130-1215). */
+int amca_get_orientations(amca_t *h, double *euler, size_t cap, size_t *n_out, int all);
+
+/* Final outputs of a finished run: finalGrains.vtk, <pvd dir>/finalResult.txt,
+ * the last VTR/PVTR/PVD snapshot and, when the deck asks for it,
+ * grainInfo<rank>.txt. Replaces CellularAutomataSolver::finalize +
+ * CellularAutomataManager_3D::output_microstructure_information
+ * (CA/src/CellularAutomataSolver.cpp:166-201, CA/src/CellularAutomataManager_3D.cpp:1221-1639,1836-1913). */
+int amca_write_outputs(amca_t *h);
+
+typedef struct {
+  int64_t step;          /* iStep_ */
+  double time;           /* time_ */
+  double dt;             /* dT_ of the last step */
+  int64_t liquid_cells;  /* interior cells still liquid */
+  int64_t grains;        /* envelopes created (grainVector_.size()) */
+  int64_t orientations;  /* orientations created */
+  int64_t active;        /* active envelopes */
+  int64_t sites;         /* distinct nucleation sites */
+  int64_t cells;         /* interior cells */
+  int64_t tests;         /* octahedron containment tests evaluated */
+  int64_t tests_fp64;    /* ... of which needed the exact FP64 evaluation */
+  int64_t generations;   /* capture generations processed */
+  int32_t done;          /* 1 when no liquid cell is left */
+  int32_t final_grain_count; /* get_amount_of_final_orientations (valid after a field read) */
+  double kernel_ms;      /* device time of the CA kernels (CUDA events), accumulated */
+  int64_t launches;      /* CA kernel launches issued, accumulated */
+} amca_stats;
+int amca_get_stats(amca_t *h, amca_stats *out);
+
+/* Message of the last failing call on h (or of the last failing
+ * amca_create when h is NULL). Never NULL. */
+const char *amca_last_error(const amca_t *h);
+
+void amca_destroy(amca_t *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
