@@ -48,8 +48,11 @@ class Stats(ctypes.Structure):
                 ("liquid_cells", ctypes.c_int64), ("grains", ctypes.c_int64), ("orientations", ctypes.c_int64),
                 ("active", ctypes.c_int64), ("sites", ctypes.c_int64), ("cells", ctypes.c_int64),
                 ("tests", ctypes.c_int64), ("tests_fp64", ctypes.c_int64), ("generations", ctypes.c_int64),
-                ("done", ctypes.c_int32), ("final_grain_count", ctypes.c_int32), ("kernel_ms", ctypes.c_double),
-                ("launches", ctypes.c_int64)]
+                ("done", ctypes.c_int32), ("reserved", ctypes.c_int32), ("kernel_ms", ctypes.c_double),
+                ("launches", ctypes.c_int64), ("sites_scanned", ctypes.c_int64), ("nucleations", ctypes.c_int64),
+                ("captures", ctypes.c_int64), ("active_grown", ctypes.c_int64),
+                ("grains_processed", ctypes.c_int64), ("algorithmic_bytes", ctypes.c_double),
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -58,6 +61,7 @@ class Stats(ctypes.Structure):
 # every entry point declared in include/amca3d.h
 EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
+           "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
            "amca_last_error", "amca_destroy")
 
 _lib = None
@@ -87,6 +91,16 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
                                           ctypes.POINTER(ctypes.c_size_t), i]
     lib.amca_write_outputs.argtypes = [vp]
     lib.amca_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.amca_envelope_eval.argtypes = [i, ctypes.c_size_t, vp, vp, vp, ctypes.c_double, vp, vp, vp, vp]
+    lib.amca_envelope_eval.restype = i
+    lib.amca_final_grain_count.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
+    lib.amca_final_grain_count.restype = i
+    lib.amca_reset.argtypes = [vp]
+    lib.amca_reset.restype = i
+    lib.amca_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
+    lib.amca_host_alloc.restype = i
+    lib.amca_host_free.argtypes = [vp]
+    lib.amca_host_free.restype = i
     lib.amca_last_error.argtypes = [vp]
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]
@@ -97,6 +111,53 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     if path is None:
         _lib = lib
     return lib
+
+
+class PinnedBuffer:
+    """Page-locked host array (cudaMallocHost) for fast field copies."""
+
+    def __init__(self, n: int, dtype=np.int32):
+        self._lib = load_library()
+        self._p = ctypes.c_void_p()
+        nbytes = int(n) * np.dtype(dtype).itemsize
+        rc = self._lib.amca_host_alloc(nbytes, ctypes.byref(self._p))
+        if rc != AMCA_OK:
+            raise AmcaError(rc, self._lib.amca_last_error(None).decode())
+        buf = (ctypes.c_char * nbytes).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(n))
+
+    def free(self) -> None:
+        if self._p:
+            self.array = None
+            self._lib.amca_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def envelope_eval(l2g: np.ndarray, gc: np.ndarray, length: np.ndarray, h: float, trunc: np.ndarray,
+                  device: int = 0):
+    """Run the envelope arithmetic (Octahedron::cell_is_captured / capture_cell)
+    on the GPU for independent pairs. Returns (captured_fp64, captured_fast, info)."""
+    lib = load_library()
+    n = len(length)
+    l2g = np.ascontiguousarray(l2g, np.float64).reshape(n, 9)
+    gc = np.ascontiguousarray(gc, np.float64).reshape(n, 3)
+    length = np.ascontiguousarray(length, np.float64)
+    trunc = np.ascontiguousarray(trunc, np.float64)
+    cap = np.empty(n, np.int32)
+    fast = np.empty(n, np.int32)
+    info = np.empty((n, 4), np.float64)
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    rc = lib.amca_envelope_eval(device, n, ptr(l2g), ptr(gc), ptr(length), h, ptr(trunc), ptr(cap), ptr(fast),
+                                ptr(info))
+    if rc != AMCA_OK:
+        raise AmcaError(rc, lib.amca_last_error(None).decode())
+    return cap, fast, info
 
 
 class CellularAutomataRealm:
@@ -178,6 +239,15 @@ class CellularAutomataRealm:
 
     def write_outputs(self) -> None:
         self._check(self._lib.amca_write_outputs(self._h))
+
+    def reset(self) -> None:
+        """Back to the state right after initialize(), tables kept in HBM."""
+        self._check(self._lib.amca_reset(self._h))
+
+    def final_grain_count(self) -> int:
+        n = ctypes.c_int32()
+        self._check(self._lib.amca_final_grain_count(self._h, ctypes.byref(n)))
+        return n.value
 
     @property
     def cells_with_ghosts(self) -> int:

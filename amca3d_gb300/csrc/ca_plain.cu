@@ -168,7 +168,8 @@ __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj,
 // ---------------------------------------------------------------------------
 // Nucleation (CellularAutomataManager.cpp:219-297) in site order.
 // ---------------------------------------------------------------------------
-__device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned long long *smem) {
+__device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned long long *smem,
+                                 unsigned long long *stat_live) {
   PlainCtrl *c = d.ctrl;
   const long long nsites = d.nsites;
   const long long ntiles = (nsites + kBlock - 1) / kBlock;
@@ -184,6 +185,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
     int cell = -1;
     unsigned nuc = 0;
     if (i < nsites && d.site_live[i]) {
+      ++*stat_live;
       cell = d.site_cell[i];
       const bool liquid = __ldcg(d.orient + cell) == kLiquid;
       if (liquid && dTu > d.site_dtc[i]) nuc = 1;
@@ -223,6 +225,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
       c->next_grain = base_grain + total;
       c->n_active = base_act + total;
       c->liquid -= total;
+      c->nucleations += (unsigned long long)total;
     }
   }
   return true;
@@ -388,14 +391,14 @@ __device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long
 __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d, long long step_limit) {
   __shared__ unsigned long long smem[kWarps + 2];
   PlainCtrl *c = d.ctrl;
-  unsigned long long tests = 0, tests64 = 0;
+  unsigned long long tests = 0, tests64 = 0, live = 0;
   for (;;) {
     const long long step = ld_volatile(&c->step);
     const double time = ld_volatile(&c->time);
     if (ld_volatile(&c->done) || !(time < d.final_time) || step >= step_limit) break;
 
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
-    if (!nucleation_phase(d, time, smem)) break;
+    if (!nucleation_phase(d, time, smem, &live)) break;
     if (!grid_barrier(c)) break;
     const long long nA = ld_volatile(&c->n_active);
     const int cur = ld_volatile(&c->cur_list);
@@ -408,11 +411,12 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
     // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
     const int32_t *act = cur ? d.act1 : d.act0;
     int32_t *next_act = cur ? d.act0 : d.act1;
-    long long n = nA, lo = 0;
+    long long n = nA, lo = 0, processed = 0;
     int kind = 0;
     unsigned gen = 0;
     bool ok = true;
     while (n > 0) {
+      processed += n;
       claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dt, vel, act, &tests, &tests64);
       if (!(ok = grid_barrier(c))) break;
       if (!(ok = resolve_phase(d, kind, lo, n, gen & 1u, act, next_act, smem))) break;
@@ -439,6 +443,8 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
       c->step = step + 1;
       c->done = c->liquid == 0;
       c->gens += gen;
+      c->active_grown += (unsigned long long)nA;
+      c->grains_processed += (unsigned long long)processed;
     }
     if (!grid_barrier(c)) break;
   }
@@ -447,10 +453,12 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
   for (int o = 16; o > 0; o >>= 1) {
     tests += __shfl_down_sync(0xffffffffu, tests, o);
     tests64 += __shfl_down_sync(0xffffffffu, tests64, o);
+    live += __shfl_down_sync(0xffffffffu, live, o);
   }
   if ((threadIdx.x & 31) == 0) {
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);
+    if (live) atomicAdd(&c->sites_scanned, live);
   }
 }
 
@@ -477,7 +485,36 @@ __global__ void grain_field_scatter_kernel(int32_t *out, const int32_t *gcell, l
     out[gcell[i]] = (int32_t)i;
 }
 
+// One (envelope, cell) pair per thread: the FP64 containment test, the
+// production decision (FP32 pre-test, FP64 when undecided) and, when
+// captured, the decentred new envelope.
+__global__ void envelope_eval_kernel(long long n, const double *l2g, const double *gc, const double *len, double h,
+                                     const double *trunc, int32_t *cap64, int32_t *capfast, double *info) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double *m = l2g + 9 * i;
+    const double gx = gc[3 * i], gy = gc[3 * i + 1], gz = gc[3 * i + 2], L = len[i];
+    const bool c64 = is_captured_f64(m, gx, gy, gz, L);
+    float m32[9];
+    for (int q = 0; q < 9; ++q) m32[q] = (float)m[q];
+    const float fx = (float)gx, fy = (float)gy, fz = (float)gz;
+    const float err = 5.9604645e-08f * (fabsf(fx) + fabsf(fy) + fabsf(fz));  // conversion rounding of gc
+    int f = L == 0 ? 0 : captured_f32(m32, fx, fy, fz, err, (float)L);
+    if (f < 0) f = c64 ? 1 : 0;
+    cap64[i] = c64 ? 1 : 0;
+    capfast[i] = f;
+    double out[4] = {0.0, 0.0, 0.0, 0.0};
+    if (c64) capture_f64(m, gx, gy, gz, L, h, trunc[i], out);
+    for (int q = 0; q < 4; ++q) info[4 * i + q] = out[q];
+  }
+}
+
 }  // namespace
+
+cudaError_t plain_envelope_eval(long long n, const double *l2g, const double *gc, const double *len, double h,
+                                const double *trunc, int32_t *cap64, int32_t *capfast, double *info, cudaStream_t s) {
+  envelope_eval_kernel<<<256, 128, 0, s>>>(n, l2g, gc, len, h, trunc, cap64, capfast, info);
+  return cudaGetLastError();
+}
 
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s) {
   init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.grid, d.ncells);

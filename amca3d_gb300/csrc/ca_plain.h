@@ -43,6 +43,11 @@ struct PlainCtrl {
   unsigned long long tests64;
   unsigned long long gens;
   unsigned long long captures;
+  // work counters behind the algorithmic-bytes figure
+  unsigned long long sites_scanned;    // live sites read by nucleation, summed over steps
+  unsigned long long nucleations;      // envelopes created by nucleation
+  unsigned long long active_grown;     // generation-0 envelopes (grown), summed over steps
+  unsigned long long grains_processed; // envelopes of every generation, summed
 };
 
 enum { kErrBarrier = 1, kErrLookback = 2 };
@@ -87,5 +92,11 @@ cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid
 // cellGrainID_ from the envelope table: -1 liquid, 0 ghost layer, else the
 // id of the envelope created for the cell.
 cudaError_t plain_grain_field(const PlainDevice &d, int32_t *out, long long ngrains, cudaStream_t s);
+
+// Device evaluation of the envelope arithmetic on n independent pairs (all
+// pointers device memory): FP64 containment, the production FP32/FP64
+// decision, and the decentred capture (info: offset xyz + new half-diagonal).
+cudaError_t plain_envelope_eval(long long n, const double *l2g, const double *gc, const double *len, double h,
+                                const double *trunc, int32_t *cap64, int32_t *capfast, double *info, cudaStream_t s);
 
 }  // namespace amca

@@ -89,8 +89,18 @@ struct amca_t {
     return workdir + "/" + p;
   }
 
+  int64_t h2d_bytes = 0, d2h_bytes = 0;
+  void h2d(void *dst, const void *src, size_t bytes) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream));
+    h2d_bytes += (int64_t)bytes;
+  }
+  void d2h(void *dst, const void *src, size_t bytes) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += (int64_t)bytes;
+  }
+
   void sync_ctrl() {
-    CK(cudaMemcpyAsync(&ctrl, dev.ctrl, sizeof(PlainCtrl), cudaMemcpyDeviceToHost, stream));
+    d2h(&ctrl, dev.ctrl, sizeof(PlainCtrl));
     CK(cudaStreamSynchronize(stream));
     if (ctrl.error) {
       throw DeviceError(std::string("CA kernel stopped: ") +
@@ -180,20 +190,15 @@ struct amca_t {
     d.scanA = alloc<unsigned long long>(ntA);
     d.scanB = alloc<unsigned long long>(ntB);
     d.ctrl = alloc<PlainCtrl>(1);
+    ntA_ = ntA;
+    ntB_ = ntB;
     if (nsites) {
-      CK(cudaMemcpyAsync(site_cell, sites.cell.data(), nsites * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
-      CK(cudaMemcpyAsync(site_dtc, sites.dtc.data(), nsites * sizeof(double), cudaMemcpyHostToDevice, stream));
-      CK(cudaMemsetAsync(d.site_live, 1, nsites, stream));
-      CK(cudaMemcpyAsync(omat, otab.l2g.data(), nsites * 9 * sizeof(double), cudaMemcpyHostToDevice, stream));
-      CK(cudaMemcpyAsync(omat32, otab.l2g32.data(), nsites * 9 * sizeof(float), cudaMemcpyHostToDevice, stream));
+      h2d(site_cell, sites.cell.data(), nsites * sizeof(int32_t));
+      h2d(site_dtc, sites.dtc.data(), nsites * sizeof(double));
+      h2d(omat, otab.l2g.data(), nsites * 9 * sizeof(double));
+      h2d(omat32, otab.l2g32.data(), nsites * 9 * sizeof(float));
     }
-    CK(cudaMemsetAsync(d.scanA, 0, ntA * sizeof(unsigned long long), stream));
-    CK(cudaMemsetAsync(d.scanB, 0, ntB * sizeof(unsigned long long), stream));
-    PlainCtrl c0{};
-    c0.liquid = (long long)c.nx * c.ny * c.nz;
-    CK(cudaMemcpyAsync(d.ctrl, &c0, sizeof c0, cudaMemcpyHostToDevice, stream));
-    CK(plain_init_field(d, stream));
-    ctrl = c0;
+    reset_device();
     grid_blocks = plain_persistent_grid(device);
     if (grid_blocks <= 0) throw CudaError("no co-resident blocks for the persistent CA kernel");
     CK(cudaStreamSynchronize(stream));
@@ -201,6 +206,43 @@ struct amca_t {
     vtr.configure(c.output, workdir);
     if (opts.write_outputs) vtr.make_dirs();
     initialized = true;
+  }
+
+  int64_t ntA_ = 0, ntB_ = 0;
+
+  // Device state right after initialize: liquid field with the ghost layer,
+  // live sites, cleared scan words, zeroed control block.
+  void reset_device() {
+    PlainDevice &d = dev;
+    if (d.nsites) CK(cudaMemsetAsync(d.site_live, 1, d.nsites, stream));
+    CK(cudaMemsetAsync(d.scanA, 0, ntA_ * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(d.scanB, 0, ntB_ * sizeof(unsigned long long), stream));
+    PlainCtrl c0{};
+    c0.liquid = (long long)cfg.nx * cfg.ny * cfg.nz;
+    h2d(d.ctrl, &c0, sizeof c0);
+    CK(plain_init_field(d, stream));
+    ctrl = c0;
+    kernel_ms = 0.0;
+    launches = 0;
+  }
+
+  void reset() {
+    if (!initialized) throw StateError("amca_reset before amca_initialize");
+    reset_device();
+    CK(cudaStreamSynchronize(stream));
+    vtr = VtrSeries();
+    vtr.configure(cfg.output, workdir);
+  }
+
+  double algorithmic_bytes() const {
+    // per step: 12 B per live site (cell id + dTc), 48 B per nucleation
+    // (new envelope 40 B + orientation id 4 B + cell write 4 B), 16 B per grown
+    // envelope (half-diagonal read + write), 216 B per envelope and
+    // generation (40 B envelope, 26 x 4 B neighbour states, 72 B matrix),
+    // 44 B per capture (cell write + 40 B envelope), 8 B per list entry.
+    const double S = (double)ctrl.sites_scanned, N = (double)ctrl.nucleations, A = (double)ctrl.active_grown;
+    const double G = (double)ctrl.grains_processed, C = (double)ctrl.captures;
+    return 12 * S + 48 * N + 16 * A + 216 * G + 44 * C + 8 * (A + C);
   }
 
   bool finished() const { return ctrl.done || !(ctrl.time < cfg.final_time); }
@@ -239,7 +281,7 @@ struct amca_t {
 
   std::vector<int32_t> orient_field() {
     std::vector<int32_t> h((size_t)dev.ncells);
-    CK(cudaMemcpyAsync(h.data(), dev.orient, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    d2h(h.data(), dev.orient, h.size() * sizeof(int32_t));
     CK(cudaStreamSynchronize(stream));
     return h;
   }
@@ -247,14 +289,14 @@ struct amca_t {
     if (!scratch_field) scratch_field = alloc<int32_t>(dev.ncells);
     CK(plain_grain_field(dev, scratch_field, ctrl.next_grain, stream));
     std::vector<int32_t> h((size_t)dev.ncells);
-    CK(cudaMemcpyAsync(h.data(), scratch_field, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    d2h(h.data(), scratch_field, h.size() * sizeof(int32_t));
     CK(cudaStreamSynchronize(stream));
     return h;
   }
   std::vector<double> site_field() {
     std::vector<uint8_t> live(sites.cell.size());
     if (!live.empty()) {
-      CK(cudaMemcpyAsync(live.data(), dev.site_live, live.size(), cudaMemcpyDeviceToHost, stream));
+      d2h(live.data(), dev.site_live, live.size());
       CK(cudaStreamSynchronize(stream));
     }
     std::vector<double> f((size_t)dev.ncells, -1.0);
@@ -315,11 +357,11 @@ struct amca_t {
       gori.resize(ng);
       gcell.resize(ng);
       if (ng) {
-        CK(cudaMemcpyAsync(gx.data(), dev.gx, ng * 8, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(gy.data(), dev.gy, ng * 8, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(gz.data(), dev.gz, ng * 8, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(gori.data(), dev.gori, ng * 4, cudaMemcpyDeviceToHost, stream));
-        CK(cudaMemcpyAsync(gcell.data(), dev.gcell, ng * 4, cudaMemcpyDeviceToHost, stream));
+        d2h(gx.data(), dev.gx, ng * 8);
+        d2h(gy.data(), dev.gy, ng * 8);
+        d2h(gz.data(), dev.gz, ng * 8);
+        d2h(gori.data(), dev.gori, ng * 4);
+        d2h(gcell.data(), dev.gcell, ng * 4);
         CK(cudaStreamSynchronize(stream));
       }
       v.grain = grain.data();
@@ -463,7 +505,7 @@ int amca_get_field(amca_t *h, int field, void *dst, size_t bytes) {
     if (field == AMCA_FIELD_ORIENTATION_ID || field == AMCA_FIELD_GRAIN_ID) {
       if (bytes != n * 4) throw std::invalid_argument("amca_get_field: bytes must be cells*4");
       if (field == AMCA_FIELD_ORIENTATION_ID) {
-        CK(cudaMemcpyAsync(dst, h->dev.orient, n * 4, cudaMemcpyDeviceToHost, h->stream));
+        h->d2h(dst, h->dev.orient, n * 4);
         CK(cudaStreamSynchronize(h->stream));
       } else {
         std::vector<int32_t> g = h->grain_field();
@@ -516,8 +558,79 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->done = c.done;
     s->kernel_ms = h->kernel_ms;
     s->launches = h->launches;
-    if (h->initialized) s->final_grain_count = h->final_grain_count(h->orient_field());
+    s->sites_scanned = (int64_t)c.sites_scanned;
+    s->nucleations = (int64_t)c.nucleations;
+    s->captures = (int64_t)c.captures;
+    s->active_grown = (int64_t)c.active_grown;
+    s->grains_processed = (int64_t)c.grains_processed;
+    s->algorithmic_bytes = h->algorithmic_bytes();
+    s->h2d_bytes = h->h2d_bytes;
+    s->d2h_bytes = h->d2h_bytes;
   });
+}
+
+int amca_final_grain_count(amca_t *h, int32_t *count) {
+  if (!h || !count) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->initialized) throw StateError("amca_final_grain_count before amca_initialize");
+    *count = h->final_grain_count(h->orient_field());
+  });
+}
+
+int amca_reset(amca_t *h) {
+  if (!h) return AMCA_ERR_ARG;
+  return guarded(h, [&] { h->reset(); });
+}
+
+int amca_host_alloc(size_t bytes, void **out) {
+  if (!out) return AMCA_ERR_ARG;
+  *out = nullptr;
+  cudaError_t e = cudaMallocHost(out, std::max<size_t>(bytes, 1));
+  if (e != cudaSuccess) {
+    g_create_error = std::string("cudaMallocHost: ") + cudaGetErrorString(e);
+    return AMCA_ERR_CUDA;
+  }
+  return AMCA_OK;
+}
+
+int amca_host_free(void *p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) return AMCA_ERR_CUDA;
+  return AMCA_OK;
+}
+
+int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc, const double *length, double h,
+                       const double *trunc, int32_t *captured, int32_t *captured_fast, double *info) {
+  if (!l2g || !gc || !length || !trunc || !captured || !captured_fast || !info) {
+    g_create_error = "amca_envelope_eval: null argument";
+    return AMCA_ERR_ARG;
+  }
+  std::vector<void *> bufs;
+  int rc = AMCA_OK;
+  try {
+    CK(cudaSetDevice(device));
+    auto up = [&](const void *src, size_t bytes) {
+      void *p = nullptr;
+      CK(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
+      bufs.push_back(p);
+      if (src && bytes) CK(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
+      return p;
+    };
+    double *dm = (double *)up(l2g, n * 9 * 8), *dg = (double *)up(gc, n * 3 * 8), *dl = (double *)up(length, n * 8);
+    double *dt = (double *)up(trunc, n * 8);
+    int32_t *c64 = (int32_t *)up(nullptr, n * 4), *cf = (int32_t *)up(nullptr, n * 4);
+    double *di = (double *)up(nullptr, n * 4 * 8);
+    if (n) {
+      CK(plain_envelope_eval((long long)n, dm, dg, dl, h, dt, c64, cf, di, 0));
+      CK(cudaMemcpy(captured, c64, n * 4, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(captured_fast, cf, n * 4, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(info, di, n * 4 * 8, cudaMemcpyDeviceToHost));
+    }
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    rc = AMCA_ERR_CUDA;
+  }
+  for (void *p : bufs) cudaFree(p);
+  return rc;
 }
 
 const char *amca_last_error(const amca_t *h) {

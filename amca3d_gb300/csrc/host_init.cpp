@@ -6,6 +6,7 @@
 #include <cstring>
 #include <random>
 #include <stdexcept>
+#include <unordered_map>
 
 namespace amca {
 
@@ -26,63 +27,69 @@ int GlibcRand::next() {
 SiteSet make_sites(const PlainConfig &c, GlibcRand &rng) {
   const int nxg = c.nx + 2, nyg = c.ny + 2, nzg = c.nz + 2;
   const int64_t nxyg = (int64_t)nxg * nyg, ncells = nxyg * nzg;
-  std::vector<double> dtc_of;  // cellNucleationDT_, -1 = no site (allocated lazily)
+  std::unordered_map<int32_t, double> dtc_of;  // cellNucleationDT_ of the cells that hold a site
   std::vector<int32_t> sites;
   SiteSet out;
   auto population = [&](double density, double mean, double sigma, bool surface) {
     std::vector<int32_t> ids;
+    int64_t numCells64 = 0;
     if (surface) {
-      // every ghost-inclusive cell; a face cell is listed once per face it lies
-      // on. The y test compares against nxLocGhost_-1 as the reference does.
-      for (int64_t i = 0; i < ncells; ++i) {
-        const int K = (int)(i / nxyg);
-        if (K == 0 || K == nzg - 1) continue;
-        const int I = (int)((i % nxyg) % nxg);
-        if (I == 0 || I == nxg - 1) continue;
-        const int J = (int)((i % nxyg) / nxg);
-        if (J == 0 || J == nxg - 1) continue;
-        if (K == 1 || K == c.nz)
-          if (I != 0 && I != c.nx + 1 && J != 0 && J != c.ny + 1) ids.push_back((int32_t)i);
-        if (I == 1 || I == c.nx)
-          if (J != 0 && J != c.ny + 1 && K != 0 && K != c.nz + 1) ids.push_back((int32_t)i);
-        if (J == 1 || J == c.ny)
-          if (I != 0 && I != c.nx + 1 && K != 0 && K != c.nz + 1) ids.push_back((int32_t)i);
-      }
+      // Ascending ghost-inclusive id; a face cell is listed once per face it
+      // lies on (bottom/top, then left/right, then front/rear). Rows with
+      // J == nx+1 are skipped: the reference tests locGhostJ against
+      // nxLocGhost_-1. Ghost rows never qualify, so only interior rows are
+      // walked, and of rows that touch no y/z face only their two x ends.
+      for (int K = 1; K <= c.nz; ++K)
+        for (int J = 1; J <= c.ny; ++J) {
+          if (J == nxg - 1) continue;
+          const bool full = K == 1 || K == c.nz || J == 1 || J == c.ny;
+          for (int I = 1; I <= c.nx; I = (full || I == c.nx) ? I + 1 : c.nx) {
+            const int32_t id = (int32_t)(K * nxyg + (int64_t)J * nxg + I);
+            if (K == 1 || K == c.nz) ids.push_back(id);
+            if (I == 1 || I == c.nx) ids.push_back(id);
+            if (J == 1 || J == c.ny) ids.push_back(id);
+          }
+        }
+      numCells64 = (int64_t)ids.size();
     } else {
-      ids.reserve((size_t)c.nx * c.ny * c.nz);
-      for (int k = 1; k < nzg - 1; ++k)
-        for (int j = 1; j < nyg - 1; ++j)
-          for (int i = 1; i < nxg - 1; ++i) ids.push_back((int32_t)(k * nxyg + (int64_t)j * nxg + i));
+      // the bulk list is every interior cell in k, j, i order; entry q is
+      // computed instead of stored
+      numCells64 = (int64_t)c.nx * c.ny * c.nz;
     }
+    auto bulk_cell = [&](int64_t q) {
+      const int64_t k = q / ((int64_t)c.nx * c.ny) + 1, j = (q / c.nx) % c.ny + 1, i = q % c.nx + 1;
+      return (int32_t)(k * nxyg + j * nxg + i);
+    };
     const double per_cell = surface ? c.h * c.h : c.h * c.h * c.h;
-    const int numCells = (int)ids.size();
+    const int numCells = (int)numCells64;
     const int numSites = round(per_cell * density * numCells) + 0.5;
     std::default_random_engine generator;
     std::normal_distribution<double> distribution(mean, sigma);
     int64_t generated = 0;
     if (numSites > 0 && numCells == 0) throw std::runtime_error("nucleation sites requested on an empty cell set");
     for (int s = 0; s < numSites; ++s) {
-      const int cell = ids[rng.next() % numCells];
+      const int q = rng.next() % numCells;
+      const int32_t cell = surface ? ids[q] : bulk_cell(q);
       double dT = distribution(generator);
       dT = (dT < 0) ? 0 : dT;
-      if (dtc_of.empty()) dtc_of.assign((size_t)ncells, -1.0);
-      const double cur = dtc_of[cell];
-      if (cur < 0) {
+      auto it = dtc_of.find(cell);
+      if (it == dtc_of.end()) {
         sites.push_back(cell);
-        dtc_of[cell] = dT;
+        dtc_of.emplace(cell, dT);
         ++generated;
-      } else if (dT < cur) {
-        dtc_of[cell] = dT;
+      } else if (dT < it->second) {
+        it->second = dT;
       }
     }
     std::sort(sites.begin(), sites.end());
     (surface ? out.surface_sites : out.bulk_sites) = generated;
   };
+  (void)ncells;
   population(c.ns, c.mu_s, c.sigma_s, true);
   population(c.nv, c.mu_v, c.sigma_v, false);
   out.cell = sites;
   out.dtc.resize(sites.size());
-  for (size_t i = 0; i < sites.size(); ++i) out.dtc[i] = dtc_of[sites[i]];
+  for (size_t i = 0; i < sites.size(); ++i) out.dtc[i] = dtc_of.at(sites[i]);
   return out;
 }
 

@@ -45,6 +45,8 @@ class PlainCase:
     output_base: str = "./Results/Grains"
     output_variables: Sequence[str] = ("grain_ID",)
     microstructure_file: Optional[str] = None
+    shuffle_vtr: bool = False
+    shuffle_vtk: Optional[bool] = None
 
     @property
     def n_interior(self) -> int:
@@ -70,6 +72,10 @@ class PlainCase:
         nv, muv, sgv = self.bulk
         a1, a2, a3 = self.a
         opts = ["         - random_type:", "             rejection_sampling: no"]
+        if self.shuffle_vtr:
+            opts.append("             shuffer_vtr_grain_ID: yes")
+        if self.shuffle_vtk is not None:
+            opts.append(f"             shuffer_vtk_grain_ID: {'yes' if self.shuffle_vtk else 'no'}")
         if self.microstructure_file:
             opts += ["         - output_microstructure_information:",
                      f"             file_name: {self.microstructure_file}"]

@@ -1,0 +1,359 @@
+"""Benchmark: plain CA timestep, uniform cooling at 320^3 (32.8M cells).
+
+One bench step = one full run of the 320^3 deck from its initial state to
+full solidification (every CA step of it), on one GPU; cell-updates/s =
+interior cells x CA steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours (default): the CUDA path. `value` is device time (CUDA events around
+  the persistent step kernel on its stream) with the realm's tables resident
+  in HBM; `e2e` is the same metric through the public C ABI per step
+  (amca_create -> amca_initialize (host sites + H2D) -> amca_run ->
+  amca_get_field into pinned host memory -> amca_destroy), wall clock.
+reference: the CPU implementation of the path (the C restatement of the
+  reference, one process per host core, each on a bounded sample of the
+  workload), same metric.
+For N > 1 (torchrun) each rank runs an independent replica ("replicas only":
+the single-domain CA does not shard); the value is the sum of cell updates
+over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from amca3d_gb300 import decks  # noqa: E402
+
+METRIC = "cell-updates/s on 1 GB300, plain vs surrogate/batched, at matched grain stats"
+UNIT = "cell-updates/s"
+
+
+def workload():
+    return decks.config_uniform_320()
+
+
+def sample_case(n: int):
+    """The workload's physics on an n^3 block: same cell size, cooling and
+    site densities (surface sites scale with area, bulk with volume)."""
+    c = workload()
+    s = n / 320
+    return dataclasses.replace(
+        c, name=f"uniform_{n}", cells=(n, n, n),
+        surface=(decks.surface_density_for_sites(4000 * s * s, (n, n, n), c.cell_size), 2.0, 0.5),
+        bulk=(decks.bulk_density_for_sites(20000 * s ** 3, (n, n, n), c.cell_size), 3.0, 1.0))
+
+
+# ----------------------------------------------------------------------------
+# distributed helpers (gloo: only a barrier and a max/sum of scalars)
+# ----------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power)}
+
+
+# ----------------------------------------------------------------------------
+# grain statistics (matched-stats columns of the metric)
+# ----------------------------------------------------------------------------
+def grain_stats(orient: np.ndarray, cells, euler: np.ndarray) -> dict:
+    nx, ny, nz = cells
+    inner = orient.reshape(nz + 2, ny + 2, nx + 2)[1:-1, 1:-1, 1:-1].ravel()
+    ids, counts = np.unique(inner[inner >= 0], return_counts=True)
+    # <100> || z within 15 deg: max over crystal axes of |z-component| of the
+    # local->global matrix column (Bunge ZXZ, Octahedron.cpp:282-310)
+    a, b, g = euler[ids, 0], euler[ids, 1], euler[ids, 2]
+    zcol = np.stack([np.sin(b) * np.sin(g), np.sin(b) * np.cos(g), np.cos(b)], 1)
+    aligned = np.abs(zcol).max(1) >= np.cos(np.deg2rad(15.0))
+    return {"grains": int(len(ids)), "mean_grain_cells": float(counts.mean()) if len(ids) else 0.0,
+            "texture_100_z_15deg": float(counts[aligned].sum() / counts.sum()) if len(ids) else 0.0}
+
+
+# ----------------------------------------------------------------------------
+# CPU oracle runs (bounded samples)
+# ----------------------------------------------------------------------------
+def _oracle_sample(n: int) -> tuple:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    case = sample_case(n)
+    t = time.perf_counter()
+    r = amca_oracle.run_plain(case, fields=False)
+    el = time.perf_counter() - t
+    return case.n_interior * r["steps"], el, r["steps"]
+
+
+def cpu_baseline(n: int = 128) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    amca_oracle.build()
+    upd, el, steps = _oracle_sample(n)
+    return {"value": upd / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"C restatement of the reference, one core: the workload's physics on a {n}^3 block "
+                      f"(same h, cooling, site densities), {steps} CA steps to full solidification, {el:.1f} s"}
+
+
+def run_reference_arm(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    amca_oracle.build()
+    cores = os.cpu_count() or 1
+    n = args.ref_sample
+    ctx = mp.get_context("spawn")
+    times, updates = [], []
+    with ctx.Pool(cores) as pool:
+        for it in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            res = pool.map(_oracle_sample, [n] * cores)
+            el = time.perf_counter() - t
+            if it >= args.warmup:
+                times.append(el)
+                updates.append(sum(r[0] for r in res))
+    value = sum(updates) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_block(None),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent single-core runs of the C restatement of the reference "
+                                   f"(the reference is sequential per MPI rank and mpirun is not used here), "
+                                   f"each the workload's physics on a {n}^3 block run to full solidification"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_block(stats) -> dict:
+    c = workload()
+    cfg = {"workload": "uniform_320: plain CA, uniform cooling, 320^3 cells of 2 um (32.8M), t_dot = -50 K/s, "
+                       "~20k bulk Gaussian sites (3 K, 1 K) + ~4k surface sites (2 K, 0.5 K), KGT a1=-0.544e-4 "
+                       "a2=2.03e-4, seed 1, every CA step to full solidification",
+           "cells": c.n_interior, "seed": c.seed, "envelopes": "fp64", "grain_ids": "int32",
+           "l2": "inputs larger than L2: orientation field 134 MB + envelope table 1.7 GB per run"}
+    if stats:
+        cfg.update(stats)
+    return cfg
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "ca_persistent_uniform_320.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            return None
+    return None
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_ours(args, dist: Dist):
+    import amca3d_gb300 as A
+
+    dev = dist.local_rank
+    case = workload()
+    deck = case.to_yaml()
+    realm = A.CellularAutomataRealm(deck, seed=case.seed, device=dev)
+    realm.initialize()
+    for _ in range(args.warmup):
+        realm.reset()
+        realm.run()
+    clocks = ClockSampler(dev)
+    dist.barrier()
+    clocks.start()
+    device_ms, updates, ca_steps, alg_bytes, launches = [], [], [], [], 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        realm.reset()
+        realm.run()
+        st = realm.stats()
+        device_ms.append(st["kernel_ms"])
+        updates.append(st["cells"] * st["step"])
+        ca_steps.append(st["step"])
+        alg_bytes.append(st["algorithmic_bytes"])
+        launches += st["launches"] + 1  # the persistent kernel launches + the field reset kernel
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clk = clocks.stop()
+    st = realm.stats()
+    orient = realm.field("orientation_id")
+    gstats = grain_stats(orient, case.cells, realm.orientations())
+    realm.close()
+
+    # end to end through the public API, host buffers, per step
+    pinned = A.PinnedBuffer(case.n_ghost, np.int32)
+    e2e_t, e2e_upd, h2d, d2h = [], [], [], []
+    for it in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        r = A.CellularAutomataRealm(deck, seed=case.seed, device=dev)
+        r.initialize()
+        r.run()
+        r.field("orientation_id", out=pinned.array)
+        s = r.stats()
+        r.close()
+        el = time.perf_counter() - t
+        if it >= args.warmup:
+            e2e_t.append(el)
+            e2e_upd.append(s["cells"] * s["step"])
+            h2d.append(s["h2d_bytes"])
+            d2h.append(s["d2h_bytes"])
+    same = bool(np.array_equal(pinned.array, orient))
+    pinned.free()
+
+    t_dev = dist.reduce(sum(device_ms) / 1e3, "max")
+    upd_total = dist.reduce(float(sum(updates)), "sum")
+    e2e_time = dist.reduce(sum(e2e_t), "max")
+    e2e_total = dist.reduce(float(sum(e2e_upd)), "sum")
+    if dist.rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    achieved = (sum(alg_bytes) / len(alg_bytes)) / (sum(device_ms) / len(device_ms) / 1e3) / 1e9
+    traffic = load_traffic()
+    line = {
+        "metric": METRIC, "value": upd_total / t_dev, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(device_ms) / len(device_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_block({"ca_steps_per_run": ca_steps[-1], "envelopes": st["grains"], **gstats,
+                                "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same}),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": f"{peak_kind} burst copy",
+                     "kernel": "plain_persistent_kernel (one launch per run)",
+                     "algorithmic_bytes_per_launch": sum(alg_bytes) / len(alg_bytes)},
+        "e2e": {"value": e2e_total / e2e_time, "unit": UNIT, "h2d_bytes_per_step": int(np.mean(h2d)),
+                "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": 1e3 * e2e_time / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    if args.gpus == 1 and dist.rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-sample", type=int, default=128, help="edge of the CPU-baseline sample block")
+    ap.add_argument("--ref-sample", type=int, default=96, help="edge of each reference-arm sample block")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference_arm(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -118,14 +118,49 @@ typedef struct {
   int64_t tests_fp64;    /* ... of which needed the exact FP64 evaluation */
   int64_t generations;   /* capture generations processed */
   int32_t done;          /* 1 when no liquid cell is left */
-  int32_t final_grain_count; /* get_amount_of_final_orientations (valid after a field read) */
-  double kernel_ms;      /* device time of the CA kernels (CUDA events), accumulated */
+  int32_t reserved;
+  double kernel_ms;    /* device time of the CA kernels (CUDA events), accumulated */
   int64_t launches;      /* CA kernel launches issued, accumulated */
+  /* work counters, summed over steps since the last reset */
+  int64_t sites_scanned;    /* live nucleation sites read */
+  int64_t nucleations;      /* envelopes created by nucleation */
+  int64_t captures;         /* envelopes created by capture */
+  int64_t active_grown;     /* generation-0 (grown) envelopes */
+  int64_t grains_processed; /* envelopes processed over all generations */
+  double algorithmic_bytes; /* HBM bytes the step must move by the counting rule of the design notes */
+  int64_t h2d_bytes;        /* host->device bytes copied by this handle */
+  int64_t d2h_bytes;        /* device->host bytes copied by this handle */
 } amca_stats;
 int amca_get_stats(amca_t *h, amca_stats *out);
 
+/* Number of distinct orientation ids present in the field, the ghost layer
+ * (id 0) included, as the reference reports "Final Number of Grains".
+ * Replaces get_amount_of_final_orientations (CA/src/CellularAutomataManager_3D.cpp:2000-2034). */
+int amca_final_grain_count(amca_t *h, int32_t *count);
+
+/* Restore the state right after amca_initialize (all cells liquid, sites
+ * live, time 0) without re-reading the deck or re-uploading tables: the
+ * same realm can be run again. Counters in amca_stats restart too. */
+int amca_reset(amca_t *h);
+
+/* Page-locked host memory for fast field copies (cudaMallocHost); free
+ * with amca_host_free. */
+int amca_host_alloc(size_t bytes, void **out);
+int amca_host_free(void *p);
+
+/* Evaluate the envelope arithmetic on the GPU for n independent
+ * (envelope, cell) pairs given in host memory: l2g = local->global matrix
+ * (9 per pair), gc = cell centre minus envelope centre (3 per pair),
+ * length = half-diagonal, trunc = truncation coefficient per pair, h = cell
+ * size. Outputs: captured (FP64 test), captured_fast (the FP32 pre-test with
+ * FP64 fallback that the step kernel uses), info = decentred new envelope
+ * (centre offset xyz, half-diagonal; zeros when not captured).
+ * Replaces Octahedron::cell_is_captured / capture_cell (CA/src/Octahedron.cpp:99-275). */
+int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc, const double *length, double h,
+                       const double *trunc, int32_t *captured, int32_t *captured_fast, double *info);
+
 /* Message of the last failing call on h (or of the last failing
- * amca_create when h is NULL). Never NULL. */
+ * amca_create / amca_envelope_eval when h is NULL). Never NULL. */
 const char *amca_last_error(const amca_t *h);
 
 void amca_destroy(amca_t *h);

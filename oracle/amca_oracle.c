@@ -91,6 +91,10 @@ void amca_oracle_orientation(int r0, int r1, int r2, double euler[3], double m[9
   euler[0] = U * 2 * ORACLE_PI;
   euler[1] = acos(2 * V - 1);
   euler[2] = (double)r2 / RAND_MAX * 0.5 * ORACLE_PI;
+  amca_oracle_rotation(euler, m);
+}
+
+void amca_oracle_rotation(const double euler[3], double m[9]) {
   double ca = cos(euler[0]), sa = sin(euler[0]);
   double cb = cos(euler[1]), sb = sin(euler[1]);
   double cg = cos(euler[2]), sg = sin(euler[2]);
@@ -467,6 +471,12 @@ int amca_oracle_run_plain(const amca_oracle_plain_params *p, int max_steps, int3
     free_state(s);
     return -1;
   }
+  /* global_mapped_grain_ID (CellularAutomataManager.cpp:471-518): with
+   * shuffled VTR ids, std::random_shuffle over numGrains = distinct sites
+   * draws one rand() per element after the first; the map itself only
+   * relabels output, so the oracle just consumes the draws. */
+  if (p->shuffle_vtr)
+    for (int64_t i = 1; i < s->nsites; ++i) (void)rand();
   int64_t liquid = (int64_t)p->nx * p->ny * p->nz;
   double time = 0.0, dt = 0.0;
   int step = 0;

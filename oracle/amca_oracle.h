@@ -34,6 +34,7 @@ typedef struct {
   double final_time;         /* termination_time */
   double time_step_factor;   /* time_step_factor_ca (default 0.2) */
   double trunc_coeff;        /* Octahedron truncation coefficient (default (double)sqrtf(3.0f)) */
+  int shuffle_vtr;           /* random_type.shuffer_vtr_grain_ID: std::random_shuffle draws rand() before nucleation */
 } amca_oracle_plain_params;
 
 typedef struct {
@@ -68,6 +69,8 @@ void amca_oracle_normal_draws(double mean, double sigma, int n, double *out);
 /* Orientation angles + local->global rotation matrix, from three glibc
  * rand() values (CellularAutomataManager_3D.cpp:839-850, Octahedron.cpp:282-310). */
 void amca_oracle_orientation(int r0, int r1, int r2, double euler[3], double l2g[9]);
+/* Octahedron::set_coordinate_transformation_matrix (Octahedron.cpp:282-310) */
+void amca_oracle_rotation(const double euler[3], double l2g[9]);
 /* Octahedron containment test and decentred capture for one (envelope, cell)
  * pair (Octahedron.cpp:99-128, 134-275). l2g is the local->global matrix. */
 int amca_oracle_is_captured(const double l2g[9], const double gc[3], double length);

@@ -24,7 +24,7 @@ class PlainParams(ctypes.Structure):
                 ("T0", ctypes.c_double), ("Tm", ctypes.c_double), ("Tdot", ctypes.c_double), ("a1", ctypes.c_double),
                 ("a2", ctypes.c_double), ("a3", ctypes.c_double), ("max_dt", ctypes.c_double),
                 ("final_time", ctypes.c_double), ("time_step_factor", ctypes.c_double),
-                ("trunc_coeff", ctypes.c_double)]
+                ("trunc_coeff", ctypes.c_double), ("shuffle_vtr", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -56,6 +56,7 @@ def lib() -> ctypes.CDLL:
         _lib.amca_oracle_run_plain.restype = ctypes.c_int
         _lib.amca_oracle_normal_draws.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, vp]
         _lib.amca_oracle_orientation.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
+        _lib.amca_oracle_rotation.argtypes = [vp, vp]
         _lib.amca_oracle_is_captured.argtypes = [vp, vp, ctypes.c_double]
         _lib.amca_oracle_is_captured.restype = ctypes.c_int
         _lib.amca_oracle_capture.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -69,7 +70,8 @@ def params_of(case) -> PlainParams:
                        case.surface[0], case.surface[1], case.surface[2], case.bulk[0], case.bulk[1], case.bulk[2],
                        case.seed, case.initial_temperature, case.melting_temperature, case.t_dot, case.a[0], case.a[1],
                        case.a[2], case.time_step, case.termination_time,
-                       0.2 if case.time_step_factor_ca is None else case.time_step_factor_ca, case.trunc_coeff())
+                       0.2 if case.time_step_factor_ca is None else case.time_step_factor_ca, case.trunc_coeff(),
+                       1 if case.shuffle_vtr else 0)
 
 
 def _p(a: Optional[np.ndarray]):
@@ -101,4 +103,25 @@ def run_plain(case, max_steps: int = -1, fields: bool = True, euler_cap: int = 0
 def normal_draws(mean: float, sigma: float, n: int) -> np.ndarray:
     out = np.empty(n, np.float64)
     lib().amca_oracle_normal_draws(mean, sigma, n, _p(out))
+    return out
+
+
+def rotation(euler) -> np.ndarray:
+    e = np.ascontiguousarray(euler, np.float64)
+    m = np.empty(9, np.float64)
+    lib().amca_oracle_rotation(_p(e), _p(m))
+    return m
+
+
+def is_captured(l2g, gc, length: float) -> bool:
+    m = np.ascontiguousarray(l2g, np.float64)
+    g = np.ascontiguousarray(gc, np.float64)
+    return bool(lib().amca_oracle_is_captured(_p(m), _p(g), float(length)))
+
+
+def capture(l2g, gc, length: float, h: float, trunc: float) -> np.ndarray:
+    m = np.ascontiguousarray(l2g, np.float64)
+    g = np.ascontiguousarray(gc, np.float64)
+    out = np.empty(4, np.float64)
+    lib().amca_oracle_capture(_p(m), _p(g), float(length), float(h), float(trunc), _p(out))
     return out

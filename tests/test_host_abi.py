@@ -1,0 +1,178 @@
+"""Host logic of the library and its C ABI, without a GPU.
+
+Checks that libamca3d.so loads and exports every entry point declared in
+include/amca3d.h, that decks parse as the reference reads them (keys,
+defaults, yaml-cpp 0.3 number rules, errors), and that the host half of
+initialize (sites, orientation stream) equals the oracle's.
+"""
+import dataclasses
+import os
+import re
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+import cases  # noqa: E402
+
+
+@pytest.fixture(scope="session")
+def amca():
+    import amca3d_gb300
+
+    if not os.path.exists(amca3d_gb300.LIB_PATH):
+        from amca3d_gb300 import build
+
+        build.build()
+    amca3d_gb300.load_library()
+    return amca3d_gb300
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "amca3d.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(amca_[a-z_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(amca):
+    lib = amca.load_library()
+    names = declared_functions()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(amca.EXPORTS) == names
+
+
+@pytest.mark.parametrize("case", cases.small_cases() + cases.large_cases(), ids=lambda c: c.name)
+def test_deck_grid(amca, case):
+    r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
+    assert r.cells == tuple(case.cells)
+    assert r.origin == tuple(case.origin)
+    assert r.cell_size == case.cell_size
+    r.close()
+
+
+def test_reference_example_deck_parses(amca):
+    deck = """
+simulations:
+  - name: test
+    time_integrator: ti_1
+solvers:
+   - cellular_automata
+realms:
+  - name: realm1
+    type: cellular_automata
+    dimension: 3
+    domain:
+      type: cubic
+      original_point: [0,0,0]
+      lateral_sizes: [0.03, 0.03, 0.03]
+    discretization:
+      cell_size: 0.0005
+      number_cells: [800, 720, 252]
+    nucleation_rules:
+      - surface:
+          type: Gaussian
+          site_density: 0.0
+          mean: 2
+          standard_deviation: 0.5
+      - bulk:
+          type: Gaussian
+          site_density: 10e6     # yaml-cpp 0.3 reads this as 1e7
+          mean: 3
+          standard_deviation: 1
+    problem_physics:
+        type: RappazGandin
+        initial_temperature: -0.2
+        melting_temperature: 0.0
+        t_dot: -20
+        a1: -0.544e-4
+        a2: 2.03e-4
+        a3: 0.0
+    solution_options:
+       name: my_options
+       options:
+         - random_type:
+             rejection_sampling: no
+         - cell_grain_length_cutoff_factor:
+             factor_value: 4.0
+         - output_microstructure_information:
+             file_name: grainInfo.txt
+         - parallel_specification:
+             direction_with_all_processes: y
+    output:
+      output_data_base_name: ./Results/Grains
+      output_frequency: 100
+      output_variables:
+        - grain_ID
+time_integrators:
+  - standard_time_integrator:
+      name: ti_1
+      termination_time: 17.81
+      termination_step_count: 10000
+      time_step: 0.001
+      realms:
+        - realm1
+"""
+    r = amca.CellularAutomataRealm(deck)
+    # lateral_sizes wins over number_cells: n = int(0.03 / 0.0005) = 60
+    assert r.cells == (60, 60, 60)
+    r.prepare()
+    cells, dtc = r.sites()
+    assert len(cells) == 269  # 270 draws at 1e7 m^-3, one duplicate
+
+
+@pytest.mark.parametrize("bad,code", [
+    ("solvers: [cellular_automata]\n", -2),                                  # no realms
+    ("realms:\n  - type: cellular_automata\n", -2),                          # no solvers
+    ("solvers: [cellular_automata]\nrealms: [\n", -2),                       # YAML syntax
+])
+def test_bad_decks_fail_with_parse_error(amca, bad, code):
+    with pytest.raises(amca.AmcaError) as e:
+        amca.CellularAutomataRealm(bad)
+    assert e.value.code == code
+
+
+def _strip_key(deck, key):
+    return "\n".join(l for l in deck.splitlines() if not l.strip().startswith(key + ":"))
+
+
+@pytest.mark.parametrize("key", ["cell_size", "original_point", "termination_time", "time_step", "site_density"])
+def test_missing_required_key_is_named(amca, key):
+    deck = _strip_key(cases.small_cases()[2].to_yaml(), key)
+    with pytest.raises(amca.AmcaError) as e:
+        amca.CellularAutomataRealm(deck)
+    assert e.value.code == -2 and key in str(e.value)
+
+
+def test_problem_physics_type_checked(amca):
+    deck = cases.small_cases()[2].to_yaml().replace("type: RappazGandin", "type: Other")
+    with pytest.raises(amca.AmcaError):
+        amca.CellularAutomataRealm(deck)
+
+
+@pytest.mark.parametrize("case", [c for c in cases.small_cases() if c.n_ghost < 60000], ids=lambda c: c.name)
+def test_host_sites_and_orientations_equal_oracle(amca, oracle, case):
+    r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
+    r.prepare()
+    cells, dtc = r.sites()
+    o = oracle.run_plain(case, max_steps=0)
+    site_cells = np.nonzero(o["site_dtc"] >= 0)[0]
+    assert np.array_equal(cells, site_cells)
+    assert np.array_equal(dtc, o["site_dtc"][site_cells])
+    full = oracle.run_plain(case, euler_cap=max(1, len(cells)))
+    e = r.orientations(all=True)
+    assert e.shape == (len(cells), 3)
+    n = full["num_orient"]
+    assert np.array_equal(e[:n], full["euler"])
+    r.close()
+
+
+def test_gpu_calls_fail_loudly_without_initialize(amca):
+    r = amca.CellularAutomataRealm(cases.small_cases()[2].to_yaml())
+    with pytest.raises(amca.AmcaError) as e:
+        r.run(1)
+    assert e.value.code == -4
+    r.close()
