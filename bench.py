@@ -256,7 +256,7 @@ def run_ours(args, dist: Dist):
     import amca3d_gb300 as A
 
     dev = dist.local_rank
-    case = workload()
+    case = workload() if args.cells == 320 else sample_case(args.cells)
     deck = case.to_yaml()
     realm = A.CellularAutomataRealm(deck, seed=case.seed, device=dev)
     realm.initialize()
@@ -344,6 +344,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=128, help="edge of the CPU-baseline sample block")
     ap.add_argument("--ref-sample", type=int, default=96, help="edge of each reference-arm sample block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=320,
+                    help="edge of the cubic block to run (320 = the measured workload; smaller blocks keep the "
+                         "workload's physics and are for profiling captures only)")
     args = ap.parse_args()
     dist = Dist()
     try:
