@@ -62,7 +62,21 @@ class Stats(ctypes.Structure):
 EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
-           "amca_last_error", "amca_destroy")
+           "amca_plain_run_noalloc", "amca_last_error", "amca_destroy")
+
+
+class PlainParams(ctypes.Structure):
+    """amca_plain_params of include/amca3d.h."""
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("x0", ctypes.c_double),
+                ("y0", ctypes.c_double), ("z0", ctypes.c_double), ("h", ctypes.c_double), ("T0", ctypes.c_double),
+                ("Tm", ctypes.c_double), ("Tdot", ctypes.c_double), ("a1", ctypes.c_double), ("a2", ctypes.c_double),
+                ("a3", ctypes.c_double), ("max_dt", ctypes.c_double), ("final_time", ctypes.c_double),
+                ("time_step_factor", ctypes.c_double), ("trunc_coeff", ctypes.c_double)]
+
+
+class PlainResult(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int64), ("time", ctypes.c_double), ("grains", ctypes.c_int64),
+                ("orientations", ctypes.c_int64), ("liquid_cells", ctypes.c_int64), ("done", ctypes.c_int32)]
 
 _lib = None
 
@@ -101,6 +115,9 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_host_alloc.restype = i
     lib.amca_host_free.argtypes = [vp]
     lib.amca_host_free.restype = i
+    lib.amca_plain_run_noalloc.argtypes = [i, ctypes.POINTER(PlainParams), vp, vp, ctypes.c_int64, vp, vp, i, vp,
+                                           ctypes.POINTER(PlainResult), ctypes.c_char_p, ctypes.c_size_t]
+    lib.amca_plain_run_noalloc.restype = i
     lib.amca_last_error.argtypes = [vp]
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]

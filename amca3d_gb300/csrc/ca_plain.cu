@@ -27,8 +27,12 @@
 //   id by the new envelopes themselves in the next generation's claim phase
 //   (the opposite parity marks them solid meanwhile).
 // Every phase boundary is a grid barrier whose waits are bounded in time.
-#include <cooperative_groups.h>
+#include <math.h>
+#include <stdio.h>
 
+#include <mutex>
+
+#include "../../include/amca3d.h"
 #include "ca_plain.h"
 
 namespace amca {
@@ -508,7 +512,202 @@ __global__ void envelope_eval_kernel(long long n, const double *l2g, const doubl
   }
 }
 
+// Set-up of the no-allocation entry point: clear the control block and the
+// scan words, mark every site live, round the orientation matrices to float.
+__global__ void noalloc_setup_kernel(PlainDevice d, long long liquid, long long ntA, long long ntB) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (tid == 0) {
+    PlainCtrl c{};
+    c.liquid = liquid;
+    *d.ctrl = c;
+  }
+  for (long long i = tid; i < d.nsites; i += stride) d.site_live[i] = 1;
+  float *m32 = const_cast<float *>(d.omat32);
+  for (long long i = tid; i < 9 * d.nsites; i += stride) m32[i] = (float)d.omat[i];
+  for (long long i = tid; i < ntA; i += stride) d.scanA[i] = 0ull;
+  for (long long i = tid; i < ntB; i += stride) d.scanB[i] = 0ull;
+}
+
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Scratch of amca_plain_run_noalloc: one file-scope device array, held by
+// every GPU that loads the library until the process exits. The entry point
+// carves the envelope table, lists, masks, scan words and control block out
+// of it instead of calling cudaMalloc.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_base[kNoAllocMaxDevices];  // device address of g_noalloc_scratch, per device
+bool g_noalloc_ready[kNoAllocMaxDevices];
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
+struct NoAllocLayout {
+  size_t ctrl, live, omat32, scanA, gx, gy, gz, glen, gdx, gdy, gdz, gori, gcell, act0, act1, liq, con, scanB, total;
+  long long ntA, ntB;
+  NoAllocLayout(long long n, long long s) {
+    ntA = (s + 255) / 256 + 1;
+    ntB = (n + 255) / 256 + 1;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t at = o;
+      o = align256(o + bytes);
+      return at;
+    };
+    ctrl = take(sizeof(PlainCtrl));
+    live = take((size_t)s);
+    omat32 = take((size_t)s * 9 * sizeof(float));
+    scanA = take((size_t)ntA * 8);
+    gx = take((size_t)n * 8);
+    gy = take((size_t)n * 8);
+    gz = take((size_t)n * 8);
+    glen = take((size_t)n * 8);
+    gdx = take((size_t)n * 4);
+    gdy = take((size_t)n * 4);
+    gdz = take((size_t)n * 4);
+    gori = take((size_t)n * 4);
+    gcell = take((size_t)n * 4);
+    act0 = take((size_t)n * 4);
+    act1 = take((size_t)n * 4);
+    liq = take((size_t)n * 4);
+    con = take((size_t)n * 4);
+    scanB = take((size_t)ntB * 8);
+    total = o;
+  }
+};
+
+int noalloc_fail(char *err, size_t errlen, int code, const char *what, const char *detail) {
+  if (err && errlen) snprintf(err, errlen, "amca_plain_run_noalloc: %s%s%s", what, detail ? ": " : "", detail ? detail : "");
+  return code;
+}
+}  // namespace
+
+}  // namespace amca
+
+extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, const int32_t *site_cell,
+                                      const double *site_dtc, int64_t nsites, const double *l2g, int32_t *orient,
+                                      int max_steps, void *stream, amca_plain_result *res, char *err,
+                                      size_t errlen) {
+  using namespace amca;
+  if (err && errlen) err[0] = '\0';
+  if (!p || !orient || !res || (nsites > 0 && (!site_cell || !site_dtc || !l2g)) || nsites < 0)
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "null pointer or negative site count", nullptr);
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1 || !(p->h > 0))
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "grid dimensions and cell size must be positive", nullptr);
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "device ordinal out of range", nullptr);
+  const long long n = (long long)p->nx * p->ny * p->nz;
+  const NoAllocLayout lay(n, nsites);
+  if (lay.total > kNoAllocScratchBytes) {
+    char detail[160];
+    snprintf(detail, sizeof detail, "needs %zu bytes of scratch for %lld cells and %lld sites, limit is %zu",
+             lay.total, n, (long long)nsites, kNoAllocScratchBytes);
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "grid too large for the static scratch", detail);
+  }
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "cudaSetDevice", cudaGetErrorString(e));
+  {
+    // once per device, with that device current: the device address of the
+    // static array (its host-side name is only a stand-in)
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ready[device]) {
+      void *base = nullptr;
+      e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+      if (e != cudaSuccess)
+        return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "cudaGetSymbolAddress", cudaGetErrorString(e));
+      g_noalloc_base[device] = base;
+      g_noalloc_ready[device] = true;
+    }
+  }
+  unsigned char *base = (unsigned char *)g_noalloc_base[device];
+  cudaStream_t s = (cudaStream_t)stream;
+  PlainDevice d{};
+  Grid &g = d.grid;
+  g.nx = p->nx;
+  g.ny = p->ny;
+  g.nz = p->nz;
+  g.nxg = p->nx + 2;
+  g.nyg = p->ny + 2;
+  g.nzg = p->nz + 2;
+  g.nxyg = g.nxg * g.nyg;
+  g.x0 = p->x0;
+  g.y0 = p->y0;
+  g.z0 = p->z0;
+  g.h = p->h;
+  d.T0 = p->T0;
+  d.Tm = p->Tm;
+  d.Tdot = p->Tdot;
+  d.a1 = p->a1;
+  d.a2 = p->a2;
+  d.a3 = p->a3;
+  d.max_dt = p->max_dt;
+  d.final_time = p->final_time;
+  d.tsf = p->time_step_factor;
+  d.trunc = p->trunc_coeff;
+  d.h32 = (float)p->h;
+  double cmax = 0;
+  const double o3[3] = {p->x0, p->y0, p->z0};
+  const int n3[3] = {g.nxg, g.nyg, g.nzg};
+  for (int a = 0; a < 3; ++a) cmax = fmax(cmax, fabs(o3[a]) + (n3[a] + 1) * p->h);
+  d.coord_err = (float)(ldexp(cmax, -49) + 1e-30);
+  d.ncells = (int64_t)g.nxyg * g.nzg;
+  d.nsites = nsites;
+  d.gcap = n;
+  d.orient = (uint32_t *)orient;
+  d.site_cell = site_cell;
+  d.site_dtc = site_dtc;
+  d.omat = l2g;
+  d.ctrl = (PlainCtrl *)(base + lay.ctrl);
+  d.site_live = base + lay.live;
+  d.omat32 = (const float *)(base + lay.omat32);
+  d.scanA = (unsigned long long *)(base + lay.scanA);
+  d.gx = (double *)(base + lay.gx);
+  d.gy = (double *)(base + lay.gy);
+  d.gz = (double *)(base + lay.gz);
+  d.glen = (double *)(base + lay.glen);
+  d.gdx = (float *)(base + lay.gdx);
+  d.gdy = (float *)(base + lay.gdy);
+  d.gdz = (float *)(base + lay.gdz);
+  d.gori = (int32_t *)(base + lay.gori);
+  d.gcell = (int32_t *)(base + lay.gcell);
+  d.act0 = (int32_t *)(base + lay.act0);
+  d.act1 = (int32_t *)(base + lay.act1);
+  d.liq = (uint32_t *)(base + lay.liq);
+  d.con = (uint32_t *)(base + lay.con);
+  d.scanB = (unsigned long long *)(base + lay.scanB);
+  // everything that must start at zero is cleared here: the array keeps the
+  // previous call's contents
+  noalloc_setup_kernel<<<256, 256, 0, s>>>(d, n, lay.ntA, lay.ntB);
+  if ((e = cudaGetLastError()) != cudaSuccess)
+    return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "set-up launch", cudaGetErrorString(e));
+  if ((e = plain_init_field(d, s)) != cudaSuccess)
+    return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "field launch", cudaGetErrorString(e));
+  const int blocks = plain_persistent_grid(device);
+  if (blocks <= 0) return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "no co-resident blocks", nullptr);
+  if ((e = plain_run_steps(d, max_steps < 0 ? (1ll << 60) : (long long)max_steps, blocks, s)) != cudaSuccess)
+    return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "step launch", cudaGetErrorString(e));
+  PlainCtrl c;
+  if ((e = cudaMemcpyAsync(&c, d.ctrl, sizeof c, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "reading the control block", cudaGetErrorString(e));
+  if (c.error) return noalloc_fail(err, errlen, AMCA_ERR_DEVICE, "a bounded device wait ran out", nullptr);
+  res->steps = c.step;
+  res->time = c.time;
+  res->grains = c.next_grain;
+  res->orientations = c.n_orient;
+  res->liquid_cells = c.liquid;
+  res->done = c.done;
+  return AMCA_OK;
+}
+
+namespace amca {
 
 cudaError_t plain_envelope_eval(long long n, const double *l2g, const double *gc, const double *len, double h,
                                 const double *trunc, int32_t *cap64, int32_t *capfast, double *info, cudaStream_t s) {

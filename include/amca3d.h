@@ -159,6 +159,52 @@ int amca_host_free(void *p);
 int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc, const double *length, double h,
                        const double *trunc, int32_t *captured, int32_t *captured_fast, double *info);
 
+/* Plain-realm parameters as plain numbers (what amca_create reads from a deck). */
+typedef struct {
+  int32_t nx, ny, nz;                 /* interior cells per axis */
+  double x0, y0, z0, h;               /* origin, cell size */
+  double T0, Tm, Tdot;                /* uniform T(t) = T0 + Tdot*t; melting temperature */
+  double a1, a2, a3;                  /* KGT coefficients */
+  double max_dt, final_time;          /* time_step, termination_time */
+  double time_step_factor;            /* time_step_factor_ca (0.2 by default) */
+  double trunc_coeff;                 /* envelope truncation coefficient ((double)sqrtf(3.0f) by default) */
+} amca_plain_params;
+
+typedef struct {
+  int64_t steps;
+  double time;
+  int64_t grains, orientations, liquid_cells;
+  int32_t done;
+} amca_plain_result;
+
+/* Whole plain-realm run that allocates no memory. This entry point has no
+ * counterpart in the reference.
+ *
+ * Who needs it: callers that cannot let a library call cudaMalloc -- a
+ * coupled solver that has already reserved the GPU's memory for its own pool,
+ * or a host loop that must not take cudaMalloc/cudaFree's implicit device
+ * synchronisation. The caller passes every input and output in device
+ * memory it owns: site cells (ascending ghost-inclusive ids) and their
+ * critical undercoolings, the local->global orientation matrices (9 doubles
+ * per site, as amca_get_orientations' angles give through the reference's
+ * Bunge formula with the host's libm), and the int32 orientation field
+ * ((nx+2)(ny+2)(nz+2) cells, filled by this call). The run's other state
+ * lives in one static device array of 32 MiB, which every GPU that loads the
+ * library holds until the process exits; grids that need more (about
+ * 68 bytes per interior cell plus 45 per site, i.e. roughly 480,000 interior
+ * cells) are rejected with AMCA_ERR_ARG and a message.
+ *
+ * The first call on a device looks up the array's device address (the host
+ * name of the array is not a device address); make that first call before
+ * any stream capture. Every call shares the one array and clears what must
+ * start at zero; calls that overlap on the GPU (two host threads, or two
+ * streams) race and corrupt each other. Runs until solid, final_time or
+ * max_steps (< 0: no limit) on `stream` (NULL: default stream) and waits for
+ * it. Errors go to err (errlen bytes, may be NULL). */
+int amca_plain_run_noalloc(int device, const amca_plain_params *p, const int32_t *site_cell, const double *site_dtc,
+                           int64_t nsites, const double *l2g, int32_t *orient, int max_steps, void *stream,
+                           amca_plain_result *res, char *err, size_t errlen);
+
 /* Message of the last failing call on h (or of the last failing
  * amca_create / amca_envelope_eval when h is NULL). Never NULL. */
 const char *amca_last_error(const amca_t *h);
