@@ -16,17 +16,26 @@
 //             margin is not enough) and atomicMin's a claim word
 //             0x80000000 | parity<<30 | rank into each cell it contains.
 //             rank order == walk order, so the smallest claim is the envelope
-//             that reaches the cell first in the reference.
+//             that reaches the cell first in the reference. An envelope of
+//             generation g+1 first builds itself: the decentred octahedron of
+//             its parent (FP64), and writes its orientation into its cell.
 //   resolve : an envelope captures the cells whose final claim is its own;
 //             it stays active iff some neighbour was liquid at its turn and
 //             not captured by it (unclaimed, or claimed by a later rank).
-//             A decoupled look-back scan over (captures, survives) gives the
-//             new envelope ids (walk order) and the order-preserving
+//             One decoupled look-back per block over (captures, survives)
+//             gives the new envelope ids (walk order), the child records
+//             (parent id, neighbour index) and the order-preserving
 //             compaction of survivors into the next active list.
-//   The claim words left in the field are overwritten with the orientation
-//   id by the new envelopes themselves in the next generation's claim phase
-//   (the opposite parity marks them solid meanwhile).
-// Every phase boundary is a grid barrier whose waits are bounded in time.
+// Each block owns one contiguous chunk of every phase's index range, so a
+// block's envelopes are neighbours in id order (and mostly in space), and the
+// look-back runs once per block and phase. Every phase boundary is a grid
+// barrier; every wait is bounded in time and reports through an error flag.
+//
+// Loads use the default (L1-cached) path: a phase only reads values written
+// before the barrier that opened it (the barrier's acquire makes them
+// visible), or, for the cell field in the claim phase, values whose changes
+// during the phase (claims, and claim words replaced by orientation ids)
+// never change the liquid / solid answer the phase needs.
 #include <math.h>
 #include <stdio.h>
 
@@ -41,6 +50,7 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
+constexpr int kMinBlocks = 3;  // co-resident blocks per SM the register budget is sized for
 constexpr unsigned long long kWaitNs = 5000000000ull;  // 5 s bound on any spin
 constexpr unsigned long long kFlagAgg = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
@@ -131,37 +141,72 @@ __device__ __forceinline__ unsigned long long from_payload(unsigned long long p)
   return ((p >> 31) << 32) | (p & 0x7fffffffull);
 }
 
-// Decoupled look-back (single thread). Publishes tile t's aggregate, walks
-// back to the nearest inclusive prefix, publishes its own. Returns false on
-// a timed-out wait.
-__device__ bool look_back(unsigned long long *status, long long t, unsigned long long agg, unsigned long long *excl,
-                          PlainCtrl *c) {
+// Decoupled look-back, run by the 32 lanes of warp 0. Lane 0 publishes tile
+// t's aggregate; each round the warp reads the 32 nearest unread predecessor
+// status words at once and sums them up to the nearest inclusive prefix.
+// Returns false (error flag set) when a wait ran out.
+__device__ bool look_back_warp(unsigned long long *status, long long t, unsigned long long agg,
+                               unsigned long long *excl, PlainCtrl *c) {
+  const int lane = threadIdx.x & 31;
   if (t == 0) {
-    atomicExch(status, kFlagPrefix | to_payload(agg));
+    if (lane == 0) atomicExch(status, kFlagPrefix | to_payload(agg));
     *excl = 0;
     return true;
   }
-  atomicExch(status + t, kFlagAgg | to_payload(agg));
+  if (lane == 0) atomicExch(status + t, kFlagAgg | to_payload(agg));
   unsigned long long sum = 0;
   long long p = t - 1;
   const unsigned long long t0 = now_ns();
   for (;;) {
-    const unsigned long long s = ld_acquire(status + p);
+    const long long q = p - lane;
+    const unsigned long long s = q >= 0 ? ld_acquire(status + q) : kFlagPrefix;  // before tile 0: prefix 0
     const unsigned long long flag = s & ~kPayload;
-    if (flag == 0) {
-      if (now_ns() - t0 > kWaitNs || ld_volatile(&c->error) != 0) {
+    const unsigned pre = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
+    const unsigned empty = __ballot_sync(0xffffffffu, flag == 0);
+    const unsigned upto = pre ? (((pre & (0u - pre)) << 1) - 1u) : 0xffffffffu;  // lanes up to the nearest prefix
+    if (empty & upto) {
+      int bail = 0;
+      if (lane == 0 && (now_ns() - t0 > kWaitNs || ld_volatile(&c->error) != 0)) {
         atomicCAS(&c->error, 0, kErrLookback);
-        return false;
+        bail = 1;
       }
+      if (__shfl_sync(0xffffffffu, bail, 0)) return false;
       continue;
     }
-    sum += from_payload(s & kPayload);
-    if (flag == kFlagPrefix) break;
-    --p;
+    unsigned long long v = ((upto >> lane) & 1u) ? from_payload(s & kPayload) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    sum += v;
+    if (pre) break;
+    p -= 32;
   }
-  atomicExch(status + t, kFlagPrefix | to_payload(sum + agg));
+  if (lane == 0) atomicExch(status + t, kFlagPrefix | to_payload(sum + agg));
   *excl = sum;
   return true;
+}
+
+// Exclusive prefix of this block's aggregate over the blocks before it
+// (tile index = block index). Returns ~0 on error.
+__device__ unsigned long long block_prefix(unsigned long long *status, unsigned long long agg,
+                                           unsigned long long *smem, PlainCtrl *c) {
+  if (threadIdx.x < 32) {
+    unsigned long long pre = 0;
+    const bool ok = look_back_warp(status, blockIdx.x, agg, &pre, c);
+    if (threadIdx.x == 0) smem[kWarps] = ok ? pre : ~0ull;
+  }
+  __syncthreads();
+  const unsigned long long pre = smem[kWarps];
+  __syncthreads();
+  return pre;
+}
+
+// This block's contiguous share [b, e) of [0, n).
+__device__ __forceinline__ void block_chunk(long long n, long long &b, long long &e) {
+  const long long per = (n + gridDim.x - 1) / gridDim.x;
+  b = per * blockIdx.x;
+  if (b > n) b = n;
+  e = b + per;
+  if (e > n) e = n;
 }
 
 __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj, int &dk) {
@@ -171,42 +216,59 @@ __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj,
 
 // ---------------------------------------------------------------------------
 // Nucleation (CellularAutomataManager.cpp:219-297) in site order.
+// Pass 1 marks sites (2 = nucleates now, 0 = removed), pass 2 hands out
+// orientation / envelope ids in site order.
 // ---------------------------------------------------------------------------
 __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned long long *smem,
                                  unsigned long long *stat_live) {
   PlainCtrl *c = d.ctrl;
-  const long long nsites = d.nsites;
-  const long long ntiles = (nsites + kBlock - 1) / kBlock;
   const long long base_orient = ld_volatile(&c->n_orient);
   const long long base_grain = ld_volatile(&c->next_grain);
   const long long base_act = ld_volatile(&c->n_active);
   int32_t *act = ld_volatile(&c->cur_list) ? d.act1 : d.act0;
   const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
   const double dTu = d.Tm - T;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // calculate_time_step (CellularAutomataManager_3D.cpp:449-507): one
+    // velocity for the uniform field; dt for "some active envelope" and for
+    // "none" (maxVelocity stays 1e-10), picked after nucleation
+    const double vel = kgt_velocity(d.Tm, T, d.a1, d.a2, d.a3);
+    const double maxV = vel > 1e-10 ? vel : 1e-10;
+    const double a = d.tsf * d.grid.h / maxV, b = d.tsf * d.grid.h / 1e-10;
+    c->vel = vel;
+    c->dt_active = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
+    c->dt_none = (d.max_dt < b) ? d.max_dt : b;
+  }
   __threadfence();
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const long long i = t * kBlock + threadIdx.x;
-    int cell = -1;
+  long long b, e;
+  block_chunk(d.nsites, b, e);
+  unsigned long long count = 0;
+  for (long long i = b + threadIdx.x; i < e; i += kBlock) {
+    if (!d.site_live[i]) continue;
+    ++*stat_live;
+    const bool liquid = d.orient[d.site_cell[i]] == kLiquid;
+    const bool nuc = liquid && dTu > d.site_dtc[i];
+    d.site_live[i] = nuc ? 2 : (liquid ? 1 : 0);
+    count += nuc ? 1u : 0u;
+  }
+  unsigned long long agg;
+  block_exclusive_scan(count, smem, &agg);
+  const unsigned long long pre = block_prefix(d.scanA, agg, smem, c);
+  if (pre == ~0ull) return false;
+  unsigned long long run = pre;
+  for (long long i0 = b; i0 < e; i0 += kBlock) {
+    const long long i = i0 + threadIdx.x;
     unsigned nuc = 0;
-    if (i < nsites && d.site_live[i]) {
-      ++*stat_live;
+    int cell = 0;
+    if (i < e && d.site_live[i] == 2) {
+      nuc = 1;
       cell = d.site_cell[i];
-      const bool liquid = __ldcg(d.orient + cell) == kLiquid;
-      if (liquid && dTu > d.site_dtc[i]) nuc = 1;
-      if (!liquid || nuc) d.site_live[i] = 0;
+      d.site_live[i] = 0;
     }
-    unsigned long long agg;
-    const unsigned long long ex = block_exclusive_scan(nuc, smem, &agg);
-    if (threadIdx.x == 0) {
-      unsigned long long pre;
-      smem[kWarps] = look_back(d.scanA, t, agg, &pre, c) ? pre : ~0ull;
-    }
-    __syncthreads();
-    const unsigned long long pre = smem[kWarps];
-    __syncthreads();
-    if (pre == ~0ull) return false;
+    unsigned long long tot;
+    const unsigned long long ex = block_exclusive_scan(nuc, smem, &tot);
     if (nuc) {
-      const long long r = (long long)(pre + ex);
+      const long long r = (long long)(run + ex);
       const int oid = (int)(base_orient + r);
       const long long gid = base_grain + r;
       int I, J, K;
@@ -223,70 +285,136 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
       d.gcell[gid] = cell;
       act[base_act + r] = (int32_t)gid;
     }
-    if (t == ntiles - 1 && threadIdx.x == 0) {
-      const long long total = (long long)(pre + agg);
-      c->n_orient = base_orient + total;
-      c->next_grain = base_grain + total;
-      c->n_active = base_act + total;
-      c->liquid -= total;
-      c->nucleations += (unsigned long long)total;
-    }
+    run += tot;
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    const long long total = (long long)(pre + agg);
+    c->n_orient = base_orient + total;
+    c->next_grain = base_grain + total;
+    c->n_active = base_act + total;
+    c->liquid -= total;
+    c->nucleations += (unsigned long long)total;
   }
   return true;
 }
 
 // ---------------------------------------------------------------------------
-// Claim: growth (generation 0), neighbour tests, atomicMin claims.
+// Claim: growth (generation 0) or self-construction (generation >= 1),
+// neighbour tests, atomicMin claims.
 // ---------------------------------------------------------------------------
 __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par, bool grow,
                             double dt, double vel, const int32_t *act, unsigned long long *stat_tests,
                             unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
-  const long long stride = (long long)gridDim.x * kBlock;
-  // the resolve phase's look-back words for this generation start cleared
-  const long long ntiles = (n + kBlock - 1) / kBlock;
-  for (long long t = (long long)blockIdx.x * kBlock + threadIdx.x; t < ntiles; t += stride) d.scanB[t] = 0ull;
+  if (threadIdx.x == 0) d.scanB[blockIdx.x] = 0ull;  // this block's look-back word of the resolve phase
+  long long b, e;
+  block_chunk(n, b, e);
   unsigned long long tests = 0, tests64 = 0;
-  for (long long r = (long long)blockIdx.x * kBlock + threadIdx.x; r < n; r += stride) {
-    const int id = kind == 0 ? __ldcg(act + r) : (int)(lo + r);
-    const int cell = __ldcg(d.gcell + id);
-    const int ori = __ldcg(d.gori + id);
-    if (kind != 0) d.orient[cell] = (uint32_t)ori;  // finalize the cell captured last generation
-    double L = __ldcg(d.glen + id);
-    if (grow) {
-      L += dt * vel;  // Grain::grow (Grain.h:27)
+  for (long long r = b + threadIdx.x; r < e; r += kBlock) {
+    int id, cell, ori;
+    double L, gxd = 0, gyd = 0, gzd = 0;
+    float dxf = 0.f, dyf = 0.f, dzf = 0.f;
+    bool have_centre = false;
+    if (kind == 0) {
+      id = act[r];
+      cell = d.gcell[id];
+      ori = d.gori[id];
+      L = d.glen[id];
+      if (grow) {
+        L += dt * vel;  // Grain::grow (Grain.h:27)
+        d.glen[id] = L;
+      }
+    } else {
+      // CellularAutomataManager_3D::capture_cell (:677-707) for the capture
+      // recorded by the parent: decentred envelope from the parent's
+      // (grown) envelope, same orientation.
+      id = (int)(lo + r);
+      const uint32_t rec = d.child[r];
+      const int parent = (int)(rec >> 5);
+      const int pnb = (int)(rec & 31u);
+      const int pcell = d.gcell[parent];
+      ori = d.gori[parent];
+      const double pL = d.glen[parent], px = d.gx[parent], py = d.gy[parent], pz = d.gz[parent];
+      int di, dj, dk, I, J, K;
+      cell = pcell + nbr_delta(g, pnb, di, dj, dk);
+      cell_ijk(g, pcell, I, J, K);
+      const double ccx = centre_coord(g.x0, g.h, I + di);
+      const double ccy = centre_coord(g.y0, g.h, J + dj);
+      const double ccz = centre_coord(g.z0, g.h, K + dk);
+      double out[4];
+      capture_f64(d.omat + 9 * ori, ccx - px, ccy - py, ccz - pz, pL, g.h, d.trunc, out);
+      gxd = out[0] + px;
+      gyd = out[1] + py;
+      gzd = out[2] + pz;
+      L = out[3];
+      dxf = (float)(gxd - ccx);
+      dyf = (float)(gyd - ccy);
+      dzf = (float)(gzd - ccz);
+      have_centre = true;
+      d.gx[id] = gxd;
+      d.gy[id] = gyd;
+      d.gz[id] = gzd;
       d.glen[id] = L;
+      d.gdx[id] = dxf;
+      d.gdy[id] = dyf;
+      d.gdz[id] = dzf;
+      d.gori[id] = ori;
+      d.gcell[id] = cell;
+      d.orient[cell] = (uint32_t)ori;  // the claim word of last generation becomes the orientation id
     }
-    int I, J, K;
-    cell_ijk(g, cell, I, J, K);
-    const float dxf = __ldcg(d.gdx + id), dyf = __ldcg(d.gdy + id), dzf = __ldcg(d.gdz + id);
-    const float errg = 4.76837158203125e-07f * (d.h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + d.coord_err;
-    const float L32 = (float)L;
-    float m32[9];
+    // all 26 neighbour states in flight at once
+    uint32_t liq = 0;
 #pragma unroll
-    for (int q = 0; q < 9; ++q) m32[q] = __ldg(d.omat32 + 9 * ori + q);
-    uint32_t liq = 0, con = 0;
-    const uint32_t mine = claim_word(par, (uint32_t)r);
     for (int nb = 0; nb < 26; ++nb) {
       int di, dj, dk;
-      const int nc = cell + nbr_delta(g, nb, di, dj, dk);
-      const uint32_t s = __ldcg(d.orient + nc);
-      if (!is_liquid_now(s, par)) continue;
-      liq |= 1u << nb;
-      if (L == 0) continue;
-      ++tests;
-      int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg, L32);
-      if (f < 0) {
-        ++tests64;
-        const double ccx = centre_coord(g.x0, g.h, I + di);
-        const double ccy = centre_coord(g.y0, g.h, J + dj);
-        const double ccz = centre_coord(g.z0, g.h, K + dk);
-        const double gcx = ccx - __ldcg(d.gx + id), gcy = ccy - __ldcg(d.gy + id), gcz = ccz - __ldcg(d.gz + id);
-        f = is_captured_f64(d.omat + 9 * ori, gcx, gcy, gcz, L) ? 1 : 0;
+      const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
+      liq |= (is_liquid_now(s, par) ? 1u : 0u) << nb;
+    }
+    uint32_t con = 0;
+    if (liq && L != 0) {  // cell_is_captured is false for a zero half-diagonal
+      int I, J, K;
+      cell_ijk(g, cell, I, J, K);
+      if (!have_centre) {
+        dxf = d.gdx[id];
+        dyf = d.gdy[id];
+        dzf = d.gdz[id];
       }
-      if (f) {
-        con |= 1u << nb;
-        atomicMin(d.orient + nc, mine);
+      const float errg = 4.76837158203125e-07f * (d.h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + d.coord_err;
+      const float L32 = (float)L;
+      float m32[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) m32[q] = __ldg(d.omat32 + 9 * ori + q);
+      uint32_t bits = liq;
+      while (bits) {
+        const int nb = __ffs(bits) - 1;
+        bits &= bits - 1;
+        int di, dj, dk;
+        nbr_offset(nb, di, dj, dk);
+        ++tests;
+        int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg,
+                             L32);
+        if (f < 0) {
+          ++tests64;
+          if (!have_centre) {
+            gxd = d.gx[id];
+            gyd = d.gy[id];
+            gzd = d.gz[id];
+            have_centre = true;
+          }
+          const double ccx = centre_coord(g.x0, g.h, I + di);
+          const double ccy = centre_coord(g.y0, g.h, J + dj);
+          const double ccz = centre_coord(g.z0, g.h, K + dk);
+          f = is_captured_f64(d.omat + 9 * ori, ccx - gxd, ccy - gyd, ccz - gzd, L) ? 1 : 0;
+        }
+        con |= (f ? 1u : 0u) << nb;
+      }
+      const uint32_t mine = claim_word(par, (uint32_t)r);
+      bits = con;
+      while (bits) {
+        const int nb = __ffs(bits) - 1;
+        bits &= bits - 1;
+        int di, dj, dk;
+        atomicMin(d.orient + cell + nbr_delta(g, nb, di, dj, dk), mine);
       }
     }
     d.liq[r] = liq;
@@ -297,7 +425,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
 }
 
 // ---------------------------------------------------------------------------
-// Resolve: captures, deactivation, new envelopes, survivor compaction.
+// Resolve: captures, deactivation, child records, survivor compaction.
 // ---------------------------------------------------------------------------
 __device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par,
                               const int32_t *act, int32_t *next_act, unsigned long long *smem) {
@@ -306,93 +434,70 @@ __device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long
   const long long base_grain = ld_volatile(&c->next_grain);
   const long long base_next = ld_volatile(&c->n_active_next);
   __threadfence();
-  const long long ntiles = (n + kBlock - 1) / kBlock;
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const long long r = t * kBlock + threadIdx.x;
-    uint32_t cap = 0;
-    unsigned surv = 0;
-    int id = -1, cell = 0;
-    if (r < n) {
-      const uint32_t lm = __ldcg(d.liq + r), cm = __ldcg(d.con + r);
-      id = kind == 0 ? __ldcg(act + r) : (int)(lo + r);
-      cell = __ldcg(d.gcell + id);
+  long long b, e;
+  block_chunk(n, b, e);
+  unsigned long long acc = 0;
+  for (long long r = b + threadIdx.x; r < e; r += kBlock) {
+    const uint32_t lm = d.liq[r], cm = d.con[r];
+    uint32_t cap = 0, surv = 0;
+    if (lm) {
+      const int id = kind == 0 ? act[r] : (int)(lo + r);
+      const int cell = d.gcell[id];
       const uint32_t mine = claim_word(par, (uint32_t)r);
-      uint32_t bits = lm;
-      while (bits) {
-        const int nb = __ffs(bits) - 1;
-        bits &= bits - 1;
+#pragma unroll
+      for (int nb = 0; nb < 26; ++nb) {
+        if (!((lm >> nb) & 1u)) continue;
         int di, dj, dk;
-        const int nc = cell + nbr_delta(g, nb, di, dj, dk);
-        const uint32_t s = __ldcg(d.orient + nc);
+        const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
         if ((cm >> nb) & 1u) {
-          if (s == mine) cap |= 1u << nb;
+          cap |= (s == mine ? 1u : 0u) << nb;
         } else if (s == kLiquid || (s & kRankMask) > (uint32_t)r) {
           surv = 1;
         }
       }
     }
-    const unsigned long long v = ((unsigned long long)__popc(cap) << 32) | surv;
-    unsigned long long agg;
-    const unsigned long long ex = block_exclusive_scan(v, smem, &agg);
-    if (threadIdx.x == 0) {
-      unsigned long long pre;
-      smem[kWarps] = look_back(d.scanB, t, agg, &pre, c) ? pre : ~0ull;
-    }
-    __syncthreads();
-    const unsigned long long pre = smem[kWarps];
-    __syncthreads();
-    if (pre == ~0ull) return false;
-    if (r < n) {
-      const unsigned long long off = pre + ex;
+    d.con[r] = cap | (surv << 31);
+    acc += ((unsigned long long)__popc(cap) << 32) | surv;
+  }
+  unsigned long long agg;
+  block_exclusive_scan(acc, smem, &agg);
+  const unsigned long long pre = block_prefix(d.scanB, agg, smem, c);
+  if (pre == ~0ull) return false;
+  unsigned long long run = pre;
+  for (long long r0 = b; r0 < e; r0 += kBlock) {
+    const long long r = r0 + threadIdx.x;
+    const uint32_t word = r < e ? d.con[r] : 0u;
+    const uint32_t cap = word & 0x03ffffffu, surv = word >> 31;
+    unsigned long long tot;
+    const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
+    if (r < e && (cap | surv)) {
+      const unsigned long long off = run + ex;
+      const int id = kind == 0 ? act[r] : (int)(lo + r);
       if (surv) next_act[base_next + (long long)(off & 0xffffffffull)] = id;
-      if (cap) {
-        long long nid = base_grain + (long long)(off >> 32);
-        const int ori = __ldcg(d.gori + id);
-        const double L = __ldcg(d.glen + id);
-        const double px = __ldcg(d.gx + id), py = __ldcg(d.gy + id), pz = __ldcg(d.gz + id);
-        const double *m = d.omat + 9 * ori;
-        int I, J, K;
-        cell_ijk(g, cell, I, J, K);
-        uint32_t bits = cap;
-        while (bits) {
-          const int nb = __ffs(bits) - 1;
-          bits &= bits - 1;
-          int di, dj, dk;
-          const int nc = cell + nbr_delta(g, nb, di, dj, dk);
-          const double ccx = centre_coord(g.x0, g.h, I + di);
-          const double ccy = centre_coord(g.y0, g.h, J + dj);
-          const double ccz = centre_coord(g.z0, g.h, K + dk);
-          double out[4];
-          capture_f64(m, ccx - px, ccy - py, ccz - pz, L, g.h, d.trunc, out);
-          const double nx = out[0] + px, ny = out[1] + py, nz = out[2] + pz;
-          d.gx[nid] = nx;
-          d.gy[nid] = ny;
-          d.gz[nid] = nz;
-          d.glen[nid] = out[3];
-          d.gdx[nid] = (float)(nx - ccx);
-          d.gdy[nid] = (float)(ny - ccy);
-          d.gdz[nid] = (float)(nz - ccz);
-          d.gori[nid] = ori;
-          d.gcell[nid] = nc;
-          ++nid;
-        }
+      long long slot = (long long)(off >> 32);  // rank of the first child in the next generation
+      uint32_t bits = cap;
+      while (bits) {
+        const int nb = __ffs(bits) - 1;
+        bits &= bits - 1;
+        d.child[slot++] = ((uint32_t)id << 5) | (uint32_t)nb;
       }
     }
-    if (t == ntiles - 1 && threadIdx.x == 0) {
-      const unsigned long long total = pre + agg;
-      const long long caps = (long long)(total >> 32), survs = (long long)(total & 0xffffffffull);
-      c->gen_lo = base_grain;
-      c->gen_n = caps;
-      c->next_grain = base_grain + caps;
-      c->n_active_next = base_next + survs;
-      c->liquid -= caps;
-      c->captures += (unsigned long long)caps;
-    }
+    run += tot;
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    const unsigned long long total = pre + agg;
+    const long long caps = (long long)(total >> 32), survs = (long long)(total & 0xffffffffull);
+    c->gen_lo = base_grain;
+    c->gen_n = caps;
+    c->next_grain = base_grain + caps;
+    c->n_active_next = base_next + survs;
+    c->liquid -= caps;
+    c->captures += (unsigned long long)caps;
   }
   return true;
 }
 
-__global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d, long long step_limit) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(PlainDevice d, long long step_limit) {
   __shared__ unsigned long long smem[kWarps + 2];
   PlainCtrl *c = d.ctrl;
   unsigned long long tests = 0, tests64 = 0, live = 0;
@@ -402,15 +507,19 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
     if (ld_volatile(&c->done) || !(time < d.final_time) || step >= step_limit) break;
 
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
+    const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+    unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
     if (!nucleation_phase(d, time, smem, &live)) break;
     if (!grid_barrier(c)) break;
+    if (timer) {
+      t_now = now_ns();
+      c->ns_nucleation += t_now - t_mark;
+      t_mark = t_now;
+    }
     const long long nA = ld_volatile(&c->n_active);
     const int cur = ld_volatile(&c->cur_list);
-    const double vel = kgt_velocity(d.Tm, d.T0 + d.Tdot * time, d.a1, d.a2, d.a3);
-    double maxV = 1e-10;
-    if (nA > 0 && vel > maxV) maxV = vel;
-    const double cand = d.tsf * d.grid.h / maxV;
-    const double dt = (d.max_dt < cand) ? d.max_dt : cand;  // std::min (:507)
+    const double vel = ld_volatile(&c->vel);
+    const double dt = nA > 0 ? ld_volatile(&c->dt_active) : ld_volatile(&c->dt_none);
 
     // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
     const int32_t *act = cur ? d.act1 : d.act0;
@@ -423,8 +532,18 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
       processed += n;
       claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dt, vel, act, &tests, &tests64);
       if (!(ok = grid_barrier(c))) break;
+      if (timer) {
+        t_now = now_ns();
+        c->ns_claim += t_now - t_mark;
+        t_mark = t_now;
+      }
       if (!(ok = resolve_phase(d, kind, lo, n, gen & 1u, act, next_act, smem))) break;
       if (!(ok = grid_barrier(c))) break;
+      if (timer) {
+        t_now = now_ns();
+        c->ns_resolve += t_now - t_mark;
+        t_mark = t_now;
+      }
       n = ld_volatile(&c->gen_n);
       lo = ld_volatile(&c->gen_lo);
       kind = 1;
@@ -432,18 +551,13 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
     }
     if (!ok) break;
     // step end: swap lists, advance time (CellularAutomataManager_3D.cpp:653-659)
-    {
-      const long long ntA = (d.nsites + kBlock - 1) / kBlock;
-      for (long long t = (long long)blockIdx.x * kBlock + threadIdx.x; t < ntA; t += (long long)gridDim.x * kBlock)
-        d.scanA[t] = 0ull;
-    }
+    if (threadIdx.x == 0) d.scanA[blockIdx.x] = 0ull;  // next step's nucleation look-back word
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       c->n_active = c->n_active_next;
       c->n_active_next = 0;
       c->cur_list = cur ^ 1;
       c->time = time + dt;
       c->dt = dt;
-      c->vel = vel;
       c->step = step + 1;
       c->done = c->liquid == 0;
       c->gens += gen;
@@ -451,6 +565,7 @@ __global__ void __launch_bounds__(kBlock) plain_persistent_kernel(PlainDevice d,
       c->grains_processed += (unsigned long long)processed;
     }
     if (!grid_barrier(c)) break;
+    if (timer) c->ns_step_end += now_ns() - t_mark;
   }
   // statistics: one atomic per warp
 #pragma unroll
@@ -513,8 +628,8 @@ __global__ void envelope_eval_kernel(long long n, const double *l2g, const doubl
 }
 
 // Set-up of the no-allocation entry point: clear the control block and the
-// scan words, mark every site live, round the orientation matrices to float.
-__global__ void noalloc_setup_kernel(PlainDevice d, long long liquid, long long ntA, long long ntB) {
+// look-back words, mark every site live, round the orientation matrices to float.
+__global__ void noalloc_setup_kernel(PlainDevice d, long long liquid) {
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
   if (tid == 0) {
@@ -525,8 +640,10 @@ __global__ void noalloc_setup_kernel(PlainDevice d, long long liquid, long long 
   for (long long i = tid; i < d.nsites; i += stride) d.site_live[i] = 1;
   float *m32 = const_cast<float *>(d.omat32);
   for (long long i = tid; i < 9 * d.nsites; i += stride) m32[i] = (float)d.omat[i];
-  for (long long i = tid; i < ntA; i += stride) d.scanA[i] = 0ull;
-  for (long long i = tid; i < ntB; i += stride) d.scanB[i] = 0ull;
+  for (long long i = tid; i < kStatusWords; i += stride) {
+    d.scanA[i] = 0ull;
+    d.scanB[i] = 0ull;
+  }
 }
 
 }  // namespace
@@ -534,8 +651,8 @@ __global__ void noalloc_setup_kernel(PlainDevice d, long long liquid, long long 
 // ---------------------------------------------------------------------------
 // Scratch of amca_plain_run_noalloc: one file-scope device array, held by
 // every GPU that loads the library until the process exits. The entry point
-// carves the envelope table, lists, masks, scan words and control block out
-// of it instead of calling cudaMalloc.
+// carves the envelope table, lists, masks, look-back words and control block
+// out of it instead of calling cudaMalloc.
 // ---------------------------------------------------------------------------
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -550,11 +667,9 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
-  size_t ctrl, live, omat32, scanA, gx, gy, gz, glen, gdx, gdy, gdz, gori, gcell, act0, act1, liq, con, scanB, total;
-  long long ntA, ntB;
+  size_t ctrl, live, omat32, scanA, gx, gy, gz, glen, gdx, gdy, gdz, gori, gcell, act0, act1, liq, con, child, scanB,
+      total;
   NoAllocLayout(long long n, long long s) {
-    ntA = (s + 255) / 256 + 1;
-    ntB = (n + 255) / 256 + 1;
     size_t o = 0;
     auto take = [&](size_t bytes) {
       const size_t at = o;
@@ -564,7 +679,7 @@ struct NoAllocLayout {
     ctrl = take(sizeof(PlainCtrl));
     live = take((size_t)s);
     omat32 = take((size_t)s * 9 * sizeof(float));
-    scanA = take((size_t)ntA * 8);
+    scanA = take((size_t)kStatusWords * 8);
     gx = take((size_t)n * 8);
     gy = take((size_t)n * 8);
     gz = take((size_t)n * 8);
@@ -578,7 +693,8 @@ struct NoAllocLayout {
     act1 = take((size_t)n * 4);
     liq = take((size_t)n * 4);
     con = take((size_t)n * 4);
-    scanB = take((size_t)ntB * 8);
+    child = take((size_t)n * 4);
+    scanB = take((size_t)kStatusWords * 8);
     total = o;
   }
 };
@@ -681,10 +797,11 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.act1 = (int32_t *)(base + lay.act1);
   d.liq = (uint32_t *)(base + lay.liq);
   d.con = (uint32_t *)(base + lay.con);
+  d.child = (uint32_t *)(base + lay.child);
   d.scanB = (unsigned long long *)(base + lay.scanB);
   // everything that must start at zero is cleared here: the array keeps the
   // previous call's contents
-  noalloc_setup_kernel<<<256, 256, 0, s>>>(d, n, lay.ntA, lay.ntB);
+  noalloc_setup_kernel<<<256, 256, 0, s>>>(d, n);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "set-up launch", cudaGetErrorString(e));
   if ((e = plain_init_field(d, s)) != cudaSuccess)
@@ -725,7 +842,8 @@ int plain_persistent_grid(int device) {
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plain_persistent_kernel, kBlock, 0) != cudaSuccess)
     return 0;
-  return sms * per_sm;
+  const int blocks = sms * per_sm;
+  return blocks < (int)kStatusWords ? blocks : (int)kStatusWords;
 }
 
 cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid_blocks, cudaStream_t s) {

@@ -10,7 +10,8 @@
 //               orientation i32, cell i32
 //   act[2]      active-envelope lists (ascending id), double-buffered per step
 //   liq/con     per-rank neighbour masks of the generation being processed
-//   scanA/scanB decoupled look-back tile status words (nucleation / capture)
+//   child       per new envelope: parent id << 5 | neighbour index
+//   scanA/scanB decoupled look-back status words, one per block (nucleation / capture)
 //   ctrl        control block: counters, time, barrier words, error flag
 #pragma once
 
@@ -20,6 +21,11 @@
 #include "ca_math.h"
 
 namespace amca {
+
+// Look-back status words per phase: an upper bound on the persistent grid.
+constexpr long long kStatusWords = 4096;
+// Child records pack an envelope id into 27 bits.
+constexpr long long kMaxCells = 1ll << 27;
 
 struct PlainCtrl {
   unsigned bar_count;
@@ -36,7 +42,9 @@ struct PlainCtrl {
   long long step;
   double time;
   double dt;
-  double vel;
+  double vel;        // growth velocity at `time` (uniform field)
+  double dt_active;  // dt when some envelope is active
+  double dt_none;    // dt when none is (maxVelocity stays 1e-10)
   int done;
   int pad;
   unsigned long long tests;
@@ -48,6 +56,8 @@ struct PlainCtrl {
   unsigned long long nucleations;      // envelopes created by nucleation
   unsigned long long active_grown;     // generation-0 envelopes (grown), summed over steps
   unsigned long long grains_processed; // envelopes of every generation, summed
+  // wall time of each phase as block 0 sees it (phase start to barrier exit), ns
+  unsigned long long ns_nucleation, ns_claim, ns_resolve, ns_step_end;
 };
 
 enum { kErrBarrier = 1, kErrLookback = 2 };
@@ -74,6 +84,7 @@ struct PlainDevice {
   int64_t gcap;
   int32_t *act0, *act1;
   uint32_t *liq, *con;
+  uint32_t *child;
   unsigned long long *scanA, *scanB;
   PlainCtrl *ctrl;
 };

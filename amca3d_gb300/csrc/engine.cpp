@@ -123,6 +123,8 @@ struct amca_t {
 
   void initialize() {
     const PlainConfig &c = cfg;
+    if ((long long)c.nx * c.ny * c.nz > kMaxCells)
+      throw std::invalid_argument("grid too large: at most 2^27 interior cells per realm");
     prepare();
     CK(cudaSetDevice(device));
     const int64_t nsites = (int64_t)sites.cell.size();
@@ -186,7 +188,8 @@ struct amca_t {
     d.act1 = alloc<int32_t>(d.gcap);
     d.liq = alloc<uint32_t>(d.gcap);
     d.con = alloc<uint32_t>(d.gcap);
-    const int64_t ntA = (nsites + 255) / 256 + 1, ntB = (d.gcap + 255) / 256 + 1;
+    d.child = alloc<uint32_t>(d.gcap);
+    const int64_t ntA = kStatusWords, ntB = kStatusWords;
     d.scanA = alloc<unsigned long long>(ntA);
     d.scanB = alloc<unsigned long long>(ntB);
     d.ctrl = alloc<PlainCtrl>(1);
@@ -566,6 +569,10 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->algorithmic_bytes = h->algorithmic_bytes();
     s->h2d_bytes = h->h2d_bytes;
     s->d2h_bytes = h->d2h_bytes;
+    s->phase_ms[0] = c.ns_nucleation * 1e-6;
+    s->phase_ms[1] = c.ns_claim * 1e-6;
+    s->phase_ms[2] = c.ns_resolve * 1e-6;
+    s->phase_ms[3] = c.ns_step_end * 1e-6;
   });
 }
 

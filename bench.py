@@ -222,12 +222,15 @@ def run_reference_arm(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
-def config_block(stats) -> dict:
-    c = workload()
-    cfg = {"workload": "uniform_320: plain CA, uniform cooling, 320^3 cells of 2 um (32.8M), t_dot = -50 K/s, "
-                       "~20k bulk Gaussian sites (3 K, 1 K) + ~4k surface sites (2 K, 0.5 K), KGT a1=-0.544e-4 "
-                       "a2=2.03e-4, seed 1, every CA step to full solidification",
-           "cells": c.n_interior, "seed": c.seed, "envelopes": "fp64", "grain_ids": "int32",
+def config_block(stats, case=None) -> dict:
+    c = case or workload()
+    if c.cells == (320, 320, 320):
+        text = ("uniform_320: plain CA, uniform cooling, 320^3 cells of 2 um (32.8M), t_dot = -50 K/s, "
+                "~20k bulk Gaussian sites (3 K, 1 K) + ~4k surface sites (2 K, 0.5 K), KGT a1=-0.544e-4 "
+                "a2=2.03e-4, seed 1, every CA step to full solidification")
+    else:
+        text = f"{c.name}: the uniform_320 physics on a {c.cells[0]}^3 block (profiling case, not the workload)"
+    cfg = {"workload": text, "cells": c.n_interior, "seed": c.seed, "envelope_arith": "fp64", "grain_ids": "int32",
            "l2": "inputs larger than L2: orientation field 134 MB + envelope table 1.7 GB per run"}
     if stats:
         cfg.update(stats)
@@ -319,7 +322,10 @@ def run_ours(args, dist: Dist):
         "warmup": args.warmup, "ms_per_step": sum(device_ms) / len(device_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_block({"ca_steps_per_run": ca_steps[-1], "envelopes": st["grains"], **gstats,
-                                "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same}),
+                                "generations_per_run": st["generations"], "tests_per_run": st["tests"],
+                                "phase_ms_nucleation_claim_resolve_end": [round(x, 3) for x in st["phase_ms"]],
+                                "fp64_tests_per_run": st["tests_fp64"],
+                                "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same}, case),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": f"{peak_kind} burst copy",
                      "kernel": "plain_persistent_kernel (one launch per run)",

@@ -130,6 +130,9 @@ typedef struct {
   double algorithmic_bytes; /* HBM bytes the step must move by the counting rule of the design notes */
   int64_t h2d_bytes;        /* host->device bytes copied by this handle */
   int64_t d2h_bytes;        /* device->host bytes copied by this handle */
+  /* device wall time per phase of the step kernel (nucleation, claim,
+   * resolve, step end; each up to the grid barrier that closes it), ms */
+  double phase_ms[4];
 } amca_stats;
 int amca_get_stats(amca_t *h, amca_stats *out);
 
