@@ -52,7 +52,7 @@ class Stats(ctypes.Structure):
                 ("launches", ctypes.c_int64), ("sites_scanned", ctypes.c_int64), ("nucleations", ctypes.c_int64),
                 ("captures", ctypes.c_int64), ("active_grown", ctypes.c_int64),
                 ("grains_processed", ctypes.c_int64), ("algorithmic_bytes", ctypes.c_double),
-                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("phase_ms", ctypes.c_double * 4)]
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("phase_ms", ctypes.c_double * 9)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -50,8 +50,12 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-constexpr int kMinBlocks = 3;  // co-resident blocks per SM the register budget is sized for
+#ifndef AMCA_MIN_BLOCKS
+#define AMCA_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocks = AMCA_MIN_BLOCKS;  // co-resident blocks per SM the register budget is sized for
 constexpr unsigned long long kWaitNs = 5000000000ull;  // 5 s bound on any spin
+constexpr long long kClaimBatch = 2 * kBlock;           // ranks a block takes per grab in the claim phase
 constexpr unsigned long long kFlagAgg = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
 constexpr unsigned long long kPayload = (1ull << 62) - 1;
@@ -225,7 +229,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
   const long long base_orient = ld_volatile(&c->n_orient);
   const long long base_grain = ld_volatile(&c->next_grain);
   const long long base_act = ld_volatile(&c->n_active);
-  int32_t *act = ld_volatile(&c->cur_list) ? d.act1 : d.act0;
+  EnvRec *act = ld_volatile(&c->cur_list) ? d.act1 : d.act0;
   const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
   const double dTu = d.Tm - T;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -277,13 +281,15 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
       d.gx[gid] = centre_coord(d.grid.x0, d.grid.h, I);
       d.gy[gid] = centre_coord(d.grid.y0, d.grid.h, J);
       d.gz[gid] = centre_coord(d.grid.z0, d.grid.h, K);
-      d.glen[gid] = 0.0;
-      d.gdx[gid] = 0.f;
-      d.gdy[gid] = 0.f;
-      d.gdz[gid] = 0.f;
       d.gori[gid] = oid;
       d.gcell[gid] = cell;
-      act[base_act + r] = (int32_t)gid;
+      EnvRec en;  // a nucleus: length 0, centred on its cell
+      en.L = 0.0;
+      en.dx = en.dy = en.dz = 0.f;
+      en.cell = cell;
+      en.ori = oid;
+      en.id = (int32_t)gid;
+      act[base_act + r] = en;
     }
     run += tot;
   }
@@ -303,82 +309,93 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
 // neighbour tests, atomicMin claims.
 // ---------------------------------------------------------------------------
 __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par, bool grow,
-                            double dt, double vel, const int32_t *act, unsigned long long *stat_tests,
+                            double dt, double vel, EnvRec *cur, const EnvRec *prev, unsigned long long *stat_tests,
                             unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
+  __shared__ long long s_batch;
   if (threadIdx.x == 0) d.scanB[blockIdx.x] = 0ull;  // this block's look-back word of the resolve phase
-  long long b, e;
-  block_chunk(n, b, e);
   unsigned long long tests = 0, tests64 = 0;
+  // Claims need no order: blocks take batches of consecutive ranks from a
+  // shared counter until none is left, so blocks that drew cheap envelopes
+  // (few liquid neighbours) take more batches. About two batches per block,
+  // 32..512 ranks each: small generations (whose envelopes each build
+  // themselves in FP64) still spread over every block.
+  long long batch = (n + 2ll * gridDim.x - 1) / (2ll * gridDim.x);
+  batch = (batch + 31) & ~31ll;
+  if (batch > kClaimBatch) batch = kClaimBatch;
+  if (batch < 32) batch = 32;
+  for (;;) {
+    if (threadIdx.x == 0) s_batch = (long long)atomicAdd(&d.ctrl->claim_next, (unsigned long long)batch);
+    __syncthreads();
+    const long long b = s_batch;
+    __syncthreads();
+    if (b >= n) break;
+    const long long e = b + batch < n ? b + batch : n;
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
-    int id, cell, ori;
-    double L, gxd = 0, gyd = 0, gzd = 0;
-    float dxf = 0.f, dyf = 0.f, dzf = 0.f;
+    EnvRec en;
+    double gxd = 0, gyd = 0, gzd = 0;
     bool have_centre = false;
+    uint32_t liq = 0;
     if (kind == 0) {
-      id = act[r];
-      cell = d.gcell[id];
-      ori = d.gori[id];
-      L = d.glen[id];
+      en = cur[r];
+      // all 26 neighbour states in flight at once
+#pragma unroll
+      for (int nb = 0; nb < 26; ++nb) {
+        int di, dj, dk;
+        const uint32_t s = d.orient[en.cell + nbr_delta(g, nb, di, dj, dk)];
+        liq |= (is_liquid_now(s, par) ? 1u : 0u) << nb;
+      }
       if (grow) {
-        L += dt * vel;  // Grain::grow (Grain.h:27)
-        d.glen[id] = L;
+        en.L += dt * vel;  // Grain::grow (Grain.h:27)
+        cur[r].L = en.L;
       }
     } else {
       // CellularAutomataManager_3D::capture_cell (:677-707) for the capture
       // recorded by the parent: decentred envelope from the parent's
       // (grown) envelope, same orientation.
-      id = (int)(lo + r);
       const uint32_t rec = d.child[r];
-      const int parent = (int)(rec >> 5);
+      const EnvRec pe = prev[rec >> 5];
       const int pnb = (int)(rec & 31u);
-      const int pcell = d.gcell[parent];
-      ori = d.gori[parent];
-      const double pL = d.glen[parent], px = d.gx[parent], py = d.gy[parent], pz = d.gz[parent];
       int di, dj, dk, I, J, K;
-      cell = pcell + nbr_delta(g, pnb, di, dj, dk);
-      cell_ijk(g, pcell, I, J, K);
+      en.cell = pe.cell + nbr_delta(g, pnb, di, dj, dk);
+      en.ori = pe.ori;
+      en.id = (int32_t)(lo + r);
+#pragma unroll
+      for (int nb = 0; nb < 26; ++nb) {
+        int ei, ej, ek;
+        const uint32_t s = d.orient[en.cell + nbr_delta(g, nb, ei, ej, ek)];
+        liq |= (is_liquid_now(s, par) ? 1u : 0u) << nb;
+      }
+      const double px = d.gx[pe.id], py = d.gy[pe.id], pz = d.gz[pe.id];
+      cell_ijk(g, pe.cell, I, J, K);
       const double ccx = centre_coord(g.x0, g.h, I + di);
       const double ccy = centre_coord(g.y0, g.h, J + dj);
       const double ccz = centre_coord(g.z0, g.h, K + dk);
       double out[4];
-      capture_f64(d.omat + 9 * ori, ccx - px, ccy - py, ccz - pz, pL, g.h, d.trunc, out);
+      capture_f64(d.omat + 9 * pe.ori, ccx - px, ccy - py, ccz - pz, pe.L, g.h, d.trunc, out);
       gxd = out[0] + px;
       gyd = out[1] + py;
       gzd = out[2] + pz;
-      L = out[3];
-      dxf = (float)(gxd - ccx);
-      dyf = (float)(gyd - ccy);
-      dzf = (float)(gzd - ccz);
+      en.L = out[3];
+      en.dx = (float)(gxd - ccx);
+      en.dy = (float)(gyd - ccy);
+      en.dz = (float)(gzd - ccz);
       have_centre = true;
-      d.gx[id] = gxd;
-      d.gy[id] = gyd;
-      d.gz[id] = gzd;
-      d.glen[id] = L;
-      d.gdx[id] = dxf;
-      d.gdy[id] = dyf;
-      d.gdz[id] = dzf;
-      d.gori[id] = ori;
-      d.gcell[id] = cell;
-      d.orient[cell] = (uint32_t)ori;  // the claim word of last generation becomes the orientation id
+      cur[r] = en;
+      d.gx[en.id] = gxd;
+      d.gy[en.id] = gyd;
+      d.gz[en.id] = gzd;
+      d.gori[en.id] = en.ori;
+      d.gcell[en.id] = en.cell;
+      d.orient[en.cell] = (uint32_t)en.ori;  // the claim word of last generation becomes the orientation id
     }
-    // all 26 neighbour states in flight at once
-    uint32_t liq = 0;
-#pragma unroll
-    for (int nb = 0; nb < 26; ++nb) {
-      int di, dj, dk;
-      const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
-      liq |= (is_liquid_now(s, par) ? 1u : 0u) << nb;
-    }
+    const int cell = en.cell, ori = en.ori, id = en.id;
+    const double L = en.L;
     uint32_t con = 0;
     if (liq && L != 0) {  // cell_is_captured is false for a zero half-diagonal
       int I, J, K;
       cell_ijk(g, cell, I, J, K);
-      if (!have_centre) {
-        dxf = d.gdx[id];
-        dyf = d.gdy[id];
-        dzf = d.gdz[id];
-      }
+      const float dxf = en.dx, dyf = en.dy, dzf = en.dz;
       const float errg = 4.76837158203125e-07f * (d.h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + d.coord_err;
       const float L32 = (float)L;
       float m32[9];
@@ -420,6 +437,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
     d.liq[r] = liq;
     d.con[r] = con;
   }
+  }
   *stat_tests += tests;
   *stat_tests64 += tests64;
 }
@@ -427,8 +445,8 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
 // ---------------------------------------------------------------------------
 // Resolve: captures, deactivation, child records, survivor compaction.
 // ---------------------------------------------------------------------------
-__device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par,
-                              const int32_t *act, int32_t *next_act, unsigned long long *smem) {
+__device__ bool resolve_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur, EnvRec *next_act,
+                              unsigned long long *smem) {
   PlainCtrl *c = d.ctrl;
   const Grid &g = d.grid;
   const long long base_grain = ld_volatile(&c->next_grain);
@@ -441,8 +459,7 @@ __device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long
     const uint32_t lm = d.liq[r], cm = d.con[r];
     uint32_t cap = 0, surv = 0;
     if (lm) {
-      const int id = kind == 0 ? act[r] : (int)(lo + r);
-      const int cell = d.gcell[id];
+      const int cell = cur[r].cell;
       const uint32_t mine = claim_word(par, (uint32_t)r);
 #pragma unroll
       for (int nb = 0; nb < 26; ++nb) {
@@ -472,14 +489,13 @@ __device__ bool resolve_phase(const PlainDevice &d, int kind, long long lo, long
     const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
     if (r < e && (cap | surv)) {
       const unsigned long long off = run + ex;
-      const int id = kind == 0 ? act[r] : (int)(lo + r);
-      if (surv) next_act[base_next + (long long)(off & 0xffffffffull)] = id;
+      if (surv) next_act[base_next + (long long)(off & 0xffffffffull)] = cur[r];
       long long slot = (long long)(off >> 32);  // rank of the first child in the next generation
       uint32_t bits = cap;
       while (bits) {
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
-        d.child[slot++] = ((uint32_t)id << 5) | (uint32_t)nb;
+        d.child[slot++] = ((uint32_t)r << 5) | (uint32_t)nb;  // parent's rank in this generation
       }
     }
     run += tot;
@@ -522,32 +538,56 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
     const double dt = nA > 0 ? ld_volatile(&c->dt_active) : ld_volatile(&c->dt_none);
 
     // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
-    const int32_t *act = cur ? d.act1 : d.act0;
-    int32_t *next_act = cur ? d.act0 : d.act1;
+    EnvRec *act = cur ? d.act1 : d.act0;
+    EnvRec *next_act = cur ? d.act0 : d.act1;
     long long n = nA, lo = 0, processed = 0;
     int kind = 0;
     unsigned gen = 0;
     bool ok = true;
+    EnvRec *list = act, *parents = nullptr;  // records of this generation / of its parents
     while (n > 0) {
       processed += n;
-      claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dt, vel, act, &tests, &tests64);
+      unsigned long long t_work = threadIdx.x == 0 ? now_ns() : 0ull;
+      claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dt, vel, list, parents, &tests, &tests64);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned long long w = now_ns() - t_work;
+        atomicAdd(&c->ns_claim_work_sum, w);
+        atomicMax(&c->phase_max_scratch[0], w);
+      }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
         t_now = now_ns();
         c->ns_claim += t_now - t_mark;
+        if (gen == 0) c->ns_claim_gen0 += t_now - t_mark;
         t_mark = t_now;
+        c->ns_claim_work_max += c->phase_max_scratch[0];
+        c->phase_max_scratch[0] = 0ull;
       }
-      if (!(ok = resolve_phase(d, kind, lo, n, gen & 1u, act, next_act, smem))) break;
+      // the next claim phase starts after the resolve barrier
+      if (blockIdx.x == 0 && threadIdx.x == 0) c->claim_next = 0ull;
+      t_work = threadIdx.x == 0 ? now_ns() : 0ull;
+      if (!(ok = resolve_phase(d, n, gen & 1u, list, next_act, smem))) break;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned long long w = now_ns() - t_work;
+        atomicAdd(&c->ns_resolve_work_sum, w);
+        atomicMax(&c->phase_max_scratch[1], w);
+      }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
         t_now = now_ns();
         c->ns_resolve += t_now - t_mark;
         t_mark = t_now;
+        c->ns_resolve_work_max += c->phase_max_scratch[1];
+        c->phase_max_scratch[1] = 0ull;
       }
       n = ld_volatile(&c->gen_n);
       lo = ld_volatile(&c->gen_lo);
       kind = 1;
       ++gen;
+      parents = list;
+      list = (gen & 1u) ? d.gen1 : d.gen0;
     }
     if (!ok) break;
     // step end: swap lists, advance time (CellularAutomataManager_3D.cpp:653-659)
@@ -667,8 +707,7 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
-  size_t ctrl, live, omat32, scanA, gx, gy, gz, glen, gdx, gdy, gdz, gori, gcell, act0, act1, liq, con, child, scanB,
-      total;
+  size_t ctrl, live, omat32, scanA, gx, gy, gz, gori, gcell, act0, act1, gen0, gen1, liq, con, child, scanB, total;
   NoAllocLayout(long long n, long long s) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -683,14 +722,12 @@ struct NoAllocLayout {
     gx = take((size_t)n * 8);
     gy = take((size_t)n * 8);
     gz = take((size_t)n * 8);
-    glen = take((size_t)n * 8);
-    gdx = take((size_t)n * 4);
-    gdy = take((size_t)n * 4);
-    gdz = take((size_t)n * 4);
     gori = take((size_t)n * 4);
     gcell = take((size_t)n * 4);
-    act0 = take((size_t)n * 4);
-    act1 = take((size_t)n * 4);
+    act0 = take((size_t)n * sizeof(EnvRec));
+    act1 = take((size_t)n * sizeof(EnvRec));
+    gen0 = take((size_t)n * sizeof(EnvRec));
+    gen1 = take((size_t)n * sizeof(EnvRec));
     liq = take((size_t)n * 4);
     con = take((size_t)n * 4);
     child = take((size_t)n * 4);
@@ -787,14 +824,12 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.gx = (double *)(base + lay.gx);
   d.gy = (double *)(base + lay.gy);
   d.gz = (double *)(base + lay.gz);
-  d.glen = (double *)(base + lay.glen);
-  d.gdx = (float *)(base + lay.gdx);
-  d.gdy = (float *)(base + lay.gdy);
-  d.gdz = (float *)(base + lay.gdz);
   d.gori = (int32_t *)(base + lay.gori);
   d.gcell = (int32_t *)(base + lay.gcell);
-  d.act0 = (int32_t *)(base + lay.act0);
-  d.act1 = (int32_t *)(base + lay.act1);
+  d.act0 = (EnvRec *)(base + lay.act0);
+  d.act1 = (EnvRec *)(base + lay.act1);
+  d.gen0 = (EnvRec *)(base + lay.gen0);
+  d.gen1 = (EnvRec *)(base + lay.gen1);
   d.liq = (uint32_t *)(base + lay.liq);
   d.con = (uint32_t *)(base + lay.con);
   d.child = (uint32_t *)(base + lay.child);

@@ -5,12 +5,13 @@
 //   orient      u32[(nx+2)(ny+2)(nz+2)]  cellOrientationID_, ghost-inclusive, reference index order
 //   site_*      nucleation sites sorted by cell id: cell i32, dTc f64, live u8
 //   omat/omat32 per orientation: local->global matrix, 9 x f64 and 9 x f32
-//   g*          envelope table (capacity = interior cells), structure of arrays:
-//               centre f64 x3, half-diagonal f64, centre minus own-cell centre f32 x3,
-//               orientation i32, cell i32
-//   act[2]      active-envelope lists (ascending id), double-buffered per step
+//   g*          envelope table by id (capacity = interior cells), written once per
+//               envelope: centre f64 x3, orientation i32, cell i32
+//   act[2]      active list as 32-byte records (ascending id), double-buffered per step
+//   gen[2]      records of the envelopes created in the generation being walked,
+//               double-buffered by generation parity
 //   liq/con     per-rank neighbour masks of the generation being processed
-//   child       per new envelope: parent id << 5 | neighbour index
+//   child       per new envelope: parent's rank in its generation << 5 | neighbour index
 //   scanA/scanB decoupled look-back status words, one per block (nucleation / capture)
 //   ctrl        control block: counters, time, barrier words, error flag
 #pragma once
@@ -58,9 +59,25 @@ struct PlainCtrl {
   unsigned long long grains_processed; // envelopes of every generation, summed
   // wall time of each phase as block 0 sees it (phase start to barrier exit), ns
   unsigned long long ns_nucleation, ns_claim, ns_resolve, ns_step_end;
+  unsigned long long ns_claim_gen0;                    // part of ns_claim spent on generation 0
+  unsigned long long ns_claim_work_sum, ns_claim_work_max;  // per-block busy time in claim phases
+  unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
+  unsigned long long phase_max_scratch[2];             // running max of the current phase
+  unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase
 };
 
 enum { kErrBarrier = 1, kErrLookback = 2 };
+
+// One envelope as the generation lists carry it: everything the neighbour
+// tests need in one 32-byte, coalesced record.
+struct alignas(16) EnvRec {
+  double L;            // half-diagonal length
+  float dx, dy, dz;    // centre minus own-cell centre, rounded to float
+  int32_t cell;        // ghost-inclusive cell index
+  int32_t ori;         // orientation id
+  int32_t id;          // envelope id (index of the by-id table)
+};
+static_assert(sizeof(EnvRec) == 32, "EnvRec must stay one 32-byte sector");
 
 struct PlainDevice {
   Grid grid;
@@ -78,11 +95,11 @@ struct PlainDevice {
   int64_t nsites;
   const double *omat;
   const float *omat32;
-  double *gx, *gy, *gz, *glen;
-  float *gdx, *gdy, *gdz;
+  double *gx, *gy, *gz;
   int32_t *gori, *gcell;
   int64_t gcap;
-  int32_t *act0, *act1;
+  EnvRec *act0, *act1;
+  EnvRec *gen0, *gen1;
   uint32_t *liq, *con;
   uint32_t *child;
   unsigned long long *scanA, *scanB;

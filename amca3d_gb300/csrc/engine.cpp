@@ -178,14 +178,12 @@ struct amca_t {
     d.gx = alloc<double>(d.gcap);
     d.gy = alloc<double>(d.gcap);
     d.gz = alloc<double>(d.gcap);
-    d.glen = alloc<double>(d.gcap);
-    d.gdx = alloc<float>(d.gcap);
-    d.gdy = alloc<float>(d.gcap);
-    d.gdz = alloc<float>(d.gcap);
     d.gori = alloc<int32_t>(d.gcap);
     d.gcell = alloc<int32_t>(d.gcap);
-    d.act0 = alloc<int32_t>(d.gcap);
-    d.act1 = alloc<int32_t>(d.gcap);
+    d.act0 = alloc<EnvRec>(d.gcap);
+    d.act1 = alloc<EnvRec>(d.gcap);
+    d.gen0 = alloc<EnvRec>(d.gcap);
+    d.gen1 = alloc<EnvRec>(d.gcap);
     d.liq = alloc<uint32_t>(d.gcap);
     d.con = alloc<uint32_t>(d.gcap);
     d.child = alloc<uint32_t>(d.gcap);
@@ -573,6 +571,12 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->phase_ms[1] = c.ns_claim * 1e-6;
     s->phase_ms[2] = c.ns_resolve * 1e-6;
     s->phase_ms[3] = c.ns_step_end * 1e-6;
+    s->phase_ms[4] = c.ns_claim_gen0 * 1e-6;
+    const double nb = h->grid_blocks > 0 ? h->grid_blocks : 1;
+    s->phase_ms[5] = c.ns_claim_work_sum * 1e-6 / nb;
+    s->phase_ms[6] = c.ns_claim_work_max * 1e-6;
+    s->phase_ms[7] = c.ns_resolve_work_sum * 1e-6 / nb;
+    s->phase_ms[8] = c.ns_resolve_work_max * 1e-6;
   });
 }
 

@@ -130,9 +130,12 @@ typedef struct {
   double algorithmic_bytes; /* HBM bytes the step must move by the counting rule of the design notes */
   int64_t h2d_bytes;        /* host->device bytes copied by this handle */
   int64_t d2h_bytes;        /* device->host bytes copied by this handle */
-  /* device wall time per phase of the step kernel (nucleation, claim,
-   * resolve, step end; each up to the grid barrier that closes it), ms */
-  double phase_ms[4];
+  /* device wall time per phase of the step kernel, ms: [0] nucleation,
+   * [1] claim, [2] resolve, [3] step end (each up to the grid barrier that
+   * closes it), [4] the generation-0 part of [1]; per-block busy time before
+   * the barrier: [5] claim mean over blocks, [6] claim slowest block,
+   * [7] resolve mean, [8] resolve slowest block (summed over phases) */
+  double phase_ms[9];
 } amca_stats;
 int amca_get_stats(amca_t *h, amca_stats *out);
 
