@@ -169,8 +169,11 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   }
   const double pC[3] = {cx, cy, cz};
   const double perp = length - interception;
+  // (perp * n_i) / 3 with n_i = +-1 equals +-(perp / 3) exactly (IEEE
+  // division is sign-symmetric), so one division serves all three terms
+  const double third = perp / 3;
   double pA[3];
-  for (int i = 0; i < 3; i++) pA[i] = pC[i] + perp * face_normal(quad, i) / 3;
+  for (int i = 0; i < 3; i++) pA[i] = pC[i] + (face_normal(quad, i) > 0 ? third : -third);
   double dist[3] = {0.0, 0.0, 0.0};
   for (int i = 0; i < 3; i++) {
     const int id = face_corner(quad, i);
@@ -214,16 +217,20 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   const double J0 = d13 / n13, J1 = n13 - J0;
   const double tv = trunc_coeff * h;
   if (I0 < tv && I1 < tv) {
-    I0 = n12 / 2;
-    I1 = n13 / 2;
+    I0 = n12 * 0.5;  // == n12 / 2 exactly
+    I1 = n13 * 0.5;
   }
   const double L1 = 0.5 * (dmin_ref(I0, tv) + dmin_ref(I1, tv));
   const double L2 = 0.5 * (dmin_ref(J0, tv) + dmin_ref(J1, tv));
   const double Lnew = (double)sqrtf(2.0f) * (dmax_ref(L1, L2));
   const double mag = (length - Lnew);
+  // (mag * c_i) / (length * T) for the corner S1 = c: only its axis component
+  // is non-zero; the others are (mag * +0) / positive = zero with mag's sign
+  const double zero = mag < 0 ? -0.0 : 0.0;
   double o0 = 0.0, o1 = 0.0, o2 = 0.0;
   for (int i = 0; i < 3; i++) {
-    const double comp = mag * (corner_unit(cid0, i) * length) / (length * kTheodorus);
+    const double c = corner_unit(cid0, i);
+    const double comp = c != 0 ? mag * (c * length) / (length * kTheodorus) : zero;
     o0 += comp * l2g[i + 0];
     o1 += comp * l2g[i + 3];
     o2 += comp * l2g[i + 6];

@@ -223,25 +223,29 @@ __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj,
 // Pass 1 marks sites (2 = nucleates now, 0 = removed), pass 2 hands out
 // orientation / envelope ids in site order.
 // ---------------------------------------------------------------------------
-__device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned long long *smem,
-                                 unsigned long long *stat_live) {
+__device__ bool nucleation_phase(const PlainDevice &d, double time, long long step, long long base_act,
+                                 EnvRec *act, unsigned long long *smem, unsigned long long *stat_live) {
   PlainCtrl *c = d.ctrl;
   const long long base_orient = ld_volatile(&c->n_orient);
   const long long base_grain = ld_volatile(&c->next_grain);
-  const long long base_act = ld_volatile(&c->n_active);
-  EnvRec *act = ld_volatile(&c->cur_list) ? d.act1 : d.act0;
+  unsigned long long *scan = d.scanA + (step & 1) * kStatusWords;
   const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
   const double dTu = d.Tm - T;
+  // next step's look-back word starts cleared: it was last read in the
+  // previous step's nucleation, which every block finished before that
+  // phase's barrier
+  if (threadIdx.x == 0) d.scanA[((step + 1) & 1) * kStatusWords + blockIdx.x] = 0ull;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // calculate_time_step (CellularAutomataManager_3D.cpp:449-507): one
     // velocity for the uniform field; dt for "some active envelope" and for
-    // "none" (maxVelocity stays 1e-10), picked after nucleation
+    // "none" (maxVelocity stays 1e-10), picked after nucleation. Slots by step
+    // parity: a slow block may still read last step's values.
     const double vel = kgt_velocity(d.Tm, T, d.a1, d.a2, d.a3);
     const double maxV = vel > 1e-10 ? vel : 1e-10;
     const double a = d.tsf * d.grid.h / maxV, b = d.tsf * d.grid.h / 1e-10;
-    c->vel = vel;
-    c->dt_active = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
-    c->dt_none = (d.max_dt < b) ? d.max_dt : b;
+    c->vel[step & 1] = vel;
+    c->dt_active[step & 1] = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
+    c->dt_none[step & 1] = (d.max_dt < b) ? d.max_dt : b;
   }
   __threadfence();
   long long b, e;
@@ -257,7 +261,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, unsigned lon
   }
   unsigned long long agg;
   block_exclusive_scan(count, smem, &agg);
-  const unsigned long long pre = block_prefix(d.scanA, agg, smem, c);
+  const unsigned long long pre = block_prefix(scan, agg, smem, c);
   if (pre == ~0ull) return false;
   unsigned long long run = pre;
   for (long long i0 = b; i0 < e; i0 += kBlock) {
@@ -445,36 +449,63 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
 // ---------------------------------------------------------------------------
 // Resolve: captures, deactivation, child records, survivor compaction.
 // ---------------------------------------------------------------------------
-__device__ bool resolve_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur, EnvRec *next_act,
+// Marking pass: per rank, the captured neighbours (final claim is its own)
+// and whether it stays active; written over the containment mask as
+// captures | survives << 31. Ranks are independent, so blocks take
+// dynamic batches as in the claim phase.
+__device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
+  const Grid &g = d.grid;
+  __shared__ long long s_batch;
+  long long batch = (n + 2ll * gridDim.x - 1) / (2ll * gridDim.x);
+  batch = (batch + 31) & ~31ll;
+  if (batch > kClaimBatch) batch = kClaimBatch;
+  if (batch < 32) batch = 32;
+  for (;;) {
+    if (threadIdx.x == 0) s_batch = (long long)atomicAdd(&d.ctrl->mark_next, (unsigned long long)batch);
+    __syncthreads();
+    const long long b = s_batch;
+    __syncthreads();
+    if (b >= n) break;
+    const long long e = b + batch < n ? b + batch : n;
+    for (long long r = b + threadIdx.x; r < e; r += kBlock) {
+      const uint32_t lm = d.liq[r], cm = d.con[r];
+      uint32_t cap = 0, surv = 0;
+      if (lm) {
+        const int cell = cur[r].cell;
+        const uint32_t mine = claim_word(par, (uint32_t)r);
+#pragma unroll
+        for (int nb = 0; nb < 26; ++nb) {
+          if (!((lm >> nb) & 1u)) continue;
+          int di, dj, dk;
+          const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
+          if ((cm >> nb) & 1u) {
+            cap |= (s == mine ? 1u : 0u) << nb;
+          } else if (s == kLiquid || (s & kRankMask) > (uint32_t)r) {
+            surv = 1;
+          }
+        }
+      }
+      d.con[r] = cap | (surv << 31);
+    }
+  }
+}
+
+// Scan pass: one look-back per block over its contiguous chunk of marks gives
+// new envelope ids (walk order), child records and the survivors' places in
+// the next active list.
+__device__ bool resolve_phase(const PlainDevice &d, long long n, long long step, const EnvRec *cur, EnvRec *next_act,
                               unsigned long long *smem) {
   PlainCtrl *c = d.ctrl;
-  const Grid &g = d.grid;
+  long long *n_next = &c->n_active_next[step & 1];
   const long long base_grain = ld_volatile(&c->next_grain);
-  const long long base_next = ld_volatile(&c->n_active_next);
+  const long long base_next = ld_volatile(n_next);
   __threadfence();
   long long b, e;
   block_chunk(n, b, e);
   unsigned long long acc = 0;
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
-    const uint32_t lm = d.liq[r], cm = d.con[r];
-    uint32_t cap = 0, surv = 0;
-    if (lm) {
-      const int cell = cur[r].cell;
-      const uint32_t mine = claim_word(par, (uint32_t)r);
-#pragma unroll
-      for (int nb = 0; nb < 26; ++nb) {
-        if (!((lm >> nb) & 1u)) continue;
-        int di, dj, dk;
-        const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
-        if ((cm >> nb) & 1u) {
-          cap |= (s == mine ? 1u : 0u) << nb;
-        } else if (s == kLiquid || (s & kRankMask) > (uint32_t)r) {
-          surv = 1;
-        }
-      }
-    }
-    d.con[r] = cap | (surv << 31);
-    acc += ((unsigned long long)__popc(cap) << 32) | surv;
+    const uint32_t word = d.con[r];
+    acc += ((unsigned long long)__popc(word & 0x03ffffffu) << 32) | (word >> 31);
   }
   unsigned long long agg;
   block_exclusive_scan(acc, smem, &agg);
@@ -506,7 +537,7 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, unsigned par, c
     c->gen_lo = base_grain;
     c->gen_n = caps;
     c->next_grain = base_grain + caps;
-    c->n_active_next = base_next + survs;
+    *n_next = base_next + survs;
     c->liquid -= caps;
     c->captures += (unsigned long long)caps;
   }
@@ -517,33 +548,37 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
   __shared__ unsigned long long smem[kWarps + 2];
   PlainCtrl *c = d.ctrl;
   unsigned long long tests = 0, tests64 = 0, live = 0;
-  for (;;) {
-    const long long step = ld_volatile(&c->step);
-    const double time = ld_volatile(&c->time);
-    if (ld_volatile(&c->done) || !(time < d.final_time) || step >= step_limit) break;
-
+  // per-step state, identical in every thread (read once, then advanced locally)
+  long long step = ld_volatile(&c->step);
+  double time = ld_volatile(&c->time), dt = ld_volatile(&c->dt);
+  long long n_act = ld_volatile(&c->n_active);
+  int cur = ld_volatile(&c->cur_list);
+  bool done = ld_volatile(&c->done) != 0;
+  bool ok = true;
+  const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
+  while (!done && time < d.final_time && step < step_limit) {
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
-    const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
-    unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
-    if (!nucleation_phase(d, time, smem, &live)) break;
-    if (!grid_barrier(c)) break;
+    EnvRec *act = cur ? d.act1 : d.act0;
+    EnvRec *next_act = cur ? d.act0 : d.act1;
+    if (!(ok = nucleation_phase(d, time, step, n_act, act, smem, &live))) break;
+    if (!(ok = grid_barrier(c))) break;
     if (timer) {
       t_now = now_ns();
       c->ns_nucleation += t_now - t_mark;
       t_mark = t_now;
+      // next step's survivor count starts at zero; every block read it last
+      // at the end of the previous step, before this barrier
+      c->n_active_next[(step + 1) & 1] = 0;
     }
     const long long nA = ld_volatile(&c->n_active);
-    const int cur = ld_volatile(&c->cur_list);
-    const double vel = ld_volatile(&c->vel);
-    const double dt = nA > 0 ? ld_volatile(&c->dt_active) : ld_volatile(&c->dt_none);
+    const double vel = ld_volatile(&c->vel[step & 1]);
+    dt = nA > 0 ? ld_volatile(&c->dt_active[step & 1]) : ld_volatile(&c->dt_none[step & 1]);
 
     // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
-    EnvRec *act = cur ? d.act1 : d.act0;
-    EnvRec *next_act = cur ? d.act0 : d.act1;
     long long n = nA, lo = 0, processed = 0;
     int kind = 0;
     unsigned gen = 0;
-    bool ok = true;
     EnvRec *list = act, *parents = nullptr;  // records of this generation / of its parents
     while (n > 0) {
       processed += n;
@@ -563,11 +598,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
         t_mark = t_now;
         c->ns_claim_work_max += c->phase_max_scratch[0];
         c->phase_max_scratch[0] = 0ull;
+        c->claim_next = 0ull;  // the next claim phase is two barriers away
       }
-      // the next claim phase starts after the resolve barrier
-      if (blockIdx.x == 0 && threadIdx.x == 0) c->claim_next = 0ull;
       t_work = threadIdx.x == 0 ? now_ns() : 0ull;
-      if (!(ok = resolve_phase(d, n, gen & 1u, list, next_act, smem))) break;
+      mark_phase(d, n, gen & 1u, list);
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
@@ -576,11 +610,16 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
       }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
+        c->mark_next = 0ull;  // the next marking pass is two barriers away
+        c->ns_resolve_work_max += c->phase_max_scratch[1];
+        c->phase_max_scratch[1] = 0ull;
+      }
+      if (!(ok = resolve_phase(d, n, step, list, next_act, smem))) break;
+      if (!(ok = grid_barrier(c))) break;
+      if (timer) {
         t_now = now_ns();
         c->ns_resolve += t_now - t_mark;
         t_mark = t_now;
-        c->ns_resolve_work_max += c->phase_max_scratch[1];
-        c->phase_max_scratch[1] = 0ull;
       }
       n = ld_volatile(&c->gen_n);
       lo = ld_volatile(&c->gen_lo);
@@ -590,22 +629,29 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
       list = (gen & 1u) ? d.gen1 : d.gen0;
     }
     if (!ok) break;
-    // step end: swap lists, advance time (CellularAutomataManager_3D.cpp:653-659)
-    if (threadIdx.x == 0) d.scanA[blockIdx.x] = 0ull;  // next step's nucleation look-back word
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      c->n_active = c->n_active_next;
-      c->n_active_next = 0;
-      c->cur_list = cur ^ 1;
-      c->time = time + dt;
-      c->dt = dt;
-      c->step = step + 1;
-      c->done = c->liquid == 0;
+    // step end (CellularAutomataManager_3D.cpp:653-659): every block advances
+    // the same locals; the survivors' count was published before the last
+    // barrier, so no further barrier is needed
+    n_act = ld_volatile(&c->n_active_next[step & 1]);
+    cur ^= 1;
+    time = time + dt;
+    ++step;
+    done = ld_volatile(&c->liquid) == 0;
+    if (timer) {
       c->gens += gen;
       c->active_grown += (unsigned long long)nA;
       c->grains_processed += (unsigned long long)processed;
     }
-    if (!grid_barrier(c)) break;
-    if (timer) c->ns_step_end += now_ns() - t_mark;
+  }
+  if (ok && timer) {
+    // the realm's state for the host and the next launch
+    c->step = step;
+    c->time = time;
+    c->dt = dt;
+    c->n_active = n_act;
+    c->cur_list = cur;
+    c->done = done ? 1 : 0;
+    c->ns_step_end += now_ns() - t_mark;
   }
   // statistics: one atomic per warp
 #pragma unroll
@@ -682,6 +728,7 @@ __global__ void noalloc_setup_kernel(PlainDevice d, long long liquid) {
   for (long long i = tid; i < 9 * d.nsites; i += stride) m32[i] = (float)d.omat[i];
   for (long long i = tid; i < kStatusWords; i += stride) {
     d.scanA[i] = 0ull;
+    d.scanA[kStatusWords + i] = 0ull;
     d.scanB[i] = 0ull;
   }
 }
@@ -718,7 +765,7 @@ struct NoAllocLayout {
     ctrl = take(sizeof(PlainCtrl));
     live = take((size_t)s);
     omat32 = take((size_t)s * 9 * sizeof(float));
-    scanA = take((size_t)kStatusWords * 8);
+    scanA = take((size_t)2 * kStatusWords * 8);
     gx = take((size_t)n * 8);
     gy = take((size_t)n * 8);
     gz = take((size_t)n * 8);

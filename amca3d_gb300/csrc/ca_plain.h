@@ -12,7 +12,8 @@
 //               double-buffered by generation parity
 //   liq/con     per-rank neighbour masks of the generation being processed
 //   child       per new envelope: parent's rank in its generation << 5 | neighbour index
-//   scanA/scanB decoupled look-back status words, one per block (nucleation / capture)
+//   scanA/scanB decoupled look-back status words, one per block: nucleation
+//               (two sets, by step parity) / capture
 //   ctrl        control block: counters, time, barrier words, error flag
 #pragma once
 
@@ -28,6 +29,10 @@ constexpr long long kStatusWords = 4096;
 // Child records pack an envelope id into 27 bits.
 constexpr long long kMaxCells = 1ll << 27;
 
+// Control block. Between launches it holds the realm's state (step, time,
+// active count, ...). Inside a launch every block keeps the per-step values
+// as identical locals; the fields written by one block in a phase are read
+// by all only after the barrier that closes that phase.
 struct PlainCtrl {
   unsigned bar_count;
   unsigned bar_gen;
@@ -35,17 +40,17 @@ struct PlainCtrl {
   int cur_list;     // which act[] holds the current active list
   long long n_orient;
   long long next_grain;
-  long long n_active;
-  long long n_active_next;
+  long long n_active;          // active envelopes (between launches; after nucleation inside one)
+  long long n_active_next[2];  // survivors of the step, by step parity
   long long liquid;
   long long gen_lo;
   long long gen_n;
   long long step;
   double time;
   double dt;
-  double vel;        // growth velocity at `time` (uniform field)
-  double dt_active;  // dt when some envelope is active
-  double dt_none;    // dt when none is (maxVelocity stays 1e-10)
+  double vel[2];        // growth velocity at the step's time (uniform field), by step parity
+  double dt_active[2];  // dt when some envelope is active, by step parity
+  double dt_none[2];    // dt when none is (maxVelocity stays 1e-10), by step parity
   int done;
   int pad;
   unsigned long long tests;
@@ -64,6 +69,7 @@ struct PlainCtrl {
   unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
   unsigned long long phase_max_scratch[2];             // running max of the current phase
   unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase
+  unsigned long long mark_next;                        // next rank batch of the resolve marking pass
 };
 
 enum { kErrBarrier = 1, kErrLookback = 2 };

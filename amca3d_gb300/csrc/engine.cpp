@@ -187,7 +187,7 @@ struct amca_t {
     d.liq = alloc<uint32_t>(d.gcap);
     d.con = alloc<uint32_t>(d.gcap);
     d.child = alloc<uint32_t>(d.gcap);
-    const int64_t ntA = kStatusWords, ntB = kStatusWords;
+    const int64_t ntA = 2 * kStatusWords, ntB = kStatusWords;
     d.scanA = alloc<unsigned long long>(ntA);
     d.scanB = alloc<unsigned long long>(ntB);
     d.ctrl = alloc<PlainCtrl>(1);
