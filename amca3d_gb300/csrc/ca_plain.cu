@@ -218,6 +218,31 @@ __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj,
   return dk * g.nxyg + dj * g.nxg + di;
 }
 
+__device__ __forceinline__ void set_solid(uint32_t *solid, int cell) {
+  atomicOr(solid + (cell >> 5), 1u << (cell & 31));
+}
+
+// Bits of a cell bitmap for the 26 neighbours of `cell`, in the reference's
+// neighbour order (bit n of the result = neighbour n): one 64-bit window per
+// row of three cells, nine rows.
+__device__ __forceinline__ uint32_t neighbour_bits(const uint32_t *map, const Grid &g, int cell) {
+  uint32_t m27 = 0;
+#pragma unroll
+  for (int dk = -1; dk <= 1; ++dk)
+#pragma unroll
+    for (int dj = -1; dj <= 1; ++dj) {
+      const long long c0 = (long long)cell + dk * g.nxyg + dj * g.nxg - 1;  // the row's di = -1 cell
+      const long long w = c0 >> 5;
+      const unsigned long long two = ((unsigned long long)map[w + 1] << 32) | map[w];
+      m27 |= ((uint32_t)(two >> (c0 & 31)) & 7u) << ((dk + 1) * 9 + (dj + 1) * 3);
+    }
+  return (m27 & 0x1fffu) | ((m27 >> 14) << 13);  // drop the centre cell (index 13 of 27)
+}
+
+__device__ __forceinline__ uint32_t liquid_neighbours(const uint32_t *solid, const Grid &g, int cell) {
+  return ~neighbour_bits(solid, g, cell) & 0x03ffffffu;
+}
+
 // ---------------------------------------------------------------------------
 // Nucleation (CellularAutomataManager.cpp:219-297) in site order.
 // Pass 1 marks sites (2 = nucleates now, 0 = removed), pass 2 hands out
@@ -282,6 +307,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
       int I, J, K;
       cell_ijk(d.grid, cell, I, J, K);
       d.orient[cell] = (uint32_t)oid;
+      set_solid(d.solid, cell);
       d.gx[gid] = centre_coord(d.grid.x0, d.grid.h, I);
       d.gy[gid] = centre_coord(d.grid.y0, d.grid.h, J);
       d.gz[gid] = centre_coord(d.grid.z0, d.grid.h, K);
@@ -342,13 +368,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
     uint32_t liq = 0;
     if (kind == 0) {
       en = cur[r];
-      // all 26 neighbour states in flight at once
-#pragma unroll
-      for (int nb = 0; nb < 26; ++nb) {
-        int di, dj, dk;
-        const uint32_t s = d.orient[en.cell + nbr_delta(g, nb, di, dj, dk)];
-        liq |= (is_liquid_now(s, par) ? 1u : 0u) << nb;
-      }
+      liq = liquid_neighbours(d.solid, g, en.cell);
       if (grow) {
         en.L += dt * vel;  // Grain::grow (Grain.h:27)
         cur[r].L = en.L;
@@ -364,12 +384,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
       en.cell = pe.cell + nbr_delta(g, pnb, di, dj, dk);
       en.ori = pe.ori;
       en.id = (int32_t)(lo + r);
-#pragma unroll
-      for (int nb = 0; nb < 26; ++nb) {
-        int ei, ej, ek;
-        const uint32_t s = d.orient[en.cell + nbr_delta(g, nb, ei, ej, ek)];
-        liq |= (is_liquid_now(s, par) ? 1u : 0u) << nb;
-      }
+      liq = liquid_neighbours(d.solid, g, en.cell);
       const double px = d.gx[pe.id], py = d.gy[pe.id], pz = d.gz[pe.id];
       cell_ijk(g, pe.cell, I, J, K);
       const double ccx = centre_coord(g.x0, g.h, I + di);
@@ -435,7 +450,9 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
         int di, dj, dk;
-        atomicMin(d.orient + cell + nbr_delta(g, nb, di, dj, dk), mine);
+        const int nc = cell + nbr_delta(g, nb, di, dj, dk);
+        atomicMin(d.orient + nc, mine);
+        atomicOr(d.claimed + (nc >> 5), 1u << (nc & 31));
       }
     }
     d.liq[r] = liq;
@@ -473,9 +490,17 @@ __device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, cons
       if (lm) {
         const int cell = cur[r].cell;
         const uint32_t mine = claim_word(par, (uint32_t)r);
+        // a liquid neighbour this envelope does not contain and nobody
+        // claimed keeps it active without a look at the cell field
+        const uint32_t other = lm & ~cm;
+        const uint32_t clm = neighbour_bits(d.claimed, g, cell);
+        surv = (other & ~clm) ? 1u : 0u;
+        // claim words are read for contained cells, and for claimed ones
+        // while survival is still open
+        const uint32_t need = cm | (surv ? 0u : (other & clm));
 #pragma unroll
         for (int nb = 0; nb < 26; ++nb) {
-          if (!((lm >> nb) & 1u)) continue;
+          if (!((need >> nb) & 1u)) continue;
           int di, dj, dk;
           const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
           if ((cm >> nb) & 1u) {
@@ -523,10 +548,13 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
       if (surv) next_act[base_next + (long long)(off & 0xffffffffull)] = cur[r];
       long long slot = (long long)(off >> 32);  // rank of the first child in the next generation
       uint32_t bits = cap;
+      const int cell = bits ? cur[r].cell : 0;
       while (bits) {
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
         d.child[slot++] = ((uint32_t)r << 5) | (uint32_t)nb;  // parent's rank in this generation
+        int di, dj, dk;
+        set_solid(d.solid, cell + nbr_delta(d.grid, nb, di, dj, dk));  // solid for the next generation
       }
     }
     run += tot;
@@ -667,12 +695,24 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
   }
 }
 
-__global__ void init_field_kernel(uint32_t *orient, Grid g, long long ncells) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < ncells; i += (long long)gridDim.x * blockDim.x) {
-    int I, J, K;
-    cell_ijk(g, i, I, J, K);
-    const bool ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
-    orient[i] = ghost ? 0u : kLiquid;
+__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, Grid g, long long ncells) {
+  // one bitmap word (32 cells) per thread; cells past the grid count as solid
+  const long long nwords = solid_words(ncells);
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (long long)gridDim.x * blockDim.x) {
+    uint32_t bits = 0;
+    for (int b = 0; b < 32; ++b) {
+      const long long i = w * 32 + b;
+      bool ghost = true;
+      if (i < ncells) {
+        int I, J, K;
+        cell_ijk(g, i, I, J, K);
+        ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
+        orient[i] = ghost ? 0u : kLiquid;
+      }
+      bits |= (ghost ? 1u : 0u) << b;
+    }
+    solid[w] = bits;
+    claimed[w] = 0u;
   }
 }
 
@@ -754,8 +794,10 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
-  size_t ctrl, live, omat32, scanA, gx, gy, gz, gori, gcell, act0, act1, gen0, gen1, liq, con, child, scanB, total;
-  NoAllocLayout(long long n, long long s) {
+  size_t ctrl, live, omat32, scanA, gx, gy, gz, gori, gcell, act0, act1, gen0, gen1, liq, con, child, solid, claimed,
+      scanB, total;
+  // n interior cells, s sites, `cells` ghost-inclusive cells
+  NoAllocLayout(long long n, long long s, long long cells) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
       const size_t at = o;
@@ -778,6 +820,8 @@ struct NoAllocLayout {
     liq = take((size_t)n * 4);
     con = take((size_t)n * 4);
     child = take((size_t)n * 4);
+    solid = take((size_t)solid_words(cells) * 4);
+    claimed = take((size_t)solid_words(cells) * 4);
     scanB = take((size_t)kStatusWords * 8);
     total = o;
   }
@@ -804,7 +848,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   if (device < 0 || device >= kNoAllocMaxDevices)
     return noalloc_fail(err, errlen, AMCA_ERR_ARG, "device ordinal out of range", nullptr);
   const long long n = (long long)p->nx * p->ny * p->nz;
-  const NoAllocLayout lay(n, nsites);
+  const NoAllocLayout lay(n, nsites, (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2));
   if (lay.total > kNoAllocScratchBytes) {
     char detail[160];
     snprintf(detail, sizeof detail, "needs %zu bytes of scratch for %lld cells and %lld sites, limit is %zu",
@@ -880,6 +924,8 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.liq = (uint32_t *)(base + lay.liq);
   d.con = (uint32_t *)(base + lay.con);
   d.child = (uint32_t *)(base + lay.child);
+  d.solid = (uint32_t *)(base + lay.solid);
+  d.claimed = (uint32_t *)(base + lay.claimed);
   d.scanB = (unsigned long long *)(base + lay.scanB);
   // everything that must start at zero is cleared here: the array keeps the
   // previous call's contents
@@ -915,7 +961,7 @@ cudaError_t plain_envelope_eval(long long n, const double *l2g, const double *gc
 }
 
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s) {
-  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.grid, d.ncells);
+  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.solid, d.claimed, d.grid, d.ncells);
   return cudaGetLastError();
 }
 

@@ -3,6 +3,11 @@
 //
 // HBM layout (one realm):
 //   orient      u32[(nx+2)(ny+2)(nz+2)]  cellOrientationID_, ghost-inclusive, reference index order
+//   solid       1 bit per cell (+2 words): solid before the current generation; the
+//               claim phase's liquidity test reads this (L2-resident) instead of orient
+//   claimed     1 bit per cell (+2 words): set with every claim. A claimed cell is
+//               captured in that generation and never liquid again, so stale bits
+//               are never looked at and the map is never cleared during a run
 //   site_*      nucleation sites sorted by cell id: cell i32, dTc f64, live u8
 //   omat/omat32 per orientation: local->global matrix, 9 x f64 and 9 x f32
 //   g*          envelope table by id (capacity = interior cells), written once per
@@ -94,6 +99,8 @@ struct PlainDevice {
   float coord_err;  // bound on FP64 cell-centre rounding, per component
   // arrays
   uint32_t *orient;
+  uint32_t *solid;    // 1 bit per cell: solid at the start of the current generation (ghosts included)
+  uint32_t *claimed;  // 1 bit per cell: some envelope claimed it (only ever read on cells still liquid)
   int64_t ncells;
   const int32_t *site_cell;
   const double *site_dtc;
@@ -113,8 +120,12 @@ struct PlainDevice {
 };
 
 // Fill the orientation field: -1 interior, 0 on the ghost layer
-// (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833).
+// (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833),
+// and the solid bitmap to match.
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s);
+
+// Words of the solid bitmap for `ncells` cells.
+AMCA_HD long long solid_words(long long ncells) { return (ncells + 31) / 32 + 2; }
 
 // Blocks of the persistent kernel that fit on the device at once.
 int plain_persistent_grid(int device);

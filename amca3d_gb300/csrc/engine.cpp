@@ -187,6 +187,8 @@ struct amca_t {
     d.liq = alloc<uint32_t>(d.gcap);
     d.con = alloc<uint32_t>(d.gcap);
     d.child = alloc<uint32_t>(d.gcap);
+    d.solid = alloc<uint32_t>(solid_words(d.ncells));
+    d.claimed = alloc<uint32_t>(solid_words(d.ncells));
     const int64_t ntA = 2 * kStatusWords, ntB = kStatusWords;
     d.scanA = alloc<unsigned long long>(ntA);
     d.scanB = alloc<unsigned long long>(ntB);
