@@ -197,8 +197,8 @@ typedef struct {
  * ((nx+2)(ny+2)(nz+2) cells, filled by this call). The run's other state
  * lives in one static device array of 32 MiB, which every GPU that loads the
  * library holds until the process exits; grids that need more (about
- * 68 bytes per interior cell plus 45 per site, i.e. roughly 480,000 interior
- * cells) are rejected with AMCA_ERR_ARG and a message.
+ * 172 bytes per interior cell plus 37 per site and 100 KB, i.e. roughly
+ * 190,000 interior cells) are rejected with AMCA_ERR_ARG and a message.
  *
  * The first call on a device looks up the array's device address (the host
  * name of the array is not a device address); make that first call before
