@@ -190,3 +190,184 @@ def config_uniform_320() -> PlainCase:
                      surface=(surface_density_for_sites(4000, cells, h), 2.0, 0.5),
                      bulk=(bulk_density_for_sites(20000, cells, h), 3.0, 1.0),
                      seed=1, t_dot=-50.0, time_step=0.001, termination_time=1.0e4)
+
+
+@dataclasses.dataclass
+class RemeltCase:
+    """One FE-coupled remelting run: a ``finite_element`` realm that replays
+    nodal temperature frames from a text file and a
+    ``cellular_automata_remelting`` realm, coupled by ``transfers``
+    (CA/src/CafeSolver.cpp:40-137, CA/src/FiniteElementManager.cpp:66-142,
+    CA/src/MapVoxelManager.cpp:62-89,
+    CA/src/CellularAutomataManager_3DRemelting.cpp:51-76)."""
+
+    name: str
+    cells: Tuple[int, int, int]
+    cell_size: float
+    origin: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    frames_file: str = "./frames.txt"
+    length_scale: float = 1.0
+    time_scale: float = 1.0
+    lines_for_title: int = 4
+    lines_for_subtitle: int = 5
+    offset: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    bin_size: Tuple[int, int, int] = (5, 5, 5)
+    tolerance: float = 1.0e-16
+    max_iterations: int = 20
+    void_temperature: Optional[float] = None
+    surface: Tuple[float, float, float] = (0.0, 0.5, 0.1)
+    bulk: Tuple[float, float, float] = (0.0, 10.0, 1.0)
+    nucleation: bool = False
+    seed: int = 0
+    melting_temperature: float = 1700.0
+    solidus_temperature: float = 1600.0
+    min_nucleation_temperature: Optional[float] = None
+    a: Tuple[float, float, float] = (0.0, 2.03e-4, 0.0)
+    has_been_melted: bool = False
+    cutoff_factor: Optional[float] = 4.0
+    microstructure: str = "random"
+    load_seeds: bool = False
+    output_microstructure_file: Optional[str] = None
+    shuffle_vtr: bool = False
+    termination_time: float = 1.0
+    time_step: float = 1.0e-6
+    time_step_factor: float = 0.4
+    time_step_factor_ca: Optional[float] = None
+    output_base: str = "./Results/Grains"
+    output_frequency: int = 100000
+    output_variables: Sequence[str] = ("grain_orientation",)
+
+    @property
+    def n_interior(self) -> int:
+        return self.cells[0] * self.cells[1] * self.cells[2]
+
+    @property
+    def n_ghost(self) -> int:
+        return (self.cells[0] + 2) * (self.cells[1] + 2) * (self.cells[2] + 2)
+
+    def to_yaml(self) -> str:
+        nx, ny, nz = self.cells
+        ns, mus, sgs = self.surface
+        nv, muv, sgv = self.bulk
+        a1, a2, a3 = self.a
+        tr = [f"     bin_size: [{self.bin_size[0]}, {self.bin_size[1]}, {self.bin_size[2]}]",
+              f"     tolerance: {_num(self.tolerance)}",
+              f"     max_iterations: {self.max_iterations}"]
+        if self.void_temperature is not None:
+            tr.append(f"     void_temperature: {_num(self.void_temperature)}")
+        phys = [f"        melting_temperature: {_num(self.melting_temperature)}",
+                f"        solidus_temperature: {_num(self.solidus_temperature)}"]
+        if self.min_nucleation_temperature is not None:
+            phys.append(f"        minimum_temperature_for_nucleation: {_num(self.min_nucleation_temperature)}")
+        phys += [f"        a1: {_num(a1)}", f"        a2: {_num(a2)}", f"        a3: {_num(a3)}"]
+        opts = ["         - random_type:", "             rejection_sampling: no"]
+        if self.shuffle_vtr:
+            opts.append("             shuffer_vtr_grain_ID: yes")
+        opts += ["         - phase_state:",
+                 f"             has_been_melted: {'yes' if self.has_been_melted else 'no'}"]
+        if self.cutoff_factor is not None:
+            opts += ["         - cell_grain_length_cutoff_factor:",
+                     f"             factor_value: {_num(self.cutoff_factor)}"]
+        if self.output_microstructure_file:
+            opts += ["         - output_microstructure_information:",
+                     f"             file_name: {self.output_microstructure_file}"]
+        opts += ["         - load_microstructure_information:",
+                 f"             file_name: {self.microstructure}"]
+        if self.load_seeds:
+            opts.append("             load_seeds: yes")
+        opts += ["         - criterion_to_activate_grain:",
+                 f"             using_nucleation_seed: {'yes' if self.nucleation else 'no'}"]
+        ti = [f"      termination_time: {_num(self.termination_time)}",
+              f"      time_step: {_num(self.time_step)}",
+              f"      time_step_factor: {_num(self.time_step_factor)}"]
+        if self.time_step_factor_ca is not None:
+            ti.append(f"      time_step_factor_ca: {_num(self.time_step_factor_ca)}")
+        outv = "\n".join(f"        - {v}" for v in self.output_variables)
+        return f"""# {self.name} (seed {self.seed})
+simulations:
+  - name: {self.name}
+    time_integrator: ti_1
+
+solvers:
+   - cellular_automata
+   - finite_element_method
+
+transfers:
+   - name: fe_ca
+{chr(10).join(tr)}
+
+realms:
+
+  - name: realm0
+    type: finite_element
+    dimension: 3
+    mesh: {self.frames_file}
+
+    solution_options:
+       name: my_options
+       options:
+         - load_data_from_file:
+             theta: theta
+             for_whole_time: yes
+             length_scale: {_num(self.length_scale)}
+             time_scale: {_num(self.time_scale)}
+             lines_for_title: {self.lines_for_title}
+             lines_for_subtitle: {self.lines_for_subtitle}
+             x_offset: {_num(self.offset[0])}
+             y_offset: {_num(self.offset[1])}
+             z_offset: {_num(self.offset[2])}
+
+    output:
+      output_data_base_name: ./Results/FEM
+      output_frequency: 100000000
+      output_variables:
+        - temperature
+
+  - name: realm1
+    type: cellular_automata_remelting
+    dimension: 3
+
+    domain:
+      type: cubic
+      original_point: [{_num(self.origin[0])}, {_num(self.origin[1])}, {_num(self.origin[2])}]
+
+    discretization:
+      cell_size: {_num(self.cell_size)}
+      number_cells: [{nx}, {ny}, {nz}]
+
+    nucleation_rules:
+      - surface:
+          type: Gaussian
+          site_density: {_num(ns)}
+          mean: {_num(mus)}
+          standard_deviation: {_num(sgs)}
+
+      - bulk:
+          type: Gaussian
+          site_density: {_num(nv)}
+          mean: {_num(muv)}
+          standard_deviation: {_num(sgv)}
+
+    problem_physics:
+        type: RappazGandin
+{chr(10).join(phys)}
+
+    solution_options:
+       name: my_options
+       options:
+{chr(10).join(opts)}
+
+    output:
+      output_data_base_name: {self.output_base}
+      output_frequency: {self.output_frequency}
+      output_variables:
+{outv}
+
+time_integrators:
+  - standard_time_integrator:
+      name: ti_1
+{chr(10).join(ti)}
+      realms:
+        - realm0
+        - realm1
+"""

@@ -77,6 +77,68 @@ int amca_oracle_is_captured(const double l2g[9], const double gc[3], double leng
 void amca_oracle_capture(const double l2g[9], const double gc[3], double length, double h, double trunc_coeff,
                          double new_info[4]);
 
+/* ---------------------------------------------------------------------
+ * FE-coupled remelting realm (CafeSolver weak coupling at np=1):
+ * FiniteElementManager replaying text frames (LoadDataFromFile.cpp),
+ * MapVoxelManager voxel tagging and trilinear interpolation
+ * (MapVoxelManager.cpp), CellularAutomataManager_3DRemelting.
+ * --------------------------------------------------------------------- */
+typedef struct {
+  /* CA grid */
+  int nx, ny, nz;
+  double x0, y0, z0, h;
+  /* problem_physics (ProblemPhysics.cpp:58-102) */
+  double Tm, Ts, Tnuc_min;
+  double a1, a2, a3, b1, b2, b3;
+  /* CA options */
+  double time_step_factor_ca; /* time_step_factor_ca, default 0.2 */
+  double trunc_coeff;         /* Octahedron truncation coefficient */
+  double cutoff_factor;       /* cell_grain_length_cutoff_factor (default 1e8), times h */
+  int initial_melted;         /* phase_state.has_been_melted (default yes) */
+  int nucleation;             /* criterion_to_activate_grain.using_nucleation_seed */
+  double ns, mu_s, sigma_s, nv, mu_v, sigma_v;
+  unsigned seed;
+  int shuffle_vtr;
+  const char *microstructure; /* NULL: random (one grain per interior cell); else restart file path */
+  int load_seeds;
+  /* transfers (MapVoxelManager.cpp:62-89) */
+  int bin[3];
+  double tolerance;
+  int max_iter;
+  double void_temperature;
+  /* finite_element realm (FiniteElementManager.cpp:66-142) */
+  const char *frames;         /* frame file path */
+  int title_lines, subtitle_lines;
+  double length_scale, time_scale;
+  double offset[3];
+  /* time integrator (CafeSolver.cpp:102-131) */
+  double final_time;
+} amca_oracle_remelt_params;
+
+typedef struct {
+  int steps;
+  double time;
+  double last_dt;
+  int64_t num_grains, num_orient, num_sites, tests;
+  int64_t nodes, elements, frames_read;
+  int frames_exhausted;       /* 1 if the run ended on the end of the frame file */
+} amca_oracle_remelt_result;
+
+/* Run the coupled loop to final_time or the end of the frames (max_steps < 0:
+ * no limit). Ghost-inclusive outputs (any may be NULL): orientation, grain,
+ * temperature, melted, cooling, liquid-neighbour flags. When dump_path is
+ * non-NULL, appends the state after every CA step in the record layout of
+ * oracle/ref_probe/state_dump.cpp. Returns 0, or <0 with a message in err. */
+int amca_oracle_run_remelt(const amca_oracle_remelt_params *p, int max_steps, const char *dump_path,
+                           int32_t *orient_out, int32_t *grain_out, double *temp_out, uint8_t *melted_out,
+                           uint8_t *cooling_out, uint8_t *flag_out, amca_oracle_remelt_result *res, char *err,
+                           int errlen);
+
+/* MapVoxelManager::is_in_element (MapVoxelManager.cpp:487-699) for one hex
+ * (8 node coordinates, reference node order) and point. */
+int amca_oracle_is_in_element(const double node_xyz[24], const double point[3], double tolerance, int max_iter,
+                              double para[3]);
+
 #ifdef __cplusplus
 }
 #endif
