@@ -27,7 +27,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libamca3d.so")
 
 AMCA_OK = 0
-FIELD_IDS = {"orientation_id": 0, "grain_id": 1, "site_undercooling": 2}
+FIELD_IDS = {"orientation_id": 0, "grain_id": 1, "site_undercooling": 2, "temperature": 3, "melted": 4,
+             "cooling": 5, "liquid_neighbour": 6}
+FIELD_DTYPES = {"orientation_id": np.int32, "grain_id": np.int32, "site_undercooling": np.float64,
+                "temperature": np.float64, "melted": np.uint8, "cooling": np.uint8, "liquid_neighbour": np.uint8}
 _ERRORS = {-1: "bad argument", -2: "deck parse error", -3: "CUDA error", -4: "call out of order",
            -5: "device-side error", -6: "output error"}
 
@@ -64,7 +67,19 @@ class Stats(ctypes.Structure):
 EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
-           "amca_plain_run_noalloc", "amca_last_error", "amca_destroy")
+           "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_last_error",
+           "amca_destroy")
+
+
+class Rosenthal(ctypes.Structure):
+    """amca_rosenthal of include/amca3d.h: synthetic frames generated on the GPU."""
+    _fields_ = [("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double), ("nodes", ctypes.c_int32 * 3),
+                ("frames", ctypes.c_int32), ("length_scale", ctypes.c_double), ("frame_dt", ctypes.c_double),
+                ("time_scale", ctypes.c_double), ("time_offset", ctypes.c_double), ("power", ctypes.c_double),
+                ("absorptivity", ctypes.c_double), ("speed", ctypes.c_double), ("conductivity", ctypes.c_double),
+                ("diffusivity", ctypes.c_double), ("t0", ctypes.c_double), ("t_cap", ctypes.c_double),
+                ("x_start", ctypes.c_double), ("y_line", ctypes.c_double), ("z_top", ctypes.c_double),
+                ("void_above_set", ctypes.c_int32), ("void_above", ctypes.c_double), ("t_void", ctypes.c_double)]
 
 
 class PlainParams(ctypes.Structure):
@@ -120,6 +135,10 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_plain_run_noalloc.argtypes = [i, ctypes.POINTER(PlainParams), vp, vp, ctypes.c_int64, vp, vp, i, vp,
                                            ctypes.POINTER(PlainResult), ctypes.c_char_p, ctypes.c_size_t]
     lib.amca_plain_run_noalloc.restype = i
+    lib.amca_set_fe_frames.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), vp, ctypes.c_int32, vp, vp]
+    lib.amca_set_fe_frames.restype = i
+    lib.amca_set_rosenthal_frames.argtypes = [vp, ctypes.POINTER(Rosenthal)]
+    lib.amca_set_rosenthal_frames.restype = i
     lib.amca_last_error.argtypes = [vp]
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]
@@ -236,10 +255,31 @@ class CellularAutomataRealm:
         self._check(self._lib.amca_get_stats(self._h, ctypes.byref(s)))
         return s.as_dict()
 
+    def set_fe_frames(self, nodes, coords: np.ndarray, times: np.ndarray, theta: np.ndarray) -> None:
+        """FE-coupled decks: frames from memory in the file's units (replaces the
+        deck's frame file)."""
+        nn = (ctypes.c_int32 * 3)(*[int(v) for v in nodes])
+        coords = np.ascontiguousarray(coords, np.float64)
+        times = np.ascontiguousarray(times, np.float64)
+        theta = np.ascontiguousarray(theta, np.float64)
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        self._check(self._lib.amca_set_fe_frames(self._h, nn, ptr(coords), len(times), ptr(times), ptr(theta)))
+
+    def set_rosenthal_frames(self, **kw) -> None:
+        """FE-coupled decks: frames generated on the GPU (fields of amca_rosenthal)."""
+        r = Rosenthal()
+        for k, v in kw.items():
+            if k in ("origin", "nodes"):
+                for a in range(3):
+                    getattr(r, k)[a] = v[a]
+            else:
+                setattr(r, k, v)
+        self._check(self._lib.amca_set_rosenthal_frames(self._h, ctypes.byref(r)))
+
     def field(self, name: str = "orientation_id", out: Optional[np.ndarray] = None) -> np.ndarray:
         fid = FIELD_IDS[name]
         n = self.cells_with_ghosts
-        dtype = np.float64 if name == "site_undercooling" else np.int32
+        dtype = FIELD_DTYPES[name]
         if out is None:
             out = np.empty(n, dtype=dtype)
         assert out.dtype == dtype and out.size == n and out.flags.c_contiguous

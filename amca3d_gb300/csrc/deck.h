@@ -53,6 +53,48 @@ struct PlainConfig {
 // message naming the key (and line) on a missing key or unsupported content.
 PlainConfig parse_plain_deck(const std::string &yaml_text);
 
+// finite_element realm replaying temperature frames from a text file
+// (FiniteElementManager::load, CA/src/FiniteElementManager.cpp:66-142).
+struct FeConfig {
+  std::string mesh;               // frame file (realm key "mesh")
+  int title_lines = -1;           // load_data_from_file.lines_for_title (no default in the reference)
+  int subtitle_lines = -1;        // lines_for_subtitle (>= 4; the 4th holds step and time)
+  double length_scale = 1.0, time_scale = 1.0;
+  double offset[3] = {0.0, 0.0, 0.0};
+  bool whole_time = false;        // for_whole_time: replay frames instead of solving
+  int output_frequency = 0;       // VtuManager output_frequency
+};
+
+// transfers (MapVoxelManager::load, CA/src/MapVoxelManager.cpp:26-89)
+struct TransferConfig {
+  int bin[3] = {10, 10, 10};
+  double tolerance = 1.0e-16;
+  int max_iter = 20;
+  double void_temperature = -1.0e8;
+};
+
+// FE-coupled remelting deck: solvers [cellular_automata, finite_element_method],
+// a finite_element realm and a cellular_automata_remelting realm
+// (CafeSolver::load, CA/src/CafeSolver.cpp:40-137;
+// CellularAutomataManager_3DRemelting::load, CA/src/CellularAutomataManager_3DRemelting.cpp:51-76).
+struct RemeltConfig {
+  PlainConfig ca;                 // grid, nucleation rules, physics, CA options, VTR output
+  FeConfig fe;
+  TransferConfig tr;
+  bool nucleation = false;        // criterion_to_activate_grain.using_nucleation_seed (setNucleationSite_)
+  bool initial_melted = true;     // phase_state.has_been_melted (setInitialStatedAsMelted_)
+  bool random_micro = true;       // load_microstructure_information.file_name: random (or no option)
+  std::string micro_file;         // restart file stem (rank suffix "0.txt" appended)
+  bool load_seeds = false;        // load_microstructure_information.load_seeds
+  double time_step_factor_fe = 0; // time_step_factor (read by CafeSolver, unused when replaying frames)
+};
+
+// true when the deck selects both the CA and the FE solver (CafeSolver)
+bool deck_is_coupled(const std::string &yaml_text);
+
+// Parse an FE-coupled remelting deck (throws like parse_plain_deck).
+RemeltConfig parse_remelt_deck(const std::string &yaml_text);
+
 // The reference's output variable names (CA/include/CafeMacro.h:16-24).
 int output_variable_id(const std::string &name);
 

@@ -17,22 +17,14 @@
 #include "../../include/amca3d.h"
 #include "ca_plain.h"
 #include "deck.h"
+#include "engine_remelt.h"
+#include "errors.h"
 #include "host_init.h"
 #include "writers.h"
 
 using namespace amca;
 
 namespace {
-
-struct CudaError : std::runtime_error {
-  explicit CudaError(const std::string &m) : std::runtime_error(m) {}
-};
-struct DeviceError : std::runtime_error {
-  explicit DeviceError(const std::string &m) : std::runtime_error(m) {}
-};
-struct StateError : std::runtime_error {
-  explicit StateError(const std::string &m) : std::runtime_error(m) {}
-};
 
 #define CK(call)                                                                                      \
   do {                                                                                                \
@@ -49,6 +41,7 @@ struct amca_t {
   amca_opts opts{};
   std::string workdir;
   PlainConfig cfg;
+  std::unique_ptr<RemeltRealm> rm;  // set for FE-coupled remelting decks
   bool initialized = false;
   // host tables
   SiteSet sites;
@@ -438,7 +431,13 @@ int amca_create(const char *yaml_text, const amca_opts *opts, amca_t **out) {
   h->device = h->opts.device;
   if (h->opts.workdir) h->workdir = h->opts.workdir;
   try {
-    h->cfg = parse_plain_deck(yaml_text);
+    if (deck_is_coupled(yaml_text)) {
+      RemeltConfig rc = parse_remelt_deck(yaml_text);
+      h->cfg = rc.ca;
+      h->rm.reset(new RemeltRealm(rc, h->opts, h->workdir));
+    } else {
+      h->cfg = parse_plain_deck(yaml_text);
+    }
   } catch (const std::exception &e) {
     g_create_error = e.what();
     return AMCA_ERR_PARSE;
@@ -465,22 +464,25 @@ int amca_get_grid(const amca_t *h, int32_t cells[3], double origin[3], double *c
 
 int amca_prepare(amca_t *h) {
   if (!h) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->prepare(); });
   return guarded(h, [&] { h->prepare(); });
 }
 
 int amca_get_sites(const amca_t *h, int32_t *cells, double *dtc, size_t cap, size_t *n_out) {
   if (!h) return AMCA_ERR_ARG;
-  if (!h->prepared) return AMCA_ERR_STATE;
-  const size_t n = h->sites.cell.size();
+  if (h->rm ? !h->rm->prepared() : !h->prepared) return AMCA_ERR_STATE;
+  const SiteSet &st = h->rm ? h->rm->sites() : h->sites;
+  const size_t n = st.cell.size();
   if (n_out) *n_out = n;
   const size_t m = std::min(n, cap);
-  if (cells && m) memcpy(cells, h->sites.cell.data(), m * sizeof(int32_t));
-  if (dtc && m) memcpy(dtc, h->sites.dtc.data(), m * sizeof(double));
+  if (cells && m) memcpy(cells, st.cell.data(), m * sizeof(int32_t));
+  if (dtc && m) memcpy(dtc, st.dtc.data(), m * sizeof(double));
   return AMCA_OK;
 }
 
 int amca_initialize(amca_t *h) {
   if (!h) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->initialize(); });
   return guarded(h, [&] {
     if (h->initialized) throw StateError("amca_initialize called twice");
     h->initialize();
@@ -489,6 +491,11 @@ int amca_initialize(amca_t *h) {
 
 int amca_step(amca_t *h, double *dt_out) {
   if (!h) return AMCA_ERR_ARG;
+  if (h->rm)
+    return guarded(h, [&] {
+      h->rm->run(1);
+      if (dt_out) *dt_out = h->rm->ctrl().dt;
+    });
   return guarded(h, [&] {
     h->run(1);
     if (dt_out) *dt_out = h->ctrl.dt;
@@ -497,11 +504,52 @@ int amca_step(amca_t *h, double *dt_out) {
 
 int amca_run(amca_t *h, int max_steps) {
   if (!h) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->run(max_steps); });
   return guarded(h, [&] { h->run(max_steps); });
+}
+
+int amca_set_fe_frames(amca_t *h, const int32_t nodes[3], const double *coords, int32_t nframes, const double *times,
+                       const double *theta) {
+  if (!h || !nodes || !coords || !times || !theta) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_set_fe_frames needs an FE-coupled deck");
+    h->rm->set_frames(nodes, coords, nframes, times, theta);
+  });
+}
+
+int amca_set_rosenthal_frames(amca_t *h, const amca_rosenthal *p) {
+  if (!h || !p) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_set_rosenthal_frames needs an FE-coupled deck");
+    RosenthalParams r{};
+    for (int a = 0; a < 3; ++a) {
+      r.origin[a] = p->origin[a];
+      r.nodes[a] = p->nodes[a];
+    }
+    r.spacing = p->spacing;
+    r.length_scale = p->length_scale;
+    r.frame_dt = p->frame_dt;
+    r.time_scale = p->time_scale;
+    r.power = p->power;
+    r.absorptivity = p->absorptivity;
+    r.speed = p->speed;
+    r.conductivity = p->conductivity;
+    r.diffusivity = p->diffusivity;
+    r.t0 = p->t0;
+    r.t_cap = p->t_cap;
+    r.x_start = p->x_start;
+    r.y_line = p->y_line;
+    r.z_top = p->z_top;
+    r.void_above_set = p->void_above_set;
+    r.void_above = p->void_above;
+    r.t_void = p->t_void;
+    h->rm->set_rosenthal(r, p->frames, p->time_offset);
+  });
 }
 
 int amca_get_field(amca_t *h, int field, void *dst, size_t bytes) {
   if (!h || !dst) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->get_field(field, dst, bytes); });
   return guarded(h, [&] {
     if (!h->initialized) throw StateError("amca_get_field before amca_initialize");
     const size_t n = (size_t)h->dev.ncells;
@@ -526,6 +574,12 @@ int amca_get_field(amca_t *h, int field, void *dst, size_t bytes) {
 
 int amca_get_orientations(amca_t *h, double *euler, size_t cap, size_t *n_out, int all) {
   if (!h) return AMCA_ERR_ARG;
+  if (h->rm)
+    return guarded(h, [&] {
+      if (all && !h->rm->prepared()) throw StateError("amca_get_orientations(all=1) before amca_prepare");
+      const size_t n = h->rm->orientations(euler, cap, all);
+      if (n_out) *n_out = n;
+    });
   return guarded(h, [&] {
     if (all && !h->prepared) throw StateError("amca_get_orientations(all=1) before amca_prepare");
     const size_t n = all ? h->otab.euler.size() / 3 : (size_t)std::max<long long>(0, h->ctrl.n_orient);
@@ -536,13 +590,14 @@ int amca_get_orientations(amca_t *h, double *euler, size_t cap, size_t *n_out, i
 
 int amca_write_outputs(amca_t *h) {
   if (!h) return AMCA_ERR_ARG;
-  int rc = guarded(h, [&] { h->write_outputs(); });
+  int rc = h->rm ? guarded(h, [&] { h->rm->write_outputs(); }) : guarded(h, [&] { h->write_outputs(); });
   if (rc == AMCA_ERR_ARG) rc = AMCA_ERR_IO;
   return rc;
 }
 
 int amca_get_stats(amca_t *h, amca_stats *s) {
   if (!h || !s) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->stats(s); });
   return guarded(h, [&] {
     memset(s, 0, sizeof *s);
     const PlainCtrl &c = h->ctrl;
@@ -584,6 +639,11 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
 
 int amca_final_grain_count(amca_t *h, int32_t *count) {
   if (!h || !count) return AMCA_ERR_ARG;
+  if (h->rm)
+    return guarded(h, [&] {
+      if (!h->rm->initialized()) throw StateError("amca_final_grain_count before amca_initialize");
+      *count = h->rm->final_grain_count();
+    });
   return guarded(h, [&] {
     if (!h->initialized) throw StateError("amca_final_grain_count before amca_initialize");
     *count = h->final_grain_count(h->orient_field());
@@ -592,6 +652,7 @@ int amca_final_grain_count(amca_t *h, int32_t *count) {
 
 int amca_reset(amca_t *h) {
   if (!h) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->reset(); });
   return guarded(h, [&] { h->reset(); });
 }
 

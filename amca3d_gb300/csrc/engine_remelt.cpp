@@ -1,0 +1,641 @@
+// engine_remelt.cpp — see engine_remelt.h.
+#include "engine_remelt.h"
+
+#include "errors.h"
+
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <stdexcept>
+#include <thread>
+
+namespace amca {
+
+namespace {
+
+#define RCK(call)                                                                                       \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess) throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+inline bool is_ghost(int I, int J, int K, int nxg, int nyg, int nzg) {
+  return I == 0 || I == nxg - 1 || J == 0 || J == nyg - 1 || K == 0 || K == nzg - 1;
+}
+
+// the device's ordered key of a double (atomicMin of minimum temperatures)
+unsigned long long host_dkey(double x) {
+  unsigned long long b;
+  memcpy(&b, &x, 8);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+}  // namespace
+
+RemeltRealm::RemeltRealm(RemeltConfig cfg, const amca_opts &opts, std::string workdir)
+    : cfg_(std::move(cfg)), opts_(opts), workdir_(std::move(workdir)) {
+  device_ = opts_.device;
+}
+
+RemeltRealm::~RemeltRealm() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (void *p : allocs_) cudaFree(p);
+  if (hostvel_) cudaFreeHost(hostvel_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <typename T>
+T *RemeltRealm::alloc(size_t n) {
+  void *p = nullptr;
+  RCK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+  allocs_.push_back(p);
+  return (T *)p;
+}
+
+void RemeltRealm::h2d(void *dst, const void *src, size_t bytes) {
+  if (!bytes) return;
+  RCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream_));
+  h2d_bytes_ += (int64_t)bytes;
+}
+void RemeltRealm::d2h(void *dst, const void *src, size_t bytes) {
+  if (!bytes) return;
+  RCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream_));
+  d2h_bytes_ += (int64_t)bytes;
+}
+
+std::string RemeltRealm::path(const std::string &p) const {
+  if (p.empty() || p[0] == '/' || workdir_.empty()) return p;
+  return workdir_ + "/" + p;
+}
+
+void RemeltRealm::set_frames(const int32_t nodes[3], const double *coords, int64_t nframes, const double *times,
+                             const double *theta) {
+  if (initialized_) throw StateError("frames must be set before amca_initialize");
+  frames_ = fe_frames_from_arrays(nodes, coords, nframes, times, theta, cfg_.fe);
+  frames_src_ = 1;
+}
+
+void RemeltRealm::set_rosenthal(const RosenthalParams &p, int nframes, double time_offset) {
+  if (initialized_) throw StateError("frames must be set before amca_initialize");
+  if (nframes < 2) throw std::invalid_argument("at least two frames");
+  for (int a = 0; a < 3; ++a)
+    if (p.nodes[a] < 2) throw std::invalid_argument("at least 2 nodes per axis");
+  ros_ = p;
+  ros_nframes_ = nframes;
+  ros_toff_ = time_offset;
+  // node coordinates and frame times exactly as the text reader would hold them
+  FeFrames fr;
+  for (int a = 0; a < 3; ++a) fr.nn[a] = p.nodes[a];
+  fr.nnodes = (int64_t)p.nodes[0] * p.nodes[1] * p.nodes[2];
+  fr.coord.resize(3 * (size_t)fr.nnodes);
+  for (int64_t n = 0; n < fr.nnodes; ++n) {
+    const int64_t I[3] = {n % p.nodes[0], (n / p.nodes[0]) % p.nodes[1], n / ((int64_t)p.nodes[0] * p.nodes[1])};
+    for (int d = 0; d < 3; ++d) {
+      double x = p.origin[d] + p.spacing * (double)I[d];
+      x += cfg_.fe.offset[d];
+      x *= cfg_.fe.length_scale;
+      fr.coord[3 * n + d] = x;
+    }
+  }
+  fr.times.resize((size_t)nframes);
+  const double t0 = time_offset + 0 * p.frame_dt;
+  fr.times[0] = 0.0;
+  for (int f = 1; f < nframes; ++f) fr.times[f] = ((time_offset + f * p.frame_dt) - t0) * cfg_.fe.time_scale;
+  fr.nframes = nframes;
+  frames_ = std::move(fr);
+  frames_src_ = 2;
+}
+
+void RemeltRealm::prepare() {
+  if (prepared_) return;
+  const PlainConfig &c = cfg_.ca;
+  if (cfg_.load_seeds) throw std::invalid_argument("load_microstructure_information.load_seeds is not supported");
+  rng_.reset(new GlibcRand(opts_.seed));  // srand in the CA manager's constructor (CellularAutomataManager_3D.cpp:40)
+  const int nxg = c.nx + 2, nyg = c.ny + 2, nzg = c.nz + 2;
+  const int64_t nxyg = (int64_t)nxg * nyg, N = nxyg * nzg;
+  orient0_.assign((size_t)N, -1);
+  grain0_.assign((size_t)N, -1);
+  melted0_.assign((size_t)N, cfg_.initial_melted ? 1 : 0);
+  rec0_.assign(4 * (size_t)N, 0.0);
+  gori0_.assign((size_t)N, -1);
+  site_field_.assign((size_t)N, -1.0);
+  grain_cell_.clear();
+  auto centre = [&](int64_t cell, double out[3]) {
+    const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
+    out[0] = centre_coord(c.x0, c.h, I);
+    out[1] = centre_coord(c.y0, c.h, J);
+    out[2] = centre_coord(c.z0, c.h, K);
+  };
+  if (cfg_.random_micro) {
+    // random_microstructure_information (CellularAutomataManager_3D.cpp:1929-1984):
+    // one orientation and one grain per interior cell, in cell order
+    const int64_t M = (int64_t)c.nx * c.ny * c.nz;
+    otab_ = make_orientations(M, *rng_);
+    int64_t q = 0;
+    for (int64_t cell = 0; cell < N; ++cell) {
+      const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
+      if (is_ghost(I, J, K, nxg, nyg, nzg)) continue;
+      orient0_[cell] = (int32_t)q;
+      grain0_[cell] = (int32_t)q;
+      gori0_[cell] = (int32_t)q;
+      centre(cell, &rec0_[4 * cell]);
+      grain_cell_.push_back((int32_t)cell);
+      ++q;
+    }
+    n_init_orient_ = M;
+    n_init_grains_ = M;
+    if (c.shuffle_vtr) mapped_vtr_ = make_mapped_ids(N, true, *rng_);
+    expected_grains_ = 0;
+  } else {
+    // load_microstructure_information + retrieve_grain_information_before_simulation
+    // (CellularAutomataManager_3DRemelting.cpp:164-332)
+    RestartData r = read_restart(path(cfg_.micro_file));
+    if (r.ncells != N)
+      throw std::runtime_error("Error : microstructure information file is not fit the current domain size");
+    if (!cfg_.nucleation && c.shuffle_vtr) mapped_vtr_ = make_mapped_ids(r.expected, true, *rng_);
+    otab_ = orientations_from_euler(r.euler);
+    orient0_ = r.orient;
+    grain0_ = r.grain;
+    melted0_ = r.melted;
+    grain_cell_ = r.gcell;
+    std::vector<uint8_t> owned((size_t)r.ngrains, 0);
+    for (int64_t cell = 0; cell < N; ++cell) {
+      const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
+      if (is_ghost(I, J, K, nxg, nyg, nzg)) {
+        orient0_[cell] = -1;
+        continue;
+      }
+      const int32_t g = grain0_[cell];
+      if (g >= 0) {
+        if (g >= r.ngrains) throw std::runtime_error("restart cell refers to a grain that is not listed");
+        if (owned[g] || r.gcell[g] != cell)
+          throw std::runtime_error("restart grains must each belong to the one interior cell that refers to them");
+        owned[g] = 1;
+        centre(cell, &rec0_[4 * cell]);  // grain centre reset to its cell centre, length 0 (:289-296)
+        gori0_[cell] = r.gori[g];
+      }
+      if (orient0_[cell] > -1) continue;
+      if (g < 0) throw std::runtime_error("restart cell has neither an orientation nor a grain");
+      orient0_[cell] = r.gori[g];
+    }
+    n_init_orient_ = r.norient;
+    n_init_grains_ = r.ngrains;
+    expected_grains_ = r.expected;
+  }
+  if (cfg_.nucleation) {
+    sites_ = make_sites(c, *rng_);
+    for (size_t i = 0; i < sites_.cell.size(); ++i) site_field_[sites_.cell[i]] = sites_.dtc[i];
+    if (c.shuffle_vtr) {  // global_mapped_grain_ID_plus (CellularAutomataManager_3DRemelting.cpp:873-931)
+      const int64_t surf = ((int64_t)c.nx * c.ny + (int64_t)c.nx * (c.nz - 2) + (int64_t)(c.ny - 2) * (c.nz - 2)) * 2;
+      const int64_t bulk = (int64_t)c.nx * c.ny * c.nz;
+      const int ss = (int)(std::round(c.ns * surf * (c.h * c.h)) + 0.5);
+      const int sb = (int)(std::round(c.nv * bulk * (c.h * c.h * c.h)) + 0.5);
+      mapped_vtr_ = make_mapped_ids((int64_t)ss + sb + expected_grains_, true, *rng_);
+    }
+    expected_grains_ += sites_.surface_sites + sites_.bulk_sites;
+    // the nucleation orientation stream, extended on demand
+    const int64_t K = std::max<int64_t>(4 * (int64_t)sites_.cell.size(), 1024);
+    append_orientations(otab_, make_orientations(K, *rng_));
+  }
+  prepared_ = true;
+}
+
+void RemeltRealm::upload_initial_state() {
+  const int64_t N = dev_.ncells;
+  h2d(dev_.orient, orient0_.data(), N * 4);
+  h2d(dev_.grain, grain0_.data(), N * 4);
+  h2d(dev_.melted, melted0_.data(), N);
+  std::vector<double> x((size_t)N), y((size_t)N), z((size_t)N), l((size_t)N);
+  for (int64_t i = 0; i < N; ++i) {
+    x[i] = rec0_[4 * i];
+    y[i] = rec0_[4 * i + 1];
+    z[i] = rec0_[4 * i + 2];
+    l[i] = rec0_[4 * i + 3];
+  }
+  h2d(dev_.gx, x.data(), N * 8);
+  h2d(dev_.gy, y.data(), N * 8);
+  h2d(dev_.gz, z.data(), N * 8);
+  h2d(dev_.glen, l.data(), N * 8);
+  h2d(dev_.gori, gori0_.data(), N * 4);
+  RCK(cudaMemsetAsync(dev_.gdx, 0, N * 4, stream_));
+  RCK(cudaMemsetAsync(dev_.gdy, 0, N * 4, stream_));
+  RCK(cudaMemsetAsync(dev_.gdz, 0, N * 4, stream_));
+  RCK(cudaMemsetAsync(dev_.flagbits, 0, ((N + 31) / 32) * 4, stream_));
+  RCK(remelt_init_theta(dev_, stream_));
+  hostvel_->seq_req = 0;
+  hostvel_->seq_done = 0;
+  h2d(dev_.ctrl, &ctrl0_, sizeof ctrl0_);
+  ctrl_ = ctrl0_;
+  RCK(cudaStreamSynchronize(stream_));
+  // the host vectors above are staged through pageable memory; the sync keeps them alive
+}
+
+void RemeltRealm::initialize() {
+  if (initialized_) throw StateError("amca_initialize called twice");
+  prepare();
+  const PlainConfig &c = cfg_.ca;
+  RCK(cudaSetDevice(device_));
+  RCK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  RCK(cudaEventCreate(&ev0_));
+  RCK(cudaEventCreate(&ev1_));
+  if (frames_src_ == 0) frames_ = read_fe_frames(path(cfg_.fe.mesh), cfg_.fe);
+  nframes_ = frames_src_ == 2 ? ros_nframes_ : frames_.nframes;
+  Grid g{};
+  g.nx = c.nx;
+  g.ny = c.ny;
+  g.nz = c.nz;
+  g.nxg = c.nx + 2;
+  g.nyg = c.ny + 2;
+  g.nzg = c.nz + 2;
+  g.nxyg = g.nxg * g.nyg;
+  g.x0 = c.x0;
+  g.y0 = c.y0;
+  g.z0 = c.z0;
+  g.h = c.h;
+  RemeltDevice &d = dev_;
+  d.g = g;
+  d.ncells = (int64_t)g.nxyg * g.nzg;
+  const int64_t N = d.ncells;
+  d.Tm = c.Tm;
+  d.Ts = c.Ts;
+  d.Tnuc = c.Tmin_nuc;
+  d.a1 = c.a1;
+  d.a2 = c.a2;
+  d.a3 = c.a3;
+  d.b1 = (int)c.b1;
+  d.b2 = (int)c.b2;
+  d.b3 = (int)c.b3;
+  d.tsf_ca = c.time_step_factor;
+  d.h = c.h;
+  d.trunc = c.trunc_coeff;
+  d.cutoff = c.length_cutoff_factor * c.h;  // cellGrainLegnthCutoff_ *= h_ (Remelting.cpp:89)
+  d.final_time = c.final_time;
+  d.void_t = cfg_.tr.void_temperature;
+  d.h32 = (float)c.h;
+  {
+    double cmax = 0;
+    const double o[3] = {c.x0, c.y0, c.z0};
+    const int nn[3] = {g.nxg, g.nyg, g.nzg};
+    for (int a = 0; a < 3; ++a) cmax = std::max(cmax, std::fabs(o[a]) + (nn[a] + 1) * c.h);
+    d.coord_err = (float)(std::ldexp(cmax, -49) + 1e-30);
+  }
+  // --- FE -> CA map (MapVoxelManager::execute_with_focus_on_CA_region) ---
+  for (int a = 0; a < 3; ++a) d.nn[a] = frames_.nn[a];
+  d.nnodes = frames_.nnodes;
+  d.nelem = frames_.nelem();
+  int32_t *tag = alloc<int32_t>(N);
+  double *pc = alloc<double>(3 * N);
+  unsigned long long *tcount = alloc<unsigned long long>(2);
+  {
+    VoxelMapPlan plan = plan_voxel_map(frames_, c, cfg_.tr);
+    std::vector<void *> tmp;
+    auto up = [&](const void *src, size_t bytes) {
+      void *p = nullptr;
+      RCK(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
+      tmp.push_back(p);
+      h2d(p, src, bytes);
+      return p;
+    };
+    TagPlan tp{};
+    memcpy(tp.mm, plan.mm, sizeof tp.mm);
+    memcpy(tp.dbin, plan.dbin, sizeof tp.dbin);
+    memcpy(tp.nbin, plan.nbin, sizeof tp.nbin);
+    tp.bin_start = (const int64_t *)up(plan.bin_start.data(), plan.bin_start.size() * 8);
+    tp.bin_elems = (const int32_t *)up(plan.bin_elems.data(), plan.bin_elems.size() * 4);
+    tp.erange = (const double *)up(plan.erange.data(), plan.erange.size() * 8);
+    tp.coord = (const double *)up(frames_.coord.data(), frames_.coord.size() * 8);
+    for (int a = 0; a < 3; ++a) tp.nn[a] = frames_.nn[a];
+    tp.tolerance = cfg_.tr.tolerance;
+    tp.max_iter = cfg_.tr.max_iter;
+    tp.counts = tcount;
+    RCK(cudaMemsetAsync(tcount, 0, 16, stream_));
+    RCK(remelt_tag_voxels(g, tp, tag, pc, stream_));
+    unsigned long long counts[2] = {0, 0};
+    d2h(counts, tcount, 16);
+    RCK(cudaStreamSynchronize(stream_));
+    for (void *p : tmp) cudaFree(p);
+    if (counts[0] == 0)
+      throw std::runtime_error(
+          "Error: a proc has no corrsponding FEM mesh!! Maybe decrease the number of multi-core parallel can help.");
+    d.force_exact = counts[1] ? 1 : 0;
+  }
+  d.tag = tag;
+  d.pc = pc;
+  // --- frames ---
+  double *frames = alloc<double>((size_t)nframes_ * d.nnodes);
+  if (frames_src_ == 2) {
+    RCK(remelt_rosenthal_frames(ros_, (int)nframes_, frames, stream_));
+  } else {
+    h2d(frames, frames_.theta.data(), frames_.theta.size() * 8);
+  }
+  double *ftime = alloc<double>(nframes_);
+  h2d(ftime, frames_.times.data(), nframes_ * 8);
+  d.frames = frames;
+  d.frame_time = ftime;
+  d.nframes = (int)nframes_;
+  d.bad_frame = (int)frames_.bad_frame;
+  for (int i = 0; i < 3; ++i) d.theta[i] = alloc<double>(d.nnodes);
+  d.emax = alloc<double>(d.nelem);
+  d.emin = alloc<double>(d.nelem);
+  d.evoid = alloc<uint8_t>(d.nelem);
+  // --- cells ---
+  d.orient = alloc<int32_t>(N);
+  d.grain = alloc<int32_t>(N);
+  d.melted = alloc<uint8_t>(N);
+  d.flagbits = alloc<uint32_t>((N + 31) / 32);
+  d.T = alloc<double>(N);
+  d.gx = alloc<double>(N);
+  d.gy = alloc<double>(N);
+  d.gz = alloc<double>(N);
+  d.glen = alloc<double>(N);
+  d.gori = alloc<int32_t>(N);
+  d.gdx = alloc<float>(N);
+  d.gdy = alloc<float>(N);
+  d.gdz = alloc<float>(N);
+  d.list_cap = N;
+  d.liq = alloc<int32_t>(N);
+  d.flagged[0] = alloc<int32_t>(N);
+  d.flagged[1] = alloc<int32_t>(N);
+  d.claimed = alloc<int32_t>(N);
+  d.newkey = alloc<unsigned long long>(kNewGrainCap);
+  d.newcell = alloc<int32_t>(kNewGrainCap);
+  d.fvel = alloc<double>(N);
+  d.hard_idx = alloc<int32_t>(N);
+  d.hard_T = alloc<double>(N);
+  {
+    void *hv = nullptr;
+    RCK(cudaHostAlloc(&hv, sizeof(HostVelocity), cudaHostAllocMapped));
+    hostvel_ = (HostVelocity *)hv;
+    memset(hostvel_, 0, sizeof(HostVelocity));
+    void *dv = nullptr;
+    RCK(cudaHostGetDevicePointer(&dv, hv, 0));
+    d.host = (HostVelocity *)dv;
+  }
+  // --- orientations and sites ---
+  orient_cap_ = (int64_t)otab_.euler.size() / 3;
+  omat_ = alloc<double>(9 * orient_cap_);
+  omat32_ = alloc<float>(9 * orient_cap_);
+  h2d(omat_, otab_.l2g.data(), otab_.l2g.size() * 8);
+  h2d(omat32_, otab_.l2g32.data(), otab_.l2g32.size() * 4);
+  d.omat = omat_;
+  d.omat32 = omat32_;
+  d.orient_cap = orient_cap_;
+  d.nsites = (int)sites_.cell.size();
+  int32_t *sc = alloc<int32_t>(d.nsites);
+  double *sd = alloc<double>(d.nsites);
+  h2d(sc, sites_.cell.data(), sites_.cell.size() * 4);
+  h2d(sd, sites_.dtc.data(), sites_.dtc.size() * 8);
+  d.site_cell = sc;
+  d.site_dtc = sd;
+  d.ctrl = alloc<RemeltCtrl>(1);
+  // --- control block: CafeSolver::time_integration_weak_coupling set-up (CafeSolver.cpp:182-184) ---
+  RemeltCtrl c0{};
+  c0.ts1 = frames_.times[0];
+  c0.ts0 = frames_.times[1];
+  c0.f_new = 1;
+  c0.f_next = 2;
+  c0.theta_init = 1;
+  c0.dT_FE = c0.ts0 - c0.ts1;  // FiniteElementManager::setup_integration
+  c0.max_ts = c0.dT_FE;        // CellularAutomataManager::setup_integration
+  c0.n_orient = n_init_orient_;
+  c0.n_grains = n_init_grains_;
+  c0.minT_key = host_dkey(c.Tm);
+  ctrl0_ = c0;
+  upload_initial_state();
+  blocks_ = remelt_persistent_grid(device_);
+  if (blocks_ <= 0) throw CudaError("no co-resident blocks for the persistent remelting kernel");
+  vtr_.configure(c.output, workdir_);
+  initialized_ = true;
+}
+
+void RemeltRealm::reset() {
+  if (!initialized_) throw StateError("amca_reset before amca_initialize");
+  upload_initial_state();
+  kernel_ms_ = 0.0;
+  launches_ = 0;
+  vtr_ = VtrSeries();
+  vtr_.configure(cfg_.ca.output, workdir_);
+}
+
+void RemeltRealm::sync_ctrl() {
+  d2h(&ctrl_, dev_.ctrl, sizeof ctrl_);
+  RCK(cudaStreamSynchronize(stream_));
+  if (ctrl_.error) {
+    static const char *msg[] = {"",
+                                "grid barrier wait timed out",
+                                "fail to read next step temperature file, please check title of line!!",
+                                "more new grain objects in one step than the library supports (16384)",
+                                "time ratio error: timeRatio is less then 0",
+                                "work list overflow",
+                                "the host did not answer a velocity request in time"};
+    const int e = ctrl_.error;
+    throw DeviceError(std::string("remelting kernel stopped: ") + (e > 0 && e < 7 ? msg[e] : "unknown error"));
+  }
+}
+
+void RemeltRealm::extend_orientations() {
+  const int64_t K = std::max<int64_t>(4 * (int64_t)sites_.cell.size(), 1024);
+  OrientationTable more = make_orientations(K, *rng_);
+  append_orientations(otab_, more);
+  const int64_t cap = (int64_t)otab_.euler.size() / 3;
+  double *m = alloc<double>(9 * cap);
+  float *m32 = alloc<float>(9 * cap);
+  RCK(cudaMemcpyAsync(m, omat_, 9 * orient_cap_ * 8, cudaMemcpyDeviceToDevice, stream_));
+  RCK(cudaMemcpyAsync(m32, omat32_, 9 * orient_cap_ * 4, cudaMemcpyDeviceToDevice, stream_));
+  h2d(m + 9 * orient_cap_, more.l2g.data(), more.l2g.size() * 8);
+  h2d(m32 + 9 * orient_cap_, more.l2g32.data(), more.l2g32.size() * 4);
+  RCK(cudaStreamSynchronize(stream_));
+  omat_ = m;
+  omat32_ = m32;
+  orient_cap_ = cap;
+  dev_.omat = m;
+  dev_.omat32 = m32;
+  dev_.orient_cap = cap;
+}
+
+// The reference's growth velocity with glibc's pow
+// (ProblemPhysics_RappazGandin1993::compute_growth_velocity_with_temperature_input,
+// CA/src/ProblemPhysics.cpp:142-158), for the arguments the kernel cannot round itself.
+static double reference_velocity(const PlainConfig &c, double T) {
+  const double dT = c.Tm - T;
+  double v = 0.0;
+  if (dT > 0) {
+    v = c.a1 * std::pow(dT, c.b1) + c.a2 * std::pow(dT, c.b2) + c.a3 * std::pow(dT, c.b3);
+    if (v < 0.0) v = 0.0;
+  }
+  return v;
+}
+
+// Runs beside a kernel launch: answers the kernel's velocity requests.
+void RemeltRealm::serve_velocities(const volatile int *stop) {
+  HostVelocity *hv = hostvel_;
+  unsigned last = __atomic_load_n(&hv->seq_done, __ATOMIC_ACQUIRE);
+  unsigned idle = 0;
+  while (!*stop) {
+    const unsigned r = __atomic_load_n(&hv->seq_req, __ATOMIC_ACQUIRE);
+    if (r == last) {
+      if (++idle > 4096) std::this_thread::yield();
+      continue;
+    }
+    idle = 0;
+    const unsigned n = __atomic_load_n(&hv->n, __ATOMIC_ACQUIRE);
+    for (unsigned i = 0; i < n && i < (unsigned)kHostVelCap; ++i) hv->v[i] = reference_velocity(cfg_.ca, hv->T[i]);
+    __atomic_store_n(&hv->seq_done, r, __ATOMIC_RELEASE);
+    last = r;
+  }
+}
+
+void RemeltRealm::run(long long max_steps) {
+  if (!initialized_) throw StateError("amca_run before amca_initialize");
+  const long long target = max_steps < 0 ? (1ll << 60) : ctrl_.step + max_steps;
+  while (ctrl_.status != kRemeltFinalTime && ctrl_.status != kRemeltFramesEnd && ctrl_.step < target) {
+    const int running = kRemeltRunning;
+    h2d(&dev_.ctrl->status, &running, sizeof running);
+    volatile int stop = 0;
+    std::thread server([&] { serve_velocities(&stop); });
+    RCK(cudaEventRecord(ev0_, stream_));
+    cudaError_t le = remelt_run_steps(dev_, target, blocks_, stream_);
+    if (le == cudaSuccess) le = cudaEventRecord(ev1_, stream_);
+    if (le == cudaSuccess) le = cudaStreamSynchronize(stream_);
+    stop = 1;
+    server.join();
+    if (le != cudaSuccess) throw CudaError(std::string("remelting kernel: ") + cudaGetErrorString(le));
+    ++launches_;
+    sync_ctrl();
+    float ms = 0.f;
+    RCK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    kernel_ms_ += ms;
+    if (ctrl_.status == kRemeltNeedOrient) {
+      extend_orientations();
+      continue;
+    }
+    if (ctrl_.status == kRemeltStepLimit) break;
+  }
+}
+
+void RemeltRealm::get_field(int field, void *dst, size_t bytes) {
+  if (!initialized_) throw StateError("amca_get_field before amca_initialize");
+  const size_t N = (size_t)dev_.ncells;
+  auto need = [&](size_t b) {
+    if (bytes != b) throw std::invalid_argument("amca_get_field: wrong byte count for this field");
+  };
+  switch (field) {
+    case AMCA_FIELD_ORIENTATION_ID:
+      need(N * 4);
+      d2h(dst, dev_.orient, N * 4);
+      RCK(cudaStreamSynchronize(stream_));
+      return;
+    case AMCA_FIELD_GRAIN_ID:
+      need(N * 4);
+      d2h(dst, dev_.grain, N * 4);
+      RCK(cudaStreamSynchronize(stream_));
+      return;
+    case AMCA_FIELD_SITE_UNDERCOOLING:
+      need(N * 8);
+      memcpy(dst, site_field_.data(), N * 8);
+      return;
+    case AMCA_FIELD_MELTED:
+      need(N);
+      d2h(dst, dev_.melted, N);
+      RCK(cudaStreamSynchronize(stream_));
+      return;
+    case AMCA_FIELD_TEMPERATURE:
+    case AMCA_FIELD_COOLING:
+    case AMCA_FIELD_LIQUID_NEIGHBOUR: {
+      const bool t = field == AMCA_FIELD_TEMPERATURE;
+      need(t ? N * 8 : N);
+      if (ctrl_.step == 0) {  // before the first step: nullMatTemp_, false, false
+        if (t) {
+          double *o = (double *)dst;
+          for (size_t i = 0; i < N; ++i) o[i] = -1.0;
+        } else {
+          memset(dst, 0, N);
+        }
+        return;
+      }
+      void *buf = nullptr;
+      RCK(cudaMalloc(&buf, t ? N * 8 : N));
+      cudaError_t e = remelt_state_fields(dev_, ctrl_.step, ctrl_.dt_prev, t ? (double *)buf : nullptr,
+                                          field == AMCA_FIELD_COOLING ? (uint8_t *)buf : nullptr,
+                                          field == AMCA_FIELD_LIQUID_NEIGHBOUR ? (uint8_t *)buf : nullptr, stream_);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dst, buf, t ? N * 8 : N, cudaMemcpyDeviceToHost, stream_);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+      cudaFree(buf);
+      if (e != cudaSuccess) throw CudaError(std::string("state fields: ") + cudaGetErrorString(e));
+      d2h_bytes_ += (int64_t)(t ? N * 8 : N);
+      return;
+    }
+    default:
+      throw std::invalid_argument("amca_get_field: unknown field");
+  }
+}
+
+size_t RemeltRealm::orientations(double *euler, size_t cap, int all) const {
+  const size_t n = all ? otab_.euler.size() / 3 : (size_t)std::max<long long>(0, ctrl_.n_orient);
+  if (euler) memcpy(euler, otab_.euler.data(), std::min(n, cap) * 3 * sizeof(double));
+  return n;
+}
+
+double RemeltRealm::algorithmic_bytes() const {
+  // per step: 8 B per interior cell (orientation + element tag); per exact
+  // temperature 33 B (parametric coordinates 24, temperature 8, flag 1); per
+  // listed liquid cell 104 B (26 neighbour states); per flagged cell 364 B
+  // (grain record 48, 26 x (state 4 + temperature 8)); per capture 80 B
+  // (winner record 36, new record 36, state 8); per node 24 B (two frame
+  // values, one write) and per element 17 B (bounds).
+  const double steps = (double)ctrl_.step;
+  const double M = (double)cfg_.ca.nx * cfg_.ca.ny * cfg_.ca.nz;
+  return 8 * M * steps + 33 * (double)ctrl_.exact_T + 104 * (double)ctrl_.liquid + 364 * (double)ctrl_.flagged +
+         80 * (double)ctrl_.captures + (24 * (double)dev_.nnodes + 17 * (double)dev_.nelem) * steps;
+}
+
+void RemeltRealm::stats(amca_stats *s) const {
+  memset(s, 0, sizeof *s);
+  const RemeltCtrl &c = ctrl_;
+  s->step = c.step;
+  s->time = c.time;
+  s->dt = c.dt;
+  s->liquid_cells = -1;
+  s->grains = c.n_grains;
+  s->orientations = c.n_orient;
+  s->active = (int64_t)c.flagged;
+  s->sites = (int64_t)sites_.cell.size();
+  s->cells = (int64_t)cfg_.ca.nx * cfg_.ca.ny * cfg_.ca.nz;
+  s->tests = (int64_t)c.tests;
+  s->tests_fp64 = (int64_t)c.tests64;
+  s->generations = (int64_t)c.exact_T;
+  s->done = (c.status == kRemeltFinalTime || c.status == kRemeltFramesEnd) ? 1 : 0;
+  s->kernel_ms = kernel_ms_;
+  s->launches = launches_;
+  s->sites_scanned = (int64_t)c.melts;
+  s->nucleations = (int64_t)c.nucleations;
+  s->captures = (int64_t)c.captures;
+  s->active_grown = (int64_t)c.flagged;
+  s->grains_processed = (int64_t)c.liquid;
+  s->algorithmic_bytes = algorithmic_bytes();
+  s->h2d_bytes = h2d_bytes_;
+  s->d2h_bytes = d2h_bytes_;
+  for (int i = 0; i < 5; ++i) s->phase_ms[i] = c.ns_phase[i] * 1e-6;
+}
+
+int RemeltRealm::final_grain_count() {
+  std::vector<int32_t> o((size_t)dev_.ncells);
+  get_field(AMCA_FIELD_ORIENTATION_ID, o.data(), o.size() * 4);
+  const int64_t n = ctrl_.n_orient;
+  if (n <= 0) return 0;
+  std::vector<char> seen((size_t)n, 0);
+  for (int32_t v : o)
+    if (v > -1 && v < n) seen[v] = 1;
+  return (int)std::count(seen.begin(), seen.end(), 1);
+}
+
+void RemeltRealm::write_outputs() {
+  if (!initialized_) throw StateError("amca_write_outputs before amca_initialize");
+  throw std::invalid_argument("output files of the remelting realm are not written by this library yet");
+}
+
+}  // namespace amca

@@ -1,0 +1,109 @@
+// engine_remelt.h — host side of the FE-coupled remelting realm behind the C ABI.
+//
+// CafeSolver (CA/src/CafeSolver.cpp:40-219) with a finite_element realm that
+// replays frames and a cellular_automata_remelting realm: parse the deck, read
+// the frames and the restart file, draw the orientation stream and the sites
+// with the reference's libraries, build the FE -> CA map on the GPU, run the
+// persistent step kernel, and hand the reference's arrays back.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/amca3d.h"
+#include "deck.h"
+#include "fe_input.h"
+#include "host_init.h"
+#include "remelt.h"
+#include "writers.h"
+
+namespace amca {
+
+class RemeltRealm {
+ public:
+  RemeltRealm(RemeltConfig cfg, const amca_opts &opts, std::string workdir);
+  ~RemeltRealm();
+
+  const RemeltConfig &config() const { return cfg_; }
+  // frame sources other than the deck's mesh file (before initialize)
+  void set_frames(const int32_t nodes[3], const double *coords, int64_t nframes, const double *times,
+                  const double *theta);
+  void set_rosenthal(const RosenthalParams &p, int nframes, double time_offset);
+
+  void prepare();     // host tables: microstructure, sites, orientation stream
+  void initialize();  // device state, frames, FE -> CA map
+  void reset();       // back to the state right after initialize
+  void run(long long max_steps);
+  bool prepared() const { return prepared_; }
+  bool initialized() const { return initialized_; }
+
+  void get_field(int field, void *dst, size_t bytes);
+  size_t orientations(double *euler, size_t cap, int all) const;
+  void stats(amca_stats *s) const;
+  int final_grain_count();
+  void write_outputs();
+  const SiteSet &sites() const { return sites_; }
+  const RemeltCtrl &ctrl() const { return ctrl_; }
+  int64_t frames_count() const { return nframes_; }
+
+ private:
+  template <typename T>
+  T *alloc(size_t n);
+  void h2d(void *dst, const void *src, size_t bytes);
+  void d2h(void *dst, const void *src, size_t bytes);
+  void sync_ctrl();
+  void extend_orientations();
+  void upload_initial_state();
+  void serve_velocities(const volatile int *stop);
+  std::string path(const std::string &p) const;
+  double algorithmic_bytes() const;
+
+  RemeltConfig cfg_;
+  amca_opts opts_{};
+  std::string workdir_;
+  bool prepared_ = false, initialized_ = false;
+  // frame source
+  int frames_src_ = 0;  // 0 deck file, 1 arrays, 2 Rosenthal generator
+  FeFrames frames_;
+  RosenthalParams ros_{};
+  int ros_nframes_ = 0;
+  double ros_toff_ = 0.0;
+  int64_t nframes_ = 0;
+  // host tables
+  std::unique_ptr<GlibcRand> rng_;
+  OrientationTable otab_;          // initial orientations, then the nucleation stream
+  int64_t n_init_orient_ = 0;
+  int64_t n_init_grains_ = 0;
+  SiteSet sites_;
+  std::vector<int32_t> mapped_vtr_;
+  std::vector<int32_t> orient0_, grain0_;  // initial cell fields
+  std::vector<uint8_t> melted0_;
+  std::vector<double> rec0_;       // initial grain records per cell: x, y, z, length
+  std::vector<int32_t> gori0_;
+  std::vector<int32_t> grain_cell_;  // grain id -> owning cell (restart + created)
+  std::vector<double> site_field_;   // cellNucleationDT_
+  int64_t expected_grains_ = 0;
+  int64_t restart_sites_ = 0;
+  // device
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  std::vector<void *> allocs_;
+  RemeltDevice dev_{};
+  RemeltCtrl ctrl_{};
+  RemeltCtrl ctrl0_{};
+  int blocks_ = 0;
+  double kernel_ms_ = 0.0;
+  long long launches_ = 0;
+  int64_t h2d_bytes_ = 0, d2h_bytes_ = 0;
+  HostVelocity *hostvel_ = nullptr;  // mapped page-locked buffer of the velocity service
+  double *omat_ = nullptr;
+  float *omat32_ = nullptr;
+  int64_t orient_cap_ = 0;
+  VtrSeries vtr_;
+};
+
+}  // namespace amca

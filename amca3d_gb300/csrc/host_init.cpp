@@ -6,6 +6,7 @@
 #include <cstring>
 #include <random>
 #include <stdexcept>
+#include <thread>
 #include <unordered_map>
 
 namespace amca {
@@ -106,36 +107,83 @@ std::vector<int32_t> make_mapped_ids(int64_t n, bool shuffle, GlibcRand &rng) {
   return m;
 }
 
+void orientation_matrix(const double a[3], double m[9], float m32[9]) {
+  // Octahedron::set_coordinate_transformation_matrix (CA/src/Octahedron.cpp:282-310)
+  const double ca = std::cos(a[0]), sa = std::sin(a[0]);
+  const double cb = std::cos(a[1]), sb = std::sin(a[1]);
+  const double cg = std::cos(a[2]), sg = std::sin(a[2]);
+  m[0] = ca * cg - sa * cb * sg;
+  m[1] = -ca * sg - sa * cb * cg;
+  m[2] = sa * sb;
+  m[3] = sa * cg + ca * cb * sg;
+  m[4] = -sa * sg + ca * cb * cg;
+  m[5] = -ca * sb;
+  m[6] = sb * sg;
+  m[7] = sb * cg;
+  m[8] = cb;
+  for (int q = 0; q < 9; ++q) m32[q] = (float)m[q];
+}
+
+namespace {
+// Run body(lo, hi) over [0, n) on up to hardware_concurrency threads.
+template <typename F>
+void parallel_ranges(int64_t n, F body) {
+  unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+  if (n < 65536) nt = 1;
+  nt = (unsigned)std::min<int64_t>(nt, 64);
+  std::vector<std::thread> th;
+  const int64_t chunk = (n + nt - 1) / nt;
+  for (unsigned t = 1; t < nt; ++t) {
+    const int64_t lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo < hi) th.emplace_back([=] { body(lo, hi); });
+  }
+  body(0, std::min(n, chunk));
+  for (auto &x : th) x.join();
+}
+}  // namespace
+
 OrientationTable make_orientations(int64_t n, GlibcRand &rng) {
   const double kPi = 3.14159265358979323846;  // CellularAutomataManager_3D.cpp:24
   OrientationTable t;
   t.euler.resize((size_t)n * 3);
   t.l2g.resize((size_t)n * 9);
   t.l2g32.resize((size_t)n * 9);
-  for (int64_t o = 0; o < n; ++o) {
-    double U, V;
-    U = static_cast<double>(rng.next()) / RAND_MAX;
-    V = static_cast<double>(rng.next()) / RAND_MAX;
-    double *a = &t.euler[o * 3];
-    a[0] = U * 2 * kPi;
-    a[1] = std::acos(2 * V - 1);
-    a[2] = static_cast<double>(rng.next()) / RAND_MAX * 0.5 * kPi;
-    const double ca = std::cos(a[0]), sa = std::sin(a[0]);
-    const double cb = std::cos(a[1]), sb = std::sin(a[1]);
-    const double cg = std::cos(a[2]), sg = std::sin(a[2]);
-    double *m = &t.l2g[o * 9];
-    m[0] = ca * cg - sa * cb * sg;
-    m[1] = -ca * sg - sa * cb * cg;
-    m[2] = sa * sb;
-    m[3] = sa * cg + ca * cb * sg;
-    m[4] = -sa * sg + ca * cb * cg;
-    m[5] = -ca * sb;
-    m[6] = sb * sg;
-    m[7] = sb * cg;
-    m[8] = cb;
-    for (int q = 0; q < 9; ++q) t.l2g32[o * 9 + q] = (float)m[q];
-  }
+  // get_random_orientation_angle (CellularAutomataManager_3D.cpp:839-850):
+  // three rand() per orientation, in draw order; the trigonometry is
+  // independent per orientation and runs on all host threads.
+  std::vector<int32_t> r((size_t)n * 3);
+  for (int64_t q = 0; q < 3 * n; ++q) r[q] = rng.next();
+  parallel_ranges(n, [&](int64_t lo, int64_t hi) {
+    for (int64_t o = lo; o < hi; ++o) {
+      double U, V;
+      U = static_cast<double>(r[3 * o]) / RAND_MAX;
+      V = static_cast<double>(r[3 * o + 1]) / RAND_MAX;
+      double *a = &t.euler[o * 3];
+      a[0] = U * 2 * kPi;
+      a[1] = std::acos(2 * V - 1);
+      a[2] = static_cast<double>(r[3 * o + 2]) / RAND_MAX * 0.5 * kPi;
+      orientation_matrix(a, &t.l2g[o * 9], &t.l2g32[o * 9]);
+    }
+  });
   return t;
+}
+
+OrientationTable orientations_from_euler(const std::vector<double> &euler) {
+  OrientationTable t;
+  const int64_t n = (int64_t)euler.size() / 3;
+  t.euler = euler;
+  t.l2g.resize((size_t)n * 9);
+  t.l2g32.resize((size_t)n * 9);
+  parallel_ranges(n, [&](int64_t lo, int64_t hi) {
+    for (int64_t o = lo; o < hi; ++o) orientation_matrix(&t.euler[o * 3], &t.l2g[o * 9], &t.l2g32[o * 9]);
+  });
+  return t;
+}
+
+void append_orientations(OrientationTable &t, const OrientationTable &more) {
+  t.euler.insert(t.euler.end(), more.euler.begin(), more.euler.end());
+  t.l2g.insert(t.l2g.end(), more.l2g.begin(), more.l2g.end());
+  t.l2g32.insert(t.l2g32.end(), more.l2g32.begin(), more.l2g32.end());
 }
 
 }  // namespace amca

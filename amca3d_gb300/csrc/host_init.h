@@ -57,4 +57,11 @@ std::vector<int32_t> make_mapped_ids(int64_t n, bool shuffle, GlibcRand &rng);
 // Orientation stream: n orientations, 3 rand() values each, in draw order.
 OrientationTable make_orientations(int64_t n, GlibcRand &rng);
 
+// Matrices of given Euler angles (restart files).
+OrientationTable orientations_from_euler(const std::vector<double> &euler);
+void append_orientations(OrientationTable &t, const OrientationTable &more);
+
+// Octahedron::set_coordinate_transformation_matrix for one orientation.
+void orientation_matrix(const double euler[3], double l2g[9], float l2g32[9]);
+
 }  // namespace amca

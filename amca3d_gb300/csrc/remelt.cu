@@ -1,0 +1,1126 @@
+// remelt.cu — the FE-coupled remelting realm on one GB300.
+//
+// Reference (np = 1): CafeSolver::time_integration_weak_coupling
+// (CA/src/CafeSolver.cpp:178-219). Per step the reference
+//   1. re-interpolates every cell's temperature from the FE nodes, melts
+//      cells at or above the liquidus (or without material), updates the
+//      cooling and melted flags (CellularAutomataManager_3DRemelting.cpp:339-404);
+//   2. flags solid cells next to undercooled liquid (:484-542);
+//   3. nucleates at sites, then takes dt from the coldest flagged cell above
+//      the solidus (:656-727, :936-999);
+//   4. sweeps the interior in i-outer, j, k-inner order: every flagged cell
+//      grows its grain and captures liquid neighbours inside its octahedron;
+//      a captured cell is not swept again in the same step (:545-652, :807-847);
+//   5. advances the FE replay and interpolates nodal temperatures between two
+//      frames (LoadDataFromFile.cpp:207-313).
+//
+// GB300 design: one persistent cooperative kernel runs whole steps, five
+// phases per step separated by bounded grid barriers.
+//   A  full-grid pass over interior cells. A cell's temperature is a pure
+//      function of the node temperatures, so it is computed in FP64 only where
+//      a decision depends on it: liquid cells, and solid cells whose element's
+//      node maximum (plus a rounding margin) reaches the liquidus. Every other
+//      solid cell costs two 4-byte loads and an L2-resident element lookup.
+//      (GB300's FP64 rate is ~1/64 of its FP32 rate; this keeps the step
+//      bandwidth-bound.) Liquid cells that can flag neighbours go to a list.
+//   B  listed liquid cells set the flag bits of their solid neighbours; each
+//      newly flagged cell is appended to the flagged list.
+//   C  block 0 nucleates (sites in ascending order, block scan for ids);
+//      the other blocks apply the grain-length cutoff and take the minimum
+//      temperature over flagged cells (atomicMin on an ordered key).
+//   D  dt (uniform); every flagged cell grows its grain and tests its liquid
+//      neighbours; a containment claims the neighbour with atomicMin of
+//      INT_MIN + sweep position, so the smallest claim is the first capturing
+//      cell of the reference's sweep (captures do not cascade within a step).
+//   E  claimed cells take the winner's orientation and decentred envelope
+//      (FP64, reference operation order); the FE replay advances and the next
+//      step's node temperatures and element bounds are computed.
+// New grain objects (cells without one) get ids in sweep order: events
+// (sweep position, neighbour index) are sorted by block 0 after the step.
+#include <math.h>
+
+#include <algorithm>
+
+#include "remelt.h"
+
+namespace amca {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr unsigned long long kWaitNs = 5000000000ull;  // 5 s bound on any spin
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T ld_volatile(const T *p) {
+  return *(const volatile T *)p;
+}
+
+// Sense-counting grid barrier bounded in time; false when a wait ran out or
+// another block reported an error.
+__device__ bool grid_barrier(RemeltCtrl *c) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned gen = ld_acquire(&c->bar_gen);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&c->bar_count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = now_ns();
+      while (ld_acquire(&c->bar_gen) == gen) {
+        if (ld_volatile(&c->error) != 0) break;
+        if (now_ns() - t0 > kWaitNs) {
+          atomicCAS(&c->error, 0, kRemeltErrBarrier);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ld_volatile(&c->error) == 0;
+}
+
+__device__ unsigned block_exclusive_scan(unsigned v, unsigned *smem, unsigned *total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned w = lane < kWarps ? smem[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < kWarps; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kWarps) smem[lane] = w;
+  }
+  __syncthreads();
+  const unsigned before = warp > 0 ? smem[warp - 1] : 0u;
+  *total = smem[kWarps - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// Order-preserving key of a double (for atomicMin); NaN never reaches it.
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_inv(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ double ulp_of(double p) {  // |p| normal
+  const long long e = (__double_as_longlong(fabs(p)) >> 52) & 0x7ff;
+  return e > 52 ? __longlong_as_double((e - 52) << 52) : 4.9406564584124654e-324;
+}
+
+// x^b for b in {1, 2, 3}, correctly rounded (square and cube through exact
+// two-products). `near` is raised when the exact power lies within 0.02 ulp
+// of a rounding midpoint: there glibc's pow, whose error bound is 0.52 ulp,
+// may round to the other neighbour. pow(x, 1) == x holds for every double.
+__device__ double ipow_checked(double x, int b, bool &near) {
+  if (b == 1) return x;
+  const double p = x * x;
+  const double e = __fma_rn(x, x, -p);
+  if (b == 2) {
+    const double u = ulp_of(p);
+    near = near || fabs(fabs(e) - 0.5 * u) <= 0.02 * u;
+    return p;
+  }
+  const double q1 = p * x;
+  const double r1 = __fma_rn(p, x, -q1);
+  const double q2 = e * x;
+  const double r2 = __fma_rn(e, x, -q2);
+  const double t = (r1 + q2) + r2;
+  const double c = q1 + t;
+  const double rem = (q1 - c) + t;
+  const double u = ulp_of(c);
+  near = near || fabs(fabs(rem) - 0.5 * u) <= 0.02 * u;
+  return c;
+}
+
+// compute_growth_velocity_with_temperature_input (ProblemPhysics.cpp:142-158).
+// `hard`: a term with a nonzero coefficient could round differently in glibc.
+__device__ double velocity(const RemeltDevice &d, double T, bool &hard) {
+  const double dT = d.Tm - T;
+  double v = 0.0;
+  hard = false;
+  if (dT > 0) {
+    bool n1 = false, n2 = false, n3 = false;
+    const double p1 = ipow_checked(dT, d.b1, n1);
+    const double p2 = ipow_checked(dT, d.b2, n2);
+    const double p3 = ipow_checked(dT, d.b3, n3);
+    hard = (d.a1 != 0 && n1) || (d.a2 != 0 && n2) || (d.a3 != 0 && n3);
+    v = d.a1 * p1 + d.a2 * p2 + d.a3 * p3;
+    if (v < 0.0) v = 0.0;
+  }
+  return v;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_sys(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_sys(unsigned *p, unsigned v) {
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Block 0: have the host evaluate the velocities flagged `hard` this step
+// (and the velocity at the minimum temperature when `min_hard`), in chunks
+// of the mapped buffer. Every wait is bounded; false on a timeout.
+__device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned nh, bool min_hard, double minT) {
+  __shared__ int s_ok;
+  const unsigned total = nh + (min_hard ? 1u : 0u);
+  if (threadIdx.x == 0) s_ok = d.host != nullptr;
+  __syncthreads();
+  for (unsigned base = 0; base < total && s_ok; base += kHostVelCap) {
+    const unsigned cnt = min(total - base, (unsigned)kHostVelCap);
+    for (unsigned k = threadIdx.x; k < cnt; k += blockDim.x) {
+      const unsigned i = base + k;
+      d.host->T[k] = i < nh ? d.hard_T[i] : minT;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned seq = c->host_seq + 1;
+      c->host_seq = seq;
+      d.host->n = cnt;
+      __threadfence_system();
+      st_release_sys(&d.host->seq_req, seq);
+      const unsigned long long t0 = now_ns();
+      while (ld_acquire_sys(&d.host->seq_done) != seq) {
+        if (now_ns() - t0 > kWaitNs) {
+          atomicCAS(&c->error, 0, kRemeltErrHost);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+      c->host_calls += 1;
+      c->host_vel += cnt;
+    }
+    __syncthreads();
+    if (!s_ok) break;
+    for (unsigned k = threadIdx.x; k < cnt; k += blockDim.x) {
+      const unsigned i = base + k;
+      const double v = ld_volatile(&d.host->v[k]);
+      if (i < nh)
+        d.fvel[d.hard_idx[i]] = v;
+      else
+        c->vmin = v;
+    }
+    __syncthreads();
+  }
+  __threadfence();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ void elem_nodes(const int nn[3], int64_t e, int64_t nid[8]) {
+  const int64_t ncx = nn[0] - 1, ncy = nn[1] - 1;
+  const int64_t i = e % ncx, j = (e / ncx) % ncy, k = e / (ncx * ncy);
+  const int64_t nxy = (int64_t)nn[0] * nn[1];
+  nid[0] = nxy * k + (int64_t)nn[0] * j + i;
+  nid[1] = nid[0] + 1;
+  nid[2] = nid[1] + nn[0];
+  nid[3] = nid[2] - 1;
+#pragma unroll
+  for (int l = 4; l < 8; l++) nid[l] = nid[l - 4] + nxy;
+}
+
+// MapVoxelManager::evaluate_temperature (MapVoxelManager.cpp:746-799):
+// false (T untouched) without an element or next to a void node.
+__device__ bool eval_T(const RemeltDevice &d, const double *th, int64_t c, double &T) {
+  const int32_t e = d.tag[c];
+  if (e < 0) return false;
+  int64_t nid[8];
+  elem_nodes(d.nn, e, nid);
+  const double nullMat = d.void_t + 0.00001;
+  double t[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    t[i] = th[nid[i]];
+    if (t[i] < nullMat) return false;
+  }
+  const double xi = d.pc[3 * c], eta = d.pc[3 * c + 1], zeta = d.pc[3 * c + 2];
+  double s[8];
+  s[0] = 0.125 * (1.0 - eta) * (1.0 - xi) * (1.0 - zeta);
+  s[1] = 0.125 * (1.0 - eta) * (1.0 + xi) * (1.0 - zeta);
+  s[2] = 0.125 * (1.0 + eta) * (1.0 + xi) * (1.0 - zeta);
+  s[3] = 0.125 * (1.0 + eta) * (1.0 - xi) * (1.0 - zeta);
+  s[4] = 0.125 * (1.0 - eta) * (1.0 - xi) * (1.0 + zeta);
+  s[5] = 0.125 * (1.0 - eta) * (1.0 + xi) * (1.0 + zeta);
+  s[6] = 0.125 * (1.0 + eta) * (1.0 + xi) * (1.0 + zeta);
+  s[7] = 0.125 * (1.0 + eta) * (1.0 - xi) * (1.0 + zeta);
+  double v = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) v += s[i] * t[i];
+  T = v;
+  return true;
+}
+
+// thetaArray_ update of pseudo_single_integration_step (LoadDataFromFile.cpp:281-290)
+__device__ __forceinline__ double lerp_node(double th0, double th1, double ratio, double null_mat) {
+  if (th0 <= null_mat) return null_mat;
+  if (th1 <= null_mat) return th0;
+  return ratio * (th0 - th1) + th1;
+}
+
+__device__ __forceinline__ bool ghost(const Grid &g, int I, int J, int K) {
+  return I == 0 || I == g.nxg - 1 || J == 0 || J == g.nyg - 1 || K == 0 || K == g.nzg - 1;
+}
+
+// Bounds of one element for the current node temperatures: the interpolated
+// temperature is a convex combination of the 8 node values (all parametric
+// coordinates lie in [-1, 1]), so it cannot exceed their maximum by more than
+// the rounding of the 8 products and sums (< 2^-48 relative); the margin
+// used is 2^-44 of the largest magnitude. NaN forces the exact path.
+__device__ void element_bounds(const RemeltDevice &d, int64_t e, const double t[8]) {
+  const double nullMat = d.void_t + 0.00001;
+  bool vo = false, nan = false;
+  double mx = -INFINITY, mn = INFINITY, mg = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const double v = t[i];
+    if (v < nullMat) vo = true;
+    if (v != v) nan = true;
+    mx = v > mx ? v : mx;
+    mn = v < mn ? v : mn;
+    const double a = fabs(v);
+    mg = a > mg ? a : mg;
+  }
+  const double margin = ldexp(mg, -44);
+  d.evoid[e] = vo ? 1 : 0;
+  d.emax[e] = (nan || d.force_exact) ? INFINITY : mx + margin;
+  d.emin[e] = (nan || d.force_exact) ? -INFINITY : mn - margin;
+}
+
+// nullMatTemp_ + 0.01: below it a cell counts as without material in the
+// liquid-neighbour pass (Remelting.cpp:504-507)
+__device__ __forceinline__ double null_plus() { return -1.0 + 0.01; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// FE -> CA map: MapVoxelManager::tag_voxels + is_in_element (MapVoxelManager.cpp:357-699)
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ bool in_element(const double X[8], const double Y[8], const double Z[8], double xp, double yp, double zp,
+                           double tol, int max_iter, double para[3]) {
+  const double *x = X, *y = Y, *z = Z;
+  double j[9], f[3], s[8];
+  double xinew = 0.5, etanew = 0.5, zetanew = 0.5;
+  double xi = 0.5, eta = 0.5, zeta = 0.5;
+  double dd[3] = {1.0, 1.0, 1.0};
+  int i = 0;
+  do {
+    j[0] = -(1.0 - eta) * (1.0 - zeta) * x[1] - (1.0 + eta) * (1.0 - zeta) * x[2] +
+           (1.0 + eta) * (1.0 - zeta) * x[3] + (1.0 - eta) * (1.0 + zeta) * x[4] -
+           (1.0 - eta) * (1.0 + zeta) * x[5] - (1.0 + eta) * (1.0 + zeta) * x[6] +
+           (1.0 + eta) * (1.0 + zeta) * x[7];
+    j[1] = (1.0 + xi) * (1.0 - zeta) * x[1] - (1.0 + xi) * (1.0 - zeta) * x[2] - (1.0 - xi) * (1.0 - zeta) * x[3] +
+           (1.0 - xi) * (1.0 + zeta) * x[4] + (1.0 + xi) * (1.0 + zeta) * x[5] - (1.0 + xi) * (1.0 + zeta) * x[6] -
+           (1.0 - xi) * (1.0 + zeta) * x[7];
+    j[2] = (1.0 - eta) * (1.0 + xi) * x[1] + (1.0 + eta) * (1.0 + xi) * x[2] + (1.0 + eta) * (1.0 - xi) * x[3] -
+           (1.0 - eta) * (1.0 - xi) * x[4] - (1.0 - eta) * (1.0 + xi) * x[5] - (1.0 + eta) * (1.0 + xi) * x[6] -
+           (1.0 + eta) * (1.0 - xi) * x[7];
+    j[3] = -(1.0 - eta) * (1.0 - zeta) * y[1] - (1.0 + eta) * (1.0 - zeta) * y[2] +
+           (1.0 + eta) * (1.0 - zeta) * y[3] + (1.0 - eta) * (1.0 + zeta) * y[4] -
+           (1.0 - eta) * (1.0 + zeta) * y[5] - (1.0 + eta) * (1.0 + zeta) * y[6] +
+           (1.0 + eta) * (1.0 + zeta) * y[7];
+    j[4] = (1.0 + xi) * (1.0 - zeta) * y[1] - (1.0 + xi) * (1.0 - zeta) * y[2] - (1.0 - xi) * (1.0 - zeta) * y[3] +
+           (1.0 - xi) * (1.0 + zeta) * y[4] + (1.0 + xi) * (1.0 + zeta) * y[5] - (1.0 + xi) * (1.0 + zeta) * y[6] -
+           (1.0 - xi) * (1.0 + zeta) * y[7];
+    j[5] = (1.0 - eta) * (1.0 + xi) * y[1] + (1.0 + eta) * (1.0 + xi) * y[2] + (1.0 + eta) * (1.0 - xi) * y[3] -
+           (1.0 - eta) * (1.0 - xi) * y[4] - (1.0 - eta) * (1.0 + xi) * y[5] - (1.0 + eta) * (1.0 + xi) * y[6] -
+           (1.0 + eta) * (1.0 - xi) * y[7];
+    j[6] = -(1.0 - eta) * (1.0 - zeta) * z[1] - (1.0 + eta) * (1.0 - zeta) * z[2] +
+           (1.0 + eta) * (1.0 - zeta) * z[3] + (1.0 - eta) * (1.0 + zeta) * z[4] -
+           (1.0 - eta) * (1.0 + zeta) * z[5] - (1.0 + eta) * (1.0 + zeta) * z[6] +
+           (1.0 + eta) * (1.0 + zeta) * z[7];
+    j[7] = (1.0 + xi) * (1.0 - zeta) * z[1] - (1.0 + xi) * (1.0 - zeta) * z[2] - (1.0 - xi) * (1.0 - zeta) * z[3] +
+           (1.0 - xi) * (1.0 + zeta) * z[4] + (1.0 + xi) * (1.0 + zeta) * z[5] - (1.0 + xi) * (1.0 + zeta) * z[6] -
+           (1.0 - xi) * (1.0 + zeta) * z[7];
+    j[8] = (1.0 - eta) * (1.0 + xi) * z[1] + (1.0 + eta) * (1.0 + xi) * z[2] + (1.0 + eta) * (1.0 - xi) * z[3] -
+           (1.0 - eta) * (1.0 - xi) * z[4] - (1.0 - eta) * (1.0 + xi) * z[5] - (1.0 + eta) * (1.0 + xi) * z[6] -
+           (1.0 + eta) * (1.0 - xi) * z[7];
+    const double jdet = -(j[2] * j[4] * j[6]) + j[1] * j[5] * j[6] + j[2] * j[3] * j[7] - j[0] * j[5] * j[7] -
+                        j[1] * j[3] * j[8] + j[0] * j[4] * j[8];
+    if (!jdet) {
+      i = max_iter;
+      break;
+    }
+    s[0] = (1.0 - eta) * (1.0 - xi) * (1.0 - zeta);
+    s[1] = (1.0 - eta) * (1.0 + xi) * (1.0 - zeta);
+    s[2] = (1.0 + eta) * (1.0 + xi) * (1.0 - zeta);
+    s[3] = (1.0 + eta) * (1.0 - xi) * (1.0 - zeta);
+    s[4] = (1.0 - eta) * (1.0 - xi) * (1.0 + zeta);
+    s[5] = (1.0 - eta) * (1.0 + xi) * (1.0 + zeta);
+    s[6] = (1.0 + eta) * (1.0 + xi) * (1.0 + zeta);
+    s[7] = (1.0 + eta) * (1.0 - xi) * (1.0 + zeta);
+    f[0] = xp - s[1] * x[1] - s[2] * x[2] - s[3] * x[3] - s[4] * x[4] - s[5] * x[5] - s[6] * x[6] - s[7] * x[7];
+    f[1] = yp - s[1] * y[1] - s[2] * y[2] - s[3] * y[3] - s[4] * y[4] - s[5] * y[5] - s[6] * y[6] - s[7] * y[7];
+    f[2] = zp - s[1] * z[1] - s[2] * z[2] - s[3] * z[3] - s[4] * z[4] - s[5] * z[5] - s[6] * z[6] - s[7] * z[7];
+    xinew = (jdet * xi + f[2] * (j[2] * j[4] - j[1] * j[5]) + f[1] * (j[1] * j[8] - j[2] * j[7]) +
+             f[0] * (j[5] * j[7] - j[4] * j[8])) /
+            jdet;
+    etanew = (eta * jdet + f[2] * (j[0] * j[5] - j[2] * j[3]) + f[1] * (j[2] * j[6] - j[0] * j[8]) +
+              f[0] * (j[3] * j[8] - j[5] * j[6])) /
+             jdet;
+    zetanew = (jdet * zeta + f[2] * (j[1] * j[3] - j[0] * j[4]) + f[1] * (j[0] * j[7] - j[1] * j[6]) +
+               f[0] * (j[4] * j[6] - j[3] * j[7])) /
+              jdet;
+    dd[0] = xinew - xi;
+    dd[1] = etanew - eta;
+    dd[2] = zetanew - zeta;
+    xi = xinew;
+    eta = etanew;
+    zeta = zetanew;
+  } while (!(fabs(0.0 + dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) < tol) && ++i < max_iter);
+  para[0] = para[1] = para[2] = 1.7976931348623157e308;
+  double dist = 1.7976931348623157e308;
+  if (i < max_iter) {
+    para[0] = xinew;
+    para[1] = etanew;
+    para[2] = zetanew;
+    dist = 0;
+    for (int c = 0; c < 3; c++) {
+      if (para[c] > 1.0 && para[c] < 1.000001) para[c] = 1.0;
+      if (para[c] < -1.0 && para[c] > -1.000001) para[c] = -1.0;
+    }
+    for (int c = 0; c < 3; c++)
+      if (dist < fabs(para[c])) dist = fabs(para[c]);
+  }
+  return !(dist > 1.0);
+}
+
+__global__ void tag_kernel(Grid g, TagPlan p, int32_t *tag, double *pc) {
+  const int64_t nvox = (int64_t)g.nxyg * g.nzg;
+  const double h = g.h;
+  const double origin[3] = {(0 - 0.5) * h + g.x0, (0 - 0.5) * h + g.y0, (0 - 0.5) * h + g.z0};
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nvox; v += (int64_t)gridDim.x * blockDim.x) {
+    tag[v] = -1;
+    pc[3 * v] = pc[3 * v + 1] = pc[3 * v + 2] = -2;
+    int idx[3], mmb[6];
+    idx[2] = (int)(v / g.nxyg);
+    idx[1] = (int)((v % g.nxyg) / g.nxg);
+    idx[0] = (int)((v % g.nxyg) % g.nxg);
+    double cv[3];
+    bool out = false;
+    for (int c = 0; c < 3; c++) {
+      cv[c] = origin[c] + idx[c] * h;
+      if (cv[c] < p.mm[2 * c] || cv[c] > p.mm[2 * c + 1]) {
+        out = true;
+        break;
+      }
+      const double dist = cv[c] - p.mm[2 * c];
+      mmb[2 * c] = (int)floor(dist / p.dbin[c]);
+      mmb[2 * c + 1] = (int)ceil(dist / p.dbin[c]);
+    }
+    if (out) continue;
+    for (int c = 0; c < 3; c++) {
+      int &lo = mmb[2 * c], &hi = mmb[2 * c + 1];
+      if (lo == hi && lo > 0 && hi < p.nbin[c]) {
+        lo -= 1;
+        hi += 1;
+      } else if (hi == 0) {
+        hi = 1;
+      } else if (hi == p.nbin[c]) {
+        if (lo > 0) lo -= 1;
+      }
+    }
+    bool got = false;
+    for (int kk = mmb[4]; kk < mmb[5] && !got; kk++)
+      for (int jj = mmb[2]; jj < mmb[3] && !got; jj++)
+        for (int ii = mmb[0]; ii < mmb[1] && !got; ii++) {
+          const int64_t ind = ii + (int64_t)jj * p.nbin[0] + (int64_t)kk * p.nbin[0] * p.nbin[1];
+          if (ind < 0 || ind >= (int64_t)p.nbin[0] * p.nbin[1] * p.nbin[2]) continue;
+          for (int64_t q = p.bin_start[ind]; q < p.bin_start[ind + 1]; ++q) {
+            const int32_t e = p.bin_elems[q];
+            const double *r = p.erange + 6 * (int64_t)e;
+            if (cv[0] < r[0] || cv[0] > r[1] || cv[1] < r[2] || cv[1] > r[3] || cv[2] < r[4] || cv[2] > r[5]) continue;
+            int64_t nid[8];
+            elem_nodes(p.nn, e, nid);
+            double X[8], Y[8], Z[8], para[3];
+            const double *o = p.coord + 3 * nid[0];
+            X[0] = Y[0] = Z[0] = 0.0;
+            for (int n = 1; n < 8; n++) {
+              const double *cn = p.coord + 3 * nid[n];
+              X[n] = 0.125 * (cn[0] - o[0]);
+              Y[n] = 0.125 * (cn[1] - o[1]);
+              Z[n] = 0.125 * (cn[2] - o[2]);
+            }
+            if (in_element(X, Y, Z, cv[0] - o[0], cv[1] - o[1], cv[2] - o[2], p.tolerance, p.max_iter, para)) {
+              tag[v] = e;
+              pc[3 * v] = para[0];
+              pc[3 * v + 1] = para[1];
+              pc[3 * v + 2] = para[2];
+              got = true;
+              atomicAdd(&p.counts[0], 1ull);
+              if (!isfinite(para[0]) || !isfinite(para[1]) || !isfinite(para[2])) atomicAdd(&p.counts[1], 1ull);
+              break;
+            }
+          }
+        }
+  }
+}
+
+}  // namespace
+
+cudaError_t remelt_tag_voxels(const Grid &g, const TagPlan &p, int32_t *tag, double *pc, cudaStream_t s) {
+  const int64_t nvox = (int64_t)g.nxyg * g.nzg;
+  const int blocks = (int)std::min<int64_t>((nvox + 127) / 128, 152 * 64);
+  tag_kernel<<<blocks > 0 ? blocks : 1, 128, 0, s>>>(g, p, tag, pc);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic frames: Rosenthal moving point source (IEEE add/mul/div/sqrt only)
+// ---------------------------------------------------------------------------
+namespace {
+
+// 1/n!, n = 0..13, as exact doubles
+__constant__ double kExpTaylor[14] = {0x1.0000000000000p+0, 0x1.0000000000000p+0, 0x1.0000000000000p-1,
+                                      0x1.5555555555555p-3, 0x1.5555555555555p-5, 0x1.1111111111111p-7,
+                                      0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
+                                      0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+                                      0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33};
+
+// exp(a) for a <= 0: k = rint(a / ln 2), r = a - k ln 2, degree-13 Taylor
+// polynomial in r (Horner), times 2^k built from the exponent bits.
+__device__ double det_exp(double a) {
+  const double kLn2 = 0x1.62e42fefa39efp-1, kInvLn2 = 0x1.71547652b82fep+0;
+  a = (a < -700.0) ? -700.0 : a;
+  const double k = rint(a * kInvLn2);
+  const double r = a - k * kLn2;
+  double p = kExpTaylor[13];
+#pragma unroll
+  for (int n = 12; n >= 0; --n) p = p * r + kExpTaylor[n];
+  const long long ki = (long long)k;
+  return p * __longlong_as_double((ki + 1023) << 52);
+}
+
+__global__ void rosenthal_kernel(RosenthalParams p, int nframes, double *frames) {
+  const int64_t nnodes = (int64_t)p.nodes[0] * p.nodes[1] * p.nodes[2];
+  const int64_t total = nnodes * nframes;
+  const double two_pi_k = 2.0 * 3.141592653589793 * p.conductivity;
+  const double ap = p.absorptivity * p.power;
+  const double two_alpha = 2.0 * p.diffusivity;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = q / nnodes, n = q % nnodes;
+    const int64_t I = n % p.nodes[0], J = (n / p.nodes[0]) % p.nodes[1], K = n / ((int64_t)p.nodes[0] * p.nodes[1]);
+    const double x = (p.origin[0] + p.spacing * (double)I) * p.length_scale;
+    const double y = (p.origin[1] + p.spacing * (double)J) * p.length_scale;
+    const double z = (p.origin[2] + p.spacing * (double)K) * p.length_scale;
+    const double t = ((double)f * p.frame_dt) * p.time_scale;
+    const double xi = x - (p.x_start + p.speed * t);
+    const double dy = y - p.y_line;
+    const double dz = z - p.z_top;
+    double r = sqrt((xi * xi + dy * dy) + dz * dz);
+    r = (r < 1e-9) ? 1e-9 : r;
+    const double qv = ap / (two_pi_k * r);
+    double T = p.t0 + qv * det_exp(-(p.speed * (r + xi)) / two_alpha);
+    T = (p.t_cap < T) ? p.t_cap : T;
+    if (p.void_above_set && z > p.z_top + p.void_above) T = p.t_void;
+    frames[q] = T;
+  }
+}
+
+__global__ void init_theta_kernel(RemeltDevice d) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.nnodes; n += stride) d.theta[0][n] = d.frames[n];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.nelem; e += stride) {
+    int64_t nid[8];
+    elem_nodes(d.nn, e, nid);
+    double t[8];
+    for (int i = 0; i < 8; ++i) t[i] = d.frames[nid[i]];
+    element_bounds(d, e, t);
+  }
+}
+
+}  // namespace
+
+cudaError_t remelt_rosenthal_frames(const RosenthalParams &p, int nframes, double *frames, cudaStream_t s) {
+  const int64_t total = (int64_t)p.nodes[0] * p.nodes[1] * p.nodes[2] * nframes;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  rosenthal_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nframes, frames);
+  return cudaGetLastError();
+}
+
+cudaError_t remelt_init_theta(const RemeltDevice &d, cudaStream_t s) {
+  const int64_t n = std::max<int64_t>(d.nnodes, d.nelem);
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  init_theta_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(d);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// The persistent step kernel
+// ---------------------------------------------------------------------------
+namespace {
+
+struct StepScalars {
+  long long step;
+  double time, dt, max_ts, dT_FE, fe_time, ts0, ts1;
+  int f_new, f_next;
+  long long n_orient, n_grains;
+};
+
+__device__ StepScalars read_scalars(const RemeltCtrl *c) {
+  StepScalars s;
+  s.step = ld_volatile(&c->step);
+  s.time = ld_volatile(&c->time);
+  s.dt = ld_volatile(&c->dt);
+  s.max_ts = ld_volatile(&c->max_ts);
+  s.dT_FE = ld_volatile(&c->dT_FE);
+  s.fe_time = ld_volatile(&c->fe_time);
+  s.ts0 = ld_volatile(&c->ts0);
+  s.ts1 = ld_volatile(&c->ts1);
+  s.f_new = ld_volatile(&c->f_new);
+  s.f_next = ld_volatile(&c->f_next);
+  s.n_orient = ld_volatile(&c->n_orient);
+  s.n_grains = ld_volatile(&c->n_grains);
+  return s;
+}
+
+// Sweep position of a cell in the reference's i-outer, j, k-inner order.
+__device__ __forceinline__ int32_t sweep_pos(const Grid &g, int I, int J, int K) {
+  return (int32_t)(((int64_t)I * g.nyg + J) * g.nzg + K);
+}
+
+// Block 0: give the new grain objects of the last step their ids in sweep
+// order (bitonic sort of the (sweep position, neighbour) keys in place).
+__device__ void assign_new_grains(const RemeltDevice &d, RemeltCtrl *c) {
+  const unsigned n = ld_volatile(&c->n_new);
+  if (n == 0) return;
+  unsigned m = 1;
+  while (m < n) m <<= 1;
+  for (unsigned i = n + threadIdx.x; i < m; i += blockDim.x) {
+    d.newkey[i] = ~0ull;
+    d.newcell[i] = -1;
+  }
+  __syncthreads();
+  for (unsigned k = 2; k <= m; k <<= 1)
+    for (unsigned j = k >> 1; j > 0; j >>= 1) {
+      for (unsigned i = threadIdx.x; i < m; i += blockDim.x) {
+        const unsigned l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = d.newkey[i], b = d.newkey[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            d.newkey[i] = b;
+            d.newkey[l] = a;
+            const int32_t t = d.newcell[i];
+            d.newcell[i] = d.newcell[l];
+            d.newcell[l] = t;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  const long long base = ld_volatile(&c->n_grains);
+  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) d.grain[d.newcell[i]] = (int32_t)(base + i);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c->n_grains = base + n;
+    c->n_new = 0;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long long limit) {
+  __shared__ unsigned smem[kWarps + 2];
+  RemeltCtrl *c = d.ctrl;
+  const Grid &g = d.g;
+  const int tid = threadIdx.x;
+  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + tid;
+  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+  const int64_t M = (int64_t)g.nx * g.ny * g.nz;
+  const int64_t nyzg = (int64_t)g.nyg * g.nzg;
+  unsigned long long tests = 0, tests64 = 0, caps = 0, exactT = 0, melts = 0;
+  bool ok = true;
+  for (;;) {
+    const StepScalars S = read_scalars(c);
+    // --- loop condition of time_integration_weak_coupling (CafeSolver.cpp:188) and launch limits ---
+    int stop = kRemeltRunning;
+    if (!(S.time < d.final_time)) stop = kRemeltFinalTime;
+    else if (S.step >= limit) stop = kRemeltStepLimit;
+    else if (d.nsites > 0 && S.n_orient + d.nsites > d.orient_cap) stop = kRemeltNeedOrient;
+    if (stop != kRemeltRunning) {
+      if (gtid == 0) c->status = stop;
+      break;
+    }
+    const int par = (int)(S.step & 1);
+    const double *th = d.theta[S.step % 3];
+    const double *thp = d.theta[(S.step + 2) % 3];
+    unsigned long long t_phase = 0;
+    if (gtid == 0) t_phase = now_ns();
+
+    // ===== A: phase update + melted flags (Remelting.cpp:339-404, :484-517) =====
+    if (blockIdx.x == 0) {
+      assign_new_grains(d, c);
+      if (tid == 0) c->n_claim = 0;
+    }
+    {  // clear the previous step's liquid-neighbour flags
+      const unsigned nprev = ld_volatile(&c->n_flag[par ^ 1]);
+      const int32_t *fl = d.flagged[par ^ 1];
+      for (int64_t q = gtid; q < nprev; q += nthr) {
+        const int32_t x = fl[q];
+        atomicAnd(&d.flagbits[x >> 5], ~(1u << (x & 31)));
+      }
+    }
+    for (int64_t q = gtid; q < M; q += nthr) {
+      const int I = (int)(q % g.nx) + 1;
+      const int J = (int)((q / g.nx) % g.ny) + 1;
+      const int K = (int)(q / ((int64_t)g.nx * g.ny)) + 1;
+      const int64_t cell = (int64_t)K * g.nxyg + (int64_t)J * g.nxg + I;
+      int32_t o = d.orient[cell];
+      const int32_t e = d.tag[cell];
+      const bool withMat = e >= 0 && !d.evoid[e];
+      double T = -1.0;  // nullMatTemp_ (Remelting.cpp:29)
+      bool haveT = !withMat;
+      if (o > -1) {
+        if (withMat) {
+          // certainly below the liquidus and above nullMatTemp_ + 0.01: nothing changes
+          if (d.emax[e] < d.Tm && d.emin[e] >= null_plus()) continue;
+          ++exactT;
+          eval_T(d, th, cell, T);
+          haveT = true;
+          if (T < d.Tm) {  // stays solid; the liquid-neighbour pass clears melted below nullMatTemp_ + 0.01
+            if (T < null_plus() && d.melted[cell]) d.melted[cell] = 0;
+            continue;
+          }
+        }
+        d.orient[cell] = -1;  // melt
+        d.melted[cell] = withMat ? 1 : 0;
+        o = -1;
+        ++melts;
+      }
+      if (!haveT) {
+        ++exactT;
+        eval_T(d, th, cell, T);
+      }
+      const bool withMat2 = !(T < null_plus());
+      const uint8_t m0 = d.melted[cell];
+      uint8_t m1 = m0;
+      if (withMat2 && S.time >= S.max_ts) m1 = 1;
+      if (!withMat2) m1 = 0;
+      if (m1 != m0) d.melted[cell] = m1;
+      d.T[cell] = T;
+      if (withMat2 && !(T >= d.Tm)) {
+        const unsigned slot = atomicAdd(&c->n_liq, 1u);
+        if (slot < d.list_cap) d.liq[slot] = (int32_t)cell;
+      }
+    }
+    if (gtid == 0) {
+      const unsigned long long t1 = now_ns();
+      atomicAdd(&c->ns_phase[0], t1 - t_phase);
+      t_phase = t1;
+    }
+    if (!(ok = grid_barrier(c))) break;
+
+    // ===== B: liquid-neighbour flags (Remelting.cpp:518-540) =====
+    {
+      const unsigned nl = ld_volatile(&c->n_liq);
+      if (nl > d.list_cap) {
+        if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
+      } else {
+        for (int64_t q = gtid; q < nl; q += nthr) {
+          const int32_t cell = d.liq[q];
+          for (int n = 0; n < 26; ++n) {
+            int di, dj, dk;
+            nbr_offset(n, di, dj, dk);
+            const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
+            if (d.orient[nb] > -1) {
+              const unsigned bit = 1u << (nb & 31);
+              const unsigned old = atomicOr(&d.flagbits[nb >> 5], bit);
+              if (!(old & bit)) {
+                const unsigned slot = atomicAdd(&c->n_flag[par], 1u);
+                if (slot < d.list_cap) d.flagged[par][slot] = nb;
+              }
+            }
+          }
+        }
+      }
+    }
+    if (gtid == 0) {
+      const unsigned long long t1 = now_ns();
+      atomicAdd(&c->ns_phase[1], t1 - t_phase);
+      t_phase = t1;
+    }
+    if (!(ok = grid_barrier(c))) break;
+
+    // ===== C: nucleation (block 0) | cutoff + minimum temperature (Remelting.cpp:656-705) =====
+    const unsigned nf = ld_volatile(&c->n_flag[par]);
+    if (nf > d.list_cap) {
+      if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
+    }
+    if (blockIdx.x == 0 && d.nsites > 0) {
+      // nucleate_at_nucleation_sites (Remelting.cpp:936-999): ascending sites,
+      // orientation id = count so far, a grain object created where the cell has none
+      unsigned done_o = 0, done_g = 0;
+      // block 0 itself gave last step's new grain objects their ids in phase A
+      const long long n_grains = ld_volatile(&c->n_grains);
+      for (int base = 0; base < d.nsites; base += kBlock) {
+        const int sidx = base + tid;
+        bool nuc = false, newg = false;
+        int32_t cell = -1;
+        if (sidx < d.nsites) {
+          cell = d.site_cell[sidx];
+          double T = -1.0;
+          const bool withMat = eval_T(d, th, cell, T);
+          bool cooling = false;
+          if (S.step > 0) {  // cooling_ of this step's phase update (Remelting.cpp:362-373)
+            double Told = -1.0;
+            eval_T(d, thp, cell, Told);
+            double rate = 410;
+            if (Told > 0) rate = (T - Told) / S.dt;
+            if (T <= 0) rate = 0;
+            cooling = withMat ? (rate < 0) : false;
+          }
+          const bool isLiquid = d.orient[cell] == -1;
+          if (cooling && isLiquid && d.melted[cell] && T > d.Tnuc) {
+            const double dT = d.Tm - T;
+            if (dT > d.site_dtc[sidx]) {
+              nuc = true;
+              newg = d.grain[cell] == -1;
+            }
+          }
+        }
+        unsigned tot_o, tot_g;
+        const unsigned r_o = block_exclusive_scan(nuc ? 1u : 0u, smem, &tot_o);
+        const unsigned r_g = block_exclusive_scan(newg ? 1u : 0u, smem, &tot_g);
+        if (nuc) {
+          const int32_t oid = (int32_t)(S.n_orient + done_o + r_o);
+          int I, J, K;
+          cell_ijk(g, cell, I, J, K);
+          d.gx[cell] = centre_coord(g.x0, g.h, I);
+          d.gy[cell] = centre_coord(g.y0, g.h, J);
+          d.gz[cell] = centre_coord(g.z0, g.h, K);
+          d.glen[cell] = 0.0;
+          d.gori[cell] = oid;
+          d.gdx[cell] = d.gdy[cell] = d.gdz[cell] = 0.0f;
+          if (newg) d.grain[cell] = (int32_t)(n_grains + done_g + r_g);
+          d.orient[cell] = oid;
+        }
+        done_o += tot_o;
+        done_g += tot_g;
+      }
+      if (tid == 0) {
+        c->n_orient = S.n_orient + done_o;
+        c->n_grains = n_grains + done_g;
+        c->nucleations += done_o;
+      }
+    }
+    {
+      const bool solo = gridDim.x == 1;
+      const int64_t g0 = solo ? gtid : gtid - blockDim.x;
+      const int64_t gn = solo ? nthr : nthr - blockDim.x;
+      if (nf <= d.list_cap && (solo || blockIdx.x > 0)) {
+        const unsigned long long key_tm = dkey(d.Tm);
+        unsigned long long best = key_tm;
+        for (int64_t q = g0; q < nf; q += gn) {
+          const int32_t cell = d.flagged[par][q];
+          int I, J, K;
+          cell_ijk(g, cell, I, J, K);
+          if (ghost(g, I, J, K)) continue;
+          if (d.grain[cell] < 0) continue;
+          if (!(d.glen[cell] < d.cutoff)) d.glen[cell] = d.h;  // length reset (:688-694)
+          double T = -1.0;
+          ++exactT;
+          eval_T(d, th, cell, T);
+          d.T[cell] = T;
+          {  // growth velocity of single_integration_step (Remelting.cpp:569-576)
+            bool hard = false;
+            const double Targ = (T < d.Ts) ? d.Ts + 0.01 : T;
+            d.fvel[q] = velocity(d, Targ, hard);
+            if (hard) {
+              const unsigned slot = atomicAdd(&c->n_hard, 1u);
+              if (slot < d.list_cap) {
+                d.hard_idx[slot] = (int32_t)q;
+                d.hard_T[slot] = Targ;
+              }
+            }
+          }
+          if (T <= d.Ts) continue;
+          if (T == T) {
+            const unsigned long long k = dkey(T);
+            best = k < best ? k : best;
+          }
+        }
+        if (best < key_tm) atomicMin(&c->minT_key, best);
+      }
+    }
+    if (gtid == 0) {
+      const unsigned long long t1 = now_ns();
+      atomicAdd(&c->ns_phase[2], t1 - t_phase);
+      t_phase = t1;
+    }
+    if (!(ok = grid_barrier(c))) break;
+
+    // ===== dt (Remelting.cpp:706-726, CafeSolver.cpp:195-199) =====
+    const double minT = dkey_inv(ld_volatile(&c->minT_key));
+    bool min_hard = false;
+    double vmin = velocity(d, minT, min_hard);
+    {
+      const unsigned nh = ld_volatile(&c->n_hard);
+      if (nh > 0 || min_hard) {  // uniform: every block read the same counter and key
+        if (blockIdx.x == 0 && !host_velocities(d, c, nh, min_hard, minT)) atomicCAS(&c->error, 0, kRemeltErrHost);
+        if (!(ok = grid_barrier(c))) break;
+        if (min_hard) vmin = ld_volatile(&c->vmin);
+      }
+    }
+    const double maxV = vmin > 0 ? vmin : 0;
+    const double a = d.tsf_ca * d.h / maxV;
+    const double dtLoc = (S.max_ts < a) ? S.max_ts : a;
+    const double dT = (S.dT_FE < dtLoc) ? S.dT_FE : dtLoc;
+
+    // ===== D: grow and claim (Remelting.cpp:545-622) =====
+    for (int64_t q = gtid; q < nf && nf <= d.list_cap; q += nthr) {
+      const int32_t cell = d.flagged[par][q];
+      int I, J, K;
+      cell_ijk(g, cell, I, J, K);
+      if (ghost(g, I, J, K)) continue;
+      if (d.grain[cell] < 0) continue;
+      const double vel = d.fvel[q];
+      const double L = d.glen[cell] + dT * vel;
+      d.glen[cell] = L;
+      if (L == 0) continue;  // Octahedron::cell_is_captured: a zero half-diagonal captures nothing
+      const int32_t ori = d.gori[cell];
+      const int32_t mine = INT_MIN + sweep_pos(g, I, J, K);
+      const float dxf = d.gdx[cell], dyf = d.gdy[cell], dzf = d.gdz[cell];
+      const float errg = 4.76837158203125e-07f * (d.h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + d.coord_err;
+      const float L32 = (float)L;
+      float m32[9];
+#pragma unroll
+      for (int qq = 0; qq < 9; ++qq) m32[qq] = d.omat32[9 * (int64_t)ori + qq];
+      for (int n = 0; n < 26; ++n) {
+        int di, dj, dk;
+        nbr_offset(n, di, dj, dk);
+        if (ghost(g, I + di, J + dj, K + dk)) continue;
+        const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
+        if (d.orient[nb] > -1) continue;
+        const double Tn = d.T[nb];
+        if (Tn > d.Tm) continue;
+        if (!(Tn > -1.0)) continue;
+        ++tests;
+        int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg,
+                             L32);
+        if (f < 0) {
+          ++tests64;
+          const double ccx = centre_coord(g.x0, g.h, I + di);
+          const double ccy = centre_coord(g.y0, g.h, J + dj);
+          const double ccz = centre_coord(g.z0, g.h, K + dk);
+          f = is_captured_f64(d.omat + 9 * (int64_t)ori, ccx - d.gx[cell], ccy - d.gy[cell], ccz - d.gz[cell], L) ? 1
+                                                                                                                  : 0;
+        }
+        if (f) {
+          const int32_t old = atomicMin(&d.orient[nb], mine);
+          if (old == -1) {
+            const unsigned slot = atomicAdd(&c->n_claim, 1u);
+            if (slot < d.list_cap) d.claimed[slot] = nb;
+          }
+        }
+      }
+    }
+    if (gtid == 0) {
+      const unsigned long long t1 = now_ns();
+      atomicAdd(&c->ns_phase[3], t1 - t_phase);
+      t_phase = t1;
+    }
+    if (!(ok = grid_barrier(c))) break;
+
+    // ===== E: captures (Remelting.cpp:807-847) and the FE replay step (LoadDataFromFile.cpp:207-313) =====
+    {
+      const unsigned nc = ld_volatile(&c->n_claim);
+      if (nc > d.list_cap) {
+        if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
+      } else {
+        for (int64_t q = gtid; q < nc; q += nthr) {
+          const int32_t nb = d.claimed[q];
+          const int32_t w = d.orient[nb] - INT_MIN;
+          const int wi = (int)(w / nyzg), wj = (int)((w / g.nzg) % g.nyg), wk = (int)(w % g.nzg);
+          const int64_t wc = (int64_t)wk * g.nxyg + (int64_t)wj * g.nxg + wi;
+          int I, J, K;
+          cell_ijk(g, nb, I, J, K);
+          const int32_t ori = d.gori[wc];
+          const double px = d.gx[wc], py = d.gy[wc], pz = d.gz[wc], L = d.glen[wc];
+          const double ccx = centre_coord(g.x0, g.h, I), ccy = centre_coord(g.y0, g.h, J),
+                       ccz = centre_coord(g.z0, g.h, K);
+          double out[4];
+          capture_f64(d.omat + 9 * (int64_t)ori, ccx - px, ccy - py, ccz - pz, L, d.h, d.trunc, out);
+          const double nx = out[0] + px, ny = out[1] + py, nz = out[2] + pz;
+          d.gx[nb] = nx;
+          d.gy[nb] = ny;
+          d.gz[nb] = nz;
+          d.glen[nb] = out[3];
+          d.gori[nb] = ori;
+          d.gdx[nb] = (float)(nx - ccx);
+          d.gdy[nb] = (float)(ny - ccy);
+          d.gdz[nb] = (float)(nz - ccz);
+          if (d.grain[nb] < 0) {  // create_new_grain: id in sweep order after the step
+            d.grain[nb] = kPendingGrain;
+            const int di = I - wi, dj = J - wj, dk = K - wk;
+            int m = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
+            m = m > 13 ? m - 1 : m;
+            const unsigned slot = atomicAdd(&c->n_new, 1u);
+            if (slot < (unsigned)kNewGrainCap) {
+              d.newkey[slot] = ((unsigned long long)(uint32_t)w << 5) | (unsigned)m;
+              d.newcell[slot] = nb;
+            } else {
+              atomicCAS(&c->error, 0, kRemeltErrNewGrains);
+            }
+          }
+          d.orient[nb] = ori;
+          ++caps;
+        }
+      }
+    }
+    // FE replay (uniform in every thread)
+    double fe_time = S.fe_time, ts0 = S.ts0, ts1 = S.ts1;
+    int f_new = S.f_new, f_next = S.f_next;
+    if (fe_time == 0) fe_time = ts1;
+    fe_time += dT;
+    bool exhausted = false, bad = false;
+    while (fe_time >= ts0) {
+      if (f_next >= d.nframes) {
+        exhausted = true;
+        bad = (d.bad_frame == f_next);
+        break;
+      }
+      ts1 = ts0;
+      ts0 = d.frame_time[f_next];
+      f_new = f_next;
+      f_next++;
+    }
+    double ratio = 0.0;
+    if (!exhausted) {
+      ratio = (fe_time - ts1) / (ts0 - ts1);
+      if (ratio < 0.0 && gtid == 0) atomicCAS(&c->error, 0, kRemeltErrRatio);
+      const double *f0 = d.frames + (int64_t)f_new * d.nnodes;
+      const double *f1 = f0 - d.nnodes;
+      double *tn = d.theta[(S.step + 1) % 3];
+      for (int64_t n = gtid; n < d.nnodes; n += nthr) tn[n] = lerp_node(f0[n], f1[n], ratio, d.void_t);
+      for (int64_t e = gtid; e < d.nelem; e += nthr) {
+        int64_t nid[8];
+        elem_nodes(d.nn, e, nid);
+        double t[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) t[i] = lerp_node(f0[nid[i]], f1[nid[i]], ratio, d.void_t);
+        element_bounds(d, e, t);
+      }
+    }
+    if (gtid == 0) {
+      if (bad) atomicCAS(&c->error, 0, kRemeltErrFrame);
+      c->step = S.step + 1;
+      c->time = S.time + dT;
+      c->dt_prev = S.dt;
+      c->dt = dT;
+      c->fe_time = fe_time;
+      c->ts0 = ts0;
+      c->ts1 = ts1;
+      c->f_new = f_new;
+      c->f_next = f_next;
+      c->ratio = ratio;
+      c->dT_FE = ts0 - fe_time;
+      c->max_ts = ts0 - fe_time;
+      c->theta_init = 0;
+      c->liquid += ld_volatile(&c->n_liq);
+      c->n_liq = 0;
+      c->n_hard = 0;
+      c->minT_key = dkey(d.Tm);
+      c->n_flag[par ^ 1] = 0;
+      c->flagged += nf;
+      if (exhausted) c->status = kRemeltFramesEnd;
+      const unsigned long long t1 = now_ns();
+      atomicAdd(&c->ns_phase[4], t1 - t_phase);
+    }
+    if (!(ok = grid_barrier(c))) break;
+    if (ld_volatile(&c->status) == kRemeltFramesEnd) break;
+  }
+  if (ok && blockIdx.x == 0) assign_new_grains(d, c);
+  if (tests) atomicAdd(&c->tests, tests);
+  if (tests64) atomicAdd(&c->tests64, tests64);
+  if (caps) atomicAdd(&c->captures, caps);
+  if (exactT) atomicAdd(&c->exact_T, exactT);
+  if (melts) atomicAdd(&c->melts, melts);
+}
+
+}  // namespace
+
+int remelt_persistent_grid(int device) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, remelt_kernel, kBlock, 0) != cudaSuccess) return 0;
+  return sms * std::max(1, std::min(per, 4));
+}
+
+cudaError_t remelt_run_steps(const RemeltDevice &d, long long limit, int blocks, cudaStream_t s) {
+  void *args[] = {(void *)&d, (void *)&limit};
+  return cudaLaunchCooperativeKernel((const void *)remelt_kernel, dim3(blocks), dim3(kBlock), args, 0, s);
+}
+
+// ---------------------------------------------------------------------------
+// Full state fields of the last completed step (reference arrays)
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void state_fields_kernel(RemeltDevice d, long long step, double dt_prev, double *T, uint8_t *cooling,
+                                    uint8_t *flag) {
+  // the last phase update ran at iStep_ = step - 1 with node temperatures
+  // theta[(step - 1) % 3]; its cooling_ compared with theta[(step - 2) % 3]
+  const long long k = step - 1;
+  const double *th = d.theta[((k % 3) + 3) % 3];
+  const double *thp = d.theta[(((k - 1) % 3) + 3) % 3];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < d.ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    double t = -1.0;
+    const bool withMat = eval_T(d, th, c, t);
+    if (T) T[c] = t;
+    if (cooling) {
+      bool cool = false;
+      if (k > 0) {
+        double told = -1.0;
+        eval_T(d, thp, c, told);
+        double rate = 410;
+        if (told > 0) rate = (t - told) / dt_prev;
+        if (t <= 0) rate = 0;
+        cool = withMat ? (rate < 0) : false;
+      }
+      cooling[c] = cool ? 1 : 0;
+    }
+    if (flag) flag[c] = (d.flagbits[c >> 5] >> (c & 31)) & 1u;
+  }
+}
+
+}  // namespace
+
+cudaError_t remelt_state_fields(const RemeltDevice &d, long long step, double dt_prev, double *T, uint8_t *cooling,
+                                uint8_t *flag, cudaStream_t s) {
+  const int blocks = (int)std::min<int64_t>((d.ncells + 255) / 256, 152 * 16);
+  state_fields_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(d, step, dt_prev, T, cooling, flag);
+  return cudaGetLastError();
+}
+
+}  // namespace amca

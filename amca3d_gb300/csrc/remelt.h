@@ -1,0 +1,164 @@
+// remelt.h — device state and launch API of the FE-coupled remelting realm.
+//
+// Reference: CafeSolver::time_integration_weak_coupling (CA/src/CafeSolver.cpp:178-219)
+// driving CellularAutomataManager_3DRemelting (CA/src/CellularAutomataManager_3DRemelting.cpp)
+// with temperatures interpolated by MapVoxelManager::evaluate_temperature
+// (CA/src/MapVoxelManager.cpp:746-799) from frames replayed by
+// FiniteElementManager::pseudo_single_integration_step (CA/src/LoadDataFromFile.cpp:207-313).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ca_math.h"
+
+namespace amca {
+
+constexpr int32_t kPendingGrain = 0x7fffffff;  // grain created this step, id assigned after the step
+constexpr int kNewGrainCap = 16384;            // new grain objects one step may create
+constexpr int kRemeltErrBarrier = 1, kRemeltErrFrame = 2, kRemeltErrNewGrains = 3, kRemeltErrRatio = 4,
+              kRemeltErrList = 5, kRemeltErrHost = 6;
+// why a launch returned
+constexpr int kRemeltRunning = 0, kRemeltFinalTime = 1, kRemeltFramesEnd = 2, kRemeltNeedOrient = 3,
+              kRemeltStepLimit = 4;
+
+// Growth velocities whose glibc pow() rounding cannot be decided on the GPU
+// (an integer power within 0.02 ulp of a rounding midpoint; glibc's pow errs
+// by at most 0.52 ulp) are evaluated by the host's libm: the kernel posts the
+// temperatures in this mapped, page-locked buffer and waits (bounded) for
+// the host service thread to answer.
+constexpr int kHostVelCap = 1 << 16;
+struct HostVelocity {
+  unsigned int seq_req, seq_done, n, pad;
+  double T[kHostVelCap];
+  double v[kHostVelCap];
+};
+
+struct RemeltCtrl {
+  unsigned int bar_count, bar_gen;
+  int error;
+  int status;
+  // coupling scalars, published by block 0 at the end of every step
+  long long step;      // completed CA steps (iStep_)
+  double time;         // CafeSolver time == CA time_
+  double dt;           // dT_ of the last step
+  double dt_prev;      // dT_ of the step before it
+  double dT_FE;        // FiniteElementManager::get_max_time_step()
+  double max_ts;       // CA maxTimestep_
+  double fe_time, ts0, ts1, ratio;  // FiniteElementManager time_, inTimeSeries_[0], [1], last ratio
+  int f_new;           // frame held in theta_[0] (theta_[1] is f_new - 1)
+  int f_next;          // next frame to load
+  int theta_init;      // thetaArray_ still equals frame 0 (no pseudo step yet)
+  int pad0;
+  long long n_orient, n_grains;
+  // work lists of the current step (parity-indexed where a list outlives a step)
+  unsigned int n_liq, n_claim, n_new, n_hard;
+  unsigned int host_seq;  // requests posted to the host so far
+  int vmin_hard;          // the velocity at the minimum temperature came from the host
+  double vmin;
+  unsigned int n_flag[2];
+  unsigned long long minT_key;
+  // counters
+  unsigned long long tests, tests64, captures, nucleations, flagged, liquid, exact_T, melts, host_vel, host_calls;
+  unsigned long long ns_phase[5];
+};
+
+struct RemeltDevice {
+  Grid g;
+  int64_t ncells;
+  // physics (ProblemPhysics.cpp:58-158)
+  double Tm, Ts, Tnuc, a1, a2, a3;
+  int b1, b2, b3;
+  double tsf_ca, h, trunc, cutoff, final_time, void_t;
+  float h32, coord_err;
+  // cells (ghost-inclusive)
+  int32_t *orient;     // cellOrientationID_ (claims during a step: INT_MIN + sweep position)
+  int32_t *grain;      // cellGrainID_
+  uint8_t *melted;     // hasBeenMelted_
+  uint32_t *flagbits;  // cellLiquidNeigh as a bitmap
+  double *T;           // exact temperature of liquid / flagged cells (this step)
+  const int32_t *tag;  // MapVoxelManager elementTagList_
+  const double *pc;    // parCoordsList_
+  // grain records, one per cell (the grain its cell owns)
+  double *gx, *gy, *gz, *glen;
+  int32_t *gori;
+  float *gdx, *gdy, *gdz;  // grain centre - own cell centre, FP32, for the pre-test
+  // orientations
+  const double *omat;
+  const float *omat32;
+  long long orient_cap;
+  // nucleation sites (ascending cell id)
+  const int32_t *site_cell;
+  const double *site_dtc;
+  int nsites;
+  // FE replay
+  int nn[3];
+  int64_t nnodes, nelem;
+  const double *frames;      // nframes x nnodes
+  const double *frame_time;  // per frame, scaled
+  int nframes;
+  int bad_frame;             // index of a malformed frame, or -1
+  double *theta[3];          // node temperatures by CA step (mod 3)
+  double *emax, *emin;       // per element bounds on the interpolated temperature (current step)
+  int force_exact;           // some parametric coordinate is not finite: no bound shortcuts
+  uint8_t *evoid;            // per element: some node below void_temperature + 1e-5
+  // lists
+  int32_t *liq;              // liquid cells whose neighbours may be flagged
+  int32_t *flagged[2];       // flagged cells, by step parity
+  int32_t *claimed;          // cells claimed in the sweep
+  unsigned long long *newkey;  // new-grain events: (sweep position << 5 | neighbour index)
+  int32_t *newcell;
+  double *fvel;              // growth velocity per flagged-list entry
+  int32_t *hard_idx;         // flagged-list entries whose velocity the host evaluates
+  double *hard_T;
+  HostVelocity *host;        // device view of the mapped host buffer
+  int64_t list_cap;
+  RemeltCtrl *ctrl;
+};
+
+// Per-voxel search of MapVoxelManager::tag_voxels / is_in_element
+// (CA/src/MapVoxelManager.cpp:357-699), one thread per ghost-inclusive voxel.
+struct TagPlan {
+  double mm[6], dbin[3];
+  int nbin[3];
+  const int64_t *bin_start;
+  const int32_t *bin_elems;
+  const double *erange;  // 6 per element
+  const double *coord;   // 3 per node
+  int nn[3];
+  double tolerance;
+  int max_iter;
+  unsigned long long *counts;  // [0] voxels with an element, [1] voxels with a non-finite parametric coordinate
+};
+cudaError_t remelt_tag_voxels(const Grid &g, const TagPlan &p, int32_t *tag, double *pc, cudaStream_t s);
+
+// Synthetic frames: the Rosenthal moving-source field on a structured node
+// grid, evaluated with IEEE add/mul/div/sqrt and a fixed exp polynomial.
+struct RosenthalParams {
+  double origin[3], spacing;  // node coordinates in file units: origin + spacing * index
+  int nodes[3];
+  double length_scale;        // file unit -> m for the field evaluation
+  double frame_dt, time_scale;  // frame f at file time f * frame_dt (plus an offset)
+  double power, absorptivity, speed, conductivity, diffusivity, t0, t_cap, x_start, y_line, z_top;
+  int void_above_set;
+  double void_above, t_void;
+};
+cudaError_t remelt_rosenthal_frames(const RosenthalParams &p, int nframes, double *frames, cudaStream_t s);
+
+// Frame-0 node temperatures and element bounds before the first step.
+cudaError_t remelt_init_theta(const RemeltDevice &d, cudaStream_t s);
+
+// Grid size for the persistent kernel (co-resident blocks).
+int remelt_persistent_grid(int device);
+
+// Run CA steps until `limit` steps in total, the final time, the end of the
+// frames, or an orientation stream shorter than a step may need.
+cudaError_t remelt_run_steps(const RemeltDevice &d, long long limit, int blocks, cudaStream_t s);
+
+// Every cell's temperature and cooling flag of the last completed step (the
+// values the reference holds in cellTemperature_ / cooling_), plus the
+// liquid-neighbour flags as bytes.
+cudaError_t remelt_state_fields(const RemeltDevice &d, long long step, double dt_prev, double *T, uint8_t *cooling,
+                                uint8_t *flag, cudaStream_t s);
+
+}  // namespace amca

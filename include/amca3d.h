@@ -82,7 +82,12 @@ int amca_run(amca_t *h, int max_steps);
 enum {
   AMCA_FIELD_ORIENTATION_ID = 0, /* int32, ghost-inclusive grid: cellOrientationID_ (the output "grain_id") */
   AMCA_FIELD_GRAIN_ID = 1,       /* int32, ghost-inclusive grid: cellGrainID_ (envelope index per cell) */
-  AMCA_FIELD_SITE_UNDERCOOLING = 2 /* float64, ghost-inclusive grid: cellNucleationDT_ */
+  AMCA_FIELD_SITE_UNDERCOOLING = 2, /* float64, ghost-inclusive grid: cellNucleationDT_ */
+  /* FE-coupled remelting realm only (CA/include/CellularAutomataManager.h:104-109): */
+  AMCA_FIELD_TEMPERATURE = 3,       /* float64: cellTemperature_ of the last step (-1: no material) */
+  AMCA_FIELD_MELTED = 4,            /* uint8: hasBeenMelted_ */
+  AMCA_FIELD_COOLING = 5,           /* uint8: cooling_ */
+  AMCA_FIELD_LIQUID_NEIGHBOUR = 6   /* uint8: cellLiquidNeigh */
 };
 /* Copy a whole field to host memory. bytes must equal cells * element size,
  * cells = (nx+2)(ny+2)(nz+2), in the reference's index order
@@ -96,6 +101,46 @@ int amca_get_field(amca_t *h, int field, void *host_dst, size_t bytes);
  * (one per site, available after amca_prepare).
  * Replaces orientationVector_ (CA/src/CellularAutomataManager_3D.cpp:1130-1215). */
 int amca_get_orientations(amca_t *h, double *euler, size_t cap, size_t *n_out, int all);
+
+/* ---- FE-coupled remelting realm (solvers [cellular_automata, finite_element_method],
+ * realm types finite_element + cellular_automata_remelting) ----
+ * amca_create selects it from the deck; amca_prepare / amca_initialize /
+ * amca_step / amca_run / amca_get_field / amca_get_stats / amca_reset then
+ * drive CafeSolver::time_integration_weak_coupling (CA/src/CafeSolver.cpp:178-219).
+ * By default the frames are read from the finite_element realm's mesh file
+ * (FiniteElementManager::load_mesh_and_first_two_steps_results_from_txt_file,
+ * CA/src/LoadDataFromFile.cpp:21-191). The two calls below replace that file;
+ * both must come before amca_initialize. */
+
+/* Frames from host memory, in the file's units: node coordinates (3 per node,
+ * x fastest over nodes[0] x nodes[1] x nodes[2]), the time of each frame and
+ * frame-major node temperatures. The deck's offsets and length/time scales are
+ * applied exactly as the reader applies them. */
+int amca_set_fe_frames(amca_t *h, const int32_t nodes[3], const double *coords, int32_t nframes,
+                       const double *times, const double *theta);
+
+/* Synthetic frames generated on the GPU: the Rosenthal quasi-steady field of a
+ * point source moving along +x over a structured node grid,
+ *   T = t0 + (A P) / (2 pi k R) exp(-v (R + xi) / (2 alpha)),  xi = x - (x_start + v t),
+ * capped at t_cap, evaluated with IEEE add/mul/div/sqrt only (exp by a fixed
+ * degree-13 polynomial after ln 2 range reduction), so the frames equal those
+ * a host writer produces with the same arithmetic. Node file coordinates are
+ * origin + spacing * index; the field is evaluated at file coordinate *
+ * length_scale; frame f has file time time_offset + f * frame_dt and the field
+ * time (f * frame_dt) * time_scale. Nodes with z > z_top + void_above (when
+ * void_above_set) hold t_void. */
+typedef struct {
+  double origin[3];
+  double spacing;
+  int32_t nodes[3];
+  int32_t frames;
+  double length_scale, frame_dt, time_scale, time_offset;
+  double power, absorptivity, speed, conductivity, diffusivity;
+  double t0, t_cap, x_start, y_line, z_top;
+  int32_t void_above_set;
+  double void_above, t_void;
+} amca_rosenthal;
+int amca_set_rosenthal_frames(amca_t *h, const amca_rosenthal *p);
 
 /* Final outputs of a finished run: finalGrains.vtk, <pvd dir>/finalResult.txt,
  * the last VTR/PVTR/PVD snapshot and, when the deck asks for it,

@@ -176,3 +176,69 @@ def test_gpu_calls_fail_loudly_without_initialize(amca):
         r.run(1)
     assert e.value.code == -4
     r.close()
+
+
+# ---------------------------------------------------------------------------
+# FE-coupled remelting decks (host half only)
+# ---------------------------------------------------------------------------
+def _remelt_fixtures():
+    import remelt_cases
+
+    return {fx.case.name: fx for fx in remelt_cases.fixtures()}
+
+
+@pytest.mark.parametrize("name", sorted(_remelt_fixtures()))
+def test_remelt_prepare_matches_reference_orientation_stream(amca, tmp_path, name):
+    """Random / restart microstructure, sites and the nucleation orientation
+    stream are drawn on the host exactly as the reference draws them: the
+    Euler angles equal the reference's orientation list after the first and
+    the last CA step."""
+    import make_remelt_golden as M
+
+    fx = _remelt_fixtures()[name]
+    M.prepare(fx, str(tmp_path))
+    r = amca.CellularAutomataRealm(fx.case.to_yaml(), seed=fx.case.seed, workdir=str(tmp_path))
+    assert r.cells == tuple(fx.case.cells)
+    r.prepare()
+    g = np.load(os.path.join(ROOT, "tests", "golden", f"{name}.npz"))
+    ie = [str(f) for f in g["fields"]].index("euler")
+    e = r.orientations(all=True)
+    for i in (0, len(g["norient"]) - 1):
+        n = int(g["norient"][i])
+        assert M.d64(np.ascontiguousarray(e[:n]).reshape(-1)) == g["digests"][i][ie]
+    cells, dtc = r.sites()
+    assert (len(cells) > 0) == fx.case.nucleation
+    assert np.all(np.diff(cells) > 0)
+    r.close()
+
+
+def test_remelt_deck_errors(amca):
+    import remelt_cases
+
+    deck = remelt_cases.fixtures()[0].case.to_yaml()
+    with pytest.raises(amca.AmcaError, match="lines_for_title"):
+        amca.CellularAutomataRealm(deck.replace("lines_for_title: 4", "lines_for_titl: 4"))
+    with pytest.raises(amca.AmcaError, match="for_whole_time"):
+        amca.CellularAutomataRealm(deck.replace("for_whole_time: yes", "for_whole_time: no"))
+    with pytest.raises(amca.AmcaError, match="b1..b3"):
+        amca.CellularAutomataRealm(deck.replace("a1: 0.0", "a1: 0.0\n        b2: 2.5"))
+    with pytest.raises(amca.AmcaError, match="time_step_factor"):
+        amca.CellularAutomataRealm(deck.replace("time_step_factor: 0.4", "time_step_facto: 0.4"))
+    r = amca.CellularAutomataRealm(deck)
+    with pytest.raises(amca.AmcaError, match="before amca_initialize|out of order"):
+        r.field("temperature")
+    r.close()
+
+
+def test_remelt_frames_from_arrays_need_two_frames(amca):
+    import remelt_cases
+
+    fx = remelt_cases.fixtures()[0]
+    r = amca.CellularAutomataRealm(fx.case.to_yaml())
+    x, y, z = fx.frames.node_coords()
+    coords = np.stack([x, y, z], axis=1)
+    with pytest.raises(amca.AmcaError, match="two frames"):
+        r.set_fe_frames(fx.frames.nodes, coords, np.zeros(1), fx.frames.frame_values(0)[None, :])
+    with pytest.raises(amca.AmcaError, match="two frames"):
+        r.set_rosenthal_frames(nodes=(3, 3, 3), frames=1, spacing=1.0)
+    r.close()
