@@ -67,8 +67,8 @@ class Stats(ctypes.Structure):
 EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
-           "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_last_error",
-           "amca_destroy")
+           "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
+           "amca_last_error", "amca_destroy")
 
 
 class Rosenthal(ctypes.Structure):
@@ -139,6 +139,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_set_fe_frames.restype = i
     lib.amca_set_rosenthal_frames.argtypes = [vp, ctypes.POINTER(Rosenthal)]
     lib.amca_set_rosenthal_frames.restype = i
+    lib.amca_set_microstructure.argtypes = [vp, vp, vp, vp, vp, i64, vp, i64, vp, vp, i64]
+    lib.amca_set_microstructure.restype = i
     lib.amca_last_error.argtypes = [vp]
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]
@@ -264,6 +266,22 @@ class CellularAutomataRealm:
         theta = np.ascontiguousarray(theta, np.float64)
         ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
         self._check(self._lib.amca_set_fe_frames(self._h, nn, ptr(coords), len(times), ptr(times), ptr(theta)))
+
+    def set_microstructure(self, grain, orient, euler, grain_cell, grain_orient, melted=None, dtc=None,
+                           expected: int = 0) -> None:
+        """FE-coupled decks: restart microstructure from memory (the content of
+        grainInfo<rank>.txt); replaces the deck's random or file microstructure."""
+        grain = np.ascontiguousarray(grain, np.int32)
+        orient = np.ascontiguousarray(orient, np.int32)
+        euler = np.ascontiguousarray(euler, np.float64).reshape(-1, 3)
+        grain_cell = np.ascontiguousarray(grain_cell, np.int32)
+        grain_orient = np.ascontiguousarray(grain_orient, np.int32)
+        melted = None if melted is None else np.ascontiguousarray(melted, np.uint8)
+        dtc = None if dtc is None else np.ascontiguousarray(dtc, np.float64)
+        ptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        self._check(self._lib.amca_set_microstructure(self._h, ptr(grain), ptr(orient), ptr(melted), ptr(dtc),
+                                                      len(euler), ptr(euler), len(grain_cell), ptr(grain_cell),
+                                                      ptr(grain_orient), int(expected)))
 
     def set_rosenthal_frames(self, **kw) -> None:
         """FE-coupled decks: frames generated on the GPU (fields of amca_rosenthal)."""

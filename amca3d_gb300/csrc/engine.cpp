@@ -517,6 +517,40 @@ int amca_set_fe_frames(amca_t *h, const int32_t nodes[3], const double *coords, 
   });
 }
 
+int amca_set_microstructure(amca_t *h, const int32_t *grain, const int32_t *orient, const uint8_t *melted,
+                            const double *dtc, int64_t norient, const double *euler, int64_t ngrains,
+                            const int32_t *grain_cell, const int32_t *grain_orient, int64_t expected) {
+  if (!h || !grain || !orient || norient < 0 || ngrains < 0 || (norient && !euler) ||
+      (ngrains && (!grain_cell || !grain_orient)))
+    return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_set_microstructure needs an FE-coupled deck");
+    const PlainConfig &c = h->rm->config().ca;
+    const int64_t N = (int64_t)(c.nx + 2) * (c.ny + 2) * (c.nz + 2);
+    RestartData r;
+    r.ncells = N;
+    r.norient = norient;
+    r.ngrains = ngrains;
+    r.expected = expected;
+    r.grain.assign(grain, grain + N);
+    r.orient.assign(orient, orient + N);
+    if (melted)
+      r.melted.assign(melted, melted + N);
+    else
+      r.melted.assign((size_t)N, 0);
+    if (dtc)
+      r.dtc.assign(dtc, dtc + N);
+    else
+      r.dtc.assign((size_t)N, -1.0);
+    r.euler.assign(euler, euler + 3 * norient);
+    r.gcell.assign(grain_cell, grain_cell + ngrains);
+    r.gori.assign(grain_orient, grain_orient + ngrains);
+    for (int64_t g = 0; g < ngrains; ++g)
+      if (r.gori[g] < 0 || r.gori[g] >= norient) throw std::invalid_argument("grain orientation out of range");
+    h->rm->set_microstructure(std::move(r));
+  });
+}
+
 int amca_set_rosenthal_frames(amca_t *h, const amca_rosenthal *p) {
   if (!h || !p) return AMCA_ERR_ARG;
   return guarded(h, [&] {

@@ -3,6 +3,7 @@
 
 #include "errors.h"
 
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -110,6 +111,14 @@ void RemeltRealm::set_rosenthal(const RosenthalParams &p, int nframes, double ti
   frames_src_ = 2;
 }
 
+void RemeltRealm::set_microstructure(RestartData r) {
+  if (prepared_) throw StateError("amca_set_microstructure after amca_prepare");
+  const PlainConfig &c = cfg_.ca;
+  const int64_t N = (int64_t)(c.nx + 2) * (c.ny + 2) * (c.nz + 2);
+  if (r.ncells != N) throw std::invalid_argument("microstructure arrays must cover the ghost-inclusive grid");
+  micro_.reset(new RestartData(std::move(r)));
+}
+
 void RemeltRealm::prepare() {
   if (prepared_) return;
   const PlainConfig &c = cfg_.ca;
@@ -130,7 +139,7 @@ void RemeltRealm::prepare() {
     out[1] = centre_coord(c.y0, c.h, J);
     out[2] = centre_coord(c.z0, c.h, K);
   };
-  if (cfg_.random_micro) {
+  if (cfg_.random_micro && !micro_) {
     // random_microstructure_information (CellularAutomataManager_3D.cpp:1929-1984):
     // one orientation and one grain per interior cell, in cell order
     const int64_t M = (int64_t)c.nx * c.ny * c.nz;
@@ -153,7 +162,7 @@ void RemeltRealm::prepare() {
   } else {
     // load_microstructure_information + retrieve_grain_information_before_simulation
     // (CellularAutomataManager_3DRemelting.cpp:164-332)
-    RestartData r = read_restart(path(cfg_.micro_file));
+    RestartData r = micro_ ? *micro_ : read_restart(path(cfg_.micro_file));
     if (r.ncells != N)
       throw std::runtime_error("Error : microstructure information file is not fit the current domain size");
     if (!cfg_.nucleation && c.shuffle_vtr) mapped_vtr_ = make_mapped_ids(r.expected, true, *rng_);
@@ -225,6 +234,7 @@ void RemeltRealm::upload_initial_state() {
   RCK(cudaMemsetAsync(dev_.gdy, 0, N * 4, stream_));
   RCK(cudaMemsetAsync(dev_.gdz, 0, N * 4, stream_));
   RCK(cudaMemsetAsync(dev_.flagbits, 0, ((N + 31) / 32) * 4, stream_));
+  RCK(cudaMemsetAsync(dev_.eliq, 0, std::max<int64_t>(dev_.nelem, 1) * 4, stream_));
   RCK(remelt_init_theta(dev_, stream_));
   hostvel_->seq_req = 0;
   hostvel_->seq_done = 0;
@@ -325,6 +335,30 @@ void RemeltRealm::initialize() {
   }
   d.tag = tag;
   d.pc = pc;
+  {  // element -> interior cells (CSR), for the phase-update pass over active elements
+    std::vector<int32_t> htag((size_t)N);
+    d2h(htag.data(), tag, N * 4);
+    RCK(cudaStreamSynchronize(stream_));
+    std::vector<int64_t> start((size_t)d.nelem + 1, 0);
+    auto interior = [&](int64_t cell) {
+      const int K = (int)(cell / g.nxyg), J = (int)((cell % g.nxyg) / g.nxg), I = (int)((cell % g.nxyg) % g.nxg);
+      return I > 0 && I < g.nxg - 1 && J > 0 && J < g.nyg - 1 && K > 0 && K < g.nzg - 1;
+    };
+    for (int64_t cell = 0; cell < N; ++cell)
+      if (htag[cell] >= 0 && interior(cell)) start[htag[cell] + 1]++;
+    for (int64_t e = 0; e < d.nelem; ++e) start[e + 1] += start[e];
+    std::vector<int32_t> list((size_t)std::max<int64_t>(start[d.nelem], 1));
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (int64_t cell = 0; cell < N; ++cell)
+      if (htag[cell] >= 0 && interior(cell)) list[fill[htag[cell]]++] = (int32_t)cell;
+    int64_t *es = alloc<int64_t>(start.size());
+    int32_t *el = alloc<int32_t>(list.size());
+    h2d(es, start.data(), start.size() * 8);
+    h2d(el, list.data(), list.size() * 4);
+    RCK(cudaStreamSynchronize(stream_));
+    d.ecell_start = es;
+    d.ecell = el;
+  }
   // --- frames ---
   double *frames = alloc<double>((size_t)nframes_ * d.nnodes);
   if (frames_src_ == 2) {
@@ -342,6 +376,14 @@ void RemeltRealm::initialize() {
   d.emax = alloc<double>(d.nelem);
   d.emin = alloc<double>(d.nelem);
   d.evoid = alloc<uint8_t>(d.nelem);
+  d.eliq = alloc<int32_t>(d.nelem);
+  for (int sl = 0; sl < 2; ++sl) {
+    d.fmax[sl] = alloc<double>(d.nelem);
+    d.fmin[sl] = alloc<double>(d.nelem);
+    d.fnear[sl] = alloc<uint8_t>(d.nelem);
+  }
+  d.eact[0] = alloc<int32_t>(d.nelem);
+  d.eact[1] = alloc<int32_t>(d.nelem);
   // --- cells ---
   d.orient = alloc<int32_t>(N);
   d.grain = alloc<int32_t>(N);
@@ -391,6 +433,7 @@ void RemeltRealm::initialize() {
   h2d(sd, sites_.dtc.data(), sites_.dtc.size() * 8);
   d.site_cell = sc;
   d.site_dtc = sd;
+  d.snuc = alloc<uint8_t>(d.nsites);
   d.ctrl = alloc<RemeltCtrl>(1);
   // --- control block: CafeSolver::time_integration_weak_coupling set-up (CafeSolver.cpp:182-184) ---
   RemeltCtrl c0{};
@@ -404,9 +447,15 @@ void RemeltRealm::initialize() {
   c0.n_orient = n_init_orient_;
   c0.n_grains = n_init_grains_;
   c0.minT_key = host_dkey(c.Tm);
+  c0.fstat_frame[0] = c0.fstat_frame[1] = -1;
   ctrl0_ = c0;
   upload_initial_state();
-  blocks_ = remelt_persistent_grid(device_);
+  {
+    // blocks per SM of the persistent kernel; AMCA_REMELT_BLOCKS_PER_SM overrides the default for tuning
+    int per_sm = 1;
+    if (const char *e = getenv("AMCA_REMELT_BLOCKS_PER_SM")) per_sm = std::max(1, atoi(e));
+    blocks_ = remelt_persistent_grid(device_, per_sm);
+  }
   if (blocks_ <= 0) throw CudaError("no co-resident blocks for the persistent remelting kernel");
   vtr_.configure(c.output, workdir_);
   initialized_ = true;
@@ -581,16 +630,17 @@ size_t RemeltRealm::orientations(double *euler, size_t cap, int all) const {
 }
 
 double RemeltRealm::algorithmic_bytes() const {
-  // per step: 8 B per interior cell (orientation + element tag); per exact
-  // temperature 33 B (parametric coordinates 24, temperature 8, flag 1); per
-  // listed liquid cell 104 B (26 neighbour states); per flagged cell 364 B
-  // (grain record 48, 26 x (state 4 + temperature 8)); per capture 80 B
-  // (winner record 36, new record 36, state 8); per node 24 B (two frame
-  // values, one write) and per element 17 B (bounds).
+  // 8 B per cell the phase update visits (orientation + element tag); per
+  // exact temperature 33 B (parametric coordinates 24, temperature 8, flag 1);
+  // per listed liquid cell 104 B (26 neighbour states); per flagged cell
+  // 364 B (grain record 48, 26 x (state 4 + temperature 8)); per capture 80 B
+  // (winner record 36, new record 36, state 8); per step and node 24 B (two
+  // frame values, one write) and per element 21 B (bounds, void flag, liquid
+  // count).
   const double steps = (double)ctrl_.step;
-  const double M = (double)cfg_.ca.nx * cfg_.ca.ny * cfg_.ca.nz;
-  return 8 * M * steps + 33 * (double)ctrl_.exact_T + 104 * (double)ctrl_.liquid + 364 * (double)ctrl_.flagged +
-         80 * (double)ctrl_.captures + (24 * (double)dev_.nnodes + 17 * (double)dev_.nelem) * steps;
+  return 8 * (double)ctrl_.cells_visited + 33 * (double)ctrl_.exact_T + 104 * (double)ctrl_.liquid +
+         364 * (double)ctrl_.flagged + 80 * (double)ctrl_.captures +
+         (24 * (double)dev_.nnodes + 21 * (double)dev_.nelem) * steps;
 }
 
 void RemeltRealm::stats(amca_stats *s) const {
@@ -611,15 +661,18 @@ void RemeltRealm::stats(amca_stats *s) const {
   s->done = (c.status == kRemeltFinalTime || c.status == kRemeltFramesEnd) ? 1 : 0;
   s->kernel_ms = kernel_ms_;
   s->launches = launches_;
-  s->sites_scanned = (int64_t)c.melts;
+  s->sites_scanned = (int64_t)c.elements_active;
   s->nucleations = (int64_t)c.nucleations;
   s->captures = (int64_t)c.captures;
-  s->active_grown = (int64_t)c.flagged;
+  s->active_grown = (int64_t)c.cells_visited;
   s->grains_processed = (int64_t)c.liquid;
+  s->reserved = (int32_t)std::min<unsigned long long>(c.host_calls, 0x7fffffff);
   s->algorithmic_bytes = algorithmic_bytes();
   s->h2d_bytes = h2d_bytes_;
   s->d2h_bytes = d2h_bytes_;
   for (int i = 0; i < 5; ++i) s->phase_ms[i] = c.ns_phase[i] * 1e-6;
+  s->phase_ms[5] = c.ns_host * 1e-6;
+  s->phase_ms[6] = c.ns_barrier * 1e-6;
 }
 
 int RemeltRealm::final_grain_count() {

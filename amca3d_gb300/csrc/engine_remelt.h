@@ -32,6 +32,8 @@ class RemeltRealm {
   void set_frames(const int32_t nodes[3], const double *coords, int64_t nframes, const double *times,
                   const double *theta);
   void set_rosenthal(const RosenthalParams &p, int nframes, double time_offset);
+  // restart microstructure from memory (before prepare)
+  void set_microstructure(RestartData r);
 
   void prepare();     // host tables: microstructure, sites, orientation stream
   void initialize();  // device state, frames, FE -> CA map
@@ -72,6 +74,7 @@ class RemeltRealm {
   int ros_nframes_ = 0;
   double ros_toff_ = 0.0;
   int64_t nframes_ = 0;
+  std::unique_ptr<RestartData> micro_;  // set_microstructure
   // host tables
   std::unique_ptr<GlibcRand> rng_;
   OrientationTable otab_;          // initial orientations, then the nucleation stream

@@ -37,6 +37,7 @@
 //      step's node temperatures and element bounds are computed.
 // New grain objects (cells without one) get ids in sweep order: events
 // (sweep position, neighbour index) are sorted by block 0 after the step.
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include <algorithm>
@@ -71,6 +72,7 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
 __device__ bool grid_barrier(RemeltCtrl *c) {
   __syncthreads();
   if (threadIdx.x == 0) {
+    const unsigned long long tb = blockIdx.x == 0 ? now_ns() : 0ull;
     const unsigned gen = ld_acquire(&c->bar_gen);
     __threadfence();
     const unsigned arrived = atomicAdd(&c->bar_count, 1u);
@@ -90,6 +92,7 @@ __device__ bool grid_barrier(RemeltCtrl *c) {
       }
     }
     __threadfence();
+    if (blockIdx.x == 0) c->ns_barrier += now_ns() - tb;
   }
   __syncthreads();
   return ld_volatile(&c->error) == 0;
@@ -119,6 +122,16 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned *smem, unsigned *t
   *total = smem[kWarps - 1];
   __syncthreads();
   return before + x - v;
+}
+
+// List append from the threads that reach it together: one atomicAdd per
+// coalesced group, ranks within the group (order within a list is free).
+__device__ __forceinline__ unsigned append_slot(unsigned *counter) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group grp = cg::coalesced_threads();
+  unsigned base = 0;
+  if (grp.thread_rank() == 0) base = atomicAdd(counter, grp.size());
+  return grp.shfl(base, 0) + grp.thread_rank();
 }
 
 // Order-preserving key of a double (for atomicMin); NaN never reaches it.
@@ -204,6 +217,7 @@ __device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned n
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+      const unsigned long long h0 = now_ns();
       const unsigned seq = c->host_seq + 1;
       c->host_seq = seq;
       d.host->n = cnt;
@@ -220,6 +234,7 @@ __device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned n
       }
       c->host_calls += 1;
       c->host_vel += cnt;
+      c->ns_host += now_ns() - h0;
     }
     __syncthreads();
     if (!s_ok) break;
@@ -314,6 +329,37 @@ __device__ void element_bounds(const RemeltDevice &d, int64_t e, const double t[
   d.evoid[e] = vo ? 1 : 0;
   d.emax[e] = (nan || d.force_exact) ? INFINITY : mx + margin;
   d.emin[e] = (nan || d.force_exact) ? -INFINITY : mn - margin;
+}
+
+// Node extrema of frame f over element e, kept per frame slot: with both
+// frames of the current pair clear of the void threshold, every interpolated
+// node value lies between them (up to rounding), so the element bounds follow
+// without interpolating. `near`: a node within 2^-48 relative of the void
+// threshold (or NaN), where the exact interpolation decides.
+__device__ void frame_extrema(const RemeltDevice &d, const int64_t nid[8], int f, int64_t e, bool stored,
+                              double &mx, double &mn, bool &near) {
+  const int sl = f & 1;
+  if (stored) {
+    mx = d.fmax[sl][e];
+    mn = d.fmin[sl][e];
+    near = d.fnear[sl][e] != 0;
+    return;
+  }
+  const double *fr = d.frames + (int64_t)f * d.nnodes;
+  const double V = d.void_t + 0.00001;
+  mx = -INFINITY;
+  mn = INFINITY;
+  near = false;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const double v = fr[nid[i]];
+    if (!(v >= V + ldexp(fmax(fabs(v), fabs(V)), -48))) near = true;
+    mx = v > mx ? v : mx;
+    mn = v < mn ? v : mn;
+  }
+  d.fmax[sl][e] = mx;
+  d.fmin[sl][e] = mn;
+  d.fnear[sl][e] = near ? 1 : 0;
 }
 
 // nullMatTemp_ + 0.01: below it a cell counts as without material in the
@@ -650,7 +696,55 @@ __device__ void assign_new_grains(const RemeltDevice &d, RemeltCtrl *c) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long long limit) {
+// checkup_current_temperature_to_update_phase_state (Remelting.cpp:339-404) and
+// the per-cell part of checkup_liquid_cell_neigh_to_growth (:484-517) for one
+// interior cell. `count_all`: add every liquid cell to its element's count
+// (first step); otherwise only cells that melt now.
+__device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell, const double *th,
+                             const StepScalars &S, bool count_all, unsigned long long &exactT,
+                             unsigned long long &melts) {
+  int32_t o = d.orient[cell];
+  const int32_t e = d.tag[cell];
+  const bool withMat = e >= 0 && !d.evoid[e];
+  double T = -1.0;  // nullMatTemp_ (Remelting.cpp:29)
+  bool haveT = !withMat;
+  if (o > -1) {
+    if (withMat) {
+      // certainly below the liquidus and above nullMatTemp_ + 0.01: nothing changes
+      if (d.emax[e] < d.Tm && d.emin[e] >= null_plus()) return;
+      ++exactT;
+      eval_T(d, th, cell, T);
+      haveT = true;
+      if (T < d.Tm) {  // stays solid; the liquid-neighbour pass clears melted below nullMatTemp_ + 0.01
+        if (T < null_plus() && d.melted[cell]) d.melted[cell] = 0;
+        return;
+      }
+    }
+    d.orient[cell] = -1;  // melt
+    d.melted[cell] = withMat ? 1 : 0;
+    o = -1;
+    ++melts;
+    if (e >= 0 && !count_all) atomicAdd(&d.eliq[e], 1);
+  }
+  if (count_all && e >= 0) atomicAdd(&d.eliq[e], 1);
+  if (!haveT) {
+    ++exactT;
+    eval_T(d, th, cell, T);
+  }
+  const bool withMat2 = !(T < null_plus());
+  const uint8_t m0 = d.melted[cell];
+  uint8_t m1 = m0;
+  if (withMat2 && S.time >= S.max_ts) m1 = 1;
+  if (!withMat2) m1 = 0;
+  if (m1 != m0) d.melted[cell] = m1;
+  d.T[cell] = T;
+  if (withMat2 && !(T >= d.Tm)) {
+    const unsigned slot = append_slot(&c->n_liq);
+    if (slot < d.list_cap) d.liq[slot] = (int32_t)cell;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long long limit) {
   __shared__ unsigned smem[kWarps + 2];
   RemeltCtrl *c = d.ctrl;
   const Grid &g = d.g;
@@ -659,7 +753,7 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
   const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
   const int64_t M = (int64_t)g.nx * g.ny * g.nz;
   const int64_t nyzg = (int64_t)g.nyg * g.nzg;
-  unsigned long long tests = 0, tests64 = 0, caps = 0, exactT = 0, melts = 0;
+  unsigned long long tests = 0, tests64 = 0, caps = 0, exactT = 0, melts = 0, visited = 0, eactive = 0;
   bool ok = true;
   for (;;) {
     const StepScalars S = read_scalars(c);
@@ -681,7 +775,10 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
     // ===== A: phase update + melted flags (Remelting.cpp:339-404, :484-517) =====
     if (blockIdx.x == 0) {
       assign_new_grains(d, c);
-      if (tid == 0) c->n_claim = 0;
+      if (tid == 0) {
+        c->n_claim = 0;
+        c->n_eact[par ^ 1] = 0;  // built in phase E for the next step; its last reader was the previous phase A
+      }
     }
     {  // clear the previous step's liquid-neighbour flags
       const unsigned nprev = ld_volatile(&c->n_flag[par ^ 1]);
@@ -691,47 +788,25 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
         atomicAnd(&d.flagbits[x >> 5], ~(1u << (x & 31)));
       }
     }
-    for (int64_t q = gtid; q < M; q += nthr) {
-      const int I = (int)(q % g.nx) + 1;
-      const int J = (int)((q / g.nx) % g.ny) + 1;
-      const int K = (int)(q / ((int64_t)g.nx * g.ny)) + 1;
-      const int64_t cell = (int64_t)K * g.nxyg + (int64_t)J * g.nxg + I;
-      int32_t o = d.orient[cell];
-      const int32_t e = d.tag[cell];
-      const bool withMat = e >= 0 && !d.evoid[e];
-      double T = -1.0;  // nullMatTemp_ (Remelting.cpp:29)
-      bool haveT = !withMat;
-      if (o > -1) {
-        if (withMat) {
-          // certainly below the liquidus and above nullMatTemp_ + 0.01: nothing changes
-          if (d.emax[e] < d.Tm && d.emin[e] >= null_plus()) continue;
-          ++exactT;
-          eval_T(d, th, cell, T);
-          haveT = true;
-          if (T < d.Tm) {  // stays solid; the liquid-neighbour pass clears melted below nullMatTemp_ + 0.01
-            if (T < null_plus() && d.melted[cell]) d.melted[cell] = 0;
-            continue;
-          }
+    if (S.step == 0) {  // every interior cell; the liquid count per element starts here
+      for (int64_t q = gtid; q < M; q += nthr) {
+        const int I = (int)(q % g.nx) + 1;
+        const int J = (int)((q / g.nx) % g.ny) + 1;
+        const int K = (int)(q / ((int64_t)g.nx * g.ny)) + 1;
+        phase_update(d, c, (int64_t)K * g.nxyg + (int64_t)J * g.nxg + I, th, S, true, exactT, melts);
+      }
+      visited += (M + nthr - 1 - gtid) / nthr;
+    } else {  // the cells of the active elements (a warp per element)
+      const unsigned na = ld_volatile(&c->n_eact[par]);
+      const int lane = tid & 31;
+      const int64_t gw = gtid >> 5, nw = nthr >> 5;
+      for (int64_t w = gw; w < na; w += nw) {
+        const int32_t e = d.eact[par][w];
+        const int64_t b = d.ecell_start[e], en = d.ecell_start[e + 1];
+        for (int64_t k = b + lane; k < en; k += 32) {
+          phase_update(d, c, d.ecell[k], th, S, false, exactT, melts);
+          ++visited;
         }
-        d.orient[cell] = -1;  // melt
-        d.melted[cell] = withMat ? 1 : 0;
-        o = -1;
-        ++melts;
-      }
-      if (!haveT) {
-        ++exactT;
-        eval_T(d, th, cell, T);
-      }
-      const bool withMat2 = !(T < null_plus());
-      const uint8_t m0 = d.melted[cell];
-      uint8_t m1 = m0;
-      if (withMat2 && S.time >= S.max_ts) m1 = 1;
-      if (!withMat2) m1 = 0;
-      if (m1 != m0) d.melted[cell] = m1;
-      d.T[cell] = T;
-      if (withMat2 && !(T >= d.Tm)) {
-        const unsigned slot = atomicAdd(&c->n_liq, 1u);
-        if (slot < d.list_cap) d.liq[slot] = (int32_t)cell;
       }
     }
     if (gtid == 0) {
@@ -757,13 +832,35 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
               const unsigned bit = 1u << (nb & 31);
               const unsigned old = atomicOr(&d.flagbits[nb >> 5], bit);
               if (!(old & bit)) {
-                const unsigned slot = atomicAdd(&c->n_flag[par], 1u);
+                const unsigned slot = append_slot(&c->n_flag[par]);
                 if (slot < d.list_cap) d.flagged[par][slot] = nb;
               }
             }
           }
         }
       }
+    }
+    // site conditions of nucleate_at_nucleation_sites (Remelting.cpp:946-960), all blocks
+    for (int64_t sidx = gtid; sidx < d.nsites; sidx += nthr) {
+      const int32_t cell = d.site_cell[sidx];
+      double T = -1.0;
+      const bool withMat = eval_T(d, th, cell, T);
+      bool cooling = false;
+      if (S.step > 0) {  // cooling_ of this step's phase update (Remelting.cpp:362-373)
+        double Told = -1.0;
+        eval_T(d, thp, cell, Told);
+        double rate = 410;
+        if (Told > 0) rate = (T - Told) / S.dt;
+        if (T <= 0) rate = 0;
+        cooling = withMat ? (rate < 0) : false;
+      }
+      uint8_t f = 0;
+      const bool isLiquid = d.orient[cell] == -1;
+      if (cooling && isLiquid && d.melted[cell] && T > d.Tnuc) {
+        const double dT = d.Tm - T;
+        if (dT > d.site_dtc[sidx]) f = d.grain[cell] == -1 ? 2 : 1;
+      }
+      d.snuc[sidx] = f;
     }
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
@@ -785,30 +882,9 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
       const long long n_grains = ld_volatile(&c->n_grains);
       for (int base = 0; base < d.nsites; base += kBlock) {
         const int sidx = base + tid;
-        bool nuc = false, newg = false;
-        int32_t cell = -1;
-        if (sidx < d.nsites) {
-          cell = d.site_cell[sidx];
-          double T = -1.0;
-          const bool withMat = eval_T(d, th, cell, T);
-          bool cooling = false;
-          if (S.step > 0) {  // cooling_ of this step's phase update (Remelting.cpp:362-373)
-            double Told = -1.0;
-            eval_T(d, thp, cell, Told);
-            double rate = 410;
-            if (Told > 0) rate = (T - Told) / S.dt;
-            if (T <= 0) rate = 0;
-            cooling = withMat ? (rate < 0) : false;
-          }
-          const bool isLiquid = d.orient[cell] == -1;
-          if (cooling && isLiquid && d.melted[cell] && T > d.Tnuc) {
-            const double dT = d.Tm - T;
-            if (dT > d.site_dtc[sidx]) {
-              nuc = true;
-              newg = d.grain[cell] == -1;
-            }
-          }
-        }
+        const uint8_t f = sidx < d.nsites ? d.snuc[sidx] : 0;
+        const bool nuc = f != 0, newg = f == 2;
+        const int32_t cell = sidx < d.nsites ? d.site_cell[sidx] : -1;
         unsigned tot_o, tot_g;
         const unsigned r_o = block_exclusive_scan(nuc ? 1u : 0u, smem, &tot_o);
         const unsigned r_g = block_exclusive_scan(newg ? 1u : 0u, smem, &tot_g);
@@ -824,6 +900,8 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
           d.gdx[cell] = d.gdy[cell] = d.gdz[cell] = 0.0f;
           if (newg) d.grain[cell] = (int32_t)(n_grains + done_g + r_g);
           d.orient[cell] = oid;
+          const int32_t e = d.tag[cell];
+          if (e >= 0) atomicSub(&d.eliq[e], 1);
         }
         done_o += tot_o;
         done_g += tot_g;
@@ -857,7 +935,7 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
             const double Targ = (T < d.Ts) ? d.Ts + 0.01 : T;
             d.fvel[q] = velocity(d, Targ, hard);
             if (hard) {
-              const unsigned slot = atomicAdd(&c->n_hard, 1u);
+              const unsigned slot = append_slot(&c->n_hard);
               if (slot < d.list_cap) {
                 d.hard_idx[slot] = (int32_t)q;
                 d.hard_T[slot] = Targ;
@@ -939,7 +1017,7 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
         if (f) {
           const int32_t old = atomicMin(&d.orient[nb], mine);
           if (old == -1) {
-            const unsigned slot = atomicAdd(&c->n_claim, 1u);
+            const unsigned slot = append_slot(&c->n_claim);
             if (slot < d.list_cap) d.claimed[slot] = nb;
           }
         }
@@ -985,7 +1063,7 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
             const int di = I - wi, dj = J - wj, dk = K - wk;
             int m = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
             m = m > 13 ? m - 1 : m;
-            const unsigned slot = atomicAdd(&c->n_new, 1u);
+            const unsigned slot = append_slot(&c->n_new);
             if (slot < (unsigned)kNewGrainCap) {
               d.newkey[slot] = ((unsigned long long)(uint32_t)w << 5) | (unsigned)m;
               d.newcell[slot] = nb;
@@ -994,6 +1072,8 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
             }
           }
           d.orient[nb] = ori;
+          const int32_t e = d.tag[nb];
+          if (e >= 0) atomicSub(&d.eliq[e], 1);
           ++caps;
         }
       }
@@ -1023,17 +1103,48 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
       const double *f1 = f0 - d.nnodes;
       double *tn = d.theta[(S.step + 1) % 3];
       for (int64_t n = gtid; n < d.nnodes; n += nthr) tn[n] = lerp_node(f0[n], f1[n], ratio, d.void_t);
+      const bool st0 = ld_volatile(&c->fstat_frame[f_new & 1]) == f_new;
+      const bool st1 = ld_volatile(&c->fstat_frame[(f_new - 1) & 1]) == f_new - 1;
       for (int64_t e = gtid; e < d.nelem; e += nthr) {
         int64_t nid[8];
         elem_nodes(d.nn, e, nid);
-        double t[8];
+        const uint8_t void_before = d.evoid[e];
+        double mx0, mn0, mx1, mn1;
+        bool near0, near1;
+        frame_extrema(d, nid, f_new, e, st0, mx0, mn0, near0);
+        frame_extrema(d, nid, f_new - 1, e, st1, mx1, mn1, near1);
+        if (near0 || near1 || d.force_exact) {
+          double t[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) t[i] = lerp_node(f0[nid[i]], f1[nid[i]], ratio, d.void_t);
-        element_bounds(d, e, t);
+          for (int i = 0; i < 8; ++i) t[i] = lerp_node(f0[nid[i]], f1[nid[i]], ratio, d.void_t);
+          element_bounds(d, e, t);
+        } else {
+          const double mx = mx0 > mx1 ? mx0 : mx1, mn = mn0 < mn1 ? mn0 : mn1;
+          const double mg = fmax(fabs(mx), fabs(mn));
+          d.evoid[e] = 0;
+          d.emax[e] = mx + ldexp(mg, -44);
+          d.emin[e] = mn - ldexp(mg, -44);
+        }
+        // the next phase update visits this element's cells when some may change: hot enough to
+        // melt or below nullMatTemp_ + 0.01, void status changed, or holding liquid with material
+        // (cells of a cold element are solid except those counted in eliq; a void element's cells
+        // are all liquid without material once it has been visited)
+        const bool v = d.evoid[e] != 0;
+        const bool active = (!v && !(d.emax[e] < d.Tm && d.emin[e] >= null_plus())) || (v != (void_before != 0)) ||
+                            (!v && ld_volatile(&d.eliq[e]) > 0);
+        if (active) {
+          const unsigned slot = append_slot(&c->n_eact[par ^ 1]);
+          if (slot < (unsigned)d.nelem) d.eact[par ^ 1][slot] = (int32_t)e;
+          ++eactive;
+        }
       }
     }
     if (gtid == 0) {
       if (bad) atomicCAS(&c->error, 0, kRemeltErrFrame);
+      if (!exhausted) {
+        c->fstat_frame[f_new & 1] = f_new;
+        c->fstat_frame[(f_new - 1) & 1] = f_new - 1;
+      }
       c->step = S.step + 1;
       c->time = S.time + dT;
       c->dt_prev = S.dt;
@@ -1066,15 +1177,17 @@ __global__ void __launch_bounds__(kBlock, 4) remelt_kernel(RemeltDevice d, long 
   if (caps) atomicAdd(&c->captures, caps);
   if (exactT) atomicAdd(&c->exact_T, exactT);
   if (melts) atomicAdd(&c->melts, melts);
+  if (visited) atomicAdd(&c->cells_visited, visited);
+  if (eactive) atomicAdd(&c->elements_active, eactive);
 }
 
 }  // namespace
 
-int remelt_persistent_grid(int device) {
+int remelt_persistent_grid(int device, int per_sm) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, remelt_kernel, kBlock, 0) != cudaSuccess) return 0;
-  return sms * std::max(1, std::min(per, 4));
+  return sms * std::max(1, std::min(per, per_sm));
 }
 
 cudaError_t remelt_run_steps(const RemeltDevice &d, long long limit, int blocks, cudaStream_t s) {

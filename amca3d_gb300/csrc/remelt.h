@@ -57,10 +57,15 @@ struct RemeltCtrl {
   int vmin_hard;          // the velocity at the minimum temperature came from the host
   double vmin;
   unsigned int n_flag[2];
+  unsigned int n_eact[2];
   unsigned long long minT_key;
   // counters
-  unsigned long long tests, tests64, captures, nucleations, flagged, liquid, exact_T, melts, host_vel, host_calls;
+  unsigned long long tests, tests64, captures, nucleations, flagged, liquid, exact_T, melts, host_vel, host_calls,
+      cells_visited, elements_active;
   unsigned long long ns_phase[5];
+  unsigned long long ns_host;  // block 0's wait for host velocity answers
+  unsigned long long ns_barrier;  // block 0's time inside grid barriers
+  int fstat_frame[2];          // frame whose per-element extrema each slot holds (-1: none)
 };
 
 struct RemeltDevice {
@@ -102,6 +107,13 @@ struct RemeltDevice {
   double *emax, *emin;       // per element bounds on the interpolated temperature (current step)
   int force_exact;           // some parametric coordinate is not finite: no bound shortcuts
   uint8_t *evoid;            // per element: some node below void_temperature + 1e-5
+  int32_t *eliq;             // per element: interior liquid cells it holds
+  double *fmax[2], *fmin[2]; // per element: node extrema of a frame (slot = frame index & 1)
+  uint8_t *fnear[2];         // per element: some node of that frame near void_temperature + 1e-5 (or NaN)
+  const int64_t *ecell_start;  // element -> its interior cells (CSR)
+  const int32_t *ecell;
+  int32_t *eact[2];          // elements whose cells the next phase update visits, by step parity
+  uint8_t *snuc;             // per site: nucleates this step (1), and creates a grain object (2)
   // lists
   int32_t *liq;              // liquid cells whose neighbours may be flagged
   int32_t *flagged[2];       // flagged cells, by step parity
@@ -148,8 +160,9 @@ cudaError_t remelt_rosenthal_frames(const RosenthalParams &p, int nframes, doubl
 // Frame-0 node temperatures and element bounds before the first step.
 cudaError_t remelt_init_theta(const RemeltDevice &d, cudaStream_t s);
 
-// Grid size for the persistent kernel (co-resident blocks).
-int remelt_persistent_grid(int device);
+// Grid size for the persistent kernel: per_sm co-resident blocks per SM (at
+// most what fits).
+int remelt_persistent_grid(int device, int per_sm);
 
 // Run CA steps until `limit` steps in total, the final time, the end of the
 // frames, or an orientation stream shorter than a step may need.

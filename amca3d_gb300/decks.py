@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+import os
 from typing import Optional, Sequence, Tuple
 
 
@@ -371,3 +372,231 @@ time_integrators:
         - realm0
         - realm1
 """
+
+
+# ---------------------------------------------------------------------------
+# Synthetic FE inputs: Rosenthal frames and columnar restart microstructures.
+# The reference's PBF examples ship without their temperature histories;
+# these stand in for them in the reference's own file formats.
+# ---------------------------------------------------------------------------
+LN2 = 0.6931471805599453
+INV_LN2 = 1.4426950408889634
+EXP_TAYLOR = [1.0 / math.factorial(n) for n in range(14)]
+
+
+def det_exp(a):
+    """exp(a) for a <= 0 from IEEE add/mul and ldexp only: k = rint(a/ln2),
+    r = a - k ln2, a degree-13 Taylor polynomial in Horner form, times 2^k.
+    Relative error below 1e-13; the point is that it is the same double on
+    every IEEE platform (no libm, no contraction), host or device
+    (amca_set_rosenthal_frames evaluates the same operations on the GPU)."""
+    import numpy as np
+
+    a = np.asarray(a, dtype=np.float64)
+    a = np.maximum(a, -700.0)
+    k = np.rint(a * INV_LN2)
+    r = a - k * LN2
+    p = np.full_like(r, EXP_TAYLOR[13])
+    for n in range(12, -1, -1):
+        p = p * r + EXP_TAYLOR[n]
+    return np.ldexp(p, k.astype(np.int64))
+
+
+@dataclasses.dataclass
+class Rosenthal:
+    """Quasi-steady field of a point source moving along +x on the top surface
+    of a semi-infinite body (SI units):
+    T = t0 + (A P)/(2 pi k R) exp(-v (R + xi)/(2 alpha)), xi = x - (x_start + v t),
+    capped at t_cap near the source."""
+
+    power: float = 30.0          # W
+    absorptivity: float = 0.4
+    speed: float = 1.0           # m/s along +x
+    conductivity: float = 20.0   # W/(m K)
+    diffusivity: float = 5e-6    # m^2/s
+    t0: float = 300.0            # K
+    t_cap: float = 3000.0        # K, cap near the source
+    x_start: float = -1.0e-5     # source x at t = 0
+    y_line: float = 2.0e-5       # track y
+    z_top: float = 2.4e-5        # surface z
+    void_above: Optional[float] = None  # nodes with z > z_top + void_above get t_void
+    t_void: float = 293.0
+
+    def field(self, x, y, z, t):
+        import numpy as np
+
+        xi = x - (self.x_start + self.speed * t)
+        dy = y - self.y_line
+        dz = z - self.z_top
+        r = np.sqrt((xi * xi + dy * dy) + dz * dz)
+        r = np.maximum(r, 1e-9)
+        q = (self.absorptivity * self.power) / ((2.0 * math.pi * self.conductivity) * r)
+        T = self.t0 + q * det_exp(-(self.speed * (r + xi)) / (2.0 * self.diffusivity))
+        T = np.minimum(T, self.t_cap)
+        if self.void_above is not None:
+            T = np.where(z > self.z_top + self.void_above, self.t_void, T)
+        return T
+
+
+@dataclasses.dataclass
+class FrameSpec:
+    """Structured FE node grid and frame times in file units; the text format
+    is the reference's (CA/src/LoadDataFromFile.cpp:21-191): title lines, then
+    per frame a subtitle whose 4th line holds "step step time time x0 x1 y0 y1
+    z0 z1" and one "x y z T" line per node, x fastest. Values are written with
+    17 significant digits, so every reader sees the same doubles."""
+
+    origin: Tuple[float, float, float]
+    spacing: float
+    nodes: Tuple[int, int, int]
+    frame_dt: float
+    frames: int
+    source: Rosenthal
+    length_scale: float = 1.0     # file coordinate * length_scale = metres
+    time_scale: float = 1.0       # file time * time_scale = seconds
+    time_offset: float = 0.0      # time written for frame 0
+
+    def node_coords(self):
+        import numpy as np
+
+        nx, ny, nz = self.nodes
+        K, J, I = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        x = self.origin[0] + self.spacing * I
+        y = self.origin[1] + self.spacing * J
+        z = self.origin[2] + self.spacing * K
+        return x.ravel(), y.ravel(), z.ravel()
+
+    def frame_values(self, f: int):
+        x, y, z = self.node_coords()
+        s = self.length_scale
+        return self.source.field(x * s, y * s, z * s, (f * self.frame_dt) * self.time_scale)
+
+    def write(self, path: str, title_lines: int = 4) -> None:
+        nx, ny, nz = self.nodes
+        x, y, z = self.node_coords()
+        xyz = [f"{a!r} {b!r} {c!r}" for a, b, c in zip(x.tolist(), y.tolist(), z.tolist())]
+        with open(path, "w") as f:
+            for t in range(title_lines):
+                f.write("Title\n" if t == 0 else ("End of title\n" if t == title_lines - 1
+                                                   else "synthetic Rosenthal frames\n"))
+            for fr in range(self.frames):
+                T = self.frame_values(fr)
+                tt = self.time_offset + fr * self.frame_dt
+                f.write("\n")
+                f.write("Subtitle\n")
+                f.write("No. step   No. step    time   time   x0    x1   y0   y1    z0   z1\n")
+                f.write(f"{fr + 1} {fr + 1} {tt!r} {tt!r} 0 {nx - 1} 0 {ny - 1} 0 {nz - 1}\n")
+                f.write("x  y  z  tn\n")
+                f.write("".join(f"{p} {v!r}\n" for p, v in zip(xyz, T.tolist())))
+
+    def rosenthal_kwargs(self) -> dict:
+        """Arguments of CellularAutomataRealm.set_rosenthal_frames for these frames."""
+        s = self.source
+        return dict(origin=self.origin, spacing=self.spacing, nodes=self.nodes, frames=self.frames,
+                    length_scale=self.length_scale, frame_dt=self.frame_dt, time_scale=self.time_scale,
+                    time_offset=self.time_offset, power=s.power, absorptivity=s.absorptivity, speed=s.speed,
+                    conductivity=s.conductivity, diffusivity=s.diffusivity, t0=s.t0, t_cap=s.t_cap,
+                    x_start=s.x_start, y_line=s.y_line, z_top=s.z_top,
+                    void_above_set=0 if s.void_above is None else 1,
+                    void_above=0.0 if s.void_above is None else s.void_above, t_void=s.t_void)
+
+
+def columnar_microstructure(cells, cell_size: float, origin, grains: int, seed: int, grainless_mod: int = 0) -> dict:
+    """Restart microstructure (the content of grainInfo<rank>.txt) of
+    `grains` columnar grains: Voronoi regions of seed points in the x-y plane,
+    extruded in z. Every interior cell is its own grain object with its
+    region's orientation; ghost cells hold grain and orientation -1. With
+    grainless_mod > 0, interior cells with (i + 2j + 3k) % grainless_mod == 0
+    keep the orientation but get no grain object. Returns the arrays of
+    CellularAutomataRealm.set_microstructure."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = cells
+    h = cell_size
+    gx, gy, gz = nx + 2, ny + 2, nz + 2
+    pts = rng.random((grains, 2)) * np.array([nx * h, ny * h]) + np.array(origin[:2])
+    # products of uniform draws and constants only: the same doubles on every platform
+    euler = np.stack([rng.random(grains) * (2 * math.pi), rng.random(grains) * math.pi,
+                      rng.random(grains) * (0.5 * math.pi)], axis=1)
+    cx = origin[0] + h * (np.arange(1, nx + 1) - 0.5)
+    cy = origin[1] + h * (np.arange(1, ny + 1) - 0.5)
+    CY, CX = np.meshgrid(cy, cx, indexing="ij")
+    CX, CY = CX.ravel(), CY.ravel()
+    region = np.empty(CX.size, np.int64)
+    for lo in range(0, CX.size, 8192):  # nearest seed, lowest index on ties
+        hi = min(CX.size, lo + 8192)
+        d2 = (CX[lo:hi, None] - pts[:, 0]) ** 2 + (CY[lo:hi, None] - pts[:, 1]) ** 2
+        region[lo:hi] = np.argmin(d2, axis=1)
+    region = region.reshape(ny, nx)
+    K, J, I = np.meshgrid(np.arange(1, nz + 1), np.arange(1, ny + 1), np.arange(1, nx + 1), indexing="ij")
+    K, J, I = K.ravel(), J.ravel(), I.ravel()
+    cell = K * gx * gy + J * gx + I
+    orient = np.full(gx * gy * gz, -1, np.int32)
+    grain = np.full(gx * gy * gz, -1, np.int32)
+    orient[cell] = region[J - 1, I - 1]
+    has = np.ones(cell.size, bool) if not grainless_mod else (I + 2 * J + 3 * K) % grainless_mod != 0
+    gcell = cell[has]
+    grain[gcell] = np.arange(gcell.size, dtype=np.int32)
+    return dict(grain=grain, orient=orient, euler=euler, grain_cell=gcell.astype(np.int32),
+                grain_orient=orient[gcell].astype(np.int32), expected=grains,
+                grain_centre=np.stack([origin[0] + h * (I[has] - 0.5), origin[1] + h * (J[has] - 0.5),
+                                       origin[2] + h * (K[has] - 0.5)], axis=1))
+
+
+def write_restart(path: str, m: dict, origin, cells, cell_size: float) -> str:
+    """Write a columnar_microstructure() as the reference's restart file
+    ("<stem>0.txt" for the stem of `path`); returns the file written."""
+    import numpy as np
+
+    nx, ny, nz = cells
+    gx, gy, gz = nx + 2, ny + 2, nz + 2
+    ncell = gx * gy * gz
+    stem = path[: path.rfind(".")] if "." in os.path.basename(path) else path
+    out = stem + "0.txt"
+    grain, orient, euler = m["grain"], m["orient"], m["euler"]
+    with open(out, "w") as f:
+        f.write("numCell; numOrientation; numLocalGrain; numGlobalExpectedGrain; start Point X; Y; Z; "
+                "number Point nx; ny; nz; dCell\n")
+        f.write(f"{ncell}  {len(euler)}  {len(m['grain_cell'])}  {m['expected']}  {float(origin[0])!r}  "
+                f"{float(origin[1])!r}  {float(origin[2])!r}  {gx}  {gy}  {gz}  {float(cell_size)!r}\n")
+        f.write("Cell informatin: ID; grainID; orientationID; hasBeenMelted; undercooling of seed\n")
+        f.write("".join(f"{c}  {g}  {o}  0  -1\n" for c, (g, o) in enumerate(zip(grain.tolist(), orient.tolist()))))
+        f.write("Orientation informatin: ID; EularAngle\n")
+        f.write("".join(f"{o}  {a!r}  {b!r}  {c!r}  \n" for o, (a, b, c) in enumerate(euler.tolist())))
+        f.write("Grain information: ID; cellID; grainCenter; orientationID\n")
+        cen = m["grain_centre"].tolist()
+        f.write("".join(f"{g}  {c}  {x!r}  {y!r}  {z!r}  {o}   \n"
+                        for g, (c, (x, y, z), o) in enumerate(zip(m["grain_cell"].tolist(), cen,
+                                                                   m["grain_orient"].tolist()))))
+    return out
+
+
+def config_pbf_500():
+    """A laser powder-bed-fusion track, the FE-coupled workload: 500 x 250 x
+    100 cells of 2 um (12.5M) on a columnar baseplate of 2,000 grains (seed 2),
+    one laser pass along x at mid-width on the top surface. Frames every 1 us
+    on 10 um FE nodes from the Rosenthal field (P = 200 W, A = 0.4, v = 1 m/s,
+    k = 20 W/(m K), alpha = 5e-6 m^2/s, T0 = 300 K), 1,550 frames (the source
+    runs from x = -50 um to 1.5 mm, past the melt-pool tail). Liquidus 1700 K,
+    solidus 1600 K, bulk sites 1e13 m^-3 (mean 8 K, std 2 K), KGT a2 = 2.03e-4.
+    Returns (deck, frames, microstructure arrays)."""
+    case = RemeltCase(name="pbf_500", cells=(500, 250, 100), cell_size=2.0e-6, nucleation=True, seed=2,
+                      bulk=(1.0e13, 8.0, 2.0), surface=(0.0, 0.5, 0.1), melting_temperature=1700.0,
+                      solidus_temperature=1600.0, a=(0.0, 2.03e-4, 0.0), microstructure="baseplate.txt",
+                      termination_time=1.0, time_step=1.0e-6, time_step_factor=0.4)
+    frames = pbf_frames(case.cells, case.cell_size, 1550)
+    micro = columnar_microstructure(case.cells, case.cell_size, case.origin, 2000, 2)
+    return case, frames, micro
+
+
+def pbf_frames(cells, cell_size: float, nframes: int) -> FrameSpec:
+    """Rosenthal frames of the PBF workload for a block of `cells`: 10 um
+    nodes from -10 um to one node past the block, the track at mid-width on
+    the top surface."""
+    nx, ny, nz = cells
+    sp = 1.0e-5
+    nodes = tuple(int(math.ceil(n * cell_size / sp)) + 3 for n in (nx, ny, nz))
+    src = Rosenthal(power=200.0, absorptivity=0.4, speed=1.0, conductivity=20.0, diffusivity=5.0e-6, t0=300.0,
+                    t_cap=3000.0, x_start=-5.0e-5, y_line=0.5 * ny * cell_size, z_top=nz * cell_size)
+    return FrameSpec(origin=(-sp, -sp, -sp), spacing=sp, nodes=nodes, frame_dt=1.0e-6, frames=nframes, source=src)

@@ -1,10 +1,13 @@
-"""Benchmark: plain CA timestep, uniform cooling at 320^3 (32.8M cells).
+"""Benchmark: plain CA timestep, uniform cooling at 320^3 (32.8M cells);
+with --workload pbf_500 the FE-coupled remelting realm on a laser track
+(500 x 250 x 100 cells, Rosenthal frames, columnar baseplate).
 
-One bench step = one full run of the 320^3 deck from its initial state to
-full solidification (every CA step of it), on one GPU; cell-updates/s =
-interior cells x CA steps / time.
+One bench step = one full run of the deck from its initial state to its end
+(full solidification, or the end of the frames), every CA step of it, on one
+GPU; cell-updates/s = interior cells x CA steps / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload uniform_320|pbf_500]
 
 ours (default): the CUDA path. `value` is device time (CUDA events around
   the persistent step kernel on its stream) with the realm's tables resident
@@ -237,8 +240,8 @@ def config_block(stats, case=None) -> dict:
     return cfg
 
 
-def load_traffic():
-    p = os.path.join(ROOT, "profiles", "ca_persistent_uniform_320.json")
+def load_traffic(name: str = "ca_persistent_uniform_320.json"):
+    p = os.path.join(ROOT, "profiles", name)
     if os.path.exists(p):
         try:
             return json.load(open(p)).get("dram_bytes_per_launch")
@@ -341,6 +344,184 @@ def run_ours(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# FE-coupled remelting workload (pbf_500)
+# ----------------------------------------------------------------------------
+PBF_TEXT = ("pbf_500: FE-coupled remelting realm, 500x250x100 cells of 2 um (12.5M) on a columnar baseplate of "
+            "2,000 grains (seed 2); one laser pass, Rosenthal frames every 1 us on 10 um FE nodes (P=200 W, A=0.4, "
+            "v=1 m/s, k=20, alpha=5e-6, T0=300 K, 1,550 frames generated on the GPU), liquidus 1700 K, solidus "
+            "1600 K, bulk sites 1e13 m^-3 (8 K, 2 K), KGT a2=2.03e-4; every CA step to the end of the frames")
+
+
+def _oracle_pbf_sample(steps: int) -> tuple:
+    """The PBF physics on a 250x125x50 block (1/8 of the cells) with a random
+    microstructure, the first `steps` CA steps, frames as text."""
+    import tempfile
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    cells = (250, 125, 50)
+    case = decks.RemeltCase(name="pbf_sample", cells=cells, cell_size=2.0e-6, nucleation=True, seed=2,
+                            bulk=(1.0e13, 8.0, 2.0), melting_temperature=1700.0, solidus_temperature=1600.0,
+                            a=(0.0, 2.03e-4, 0.0), microstructure="random", termination_time=1.0)
+    fr = decks.pbf_frames(cells, case.cell_size, steps + 20)
+    wd = tempfile.mkdtemp(prefix="pbf_sample_")
+    fr.write(os.path.join(wd, "frames.txt"))
+    r = amca_oracle.run_remelt(case, wd, max_steps=steps, fields=False)
+    return case.n_interior * r["steps"], r["loop_seconds"], r["steps"]
+
+
+def cpu_baseline_pbf(steps: int = 40) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    amca_oracle.build()
+    upd, el, n = _oracle_pbf_sample(steps)
+    return {"value": upd / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"C restatement of the reference, one core: the pbf_500 physics on a 250x125x50 block "
+                      f"(random microstructure), its first {n} CA steps, time loop only ({el:.1f} s)"}
+
+
+def run_reference_arm_pbf(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    amca_oracle.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    times, updates = [], []
+    with ctx.Pool(cores) as pool:
+        for it in range(args.warmup + args.steps):
+            res = pool.map(_oracle_pbf_sample, [args.ref_pbf_steps] * cores)
+            el = max(r[1] for r in res)
+            if it >= args.warmup:
+                times.append(el)
+                updates.append(sum(r[0] for r in res))
+    value = sum(updates) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": PBF_TEXT, "cells": 12500000},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent single-core runs of the C restatement of the reference, "
+                                   f"each the pbf_500 physics on a 250x125x50 block, first {args.ref_pbf_steps} "
+                                   f"CA steps, time loop only (the slowest process's loop time)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours_pbf(args, dist: Dist):
+    import amca3d_gb300 as A
+
+    dev = dist.local_rank
+    case, frames, m = decks.config_pbf_500()
+    if args.pbf_block:  # a profiling case with the workload's physics, not the workload
+        cells = tuple(int(v) for v in args.pbf_block.split(","))
+        case = dataclasses.replace(case, name="pbf_block", cells=cells)
+        frames = decks.pbf_frames(cells, case.cell_size, args.pbf_frames or frames.frames)
+        m = decks.columnar_microstructure(cells, case.cell_size, case.origin, 2000, 2)
+    deck = case.to_yaml()
+    rk = frames.rosenthal_kwargs()
+
+    def make():
+        r = A.CellularAutomataRealm(deck, seed=case.seed, device=dev)
+        r.set_microstructure(m["grain"], m["orient"], m["euler"], m["grain_cell"], m["grain_orient"],
+                             expected=m["expected"])
+        r.set_rosenthal_frames(**rk)
+        return r
+
+    realm = make()
+    realm.initialize()
+    for _ in range(args.warmup):
+        realm.reset()
+        realm.run()
+    clocks = ClockSampler(dev)
+    dist.barrier()
+    clocks.start()
+    device_ms, updates, ca_steps, alg_bytes, launches = [], [], [], [], 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        realm.reset()
+        realm.run()
+        st = realm.stats()
+        device_ms.append(st["kernel_ms"])
+        updates.append(st["cells"] * st["step"])
+        ca_steps.append(st["step"])
+        alg_bytes.append(st["algorithmic_bytes"])
+        launches += st["launches"] + 1  # step kernel launches + the frame-0 node kernel of the reset
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clk = clocks.stop()
+    st = realm.stats()
+    orient = realm.field("orientation_id")
+    gstats = grain_stats(orient, case.cells, realm.orientations())
+    realm.close()
+
+    pinned = A.PinnedBuffer(case.n_ghost, np.int32)
+    e2e_t, e2e_upd, h2d, d2h = [], [], [], []
+    for it in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        r = make()
+        r.initialize()
+        r.run()
+        r.field("orientation_id", out=pinned.array)
+        s_ = r.stats()
+        r.close()
+        el = time.perf_counter() - t
+        if it >= args.warmup:
+            e2e_t.append(el)
+            e2e_upd.append(s_["cells"] * s_["step"])
+            h2d.append(s_["h2d_bytes"])
+            d2h.append(s_["d2h_bytes"])
+    same = bool(np.array_equal(pinned.array, orient))
+    pinned.free()
+
+    t_dev = dist.reduce(sum(device_ms) / 1e3, "max")
+    upd_total = dist.reduce(float(sum(updates)), "sum")
+    e2e_time = dist.reduce(sum(e2e_t), "max")
+    e2e_total = dist.reduce(float(sum(e2e_upd)), "sum")
+    if dist.rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    achieved = (sum(alg_bytes) / len(alg_bytes)) / (sum(device_ms) / len(device_ms) / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": upd_total / t_dev, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(device_ms) / len(device_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": PBF_TEXT if not args.pbf_block else
+                   f"pbf_block {args.pbf_block}: the pbf_500 physics on another block (profiling case, not the "
+                   f"workload)", "cells": case.n_interior, "seed": case.seed,
+                   "l2": "inputs larger than L2: frames 1.6 GB + cell state 1.4 GB per run",
+                   "ca_steps_per_run": ca_steps[-1], "grain_objects": st["grains"], **gstats,
+                   "nucleations": st["nucleations"], "captures_per_run": st["captures"],
+                   "exact_temperatures_per_run": st["generations"], "flagged_per_run": st["active"],
+                   "cells_visited_per_run": st["active_grown"], "active_elements_per_run": st["sites_scanned"],
+                   "liquid_listed_per_run": st["grains_processed"], "host_velocity_round_trips": st["reserved"],
+                   "blocks_per_sm": int(os.environ.get("AMCA_REMELT_BLOCKS_PER_SM", "1")),
+                   "phase_ms_update_flags_dt_claim_capture": [round(x, 3) for x in st["phase_ms"][:5]],
+                   "host_velocity_wait_ms": round(st["phase_ms"][5], 3),
+                   "grid_barrier_ms": round(st["phase_ms"][6], 3),
+                   "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": load_traffic("remelt_persistent_pbf_500.json"),
+                     "peak_kind": f"{peak_kind} burst copy", "kernel": "remelt_kernel (persistent, one launch per run)",
+                     "algorithmic_bytes_per_launch": sum(alg_bytes) / len(alg_bytes)},
+        "e2e": {"value": e2e_total / e2e_time, "unit": UNIT, "h2d_bytes_per_step": int(np.mean(h2d)),
+                "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": 1e3 * e2e_time / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    if args.gpus == 1 and dist.rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_pbf(args.cpu_pbf_steps)
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -350,13 +531,21 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=128, help="edge of the CPU-baseline sample block")
     ap.add_argument("--ref-sample", type=int, default=96, help="edge of each reference-arm sample block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["uniform_320", "pbf_500"], default="uniform_320")
+    ap.add_argument("--cpu-pbf-steps", type=int, default=40, help="CA steps of the pbf_500 CPU-baseline sample")
+    ap.add_argument("--ref-pbf-steps", type=int, default=20, help="CA steps of each pbf_500 reference-arm sample")
+    ap.add_argument("--pbf-block", default="", help="X,Y,Z cells: run the pbf_500 physics on another block "
+                                                    "(profiling captures only, not the workload)")
+    ap.add_argument("--pbf-frames", type=int, default=0, help="frames of the --pbf-block case")
     ap.add_argument("--cells", type=int, default=320,
                     help="edge of the cubic block to run (320 = the measured workload; smaller blocks keep the "
                          "workload's physics and are for profiling captures only)")
     args = ap.parse_args()
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.workload == "pbf_500":
+            (run_reference_arm_pbf if args.impl == "reference" else run_ours_pbf)(args, dist)
+        elif args.impl == "reference":
             run_reference_arm(args, dist)
         else:
             run_ours(args, dist)

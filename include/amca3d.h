@@ -142,6 +142,18 @@ typedef struct {
 } amca_rosenthal;
 int amca_set_rosenthal_frames(amca_t *h, const amca_rosenthal *p);
 
+/* Restart microstructure from memory instead of the deck's
+ * load_microstructure_information file (same content as grainInfo<rank>.txt,
+ * CellularAutomataManager_3DRemelting::load_microstructure_information,
+ * CA/src/CellularAutomataManager_3DRemelting.cpp:164-307): per ghost-inclusive
+ * cell its grain id, orientation id (-1: take the grain's), melted flag and
+ * seed undercooling (dtc may be NULL: no seeds; melted may be NULL: 0); the
+ * Euler angles of norient orientations; per grain its cell and orientation;
+ * expected = the header's numGlobalExpectedGrains. Before amca_prepare. */
+int amca_set_microstructure(amca_t *h, const int32_t *grain, const int32_t *orient, const uint8_t *melted,
+                            const double *dtc, int64_t norient, const double *euler, int64_t ngrains,
+                            const int32_t *grain_cell, const int32_t *grain_orient, int64_t expected);
+
 /* Final outputs of a finished run: finalGrains.vtk, <pvd dir>/finalResult.txt,
  * the last VTR/PVTR/PVD snapshot and, when the deck asks for it,
  * grainInfo<rank>.txt. Replaces CellularAutomataSolver::finalize +
@@ -182,6 +194,16 @@ typedef struct {
    * [7] resolve mean, [8] resolve slowest block (summed over phases) */
   double phase_ms[9];
 } amca_stats;
+/* For the FE-coupled remelting realm the fields mean: liquid_cells -1 (not
+ * tracked), grains = grain objects, active = flagged (liquid-neighbour) cells
+ * summed over steps, generations = exact FP64 cell temperatures evaluated,
+ * done = the run reached termination_time or the end of the frames,
+ * reserved = host velocity round trips, sites_scanned = active elements
+ * visited, active_grown = cells visited by the phase update, grains_processed =
+ * liquid cells that flagged neighbours, phase_ms[0..4] = phase update,
+ * liquid-neighbour flags + site conditions, nucleation + minimum temperature,
+ * velocities + growth + claims, captures + frame replay; phase_ms[5] = block 0's
+ * wait for host velocity answers, phase_ms[6] = block 0's time in grid barriers. */
 int amca_get_stats(amca_t *h, amca_stats *out);
 
 /* Number of distinct orientation ids present in the field, the ghost layer

@@ -11,10 +11,12 @@
  * Build with -ffp-contract=off: the reference's x86-64 build has no FMA, so
  * a*b+c must stay two roundings on every host.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime */
 #include "amca_oracle.h"
 
 #include <float.h>
 #include <math.h>
+#include <time.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1523,6 +1525,8 @@ int amca_oracle_run_remelt(const amca_oracle_remelt_params *p, int max_steps, co
           nb[c++] = k * s->nxyg + j * s->nxg + i;
         }
   }
+  struct timespec loop_t0, loop_t1;
+  clock_gettime(CLOCK_MONOTONIC, &loop_t0);
   FE.dT = FE.ts0 - FE.ts1;   /* FiniteElementManager::setup_integration */
   double dT_FE = FE.dT;
   double maxTimestep = dT_FE; /* CellularAutomataManager::setup_integration */
@@ -1683,6 +1687,7 @@ int amca_oracle_run_remelt(const amca_oracle_remelt_params *p, int max_steps, co
     dT_FE = FE.ts0 - FE.time; /* get_max_time_step (LoadDataFromFile.cpp:197-205) */
     maxTimestep = dT_FE;
   }
+  clock_gettime(CLOCK_MONOTONIC, &loop_t1);
   if (orient_out) memcpy(orient_out, s->orient, N * sizeof(int32_t));
   if (grain_out) memcpy(grain_out, s->grain, N * sizeof(int32_t));
   if (temp_out) memcpy(temp_out, R.T, N * sizeof(double));
@@ -1701,6 +1706,7 @@ int amca_oracle_run_remelt(const amca_oracle_remelt_params *p, int max_steps, co
     res->elements = FE.nelem;
     res->frames_read = FE.frames;
     res->frames_exhausted = exhausted;
+    res->loop_seconds = (double)(loop_t1.tv_sec - loop_t0.tv_sec) + 1e-9 * (double)(loop_t1.tv_nsec - loop_t0.tv_nsec);
   }
   rc = 0;
 done:

@@ -122,6 +122,7 @@ typedef struct {
   int64_t num_grains, num_orient, num_sites, tests;
   int64_t nodes, elements, frames_read;
   int frames_exhausted;       /* 1 if the run ended on the end of the frame file */
+  double loop_seconds;        /* wall time of the coupled time loop (set-up excluded) */
 } amca_oracle_remelt_result;
 
 /* Run the coupled loop to final_time or the end of the frames (max_steps < 0:

@@ -157,7 +157,7 @@ class RemeltResult(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int), ("time", ctypes.c_double), ("last_dt", ctypes.c_double),
                 ("num_grains", ctypes.c_int64), ("num_orient", ctypes.c_int64), ("num_sites", ctypes.c_int64),
                 ("tests", ctypes.c_int64), ("nodes", ctypes.c_int64), ("elements", ctypes.c_int64),
-                ("frames_read", ctypes.c_int64), ("frames_exhausted", ctypes.c_int)]
+                ("frames_read", ctypes.c_int64), ("frames_exhausted", ctypes.c_int), ("loop_seconds", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

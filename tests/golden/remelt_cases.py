@@ -37,157 +37,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
-from amca3d_gb300.decks import RemeltCase  # noqa: E402
-
-
-@dataclasses.dataclass
-class Rosenthal:
-    """Moving point source (SI units)."""
-
-    power: float = 30.0          # W
-    absorptivity: float = 0.4
-    speed: float = 1.0           # m/s along +x
-    conductivity: float = 20.0   # W/(m K)
-    diffusivity: float = 5e-6    # m^2/s
-    t0: float = 300.0            # K
-    t_cap: float = 3000.0        # K, cap near the source
-    x_start: float = -1.0e-5     # source x at t = 0
-    y_line: float = 2.0e-5       # track y
-    z_top: float = 2.4e-5        # surface z
-    void_above: Optional[float] = None  # nodes with z > z_top + void_above get t_void
-    t_void: float = 293.0
-
-    def field(self, x, y, z, t):
-        xi = x - (self.x_start + self.speed * t)
-        dy = y - self.y_line
-        dz = z - self.z_top
-        r = np.sqrt((xi * xi + dy * dy) + dz * dz)
-        r = np.maximum(r, 1e-9)
-        q = (self.absorptivity * self.power) / ((2.0 * math.pi * self.conductivity) * r)
-        T = self.t0 + q * det_exp(-(self.speed * (r + xi)) / (2.0 * self.diffusivity))
-        T = np.minimum(T, self.t_cap)
-        if self.void_above is not None:
-            T = np.where(z > self.z_top + self.void_above, self.t_void, T)
-        return T
-
-
-LN2 = 0.6931471805599453
-INV_LN2 = 1.4426950408889634
-EXP_TAYLOR = [1.0 / math.factorial(n) for n in range(14)]
-
-
-def det_exp(a):
-    """exp(a) for a <= 0 from IEEE add/mul and ldexp only: k = rint(a/ln2),
-    r = a - k ln2, a degree-13 Taylor polynomial in Horner form, times 2^k.
-    Relative error below 1e-13; the point is that it is the same double on
-    every IEEE platform (no libm, no contraction), host or device."""
-    a = np.asarray(a, dtype=np.float64)
-    a = np.maximum(a, -700.0)
-    k = np.rint(a * INV_LN2)
-    r = a - k * LN2
-    p = np.full_like(r, EXP_TAYLOR[13])
-    for n in range(12, -1, -1):
-        p = p * r + EXP_TAYLOR[n]
-    return np.ldexp(p, k.astype(np.int64))
-
-
-@dataclasses.dataclass
-class FrameSpec:
-    """Structured FE node grid and frame times (file units, before length_scale)."""
-
-    origin: Tuple[float, float, float]
-    spacing: float
-    nodes: Tuple[int, int, int]
-    frame_dt: float
-    frames: int
-    source: Rosenthal
-    length_scale: float = 1.0     # file coordinate * length_scale = metres
-    time_scale: float = 1.0       # file time * time_scale = seconds
-    time_offset: float = 0.0      # time written for frame 0
-
-    def node_coords(self):
-        nx, ny, nz = self.nodes
-        i = np.arange(nx)
-        j = np.arange(ny)
-        k = np.arange(nz)
-        K, J, I = np.meshgrid(k, j, i, indexing="ij")
-        x = self.origin[0] + self.spacing * I
-        y = self.origin[1] + self.spacing * J
-        z = self.origin[2] + self.spacing * K
-        return x.ravel(), y.ravel(), z.ravel()
-
-    def frame_values(self, f: int) -> np.ndarray:
-        x, y, z = self.node_coords()
-        s = self.length_scale
-        return self.source.field(x * s, y * s, z * s, (f * self.frame_dt) * self.time_scale)
-
-    def write(self, path: str, title_lines: int = 4) -> None:
-        nx, ny, nz = self.nodes
-        x, y, z = self.node_coords()
-        xyz = [f"{a!r} {b!r} {c!r}" for a, b, c in zip(x.tolist(), y.tolist(), z.tolist())]
-        with open(path, "w") as f:
-            for t in range(title_lines):
-                f.write("Title\n" if t == 0 else ("End of title\n" if t == title_lines - 1 else "synthetic Rosenthal frames\n"))
-            for fr in range(self.frames):
-                T = self.frame_values(fr)
-                tt = self.time_offset + fr * self.frame_dt
-                f.write("\n")
-                f.write("Subtitle\n")
-                f.write("No. step   No. step    time   time   x0    x1   y0   y1    z0   z1\n")
-                f.write(f"{fr + 1} {fr + 1} {tt!r} {tt!r} 0 {nx - 1} 0 {ny - 1} 0 {nz - 1}\n")
-                f.write("x  y  z  tn\n")
-                f.write("".join(f"{p} {v!r}\n" for p, v in zip(xyz, T.tolist())))
+from amca3d_gb300 import decks  # noqa: E402
+from amca3d_gb300.decks import FrameSpec, RemeltCase, Rosenthal, det_exp  # noqa: E402,F401
 
 
 def columnar_microstructure(case: RemeltCase, grains: int, seed: int, path: str, grainless_mod: int = 0) -> None:
-    """Write a restart file (``<stem>0.txt``) holding ``grains`` columnar
-    grains: Voronoi regions of seed points in the x-y plane, extruded in z.
-    Every interior cell is its own grain object carrying its region's
-    orientation; ghost cells carry grain and orientation -1. With
-    grainless_mod > 0, interior cells with (i + 2j + 3k) % grainless_mod == 0
-    keep their orientation but get no grain object (grain id -1), so that
-    captures and nucleations there create new grains."""
-    rng = np.random.default_rng(seed)
-    nx, ny, nz = case.cells
-    h = case.cell_size
-    gx, gy, gz = nx + 2, ny + 2, nz + 2
-    pts = rng.random((grains, 2)) * np.array([nx * h, ny * h]) + np.array(case.origin[:2])
-    # products of uniform draws and constants only: the same doubles on every platform
-    euler = np.stack([rng.random(grains) * (2 * math.pi), rng.random(grains) * math.pi,
-                      rng.random(grains) * (0.5 * math.pi)], axis=1)
-    I = np.arange(1, nx + 1)
-    J = np.arange(1, ny + 1)
-    cx = case.origin[0] + h * (I - 0.5)
-    cy = case.origin[1] + h * (J - 0.5)
-    CY, CX = np.meshgrid(cy, cx, indexing="ij")
-    d2 = (CX[..., None] - pts[:, 0]) ** 2 + (CY[..., None] - pts[:, 1]) ** 2
-    region = np.argmin(d2, axis=2)  # [ny, nx]
-    ncell = gx * gy * gz
-    grain = np.full(ncell, -1, np.int64)
-    orient = np.full(ncell, -1, np.int64)
-    glist = []
-    for k in range(1, nz + 1):
-        for j in range(1, ny + 1):
-            for i in range(1, nx + 1):
-                c = k * gx * gy + j * gx + i
-                orient[c] = region[j - 1, i - 1]
-                if grainless_mod and (i + 2 * j + 3 * k) % grainless_mod == 0:
-                    continue
-                grain[c] = len(glist)
-                glist.append((c, case.origin[0] + h * (i - 0.5), case.origin[1] + h * (j - 0.5),
-                              case.origin[2] + h * (k - 0.5), int(orient[c])))
-    stem = path[: path.rfind(".")] if "." in os.path.basename(path) else path
-    with open(stem + "0.txt", "w") as f:
-        f.write("numCell; numOrientation; numLocalGrain; numGlobalExpectedGrain; start Point X; Y; Z; number Point nx; ny; nz; dCell\n")
-        f.write(f"{ncell}  {grains}  {len(glist)}  {grains}  {case.origin[0]!r}  {case.origin[1]!r}  {case.origin[2]!r}  "
-                f"{gx}  {gy}  {gz}  {h!r}\n")
-        f.write("Cell informatin: ID; grainID; orientationID; hasBeenMelted; undercooling of seed\n")
-        f.write("".join(f"{c}  {grain[c]}  {orient[c]}  0  -1\n" for c in range(ncell)))
-        f.write("Orientation informatin: ID; EularAngle\n")
-        f.write("".join(f"{o}  {float(euler[o, 0])!r}  {float(euler[o, 1])!r}  {float(euler[o, 2])!r}  \n"
-                        for o in range(grains)))
-        f.write("Grain information: ID; cellID; grainCenter; orientationID\n")
-        f.write("".join(f"{g}  {c}  {x!r}  {y!r}  {z!r}  {o}   \n" for g, (c, x, y, z, o) in enumerate(glist)))
+    """Write a restart file (``<stem>0.txt``) of ``grains`` columnar grains
+    (amca3d_gb300.decks.columnar_microstructure) for the case's grid."""
+    m = decks.columnar_microstructure(case.cells, case.cell_size, case.origin, grains, seed, grainless_mod)
+    decks.write_restart(path, m, case.origin, case.cells, case.cell_size)
 
 
 @dataclasses.dataclass

@@ -34,22 +34,12 @@ def amca():
     return A
 
 
-def rosenthal_kwargs(fs: remelt_cases.FrameSpec) -> dict:
-    s = fs.source
-    return dict(origin=fs.origin, spacing=fs.spacing, nodes=fs.nodes, frames=fs.frames, length_scale=fs.length_scale,
-                frame_dt=fs.frame_dt, time_scale=fs.time_scale, time_offset=fs.time_offset, power=s.power,
-                absorptivity=s.absorptivity, speed=s.speed, conductivity=s.conductivity, diffusivity=s.diffusivity,
-                t0=s.t0, t_cap=s.t_cap, x_start=s.x_start, y_line=s.y_line, z_top=s.z_top,
-                void_above_set=0 if s.void_above is None else 1,
-                void_above=0.0 if s.void_above is None else s.void_above, t_void=s.t_void)
-
-
 def make_realm(A, fx, wd, frames="file"):
     M.prepare(fx, wd)
     r = A.CellularAutomataRealm(fx.case.to_yaml(), seed=fx.case.seed, workdir=wd)
     fs = fx.frames
     if frames == "rosenthal":
-        r.set_rosenthal_frames(**rosenthal_kwargs(fs))
+        r.set_rosenthal_frames(**fs.rosenthal_kwargs())
     elif frames == "arrays":
         x, y, z = fs.node_coords()
         coords = np.stack([x, y, z], axis=1)
@@ -116,4 +106,26 @@ def test_remelt_gpu_bad_frame_stops_like_the_reference(amca, tmp_path):
     r.initialize()
     with pytest.raises(amca.AmcaError, match="check title of line"):
         r.run()
+    r.close()
+
+
+@pytest.mark.parametrize("name", ["remelt_columnar", "remelt_new_grains"])
+def test_remelt_gpu_microstructure_from_memory(amca, tmp_path, name):
+    """amca_set_microstructure with the restart file's content gives the
+    file's run."""
+    from amca3d_gb300 import decks
+
+    fx = FIX[name]
+    M.prepare(fx, str(tmp_path))
+    m = decks.columnar_microstructure(fx.case.cells, fx.case.cell_size, fx.case.origin, fx.columnar_grains,
+                                      fx.columnar_seed, fx.grainless_mod)
+    r = amca.CellularAutomataRealm(fx.case.to_yaml(), seed=fx.case.seed, workdir=str(tmp_path))
+    r.set_microstructure(m["grain"], m["orient"], m["euler"], m["grain_cell"], m["grain_orient"],
+                         expected=m["expected"])
+    r.set_rosenthal_frames(**fx.frames.rosenthal_kwargs())
+    r.initialize()
+    r.run()
+    g = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    for k in ("orient", "grain", "melted"):
+        assert np.array_equal(r.field(FIELD_OF[k]).astype(g[k].dtype), g[k]), k
     r.close()
