@@ -335,6 +335,11 @@ void RemeltRealm::initialize() {
   }
   d.tag = tag;
   d.pc = pc;
+  {
+    float *pc32 = alloc<float>(3 * N);
+    RCK(remelt_round_coords(pc, pc32, 3 * N, stream_));
+    d.pc32 = pc32;
+  }
   {  // element -> interior cells (CSR), for the phase-update pass over active elements
     std::vector<int32_t> htag((size_t)N);
     d2h(htag.data(), tag, N * 4);
@@ -372,7 +377,10 @@ void RemeltRealm::initialize() {
   d.frame_time = ftime;
   d.nframes = (int)nframes_;
   d.bad_frame = (int)frames_.bad_frame;
-  for (int i = 0; i < 3; ++i) d.theta[i] = alloc<double>(d.nnodes);
+  for (int i = 0; i < 3; ++i) {
+    d.theta[i] = alloc<double>(d.nnodes);
+    d.theta32[i] = alloc<float>(d.nnodes);
+  }
   d.emax = alloc<double>(d.nelem);
   d.emin = alloc<double>(d.nelem);
   d.evoid = alloc<uint8_t>(d.nelem);
@@ -389,7 +397,7 @@ void RemeltRealm::initialize() {
   d.grain = alloc<int32_t>(N);
   d.melted = alloc<uint8_t>(N);
   d.flagbits = alloc<uint32_t>((N + 31) / 32);
-  d.T = alloc<double>(N);
+  d.tcls = alloc<uint8_t>(N);
   d.gx = alloc<double>(N);
   d.gy = alloc<double>(N);
   d.gz = alloc<double>(N);

@@ -295,6 +295,30 @@ __device__ bool eval_T(const RemeltDevice &d, const double *th, int64_t c, doubl
   return true;
 }
 
+// FP32 estimate of evaluate_temperature's value for a cell with material,
+// with a bound on its error: the shape functions are convex weights
+// (parametric coordinates in [-1, 1]), so the FP32 evaluation of the
+// weighted sum, with the coordinates and node values rounded to float, errs
+// by less than 2e-6 of the largest node magnitude; the bound returned is
+// 2^-16 of it (plus 2^-16 absolute).
+__device__ float eval_T32(const RemeltDevice &d, const float *th32, int64_t c, int32_t e, float &err) {
+  int64_t nid[8];
+  elem_nodes(d.nn, e, nid);
+  const float xi = d.pc32[3 * c], eta = d.pc32[3 * c + 1], zeta = d.pc32[3 * c + 2];
+  const float a0 = 1.0f - eta, a1 = 1.0f + eta, b0 = 1.0f - xi, b1 = 1.0f + xi, c0 = 1.0f - zeta, c1 = 1.0f + zeta;
+  float t[8];
+  float mg = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    t[i] = th32[nid[i]];
+    mg = fmaxf(mg, fabsf(t[i]));
+  }
+  const float v = 0.125f * (a0 * b0 * c0 * t[0] + a0 * b1 * c0 * t[1] + a1 * b1 * c0 * t[2] + a1 * b0 * c0 * t[3] +
+                            a0 * b0 * c1 * t[4] + a0 * b1 * c1 * t[5] + a1 * b1 * c1 * t[6] + a1 * b0 * c1 * t[7]);
+  err = ldexpf(mg, -16) + 1.52587890625e-05f;
+  return v;
+}
+
 // thetaArray_ update of pseudo_single_integration_step (LoadDataFromFile.cpp:281-290)
 __device__ __forceinline__ double lerp_node(double th0, double th1, double ratio, double null_mat) {
   if (th0 <= null_mat) return null_mat;
@@ -596,7 +620,10 @@ __global__ void rosenthal_kernel(RosenthalParams p, int nframes, double *frames)
 
 __global__ void init_theta_kernel(RemeltDevice d) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.nnodes; n += stride) d.theta[0][n] = d.frames[n];
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.nnodes; n += stride) {
+    d.theta[0][n] = d.frames[n];
+    d.theta32[0][n] = (float)d.frames[n];
+  }
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.nelem; e += stride) {
     int64_t nid[8];
     elem_nodes(d.nn, e, nid);
@@ -612,6 +639,19 @@ cudaError_t remelt_rosenthal_frames(const RosenthalParams &p, int nframes, doubl
   const int64_t total = (int64_t)p.nodes[0] * p.nodes[1] * p.nodes[2] * nframes;
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
   rosenthal_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, nframes, frames);
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void round_coords_kernel(const double *pc, float *pc32, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    pc32[i] = (float)pc[i];
+}
+}  // namespace
+
+cudaError_t remelt_round_coords(const double *pc, float *pc32, int64_t n, cudaStream_t s) {
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  round_coords_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(pc, pc32, n);
   return cudaGetLastError();
 }
 
@@ -701,22 +741,49 @@ __device__ void assign_new_grains(const RemeltDevice &d, RemeltCtrl *c) {
 // interior cell. `count_all`: add every liquid cell to its element's count
 // (first step); otherwise only cells that melt now.
 __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell, const double *th,
-                             const StepScalars &S, bool count_all, unsigned long long &exactT,
+                             const float *th32, const StepScalars &S, bool count_all, unsigned long long &exactT,
                              unsigned long long &melts) {
   int32_t o = d.orient[cell];
   const int32_t e = d.tag[cell];
   const bool withMat = e >= 0 && !d.evoid[e];
+  const double np = null_plus();
+  // the FP32 estimate decides each comparison unless it is within its error
+  // bound of the threshold; then the exact FP64 temperature decides them all
+  float T32 = -1.0f, err = 0.0f;
+  bool have32 = false;
   double T = -1.0;  // nullMatTemp_ (Remelting.cpp:29)
-  bool haveT = !withMat;
+  bool exact = !withMat;
+  auto below = [&](double thr) -> int {  // 1: T < thr, 0: T >= thr, -1: undecided
+    if (exact) return T < thr ? 1 : 0;
+    if ((double)T32 + (double)err < thr) return 1;
+    if ((double)T32 - (double)err >= thr) return 0;
+    return -1;
+  };
+  auto make_exact = [&]() {
+    if (!exact) {
+      ++exactT;
+      eval_T(d, th, cell, T);
+      exact = true;
+    }
+  };
   if (o > -1) {
     if (withMat) {
       // certainly below the liquidus and above nullMatTemp_ + 0.01: nothing changes
-      if (d.emax[e] < d.Tm && d.emin[e] >= null_plus()) return;
-      ++exactT;
-      eval_T(d, th, cell, T);
-      haveT = true;
-      if (T < d.Tm) {  // stays solid; the liquid-neighbour pass clears melted below nullMatTemp_ + 0.01
-        if (T < null_plus() && d.melted[cell]) d.melted[cell] = 0;
+      if (d.emax[e] < d.Tm && d.emin[e] >= np) return;
+      T32 = eval_T32(d, th32, cell, e, err);
+      have32 = true;
+      int b = below(d.Tm);
+      if (b < 0) {
+        make_exact();
+        b = below(d.Tm);
+      }
+      if (b == 1) {  // stays solid; the liquid-neighbour pass clears melted below nullMatTemp_ + 0.01
+        int bn = below(np);
+        if (bn < 0) {
+          make_exact();
+          bn = below(np);
+        }
+        if (bn == 1 && d.melted[cell]) d.melted[cell] = 0;
         return;
       }
     }
@@ -727,18 +794,39 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
     if (e >= 0 && !count_all) atomicAdd(&d.eliq[e], 1);
   }
   if (count_all && e >= 0) atomicAdd(&d.eliq[e], 1);
-  if (!haveT) {
-    ++exactT;
-    eval_T(d, th, cell, T);
+  // the four comparisons made with a liquid cell's temperature, with the
+  // reference's expressions: withMat (Remelting.cpp:505-507), the liquidus
+  // test of the liquid-neighbour pass (:521), and the capture sweep's
+  // overhot / no-material tests (:588-597)
+  bool wm2, flags, le, gtn;
+  bool decided = false;
+  if (!exact) {
+    if (!have32) T32 = eval_T32(d, th32, cell, e, err);
+    const double lo = (double)T32 - (double)err, hi = (double)T32 + (double)err;
+    const bool ok_np = hi < np || lo >= np, ok_tm = hi < d.Tm || lo > d.Tm, ok_nl = hi <= -1.0 || lo > -1.0;
+    if (ok_np && ok_tm && ok_nl && T32 == T32) {
+      wm2 = lo >= np;
+      flags = hi < d.Tm;
+      le = hi < d.Tm;
+      gtn = lo > -1.0;
+      decided = true;
+    } else {
+      make_exact();
+    }
   }
-  const bool withMat2 = !(T < null_plus());
+  if (!decided) {
+    wm2 = !(T < np);
+    flags = !(T >= d.Tm);
+    le = !(T > d.Tm);
+    gtn = T > -1.0;
+  }
   const uint8_t m0 = d.melted[cell];
   uint8_t m1 = m0;
-  if (withMat2 && S.time >= S.max_ts) m1 = 1;
-  if (!withMat2) m1 = 0;
+  if (wm2 && S.time >= S.max_ts) m1 = 1;
+  if (!wm2) m1 = 0;
   if (m1 != m0) d.melted[cell] = m1;
-  d.T[cell] = T;
-  if (withMat2 && !(T >= d.Tm)) {
+  d.tcls[cell] = (uint8_t)((flags ? kTlt : 0) | (le ? kTle : 0) | (gtn ? kTgtNull : 0) | (wm2 ? kTgeNullPlus : 0));
+  if (wm2 && flags) {  // the cell flags its solid neighbours
     const unsigned slot = append_slot(&c->n_liq);
     if (slot < d.list_cap) d.liq[slot] = (int32_t)cell;
   }
@@ -768,6 +856,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
     }
     const int par = (int)(S.step & 1);
     const double *th = d.theta[S.step % 3];
+    const float *th32 = d.theta32[S.step % 3];
     const double *thp = d.theta[(S.step + 2) % 3];
     unsigned long long t_phase = 0;
     if (gtid == 0) t_phase = now_ns();
@@ -793,7 +882,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
         const int I = (int)(q % g.nx) + 1;
         const int J = (int)((q / g.nx) % g.ny) + 1;
         const int K = (int)(q / ((int64_t)g.nx * g.ny)) + 1;
-        phase_update(d, c, (int64_t)K * g.nxyg + (int64_t)J * g.nxg + I, th, S, true, exactT, melts);
+        phase_update(d, c, (int64_t)K * g.nxyg + (int64_t)J * g.nxg + I, th, th32, S, true, exactT, melts);
       }
       visited += (M + nthr - 1 - gtid) / nthr;
     } else {  // the cells of the active elements (a warp per element)
@@ -804,7 +893,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
         const int32_t e = d.eact[par][w];
         const int64_t b = d.ecell_start[e], en = d.ecell_start[e + 1];
         for (int64_t k = b + lane; k < en; k += 32) {
-          phase_update(d, c, d.ecell[k], th, S, false, exactT, melts);
+          phase_update(d, c, d.ecell[k], th, th32, S, false, exactT, melts);
           ++visited;
         }
       }
@@ -929,7 +1018,6 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
           double T = -1.0;
           ++exactT;
           eval_T(d, th, cell, T);
-          d.T[cell] = T;
           {  // growth velocity of single_integration_step (Remelting.cpp:569-576)
             bool hard = false;
             const double Targ = (T < d.Ts) ? d.Ts + 0.01 : T;
@@ -1000,9 +1088,9 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
         if (ghost(g, I + di, J + dj, K + dk)) continue;
         const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
         if (d.orient[nb] > -1) continue;
-        const double Tn = d.T[nb];
-        if (Tn > d.Tm) continue;
-        if (!(Tn > -1.0)) continue;
+        const uint8_t cls = d.tcls[nb];  // the neighbour is liquid: its classes are this step's
+        if (!(cls & kTle)) continue;      // overhot (T > Tm)
+        if (!(cls & kTgtNull)) continue;  // no material
         ++tests;
         int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg,
                              L32);
@@ -1102,10 +1190,27 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       const double *f0 = d.frames + (int64_t)f_new * d.nnodes;
       const double *f1 = f0 - d.nnodes;
       double *tn = d.theta[(S.step + 1) % 3];
-      for (int64_t n = gtid; n < d.nnodes; n += nthr) tn[n] = lerp_node(f0[n], f1[n], ratio, d.void_t);
+      float *tn32 = d.theta32[(S.step + 1) % 3];
+      for (int64_t n = gtid; n < d.nnodes; n += nthr) {
+        const double v = lerp_node(f0[n], f1[n], ratio, d.void_t);
+        tn[n] = v;
+        tn32[n] = (float)v;
+      }
+      // Element bounds depend on the frame pair only (every interpolated node value lies between
+      // its two frame values), so the active list is rebuilt when the pair changes; elements near
+      // the void threshold need the exact interpolation and force a rebuild every step.
+      const bool rebuild = S.step == 0 || f_new != S.f_new || ld_volatile(&c->any_near) || d.force_exact;
+      if (!rebuild) {
+        const unsigned na = ld_volatile(&c->n_eact[par]);
+        for (int64_t q = gtid; q < na; q += nthr) d.eact[par ^ 1][q] = d.eact[par][q];
+        if (gtid == 0) {
+          c->n_eact[par ^ 1] = na;
+          eactive += na;
+        }
+      }
       const bool st0 = ld_volatile(&c->fstat_frame[f_new & 1]) == f_new;
       const bool st1 = ld_volatile(&c->fstat_frame[(f_new - 1) & 1]) == f_new - 1;
-      for (int64_t e = gtid; e < d.nelem; e += nthr) {
+      for (int64_t e = gtid; e < d.nelem && rebuild; e += nthr) {
         int64_t nid[8];
         elem_nodes(d.nn, e, nid);
         const uint8_t void_before = d.evoid[e];
@@ -1114,6 +1219,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
         frame_extrema(d, nid, f_new, e, st0, mx0, mn0, near0);
         frame_extrema(d, nid, f_new - 1, e, st1, mx1, mn1, near1);
         if (near0 || near1 || d.force_exact) {
+          if (!ld_volatile(&c->any_near)) atomicOr(&c->any_near, 1);
           double t[8];
 #pragma unroll
           for (int i = 0; i < 8; ++i) t[i] = lerp_node(f0[nid[i]], f1[nid[i]], ratio, d.void_t);

@@ -34,6 +34,11 @@ struct HostVelocity {
   double v[kHostVelCap];
 };
 
+// Temperature classes of a liquid cell (the comparisons the capture sweep and
+// the liquid-neighbour pass make with it): T < Tm, T <= Tm, T > nullMatTemp_,
+// T >= nullMatTemp_ + 0.01.
+constexpr uint8_t kTlt = 1, kTle = 2, kTgtNull = 4, kTgeNullPlus = 8;
+
 struct RemeltCtrl {
   unsigned int bar_count, bar_gen;
   int error;
@@ -66,6 +71,7 @@ struct RemeltCtrl {
   unsigned long long ns_host;  // block 0's wait for host velocity answers
   unsigned long long ns_barrier;  // block 0's time inside grid barriers
   int fstat_frame[2];          // frame whose per-element extrema each slot holds (-1: none)
+  int any_near;                // some element met a frame near the void threshold: rebuild every step
 };
 
 struct RemeltDevice {
@@ -81,7 +87,8 @@ struct RemeltDevice {
   int32_t *grain;      // cellGrainID_
   uint8_t *melted;     // hasBeenMelted_
   uint32_t *flagbits;  // cellLiquidNeigh as a bitmap
-  double *T;           // exact temperature of liquid / flagged cells (this step)
+  uint8_t *tcls;       // liquid cells, this step: temperature classes (kTlt.. bits below)
+  const float *pc32;   // parCoordsList_ rounded to float, for the FP32 classification
   const int32_t *tag;  // MapVoxelManager elementTagList_
   const double *pc;    // parCoordsList_
   // grain records, one per cell (the grain its cell owns)
@@ -104,6 +111,7 @@ struct RemeltDevice {
   int nframes;
   int bad_frame;             // index of a malformed frame, or -1
   double *theta[3];          // node temperatures by CA step (mod 3)
+  float *theta32[3];         // the same, rounded to float
   double *emax, *emin;       // per element bounds on the interpolated temperature (current step)
   int force_exact;           // some parametric coordinate is not finite: no bound shortcuts
   uint8_t *evoid;            // per element: some node below void_temperature + 1e-5
@@ -156,6 +164,9 @@ struct RosenthalParams {
   double void_above, t_void;
 };
 cudaError_t remelt_rosenthal_frames(const RosenthalParams &p, int nframes, double *frames, cudaStream_t s);
+
+// pc32[i] = (float)pc[i]
+cudaError_t remelt_round_coords(const double *pc, float *pc32, int64_t n, cudaStream_t s);
 
 // Frame-0 node temperatures and element bounds before the first step.
 cudaError_t remelt_init_theta(const RemeltDevice &d, cudaStream_t s);
