@@ -133,6 +133,7 @@ void RemeltRealm::prepare() {
   gori0_.assign((size_t)N, -1);
   site_field_.assign((size_t)N, -1.0);
   grain_cell_.clear();
+  grain_ori0_.clear();
   auto centre = [&](int64_t cell, double out[3]) {
     const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
     out[0] = centre_coord(c.x0, c.h, I);
@@ -153,6 +154,7 @@ void RemeltRealm::prepare() {
       gori0_[cell] = (int32_t)q;
       centre(cell, &rec0_[4 * cell]);
       grain_cell_.push_back((int32_t)cell);
+      grain_ori0_.push_back((int32_t)q);
       ++q;
     }
     n_init_orient_ = M;
@@ -171,6 +173,7 @@ void RemeltRealm::prepare() {
     grain0_ = r.grain;
     melted0_ = r.melted;
     grain_cell_ = r.gcell;
+    grain_ori0_ = r.gori;
     std::vector<uint8_t> owned((size_t)r.ngrains, 0);
     for (int64_t cell = 0; cell < N; ++cell) {
       const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
@@ -195,6 +198,7 @@ void RemeltRealm::prepare() {
     n_init_grains_ = r.ngrains;
     expected_grains_ = r.expected;
   }
+  init_draws_ = rng_->draws();
   if (cfg_.nucleation) {
     sites_ = make_sites(c, *rng_);
     for (size_t i = 0; i < sites_.cell.size(); ++i) site_field_[sites_.cell[i]] = sites_.dtc[i];
@@ -206,6 +210,7 @@ void RemeltRealm::prepare() {
       mapped_vtr_ = make_mapped_ids((int64_t)ss + sb + expected_grains_, true, *rng_);
     }
     expected_grains_ += sites_.surface_sites + sites_.bulk_sites;
+    init_draws_ = rng_->draws();
     // the nucleation orientation stream, extended on demand
     const int64_t K = std::max<int64_t>(4 * (int64_t)sites_.cell.size(), 1024);
     append_orientations(otab_, make_orientations(K, *rng_));
@@ -466,6 +471,7 @@ void RemeltRealm::initialize() {
   }
   if (blocks_ <= 0) throw CudaError("no co-resident blocks for the persistent remelting kernel");
   vtr_.configure(c.output, workdir_);
+  if (opts_.write_outputs) vtr_.make_dirs();  // VtrManager::initialize
   initialized_ = true;
 }
 
@@ -549,13 +555,33 @@ void RemeltRealm::serve_velocities(const volatile int *stop) {
 void RemeltRealm::run(long long max_steps) {
   if (!initialized_) throw StateError("amca_run before amca_initialize");
   const long long target = max_steps < 0 ? (1ll << 60) : ctrl_.step + max_steps;
+  const OutputConfig &oc = cfg_.ca.output;
   while (ctrl_.status != kRemeltFinalTime && ctrl_.status != kRemeltFramesEnd && ctrl_.step < target) {
+    long long limit = target;
+    if (opts_.write_outputs) {  // VtrManager::execute after every step (Remelting.cpp:640)
+      if (oc.frequency >= 1)
+        limit = std::min(limit, (ctrl_.step / oc.frequency + 1) * (long long)oc.frequency);
+      else if (oc.time_interval_set && oc.time_interval > 0)
+        limit = std::min(limit, ctrl_.step + 1);
+    }
+    const long long before = ctrl_.step;
+    launch(limit);
+    if (ctrl_.status == kRemeltNeedOrient) {
+      extend_orientations();
+      continue;
+    }
+    if (opts_.write_outputs && ctrl_.step != before && vtr_.due((int)ctrl_.step, ctrl_.time)) write_snapshot();
+  }
+}
+
+void RemeltRealm::launch(long long limit) {
+  {
     const int running = kRemeltRunning;
     h2d(&dev_.ctrl->status, &running, sizeof running);
     volatile int stop = 0;
     std::thread server([&] { serve_velocities(&stop); });
     RCK(cudaEventRecord(ev0_, stream_));
-    cudaError_t le = remelt_run_steps(dev_, target, blocks_, stream_);
+    cudaError_t le = remelt_run_steps(dev_, limit, blocks_, stream_);
     if (le == cudaSuccess) le = cudaEventRecord(ev1_, stream_);
     if (le == cudaSuccess) le = cudaStreamSynchronize(stream_);
     stop = 1;
@@ -566,11 +592,6 @@ void RemeltRealm::run(long long max_steps) {
     float ms = 0.f;
     RCK(cudaEventElapsedTime(&ms, ev0_, ev1_));
     kernel_ms_ += ms;
-    if (ctrl_.status == kRemeltNeedOrient) {
-      extend_orientations();
-      continue;
-    }
-    if (ctrl_.status == kRemeltStepLimit) break;
   }
 }
 
@@ -694,9 +715,129 @@ int RemeltRealm::final_grain_count() {
   return (int)std::count(seen.begin(), seen.end(), 1);
 }
 
+RemeltRealm::Fields RemeltRealm::fetch_fields(bool grain) {
+  Fields f;
+  const size_t N = (size_t)dev_.ncells;
+  f.orient.resize(N);
+  get_field(AMCA_FIELD_ORIENTATION_ID, f.orient.data(), N * 4);
+  f.melted.resize(N);
+  get_field(AMCA_FIELD_MELTED, f.melted.data(), N);
+  f.temperature.resize(N);
+  get_field(AMCA_FIELD_TEMPERATURE, f.temperature.data(), N * 8);
+  if (grain) {
+    f.grain.resize(N);
+    get_field(AMCA_FIELD_GRAIN_ID, f.grain.data(), N * 4);
+  }
+  return f;
+}
+
+OutputView RemeltRealm::view(const Fields &f) const {
+  const PlainConfig &c = cfg_.ca;
+  OutputView v{};
+  v.nx = c.nx;
+  v.ny = c.ny;
+  v.nz = c.nz;
+  v.x0 = c.x0;
+  v.y0 = c.y0;
+  v.z0 = c.z0;
+  v.h = c.h;
+  v.orient = f.orient.data();
+  v.euler = otab_.euler.data();
+  v.n_orient = ctrl_.n_orient;
+  v.mapped_vtr = (c.shuffle_vtr && !mapped_vtr_.empty()) ? &mapped_vtr_ : nullptr;
+  v.shuffle_vtk = c.shuffle_vtk;
+  v.expected_grains = expected_grains_;
+  v.melted = f.melted.data();
+  v.temperature = f.temperature.data();
+  return v;
+}
+
+void RemeltRealm::write_snapshot() {
+  Fields f = fetch_fields(false);
+  vtr_.make_dirs();
+  vtr_.write(view(f), ctrl_.time);
+}
+
+// CafeSolver::finalize (CA/src/CafeSolver.cpp:224-261): the restart file when
+// asked for, the last VTR snapshot (output_last_step_result), finalGrains.vtk
+// and finalResult.txt (output_orientations).
 void RemeltRealm::write_outputs() {
   if (!initialized_) throw StateError("amca_write_outputs before amca_initialize");
-  throw std::invalid_argument("output files of the remelting realm are not written by this library yet");
+  const PlainConfig &c = cfg_.ca;
+  Fields f = fetch_fields(c.micro_out);
+  OutputView v = view(f);
+  std::vector<double> gx, gy, gz;
+  std::vector<int32_t> gori, gcell;
+  if (c.micro_out) {
+    // grain table: a grain's record lives with the interior cell that owns it
+    const size_t N = (size_t)dev_.ncells;
+    std::vector<double> x(N), y(N), z(N);
+    std::vector<int32_t> o(N);
+    d2h(x.data(), dev_.gx, N * 8);
+    d2h(y.data(), dev_.gy, N * 8);
+    d2h(z.data(), dev_.gz, N * 8);
+    d2h(o.data(), dev_.gori, N * 4);
+    RCK(cudaStreamSynchronize(stream_));
+    const int64_t ng = ctrl_.n_grains;
+    gcell.assign((size_t)ng, -1);
+    for (int64_t g = 0; g < (int64_t)grain_cell_.size() && g < ng; ++g) gcell[g] = grain_cell_[g];
+    const int nxg = c.nx + 2, nyg = c.ny + 2, nzg = c.nz + 2;
+    const int64_t nxyg = (int64_t)nxg * nyg;
+    std::vector<char> owned((size_t)ng, 0);
+    for (size_t cell = 0; cell < N; ++cell) {
+      const int32_t g = f.grain[cell];
+      const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
+      if (g < 0 || g >= ng || is_ghost(I, J, K, nxg, nyg, nzg)) continue;
+      gcell[g] = (int32_t)cell;
+      owned[g] = 1;
+    }
+    gx.resize((size_t)ng);
+    gy.resize((size_t)ng);
+    gz.resize((size_t)ng);
+    gori.resize((size_t)ng);
+    for (int64_t g = 0; g < ng; ++g) {
+      const int64_t cell = gcell[g];
+      if (owned[g]) {
+        gx[g] = x[cell];
+        gy[g] = y[cell];
+        gz[g] = z[cell];
+        gori[g] = o[cell];
+      } else {  // never touched: as loaded, centred on its cell
+        const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
+        gx[g] = centre_coord(c.x0, c.h, I);
+        gy[g] = centre_coord(c.y0, c.h, J);
+        gz[g] = centre_coord(c.z0, c.h, K);
+        gori[g] = g < (int64_t)grain_ori0_.size() ? grain_ori0_[g] : -1;
+      }
+    }
+    v.grain = f.grain.data();
+    v.site_dtc = site_field_.data();
+    v.n_grains = ng;
+    v.gx = gx.data();
+    v.gy = gy.data();
+    v.gz = gz.data();
+    v.gori = gori.data();
+    v.gcell = gcell.data();
+    write_grain_info(v, path(c.micro_out_file));
+  }
+  std::vector<int32_t> mapped_vtk;
+  if (c.shuffle_vtk) {  // writeToFile's shuffle draws from the glibc stream where the run left it
+    int maxVal = -1;
+    for (int k = 1; k <= c.nz; ++k)
+      for (int j = 1; j <= c.ny; ++j)
+        for (int i = 1; i <= c.nx; ++i)
+          maxVal = std::max(maxVal, (int)f.orient[((int64_t)k * (c.ny + 2) + j) * (c.nx + 2) + i]);
+    GlibcRand rng(opts_.seed);
+    const int64_t skip = init_draws_ + 3 * (ctrl_.n_orient - n_init_orient_);
+    for (int64_t i = 0; i < skip; ++i) rng.next();
+    mapped_vtk = make_mapped_ids(maxVal + 1, true, rng);
+    v.mapped_vtk = &mapped_vtk;
+  }
+  if (vtr_.due(0, ctrl_.time)) {
+    vtr_.make_dirs();
+    vtr_.write(v, ctrl_.time);
+  }
+  write_final_grains(v, path("finalGrains.vtk"), vtr_.pvd_path());
 }
 
 }  // namespace amca

@@ -60,6 +60,16 @@ class RemeltRealm {
   void extend_orientations();
   void upload_initial_state();
   void serve_velocities(const volatile int *stop);
+  void launch(long long limit);
+  void write_snapshot();
+  // host copies of the output fields of the current state
+  struct Fields {
+    std::vector<int32_t> orient, grain;
+    std::vector<uint8_t> melted;
+    std::vector<double> temperature;
+  };
+  Fields fetch_fields(bool grain);
+  OutputView view(const Fields &f) const;
   std::string path(const std::string &p) const;
   double algorithmic_bytes() const;
 
@@ -87,6 +97,8 @@ class RemeltRealm {
   std::vector<double> rec0_;       // initial grain records per cell: x, y, z, length
   std::vector<int32_t> gori0_;
   std::vector<int32_t> grain_cell_;  // grain id -> owning cell (restart + created)
+  std::vector<int32_t> grain_ori0_;  // grain id -> initial orientation
+  int64_t init_draws_ = 0;           // glibc rand() values consumed before the nucleation stream
   std::vector<double> site_field_;   // cellNucleationDT_
   int64_t expected_grains_ = 0;
   int64_t restart_sites_ = 0;

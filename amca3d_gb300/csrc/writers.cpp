@@ -92,7 +92,20 @@ void VtrSeries::write(const OutputView &v, double time) {
       << "\">\n";
     f << W4 << "<CellData Scalars=\"grain_id\">\n";
     for (int var : cfg_.variables) {
-      if (var == 2) {  // grain_ID
+      if (var == 0 && v.temperature) {  // temperature, written through an int (VtrManager.cpp:231-245)
+        f << W5 << "<DataArray type=\"Float64\" Name=\"cell_temperature\" format=\"ascii\">\n";
+        for (int k = 1; k < nzg - 1; k++)
+          for (int j = 1; j < nyg - 1; j++) {
+            f << W6;
+            for (int i = 1; i < nxg - 1; i++) {
+              const int val = (int)v.temperature[k * nxyg + j * nxg + i];
+              f << val << " ";
+            }
+            f << std::endl;
+          }
+        f << "\n";
+        f << W5 << "</DataArray>" << std::endl;
+      } else if (var == 2) {  // grain_ID
         f << W5 << "<DataArray type=\"Int64\" Name=\"grain_id\" format=\"ascii\">\n";
         for (int k = 1; k < nzg - 1; k++)
           for (int j = 1; j < nyg - 1; j++) {
@@ -128,7 +141,7 @@ void VtrSeries::write(const OutputView &v, double time) {
         for (int k = 1; k < nzg - 1; k++)
           for (int j = 1; j < nyg - 1; j++) {
             f << W6;
-            for (int i = 1; i < nxg - 1; i++) f << 1 << " ";
+            for (int i = 1; i < nxg - 1; i++) f << (v.melted ? (int)v.melted[k * nxyg + j * nxg + i] : 1) << " ";
             f << "\n";
           }
         f << "\n";
@@ -298,7 +311,7 @@ void write_final_grains(const OutputView &v, const std::string &vtk_path, const 
   for (int k = 1; k < nz - 1; ++k)
     for (int j = 1; j < ny - 1; ++j)
       for (int i = 1; i < nx - 1; ++i) {
-        vtk << 1 << " ";  // a plain realm has no melt history: every cell reports 1 (outputToFile)
+        vtk << (v.melted ? (int)v.melted[k * nxy + j * nx + i] : 1) << " ";  // plain realm: 1 (outputToFile)
         count++;
         if (count % 10 == 0) {
           vtk << std::endl;
@@ -339,7 +352,7 @@ void write_final_grains(const OutputView &v, const std::string &vtk_path, const 
         val = u[k * nxy + j * nx + i];
         if (val >= 0) val = numCells[val];
         one << val << " ";
-        one << 1 << " ";
+        one << (v.melted ? (int)v.melted[k * nxy + j * nx + i] : 1) << " ";
         val = u[k * nxy + j * nx + i];
         if (val >= 0) {
           const double *e = v.euler + 3 * (int64_t)val;
@@ -364,7 +377,7 @@ void write_grain_info(const OutputView &v, const std::string &file_name) {
     << "  " << v.z0 << "  " << nxg << "  " << nyg << "  " << nzg << "  " << v.h << std::endl;
   f << "Cell informatin: ID; grainID; orientationID; hasBeenMelted; undercooling of seed" << std::endl;
   for (int64_t c = 0; c < ncells; ++c) {
-    const bool melted = false;
+    const bool melted = v.melted ? v.melted[c] != 0 : false;
     f << c << "  " << v.grain[c] << "  " << v.orient[c] << "  " << melted << "  " << v.site_dtc[c];
     f << std::endl;
   }

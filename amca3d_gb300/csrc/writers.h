@@ -32,6 +32,10 @@ struct OutputView {
   const double *gx, *gy, *gz;
   const int32_t *gori, *gcell;
   int64_t expected_grains;  // numSitesSurface_ + numSitesBulk_
+  // remelting realm: hasBeenMelted_ and cellTemperature_ (ghost-inclusive);
+  // nullptr for the plain realm (melted flags report 1, no temperature output)
+  const uint8_t *melted = nullptr;
+  const double *temperature = nullptr;
 };
 
 // VtrManager state across calls (numOutputStep_, timeVec_, time threshold).

@@ -131,11 +131,41 @@ def run_reference(fx, workdir: str):
     return read_dump(dump)
 
 
+def output_digests(workdir: str) -> dict:
+    """SHA-256 of every output file under workdir (inputs and the log excluded)."""
+    skip = {"Inputfile.i", "frames.txt", "run.log", "state.bin", "timeLog.dat"}
+    out = {}
+    for root, _, files in os.walk(workdir):
+        for f in files:
+            rel = os.path.relpath(os.path.join(root, f), workdir)
+            if rel in skip or rel.startswith("grainInfoIn"):
+                continue
+            out[rel] = hashlib.sha256(open(os.path.join(root, f), "rb").read()).hexdigest()
+    return out
+
+
+def make_outputs_golden() -> None:
+    fx = remelt_cases.output_fixture()
+    wd = tempfile.mkdtemp(prefix="remelt_out_")
+    try:
+        tags, pc, steps = run_reference(fx, wd)
+        dig = output_digests(wd)
+        with open(os.path.join(HERE, "remelt_outputs.json"), "w") as f:
+            json.dump({"steps": len(steps), "files": dig}, f, indent=1, sort_keys=True)
+        print(f"remelt_outputs: {len(steps)} steps, {len(dig)} output files")
+    finally:
+        shutil.rmtree(wd, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default=None)
+    ap.add_argument("--outputs", action="store_true", help="only the output-file digests of output_fixture()")
     ap.add_argument("--keep", default=None, help="keep the run directories under this folder")
     args = ap.parse_args()
+    if args.outputs:
+        make_outputs_golden()
+        return
     out_json = os.path.join(HERE, "remelt_golden.json")
     golden = json.load(open(out_json)) if os.path.exists(out_json) else {}
     for fx in remelt_cases.fixtures():

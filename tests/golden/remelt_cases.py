@@ -95,3 +95,17 @@ def fixtures() -> list:
                       time_scale=1.0e-3, time_offset=5.0,
                       src=dict(x_start=0.99e-3, y_line=2.02e-3, z_top=2.4e-5))))
     return out
+
+
+def output_fixture() -> RemeltFixture:
+    """A tiny deck whose every output file is compared byte for byte: VTR
+    snapshots of temperature, grain id, orientation and melted flag, the
+    restart file, finalGrains.vtk and finalResult.txt."""
+    cells = (12, 8, 6)
+    case = RemeltCase(name="remelt_outputs", cells=cells, cell_size=2.0e-6, nucleation=True, seed=4,
+                      bulk=(2.0e15, 15.0, 4.0), termination_time=1.0, time_step=1.0e-6, output_frequency=150,
+                      output_base="./Results/Grains", output_microstructure_file="grainOut.txt",
+                      output_variables=("temperature", "grain_ID", "grain_orientation", "melted_flag"))
+    frames = FrameSpec(origin=(-1.0e-5, -1.0e-5, -1.0e-5), spacing=1.0e-5, nodes=(6, 5, 5), frame_dt=1.0e-6,
+                       frames=110, source=Rosenthal(power=14.0, x_start=-1.0e-5, y_line=8.0e-6, z_top=1.2e-5))
+    return RemeltFixture(case, frames)

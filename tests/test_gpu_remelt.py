@@ -129,3 +129,24 @@ def test_remelt_gpu_microstructure_from_memory(amca, tmp_path, name):
     for k in ("orient", "grain", "melted"):
         assert np.array_equal(r.field(FIELD_OF[k]).astype(g[k].dtype), g[k]), k
     r.close()
+
+
+def test_remelt_gpu_output_files_match_reference(amca, tmp_path):
+    """VTR snapshots (temperature, grain id, orientation, melted flag), PVTR/PVD,
+    the restart file, finalGrains.vtk and finalResult.txt: byte for byte the
+    reference's (SHA-256 of each file)."""
+    import json
+
+    fx = remelt_cases.output_fixture()
+    M.prepare(fx, str(tmp_path))
+    r = amca.CellularAutomataRealm(fx.case.to_yaml(), seed=fx.case.seed, workdir=str(tmp_path), write_outputs=True)
+    r.initialize()
+    r.run()
+    r.write_outputs()
+    golden = json.load(open(os.path.join(HERE, "golden", "remelt_outputs.json")))
+    assert r.stats()["step"] == golden["steps"]
+    r.close()
+    got = M.output_digests(str(tmp_path))
+    assert sorted(got) == sorted(golden["files"])
+    bad = [f for f in golden["files"] if got[f] != golden["files"][f]]
+    assert not bad, bad
