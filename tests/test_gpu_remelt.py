@@ -150,3 +150,22 @@ def test_remelt_gpu_output_files_match_reference(amca, tmp_path):
     assert sorted(got) == sorted(golden["files"])
     bad = [f for f in golden["files"] if got[f] != golden["files"][f]]
     assert not bad, bad
+
+
+def test_cli_runs_the_deck_like_the_reference(amca, tmp_path):
+    """amca3d -i Inputfile.i -o run.log in the deck's directory writes the
+    reference's output files."""
+    import json
+    import subprocess
+
+    fx = remelt_cases.output_fixture()
+    M.prepare(fx, str(tmp_path))
+    cli = os.path.join(os.path.dirname(HERE), "amca3d_gb300", "amca3d")
+    r = subprocess.run([cli, "-i", "Inputfile.i", "-o", "cli.log", "--seed", str(fx.case.seed)], cwd=str(tmp_path),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    golden = json.load(open(os.path.join(HERE, "golden", "remelt_outputs.json")))
+    got = M.output_digests(str(tmp_path))
+    got.pop("cli.log", None)
+    assert got == golden["files"]
+    assert f"Time Step Count: {golden['steps']}" in (tmp_path / "cli.log").read_text()

@@ -242,3 +242,18 @@ def test_remelt_frames_from_arrays_need_two_frames(amca):
     with pytest.raises(amca.AmcaError, match="two frames"):
         r.set_rosenthal_frames(nodes=(3, 3, 3), frames=1, spacing=1.0)
     r.close()
+
+
+def test_cli_help_and_missing_deck(amca, tmp_path):
+    import subprocess
+
+    cli = os.path.join(ROOT, "amca3d_gb300", "amca3d")
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    r = subprocess.run([cli, "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "--input-deck" in r.stderr
+    r = subprocess.run([cli, "-i", str(tmp_path / "none.i")], capture_output=True, text=True)
+    assert r.returncode == 0 and "does not exist" in r.stderr
+    (tmp_path / "bad.i").write_text("solvers: [nothing]\n")
+    r = subprocess.run([cli, "-i", str(tmp_path / "bad.i")], capture_output=True, text=True)
+    assert r.returncode == 1 and "parsing the deck" in r.stderr
