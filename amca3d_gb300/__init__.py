@@ -68,7 +68,8 @@ EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "am
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
            "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
-           "amca_last_error", "amca_destroy")
+           "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_get_stats", "amca_batch_last_error",
+           "amca_batch_destroy", "amca_last_error", "amca_destroy")
 
 
 class Rosenthal(ctypes.Structure):
@@ -80,6 +81,20 @@ class Rosenthal(ctypes.Structure):
                 ("diffusivity", ctypes.c_double), ("t0", ctypes.c_double), ("t_cap", ctypes.c_double),
                 ("x_start", ctypes.c_double), ("y_line", ctypes.c_double), ("z_top", ctypes.c_double),
                 ("void_above_set", ctypes.c_int32), ("void_above", ctypes.c_double), ("t_void", ctypes.c_double)]
+
+
+class BatchStats(ctypes.Structure):
+    """amca_batch_stats of include/amca3d.h."""
+    _fields_ = [("realms", ctypes.c_int32), ("team_size", ctypes.c_int32), ("teams", ctypes.c_int32),
+                ("max_blocks", ctypes.c_int32), ("graph", ctypes.c_int32), ("n_tuned", ctypes.c_int32),
+                ("runs", ctypes.c_int64), ("last_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("cell_updates", ctypes.c_int64), ("tuned_team", ctypes.c_int32 * 8),
+                ("tuned_ms", ctypes.c_double * 8)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("tuned_")}
+        d["tuned"] = {int(self.tuned_team[i]): float(self.tuned_ms[i]) for i in range(self.n_tuned)}
+        return d
 
 
 class PlainParams(ctypes.Structure):
@@ -141,6 +156,18 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_set_rosenthal_frames.restype = i
     lib.amca_set_microstructure.argtypes = [vp, vp, vp, vp, vp, i64, vp, i64, vp, vp, i64]
     lib.amca_set_microstructure.restype = i
+    lib.amca_batch_create.argtypes = [ctypes.POINTER(vp), i, i, ctypes.POINTER(vp)]
+    lib.amca_batch_create.restype = i
+    lib.amca_batch_run.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    lib.amca_batch_run.restype = i
+    lib.amca_batch_tune.argtypes = [vp, i, ctypes.POINTER(ctypes.c_int)]
+    lib.amca_batch_tune.restype = i
+    lib.amca_batch_get_stats.argtypes = [vp, ctypes.POINTER(BatchStats)]
+    lib.amca_batch_get_stats.restype = i
+    lib.amca_batch_last_error.argtypes = [vp]
+    lib.amca_batch_last_error.restype = cp
+    lib.amca_batch_destroy.argtypes = [vp]
+    lib.amca_batch_destroy.restype = None
     lib.amca_last_error.argtypes = [vp]
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]
@@ -334,6 +361,59 @@ class CellularAutomataRealm:
         if self._h:
             self._lib.amca_destroy(self._h)
             self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Batch:
+    """Many initialized plain realms run in one cooperative launch
+    (amca_batch_*): teams of blocks pull realms from a queue; every realm's
+    result is the one it gives when run alone. The realms must stay open
+    while the batch exists."""
+
+    def __init__(self, realms, team_size: int = 0):
+        self._lib = load_library()
+        self.realms = list(realms)
+        arr = (ctypes.c_void_p * max(len(self.realms), 1))(*[r._h.value for r in self.realms])
+        self._b = ctypes.c_void_p()
+        rc = self._lib.amca_batch_create(arr, len(self.realms), int(team_size), ctypes.byref(self._b))
+        if rc != AMCA_OK:
+            raise AmcaError(rc, self._lib.amca_batch_last_error(None).decode())
+
+    def _check(self, rc: int) -> None:
+        if rc != AMCA_OK:
+            raise AmcaError(rc, self._lib.amca_batch_last_error(self._b).decode())
+
+    def run(self) -> float:
+        """Every realm from its initial state to its end; returns device ms."""
+        ms = ctypes.c_double()
+        self._check(self._lib.amca_batch_run(self._b, ctypes.byref(ms)))
+        return ms.value
+
+    def tune(self, repeats: int = 1) -> int:
+        t = ctypes.c_int()
+        self._check(self._lib.amca_batch_tune(self._b, int(repeats), ctypes.byref(t)))
+        return t.value
+
+    def stats(self) -> dict:
+        s = BatchStats()
+        self._check(self._lib.amca_batch_get_stats(self._b, ctypes.byref(s)))
+        return s.as_dict()
+
+    def close(self) -> None:
+        if self._b:
+            self._lib.amca_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
 
     def __del__(self):
         try:

@@ -60,6 +60,11 @@ constexpr unsigned long long kFlagAgg = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
 constexpr unsigned long long kPayload = (1ull << 62) - 1;
 
+// The blocks that run one realm together (the team) and this block's rank in
+// it: the whole grid for one realm, a slice of it in the batched launch.
+__shared__ int t_nb;
+__shared__ int t_b;
+
 __device__ __forceinline__ unsigned long long now_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -80,24 +85,25 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
   return *(const volatile T *)p;
 }
 
-// Sense-counting grid barrier. Returns false (with ctrl->error set) when a
-// wait ran out or another block reported an error.
-__device__ bool grid_barrier(PlainCtrl *c) {
+// Sense-counting barrier of the t_nb blocks of the team over the words
+// (count, gen). Returns false (with *error set) when a wait ran out or
+// another block reported an error.
+__device__ bool team_barrier(unsigned *count, unsigned *gen_word, int *error) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned gen = ld_acquire(&c->bar_gen);
+    const unsigned gen = ld_acquire(gen_word);
     __threadfence();
-    const unsigned arrived = atomicAdd(&c->bar_count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&c->bar_count, 0u);
+    const unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == t_nb - 1) {
+      atomicExch(count, 0u);
       __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
+      atomicAdd(gen_word, 1u);
     } else {
       const unsigned long long t0 = now_ns();
-      while (ld_acquire(&c->bar_gen) == gen) {
-        if (ld_volatile(&c->error) != 0) break;
+      while (ld_acquire(gen_word) == gen) {
+        if (ld_volatile(error) != 0) break;
         if (now_ns() - t0 > kWaitNs) {
-          atomicCAS(&c->error, 0, kErrBarrier);
+          atomicCAS(error, 0, kErrBarrier);
           break;
         }
         __nanosleep(32);
@@ -106,8 +112,11 @@ __device__ bool grid_barrier(PlainCtrl *c) {
     __threadfence();
   }
   __syncthreads();
-  return ld_volatile(&c->error) == 0;
+  return ld_volatile(error) == 0;
 }
+
+// Barrier over the blocks that run the realm; false when it failed.
+__device__ __forceinline__ bool grid_barrier(PlainCtrl *c) { return team_barrier(&c->bar_count, &c->bar_gen, &c->error); }
 
 // Exclusive scan of one u64 per thread over the block; *total = block sum.
 __device__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long *smem,
@@ -195,7 +204,7 @@ __device__ unsigned long long block_prefix(unsigned long long *status, unsigned 
                                            unsigned long long *smem, PlainCtrl *c) {
   if (threadIdx.x < 32) {
     unsigned long long pre = 0;
-    const bool ok = look_back_warp(status, blockIdx.x, agg, &pre, c);
+    const bool ok = look_back_warp(status, t_b, agg, &pre, c);
     if (threadIdx.x == 0) smem[kWarps] = ok ? pre : ~0ull;
   }
   __syncthreads();
@@ -206,8 +215,8 @@ __device__ unsigned long long block_prefix(unsigned long long *status, unsigned 
 
 // This block's contiguous share [b, e) of [0, n).
 __device__ __forceinline__ void block_chunk(long long n, long long &b, long long &e) {
-  const long long per = (n + gridDim.x - 1) / gridDim.x;
-  b = per * blockIdx.x;
+  const long long per = (n + t_nb - 1) / t_nb;
+  b = per * t_b;
   if (b > n) b = n;
   e = b + per;
   if (e > n) e = n;
@@ -259,8 +268,8 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
   // next step's look-back word starts cleared: it was last read in the
   // previous step's nucleation, which every block finished before that
   // phase's barrier
-  if (threadIdx.x == 0) d.scanA[((step + 1) & 1) * kStatusWords + blockIdx.x] = 0ull;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (threadIdx.x == 0) d.scanA[((step + 1) & 1) * kStatusWords + t_b] = 0ull;
+  if (t_b == 0 && threadIdx.x == 0) {
     // calculate_time_step (CellularAutomataManager_3D.cpp:449-507): one
     // velocity for the uniform field; dt for "some active envelope" and for
     // "none" (maxVelocity stays 1e-10), picked after nucleation. Slots by step
@@ -323,7 +332,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
     }
     run += tot;
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+  if (t_b == t_nb - 1 && threadIdx.x == 0) {
     const long long total = (long long)(pre + agg);
     c->n_orient = base_orient + total;
     c->next_grain = base_grain + total;
@@ -343,14 +352,14 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
                             unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
   __shared__ long long s_batch;
-  if (threadIdx.x == 0) d.scanB[blockIdx.x] = 0ull;  // this block's look-back word of the resolve phase
+  if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
   unsigned long long tests = 0, tests64 = 0;
   // Claims need no order: blocks take batches of consecutive ranks from a
   // shared counter until none is left, so blocks that drew cheap envelopes
   // (few liquid neighbours) take more batches. About two batches per block,
   // 32..512 ranks each: small generations (whose envelopes each build
   // themselves in FP64) still spread over every block.
-  long long batch = (n + 2ll * gridDim.x - 1) / (2ll * gridDim.x);
+  long long batch = (n + 2ll * t_nb - 1) / (2ll * t_nb);
   batch = (batch + 31) & ~31ll;
   if (batch > kClaimBatch) batch = kClaimBatch;
   if (batch < 32) batch = 32;
@@ -473,7 +482,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
 __device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
   const Grid &g = d.grid;
   __shared__ long long s_batch;
-  long long batch = (n + 2ll * gridDim.x - 1) / (2ll * gridDim.x);
+  long long batch = (n + 2ll * t_nb - 1) / (2ll * t_nb);
   batch = (batch + 31) & ~31ll;
   if (batch > kClaimBatch) batch = kClaimBatch;
   if (batch < 32) batch = 32;
@@ -559,7 +568,7 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
     }
     run += tot;
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+  if (t_b == t_nb - 1 && threadIdx.x == 0) {
     const unsigned long long total = pre + agg;
     const long long caps = (long long)(total >> 32), survs = (long long)(total & 0xffffffffull);
     c->gen_lo = base_grain;
@@ -572,8 +581,9 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   return true;
 }
 
-__global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(PlainDevice d, long long step_limit) {
-  __shared__ unsigned long long smem[kWarps + 2];
+// Whole CA steps of one realm by the current team, until it is solid, its
+// termination time, or step_limit.
+__device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned long long *smem) {
   PlainCtrl *c = d.ctrl;
   unsigned long long tests = 0, tests64 = 0, live = 0;
   // per-step state, identical in every thread (read once, then advanced locally)
@@ -583,7 +593,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
   int cur = ld_volatile(&c->cur_list);
   bool done = ld_volatile(&c->done) != 0;
   bool ok = true;
-  const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool timer = t_b == 0 && threadIdx.x == 0;
   unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
   while (!done && time < d.final_time && step < step_limit) {
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
@@ -695,25 +705,124 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
   }
 }
 
-__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, Grid g, long long ncells) {
-  // one bitmap word (32 cells) per thread; cells past the grid count as solid
-  const long long nwords = solid_words(ncells);
-  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (long long)gridDim.x * blockDim.x) {
-    uint32_t bits = 0;
-    for (int b = 0; b < 32; ++b) {
-      const long long i = w * 32 + b;
-      bool ghost = true;
-      if (i < ncells) {
-        int I, J, K;
-        cell_ijk(g, i, I, J, K);
-        ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
-        orient[i] = ghost ? 0u : kLiquid;
-      }
-      bits |= (ghost ? 1u : 0u) << b;
-    }
-    solid[w] = bits;
-    claimed[w] = 0u;
+__global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(PlainDevice d, long long step_limit) {
+  __shared__ unsigned long long smem[kWarps + 2];
+  if (threadIdx.x == 0) {
+    t_nb = gridDim.x;
+    t_b = blockIdx.x;
   }
+  __syncthreads();
+  run_realm(d, step_limit, smem);
+}
+
+// One bitmap word (32 cells) of the initial field: cells past the grid count
+// as solid.
+__device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *solid, uint32_t *claimed, const Grid &g,
+                                                long long ncells, long long w) {
+  uint32_t bits = 0;
+  for (int b = 0; b < 32; ++b) {
+    const long long i = w * 32 + b;
+    bool ghost = true;
+    if (i < ncells) {
+      int I, J, K;
+      cell_ijk(g, i, I, J, K);
+      ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
+      orient[i] = ghost ? 0u : kLiquid;
+    }
+    bits |= (ghost ? 1u : 0u) << b;
+  }
+  solid[w] = bits;
+  claimed[w] = 0u;
+}
+
+__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, Grid g, long long ncells) {
+  const long long nwords = solid_words(ncells);
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (long long)gridDim.x * blockDim.x)
+    init_field_word(orient, solid, claimed, g, ncells, w);
+}
+
+// ---------------------------------------------------------------------------
+// Batched launch: many independent realms in one cooperative launch. The
+// grid is cut into teams of team_size consecutive blocks; the first block of
+// a team pulls the next queue position q and publishes order[q] in the team's
+// slot (by round parity); after a team barrier every block of the team runs
+// that realm with run_realm, the team standing in for the grid (its barriers
+// count team_size arrivals on the realm's own control words). A realm's
+// result does not depend on how many blocks run it, so the team size and the
+// queue order are free to tune.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock, kMinBlocks)
+    plain_batched_kernel(const PlainDevice *insts, const int *order, int ninst, int team_size, unsigned *queue,
+                         BatchTeam *teams, int *error, long long step_limit) {
+  __shared__ unsigned long long smem[kWarps + 2];
+  __shared__ PlainDevice sd;  // the descriptor of the realm this team runs
+  __shared__ int s_idx;
+  const int team = blockIdx.x / team_size;
+  if (threadIdx.x == 0) {
+    t_nb = team_size;
+    t_b = blockIdx.x - team * team_size;
+  }
+  __syncthreads();
+  BatchTeam *tw = teams + team;
+  for (int round = 0;; ++round) {
+    // the slot written here was last read in round - 2, before every block
+    // of the team arrived at the barrier of round - 1
+    if (t_b == 0 && threadIdx.x == 0) {
+      const unsigned q = atomicAdd(queue, 1u);
+      tw->slot[round & 1] = q < (unsigned)ninst ? order[q] : -1;
+    }
+    if (!team_barrier(&tw->count, &tw->gen, error)) break;
+    if (threadIdx.x == 0) s_idx = ld_volatile(&tw->slot[round & 1]);
+    __syncthreads();
+    const int idx = s_idx;
+    if (idx < 0 || idx >= ninst) break;
+    const int *src = (const int *)(insts + idx);
+    int *dst = (int *)&sd;
+    for (int w = threadIdx.x; w < (int)(sizeof(PlainDevice) / 4); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    run_realm(sd, step_limit, smem);
+    __syncthreads();  // sd and s_idx are rewritten in the next round
+  }
+}
+
+// Every realm of a batch back to its state right after initialize (site
+// flags, look-back words, control block, field), and the queue and team
+// words to zero. blockIdx.y is the realm.
+__global__ void batch_reset_kernel(const PlainDevice *insts, int ninst, unsigned *queue, BatchTeam *teams, int nteams,
+                                   int *error) {
+  const int r = blockIdx.y;
+  const PlainDevice &d = insts[r];
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (tid == 0) {
+    PlainCtrl c{};
+    c.liquid = d.gcap;  // every interior cell
+    *d.ctrl = c;
+  }
+  if (r == 0) {
+    if (tid == 0) {
+      *queue = 0u;
+      *error = 0;
+    }
+    for (long long t = tid; t < nteams; t += stride) teams[t] = BatchTeam{0u, 0u, {-1, -1}};
+  }
+  for (long long i = tid; i < d.nsites; i += stride) d.site_live[i] = 1;
+  for (long long i = tid; i < kStatusWords; i += stride) {
+    d.scanA[i] = 0ull;
+    d.scanA[kStatusWords + i] = 0ull;
+    d.scanB[i] = 0ull;
+  }
+  const long long nwords = solid_words(d.ncells);
+  for (long long w = tid; w < nwords; w += stride) init_field_word(d.orient, d.solid, d.claimed, d.grid, d.ncells, w);
+}
+
+// out[r] = realm r's control block.
+__global__ void batch_gather_kernel(const PlainDevice *insts, int ninst, PlainCtrl *out) {
+  const int r = blockIdx.x;
+  if (r >= ninst) return;
+  const unsigned *src = (const unsigned *)insts[r].ctrl;
+  unsigned *dst = (unsigned *)(out + r);
+  for (int w = threadIdx.x; w < (int)(sizeof(PlainCtrl) / 4); w += blockDim.x) dst[w] = src[w];
 }
 
 __global__ void grain_field_init_kernel(int32_t *out, const uint32_t *orient, Grid g, long long ncells) {
@@ -979,6 +1088,43 @@ cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid
   void *args[] = {(void *)&dd, (void *)&step_limit};
   return cudaLaunchCooperativeKernel((const void *)plain_persistent_kernel, dim3(grid_blocks), dim3(kBlock), args, 0,
                                      s);
+}
+
+int plain_batched_grid(int device) {
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plain_batched_kernel, kBlock, 0) != cudaSuccess)
+    return 0;
+  return sms * per_sm;
+}
+
+cudaError_t plain_batch_reset(const PlainDevice *insts, int ninst, unsigned *queue, BatchTeam *teams, int nteams,
+                              int *error, cudaStream_t s) {
+  if (ninst <= 0) return cudaSuccess;
+  batch_reset_kernel<<<dim3(64, ninst), 256, 0, s>>>(insts, ninst, queue, teams, nteams, error);
+  return cudaGetLastError();
+}
+
+cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ninst, int team_size, int nteams,
+                              unsigned *queue, BatchTeam *teams, int *error, long long step_limit, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nteams * team_size);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, plain_batched_kernel, insts, order, ninst, team_size, queue, teams, error,
+                            step_limit);
+}
+
+cudaError_t plain_batch_gather(const PlainDevice *insts, int ninst, PlainCtrl *out, cudaStream_t s) {
+  if (ninst <= 0) return cudaSuccess;
+  batch_gather_kernel<<<ninst, 128, 0, s>>>(insts, ninst, out);
+  return cudaGetLastError();
 }
 
 cudaError_t plain_grain_field(const PlainDevice &d, int32_t *out, long long ngrains, cudaStream_t s) {

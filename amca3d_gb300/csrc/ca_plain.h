@@ -119,6 +119,14 @@ struct PlainDevice {
   PlainCtrl *ctrl;
 };
 
+// One team of the batched launch: its barrier words and the realm it runs in
+// the current round, by round parity (-1: none left).
+struct BatchTeam {
+  unsigned count;
+  unsigned gen;
+  int slot[2];
+};
+
 // Fill the orientation field: -1 interior, 0 on the ghost layer
 // (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833),
 // and the solid bitmap to match.
@@ -133,6 +141,26 @@ int plain_persistent_grid(int device);
 // Run CA steps until solid, final_time, or ctrl->step reaches step_limit.
 // One cooperative launch; every phase boundary is a bounded grid barrier.
 cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid_blocks, cudaStream_t s);
+
+// Blocks of the batched kernel that fit on the device at once.
+int plain_batched_grid(int device);
+
+// Every realm of insts[0..ninst) (a device array) back to its state right
+// after initialize; the queue, the error word and the nteams team records
+// to zero.
+cudaError_t plain_batch_reset(const PlainDevice *insts, int ninst, unsigned *queue, BatchTeam *teams, int nteams,
+                              int *error, cudaStream_t s);
+
+// One cooperative launch of nteams * team_size blocks: each team of
+// team_size blocks takes realms order[0], order[1], ... from the queue and
+// runs each to solid, final_time or step_limit, as plain_run_steps would.
+// A team barrier that ran out sets *error; a realm's own failures go to its
+// control block.
+cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ninst, int team_size, int nteams,
+                              unsigned *queue, BatchTeam *teams, int *error, long long step_limit, cudaStream_t s);
+
+// out[r] (device) = realm r's control block.
+cudaError_t plain_batch_gather(const PlainDevice *insts, int ninst, PlainCtrl *out, cudaStream_t s);
 
 // cellGrainID_ from the envelope table: -1 liquid, 0 ghost layer, else the
 // id of the envelope created for the cell.

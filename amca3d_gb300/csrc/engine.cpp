@@ -318,6 +318,16 @@ struct amca_t {
     return v;
   }
 
+  // State after a batched run of this realm (which started from the state
+  // reset_device gives): its control block and the launch's time.
+  void adopt_batch_run(const PlainCtrl &c, double ms) {
+    ctrl = c;
+    kernel_ms = ms;
+    launches = 1;
+    vtr = VtrSeries();
+    vtr.configure(cfg.output, workdir);
+  }
+
   void write_snapshot() {
     std::vector<int32_t> o = orient_field();
     OutputView v = view(o);
@@ -393,10 +403,193 @@ struct amca_t {
   }
 };
 
+// Many plain realms in one cooperative launch (amca_batch_*).
+struct amca_batch {
+  std::string err;
+  std::vector<amca_t *> realms;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  PlainDevice *d_insts = nullptr;
+  int *d_order = nullptr;
+  unsigned *d_queue = nullptr;
+  BatchTeam *d_teams = nullptr;
+  int *d_error = nullptr;
+  PlainCtrl *d_ctrls = nullptr;
+  PlainCtrl *h_ctrls = nullptr;  // pinned
+  int *h_error = nullptr;        // pinned
+  int max_blocks = 0, team_size = 8, nteams = 0;
+  std::vector<int> order;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_ok = true;     // capture works on this device / driver
+  bool graph_stale = true;  // launch shape changed since the capture
+  int64_t runs = 0, cell_updates = 0;
+  double last_ms = 0.0, total_ms = 0.0;
+  std::vector<std::pair<int, double>> tuned;
+
+  ~amca_batch() {
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graph();
+    for (void *p : {(void *)d_insts, (void *)d_order, (void *)d_queue, (void *)d_teams, (void *)d_error,
+                    (void *)d_ctrls})
+      if (p) cudaFree(p);
+    if (h_ctrls) cudaFreeHost(h_ctrls);
+    if (h_error) cudaFreeHost(h_error);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+
+  int n() const { return (int)realms.size(); }
+
+  void setup(int team) {
+    const int nr = n();
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    max_blocks = plain_batched_grid(device);
+    if (max_blocks <= 0) throw CudaError("no co-resident blocks for the batched CA kernel");
+    std::vector<PlainDevice> descs((size_t)nr);
+    for (int r = 0; r < nr; ++r) descs[r] = realms[r]->dev;
+    CK(cudaMalloc(&d_insts, nr * sizeof(PlainDevice)));
+    CK(cudaMalloc(&d_order, nr * sizeof(int)));
+    CK(cudaMalloc(&d_queue, sizeof(unsigned)));
+    CK(cudaMalloc(&d_teams, max_blocks * sizeof(BatchTeam)));
+    CK(cudaMalloc(&d_error, sizeof(int)));
+    CK(cudaMalloc(&d_ctrls, nr * sizeof(PlainCtrl)));
+    CK(cudaMallocHost(&h_ctrls, nr * sizeof(PlainCtrl)));
+    CK(cudaMallocHost(&h_error, sizeof(int)));
+    CK(cudaMemcpyAsync(d_insts, descs.data(), nr * sizeof(PlainDevice), cudaMemcpyHostToDevice, stream));
+    order.resize(nr);
+    for (int r = 0; r < nr; ++r) order[r] = r;
+    upload_order();
+    set_team(team > 0 ? team : 8);
+  }
+
+  void upload_order() {
+    CK(cudaMemcpyAsync(d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  void set_team(int team) {
+    if (team < 1 || team > max_blocks)
+      throw std::invalid_argument("team size must be between 1 and the co-resident blocks (" +
+                                  std::to_string(max_blocks) + ")");
+    team_size = team;
+    nteams = std::min(max_blocks / team, n());
+    graph_stale = true;
+  }
+
+  void enqueue() {
+    const int nr = n();
+    CK(plain_batch_reset(d_insts, nr, d_queue, d_teams, nteams, d_error, stream));
+    CK(plain_batched_run(d_insts, d_order, nr, team_size, nteams, d_queue, d_teams, d_error, 1ll << 60, stream));
+    CK(plain_batch_gather(d_insts, nr, d_ctrls, stream));
+    CK(cudaMemcpyAsync(h_ctrls, d_ctrls, nr * sizeof(PlainCtrl), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_error, d_error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  }
+
+  // Capture enqueue() into a graph; on a capture failure runs use plain launches.
+  void capture() {
+    drop_graph();
+    graph_stale = false;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      graph_ok = false;
+      return;
+    }
+    bool ok = true;
+    try {
+      enqueue();
+    } catch (const CudaError &) {
+      ok = false;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (!ok || e != cudaSuccess || !g || cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      exec = nullptr;
+      cudaGetLastError();
+      graph_ok = false;
+      return;
+    }
+    graph = g;
+  }
+
+  double run() {
+    if (graph_ok && graph_stale) capture();
+    CK(cudaEventRecord(ev0, stream));
+    if (graph_ok)
+      CK(cudaGraphLaunch(exec, stream));
+    else
+      enqueue();
+    CK(cudaEventRecord(ev1, stream));
+    CK(cudaStreamSynchronize(stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    ++runs;
+    last_ms = ms;
+    total_ms += ms;
+    if (*h_error) throw DeviceError("batched CA launch stopped: a team barrier wait timed out");
+    cell_updates = 0;
+    for (int r = 0; r < n(); ++r) {
+      amca_t *h = realms[r];
+      const PlainCtrl &c = h_ctrls[r];
+      h->adopt_batch_run(c, ms);
+      cell_updates += (int64_t)c.step * ((int64_t)h->cfg.nx * h->cfg.ny * h->cfg.nz);
+      if (c.error)
+        throw DeviceError("realm " + std::to_string(r) + " of the batch stopped: " +
+                          (c.error == kErrBarrier ? "grid barrier wait timed out" : "scan look-back wait timed out"));
+    }
+    return ms;
+  }
+
+  // Block 0 of a realm's team timed every phase of its run; their sum is the
+  // realm's time in the launch.
+  static double realm_ns(const PlainCtrl &c) {
+    return (double)(c.ns_nucleation + c.ns_claim + c.ns_resolve + c.ns_step_end);
+  }
+
+  int tune(int repeats) {
+    repeats = std::max(repeats, 1);
+    run();
+    std::vector<double> t((size_t)n());
+    for (int r = 0; r < n(); ++r) t[r] = realm_ns(h_ctrls[r]);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return t[a] > t[b]; });
+    upload_order();
+    tuned.clear();
+    int best = team_size;
+    double best_ms = 1e300;
+    std::vector<int> sizes;
+    for (int s = 1; s <= 64 && s <= max_blocks; s *= 2) sizes.push_back(s);
+    for (int s : sizes) {
+      set_team(s);
+      double m = 1e300;
+      for (int k = 0; k < repeats; ++k) m = std::min(m, run());
+      tuned.emplace_back(s, m);
+      if (m < best_ms) {
+        best_ms = m;
+        best = s;
+      }
+    }
+    set_team(best);
+    return best;
+  }
+};
+
 namespace {
 
-template <typename F>
-int guarded(amca_t *h, F &&f) {
+template <typename H, typename F>
+int guarded(H *h, F &&f) {
   try {
     f();
     if (h) h->err.clear();
@@ -740,6 +933,86 @@ int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc
   for (void *p : bufs) cudaFree(p);
   return rc;
 }
+
+int amca_batch_create(amca_t *const *realms, int n, int team_size, amca_batch **out) {
+  if (!out || !realms || n < 1 || n > 65535) {
+    g_create_error = "amca_batch_create: null argument, or not 1 to 65535 realms";
+    return AMCA_ERR_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<amca_batch> b(new amca_batch);
+  try {
+    for (int r = 0; r < n; ++r) {
+      amca_t *h = realms[r];
+      if (!h) throw std::invalid_argument("amca_batch_create: null realm handle");
+      if (h->rm) throw std::invalid_argument("amca_batch_create: batches run plain realms only");
+      if (!h->initialized) throw StateError("amca_batch_create: realm " + std::to_string(r) + " is not initialized");
+      if (r > 0 && h->device != realms[0]->device)
+        throw std::invalid_argument("amca_batch_create: realms on different devices");
+      if (std::find(b->realms.begin(), b->realms.end(), h) != b->realms.end())
+        throw std::invalid_argument("amca_batch_create: a realm appears twice");
+      b->realms.push_back(h);
+    }
+    b->device = realms[0]->device;
+    for (amca_t *h : b->realms) CK(cudaStreamSynchronize(h->stream));
+    b->setup(team_size);
+  } catch (const StateError &e) {
+    g_create_error = e.what();
+    return AMCA_ERR_STATE;
+  } catch (const CudaError &e) {
+    g_create_error = e.what();
+    return AMCA_ERR_CUDA;
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    return AMCA_ERR_ARG;
+  }
+  *out = b.release();
+  return AMCA_OK;
+}
+
+int amca_batch_run(amca_batch *b, double *device_ms) {
+  if (!b) return AMCA_ERR_ARG;
+  return guarded(b, [&] {
+    const double ms = b->run();
+    if (device_ms) *device_ms = ms;
+  });
+}
+
+int amca_batch_tune(amca_batch *b, int repeats, int *team_size_out) {
+  if (!b) return AMCA_ERR_ARG;
+  return guarded(b, [&] {
+    const int t = b->tune(repeats);
+    if (team_size_out) *team_size_out = t;
+  });
+}
+
+int amca_batch_get_stats(const amca_batch *b, amca_batch_stats *s) {
+  if (!b || !s) return AMCA_ERR_ARG;
+  memset(s, 0, sizeof *s);
+  s->realms = b->n();
+  s->team_size = b->team_size;
+  s->teams = b->nteams;
+  s->max_blocks = b->max_blocks;
+  s->graph = b->graph_ok ? 1 : 0;
+  s->runs = b->runs;
+  s->last_ms = b->last_ms;
+  s->total_ms = b->total_ms;
+  s->cell_updates = b->cell_updates;
+  const int nt = std::min<int>((int)b->tuned.size(), 8);
+  s->n_tuned = nt;
+  for (int i = 0; i < nt; ++i) {
+    s->tuned_team[i] = b->tuned[i].first;
+    s->tuned_ms[i] = b->tuned[i].second;
+  }
+  return AMCA_OK;
+}
+
+const char *amca_batch_last_error(const amca_batch *b) {
+  if (!b) return g_create_error.c_str();
+  return b->err.c_str();
+}
+
+void amca_batch_destroy(amca_batch *b) { delete b; }
 
 const char *amca_last_error(const amca_t *h) {
   if (!h) return g_create_error.c_str();

@@ -193,6 +193,38 @@ def config_uniform_320() -> PlainCase:
                      seed=1, t_dot=-50.0, time_step=0.001, termination_time=1.0e4)
 
 
+def batched_instances(count: int, seed: int, edges=(32, 128), t_dot=(-200.0, -5.0), sites=(50, 2000),
+                      cell_size: float = 2e-6, prefix: str = "batched") -> list:
+    """Independent uniform-cooling instances: cube edges uniform on the
+    integers edges[0]..edges[1], t_dot log-uniform on t_dot, bulk Gaussian
+    sites (mean 3 K, std 1 K) with a density that draws a uniform integer
+    count in sites[0]..sites[1], no surface sites, the KGT coefficients and
+    temperatures of nucleation_60, and seed 0 (the reference's srand at np=1).
+    Draws come from Python's Mersenne Twister ``random()`` alone, whose
+    sequence for a seed is fixed across Python versions."""
+    import random
+
+    rng = random.Random(seed)
+    out = []
+    lo_t, hi_t = math.log(-t_dot[1]), math.log(-t_dot[0])
+    for i in range(count):
+        e = edges[0] + int(rng.random() * (edges[1] - edges[0] + 1))
+        td = -math.exp(lo_t + rng.random() * (hi_t - lo_t))
+        ns = sites[0] + int(rng.random() * (sites[1] - sites[0] + 1))
+        cells = (e, e, e)
+        out.append(PlainCase(name=f"{prefix}_{i:02d}", cells=cells, cell_size=cell_size,
+                             surface=(0.0, 2.0, 0.5), bulk=(bulk_density_for_sites(ns, cells, cell_size), 3.0, 1.0),
+                             seed=0, t_dot=td, time_step=0.001, termination_time=1.0e4))
+    return out
+
+
+def config_batched_64() -> list:
+    """64 independent uniform-cooling instances: edges 32..128 cells of 2 um
+    (seed 3), t_dot log-uniform on [-200, -5] K/s, 50..2,000 bulk sites each;
+    about 44M interior cells in all."""
+    return batched_instances(64, 3)
+
+
 @dataclasses.dataclass
 class RemeltCase:
     """One FE-coupled remelting run: a ``finite_element`` realm that replays

@@ -1,13 +1,15 @@
 """Benchmark: plain CA timestep, uniform cooling at 320^3 (32.8M cells);
 with --workload pbf_500 the FE-coupled remelting realm on a laser track
-(500 x 250 x 100 cells, Rosenthal frames, columnar baseplate).
+(500 x 250 x 100 cells, Rosenthal frames, columnar baseplate); with
+--workload batched_64 64 independent plain instances (edges 32..128) in one
+graph-replayed launch, beside the same instances as 64 sequential launches.
 
 One bench step = one full run of the deck from its initial state to its end
 (full solidification, or the end of the frames), every CA step of it, on one
 GPU; cell-updates/s = interior cells x CA steps / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload uniform_320|pbf_500]
+                  [--workload uniform_320|pbf_500|batched_64]
 
 ours (default): the CUDA path. `value` is device time (CUDA events around
   the persistent step kernel on its stream) with the realm's tables resident
@@ -522,6 +524,198 @@ def run_ours_pbf(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# Batched instances (batched_64)
+# ----------------------------------------------------------------------------
+BATCH_TEXT = ("batched_64: 64 independent plain CA instances, cube edges uniform on 32..128 cells of 2 um "
+              "(seed 3; 43.8M cells in all), t_dot log-uniform on [-200, -5] K/s, 50..2,000 bulk Gaussian sites "
+              "(3 K, 1 K) each, KGT a1=-0.544e-4 a2=2.03e-4, srand seed 0 per instance; every instance to full "
+              "solidification, all in one graph-replayed cooperative launch with an autotuned team size")
+
+
+def _oracle_instance(case) -> tuple:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    t = time.perf_counter()
+    r = amca_oracle.run_plain(case, fields=False)
+    return case.n_interior * r["steps"], time.perf_counter() - t
+
+
+def cpu_baseline_batched(count: int = 8) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    amca_oracle.build()
+    upd, el = 0, 0.0
+    for c in decks.config_batched_64()[:count]:
+        u, e = _oracle_instance(c)
+        upd += u
+        el += e
+    return {"value": upd / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"C restatement of the reference, one core: the first {count} of the 64 instances, each to "
+                      f"full solidification, one after another ({el:.1f} s)"}
+
+
+def run_reference_arm_batched(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    amca_oracle.build()
+    cores = os.cpu_count() or 1
+    todo = sorted(decks.config_batched_64(), key=lambda c: -c.n_interior)  # longest first
+    ctx = mp.get_context("spawn")
+    times, updates = [], []
+    with ctx.Pool(cores) as pool:
+        for it in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            res = list(pool.imap_unordered(_oracle_instance, todo))
+            el = time.perf_counter() - t
+            if it >= args.warmup:
+                times.append(el)
+                updates.append(sum(r[0] for r in res))
+    value = sum(updates) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": BATCH_TEXT, "instances": len(todo), "cells": sum(c.n_interior for c in todo)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"the whole workload: the 64 instances as single-core runs of the C "
+                                   f"restatement of the reference, {cores} at a time, longest first"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _batch_grain_stats(realms, decks_) -> dict:
+    grains, cells, aligned = 0, 0, 0.0
+    for r, c in zip(realms, decks_):
+        g = grain_stats(r.field("orientation_id"), c.cells, r.orientations())
+        grains += g["grains"]
+        cells += c.n_interior
+        aligned += g["texture_100_z_15deg"] * c.n_interior
+    return {"grains": grains, "mean_grain_cells": cells / max(grains, 1), "texture_100_z_15deg": aligned / cells}
+
+
+def run_ours_batched(args, dist: Dist):
+    import amca3d_gb300 as A
+
+    dev = dist.local_rank
+    decks_ = decks.config_batched_64()
+    realms = []
+    for c in decks_:
+        r = A.CellularAutomataRealm(c.to_yaml(), seed=c.seed, device=dev)
+        r.initialize()
+        realms.append(r)
+    batch = A.Batch(realms)
+    team = batch.tune(repeats=2)
+    for _ in range(args.warmup):
+        batch.run()
+    clocks = ClockSampler(dev)
+    dist.barrier()
+    clocks.start()
+    device_ms, updates, alg_bytes = [], [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        device_ms.append(batch.run())
+        bs = batch.stats()
+        updates.append(bs["cell_updates"])
+        alg_bytes.append(sum(r.stats()["algorithmic_bytes"] for r in realms))
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clk = clocks.stop()
+    bs = batch.stats()
+    per = [r.stats() for r in realms]
+    gstats = _batch_grain_stats(realms, decks_)
+    orient_last = [r.field("orientation_id") for r in realms[:4]]
+    batch.close()
+
+    # the same 64 instances as 64 sequential plain launches (one persistent
+    # launch per instance on the whole GPU), device time
+    seq_ms = []
+    for it in range(2):
+        tot = 0.0
+        for r in realms:
+            r.reset()
+            r.run()
+            tot += r.stats()["kernel_ms"]
+        seq_ms.append(tot)
+    seq_same = all(np.array_equal(realms[i].field("orientation_id"), orient_last[i]) for i in range(4))
+    for r in realms:
+        r.close()
+
+    # end to end through the public API per step: decks -> 64 realms
+    # (host sites + H2D) -> one batch run -> every orientation field into
+    # pinned host memory -> close
+    pinned = [A.PinnedBuffer(c.n_ghost, np.int32) for c in decks_]
+    e2e_t, e2e_upd, h2d, d2h = [], [], [], []
+    for it in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        rs = []
+        for c in decks_:
+            r = A.CellularAutomataRealm(c.to_yaml(), seed=c.seed, device=dev)
+            r.initialize()
+            rs.append(r)
+        with A.Batch(rs, team_size=team) as b:
+            b.run()
+            upd = b.stats()["cell_updates"]
+        for r, p in zip(rs, pinned):
+            r.field("orientation_id", out=p.array)
+        sts = [r.stats() for r in rs]
+        for r in rs:
+            r.close()
+        el = time.perf_counter() - t
+        if it >= args.warmup:
+            e2e_t.append(el)
+            e2e_upd.append(upd)
+            h2d.append(sum(s_["h2d_bytes"] for s_ in sts))
+            d2h.append(sum(s_["d2h_bytes"] for s_ in sts))
+    same = all(np.array_equal(pinned[i].array, orient_last[i]) for i in range(4))
+    for p in pinned:
+        p.free()
+
+    t_dev = dist.reduce(sum(device_ms) / 1e3, "max")
+    upd_total = dist.reduce(float(sum(updates)), "sum")
+    e2e_time = dist.reduce(sum(e2e_t), "max")
+    e2e_total = dist.reduce(float(sum(e2e_upd)), "sum")
+    if dist.rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    ms = sum(device_ms) / len(device_ms)
+    achieved = (sum(alg_bytes) / len(alg_bytes)) / (ms / 1e3) / 1e9
+    seq = min(seq_ms)
+    steps_all = [p_["step"] for p_ in per]
+    line = {
+        "metric": METRIC, "value": upd_total / t_dev, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": BATCH_TEXT, "instances": len(decks_), "cells": sum(c.n_interior for c in decks_),
+                   "ca_steps_min_mean_max": [min(steps_all), float(np.mean(steps_all)), max(steps_all)],
+                   "cell_updates_per_run": bs["cell_updates"], **gstats,
+                   "team_size": bs["team_size"], "teams": bs["teams"], "max_blocks": bs["max_blocks"],
+                   "cuda_graph": bool(bs["graph"]), "autotune_ms_by_team": bs["tuned"],
+                   "sequential_plain_ms": seq, "sequential_plain_cell_updates_per_s": bs["cell_updates"] / (seq / 1e3),
+                   "speedup_vs_sequential_plain": seq / ms, "sequential_fields_match": seq_same,
+                   "e2e_fields_match": same, "parallelism": f"replicas x{args.gpus}",
+                   "l2": "inputs larger than L2: 64 orientation fields 183 MB + envelope tables 1.9 GB per run"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": load_traffic("ca_batched_64.json"), "peak_kind": f"{peak_kind} burst copy",
+                     "kernel": "plain_batched_kernel (one launch per run)",
+                     "algorithmic_bytes_per_launch": sum(alg_bytes) / len(alg_bytes)},
+        "e2e": {"value": e2e_total / e2e_time, "unit": UNIT, "h2d_bytes_per_step": int(np.mean(h2d)),
+                "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": 1e3 * e2e_time / args.steps},
+        "gpu_launches": 3 * args.steps,  # per run: reset, batched step kernel, control-block gather
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    if args.gpus == 1 and dist.rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_batched()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -531,7 +725,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=128, help="edge of the CPU-baseline sample block")
     ap.add_argument("--ref-sample", type=int, default=96, help="edge of each reference-arm sample block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["uniform_320", "pbf_500"], default="uniform_320")
+    ap.add_argument("--workload", choices=["uniform_320", "pbf_500", "batched_64"], default="uniform_320")
     ap.add_argument("--cpu-pbf-steps", type=int, default=40, help="CA steps of the pbf_500 CPU-baseline sample")
     ap.add_argument("--ref-pbf-steps", type=int, default=20, help="CA steps of each pbf_500 reference-arm sample")
     ap.add_argument("--pbf-block", default="", help="X,Y,Z cells: run the pbf_500 physics on another block "
@@ -545,6 +739,8 @@ def main():
     try:
         if args.workload == "pbf_500":
             (run_reference_arm_pbf if args.impl == "reference" else run_ours_pbf)(args, dist)
+        elif args.workload == "batched_64":
+            (run_reference_arm_batched if args.impl == "reference" else run_ours_batched)(args, dist)
         elif args.impl == "reference":
             run_reference_arm(args, dist)
         else:

@@ -278,6 +278,62 @@ int amca_plain_run_noalloc(int device, const amca_plain_params *p, const int32_t
                            int64_t nsites, const double *l2g, int32_t *orient, int max_steps, void *stream,
                            amca_plain_result *res, char *err, size_t errlen);
 
+/* ---- Batches: many independent plain realms in one launch -------------
+ * No counterpart in the reference, which runs one deck per process: a batch
+ * stands in for n separate np=1 runs of the reference program (CA/src/Cafe.cpp:39-120),
+ * each CellularAutomataSolver::execute -> CellularAutomataManager_3D::time_integration
+ * (CA/src/CellularAutomataSolver.cpp:148-160). Every realm's result is the one
+ * it gives when run alone. */
+typedef struct amca_batch amca_batch;
+
+/* A batch over n distinct, initialized plain-realm handles on one device
+ * (1 <= n <= 65535). The handles stay the caller's and must outlive the
+ * batch; while it exists they are run only through it. team_size = blocks
+ * that run one realm (0: 8, until amca_batch_tune picks one). */
+int amca_batch_create(amca_t *const *realms, int n, int team_size, amca_batch **out);
+
+/* Run every realm of the batch from its initial state (what amca_reset
+ * gives) to its end (solid, or termination_time), all in one cooperative
+ * launch: teams of team_size blocks take realms from a queue, longest first
+ * once amca_batch_tune has measured them. Each run replays one CUDA graph
+ * (reset of every realm, the launch, a gather of the realms' control
+ * blocks) on the batch's own stream and waits for it. Afterwards each handle
+ * reads as after amca_reset + amca_run(h, -1) (amca_get_field,
+ * amca_get_stats, amca_write_outputs, ...), except that no VTR snapshot is
+ * written during the run. device_ms (may be NULL): CUDA-event time of the
+ * graph on that stream. AMCA_ERR_DEVICE names the realm whose bounded wait
+ * ran out. */
+int amca_batch_run(amca_batch *b, double *device_ms);
+
+/* Autotuning: runs the batch once to measure each realm, orders the queue
+ * longest realm first, then times team sizes 1, 2, 4, ... (up to 64, and
+ * the largest that fits) `repeats` times each (at least 1) and keeps the
+ * fastest. *team_size_out (may be NULL) = the size kept. */
+int amca_batch_tune(amca_batch *b, int repeats, int *team_size_out);
+
+typedef struct {
+  int32_t realms;
+  int32_t team_size;     /* blocks per realm */
+  int32_t teams;         /* teams in the launch */
+  int32_t max_blocks;    /* co-resident blocks of the batched kernel on this device */
+  int32_t graph;         /* 1: runs replay a CUDA graph; 0: plain launches (capture unavailable) */
+  int32_t n_tuned;       /* entries of tuned_* filled by the last amca_batch_tune */
+  int64_t runs;
+  double last_ms;        /* device time of the last run */
+  double total_ms;
+  int64_t cell_updates;  /* sum over realms of interior cells x CA steps, last run */
+  int32_t tuned_team[8];
+  double tuned_ms[8];    /* best time of each team size tried */
+} amca_batch_stats;
+
+int amca_batch_get_stats(const amca_batch *b, amca_batch_stats *out);
+
+/* Message of the last failing call on b (or of the last failing
+ * amca_batch_create when b is NULL). Never NULL. */
+const char *amca_batch_last_error(const amca_batch *b);
+
+void amca_batch_destroy(amca_batch *b);
+
 /* Message of the last failing call on h (or of the last failing
  * amca_create / amca_envelope_eval when h is NULL). Never NULL. */
 const char *amca_last_error(const amca_t *h);

@@ -10,7 +10,12 @@ cases.py it writes the deck, runs the reference at np=1 with AMCA_SEED set
     digests of the int32 orientation / grain fields;
   * outputs_tiny/: every output file of the tiny output deck, verbatim.
 
-Usage: python tests/golden/make_golden.py [--large] [--only NAME]
+With --batched it instead runs the 64 instances of the batched workload
+(decks.config_batched_64), one reference process per host core, and writes
+batched_64_golden.json: per instance, step count, final grain count and the
+SHA-256 digests of its orientation / grain fields.
+
+Usage: python tests/golden/make_golden.py [--large] [--only NAME] [--batched]
 """
 from __future__ import annotations
 
@@ -74,13 +79,40 @@ def run_reference(case, workdir: str):
                 orient=orient, grain=grain, dtc=dtc)
 
 
+def _batched_entry(case) -> tuple:
+    with tempfile.TemporaryDirectory() as wd:
+        res = run_reference(case, wd)
+    return case.name, dict(steps=res["steps"], final_grains=res["final_grains"], orient_sha256=sha(res["orient"]),
+                           grain_sha256=sha(res["grain"]), cells=list(case.cells), t_dot=case.t_dot,
+                           bulk_density=case.bulk[0])
+
+
+def make_batched() -> None:
+    import multiprocessing as mp
+
+    from amca3d_gb300 import decks
+
+    todo = sorted(decks.config_batched_64(), key=lambda c: -c.n_interior)  # longest first
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        out = dict(pool.imap_unordered(_batched_entry, todo))
+    with open(os.path.join(HERE, "batched_64_golden.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print(f"batched_64_golden.json: {len(out)} instances")
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--batched", action="store_true", help="only the 64 instances of the batched workload")
     ap.add_argument("--large", action="store_true", help="also run the 320^3 case (tens of minutes)")
     ap.add_argument("--only", default=None)
     ap.add_argument("--from-dir", nargs=2, metavar=("CASE", "DIR"),
                     help="record a finished reference run of CASE (its directory holds run.log and grainInfo0.txt)")
     args = ap.parse_args()
+    if args.batched:
+        if not os.path.exists(REF_BIN):
+            sys.exit(f"{REF_BIN} missing: run `make -C oracle ref REF=<reference checkout>` first")
+        make_batched()
+        return
     jpath = os.path.join(HERE, "plain_golden.json")
     golden = json.load(open(jpath)) if os.path.exists(jpath) else {}
     if args.from_dir:

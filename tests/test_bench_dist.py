@@ -63,4 +63,5 @@ def test_reference_arm_prints_only_on_rank_zero(capsys):
 
     bench.run_reference_arm(Args(), FakeDist())
     bench.run_reference_arm_pbf(Args(), FakeDist())
+    bench.run_reference_arm_batched(Args(), FakeDist())
     assert capsys.readouterr().out == ""

@@ -178,6 +178,32 @@ def test_gpu_calls_fail_loudly_without_initialize(amca):
     r.close()
 
 
+def test_batch_checks_handles_before_touching_the_gpu(amca):
+    """amca_batch_create: uninitialized realms are a state error, remelting
+    realms and empty lists an argument error; no GPU call is made."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import remelt_cases
+
+    r = amca.CellularAutomataRealm(cases.small_cases()[2].to_yaml())
+    with pytest.raises(amca.AmcaError) as e:
+        amca.Batch([r])
+    assert e.value.code == -4 and "not initialized" in str(e.value)
+    rm = amca.CellularAutomataRealm(remelt_cases.fixtures()[0].case.to_yaml())
+    with pytest.raises(amca.AmcaError) as e:
+        amca.Batch([rm])
+    assert e.value.code == -1 and "plain realms" in str(e.value)
+    with pytest.raises(amca.AmcaError) as e:
+        amca.Batch([])
+    assert e.value.code == -1
+    lib = amca.load_library()
+    assert lib.amca_batch_run(None, None) == -1
+    assert lib.amca_batch_get_stats(None, None) == -1
+    assert lib.amca_batch_last_error(None)
+    lib.amca_batch_destroy(None)
+    r.close()
+    rm.close()
+
+
 # ---------------------------------------------------------------------------
 # FE-coupled remelting decks (host half only)
 # ---------------------------------------------------------------------------
