@@ -234,6 +234,13 @@ void parse_ca_realm(const Node &realm, PlainConfig &c, RemeltConfig *rm) {
     }
   }
   if (c.output.variables.empty()) c.output.variables.push_back(output_variable_id("grain_ID"));
+  if (const Node *fmt = out->find("output_format")) {
+    const std::string f = fmt->as_string();
+    if (f == "appended" || f == "binary")
+      c.output.appended = true;
+    else if (f != "ascii")
+      fail("output_format must be ascii or appended", fmt);
+  }
 
   // ProblemPhysics_RappazGandin1993::load
   const Node *pp = realm.find("problem_physics");

@@ -20,6 +20,10 @@ struct OutputConfig {
   double time_interval = 0.0;              // output_time_interval
   bool time_interval_set = false;
   std::vector<int> variables;              // ids into the reference's variable-name table
+  // output_format: "ascii" (the reference's text pieces, default) or
+  // "appended" (the same arrays as raw little-endian binary in one appended
+  // block; a key of this library, which the reference does not read)
+  bool appended = false;
 };
 
 struct PlainConfig {

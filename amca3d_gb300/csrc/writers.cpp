@@ -7,6 +7,8 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <string.h>
+
 #include <algorithm>
 #include <fstream>
 #include <sstream>
@@ -40,6 +42,115 @@ std::string cwd() {
   char buf[4096];
   if (!getcwd(buf, sizeof buf)) return ".";
   return buf;
+}
+
+static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "appended VTR pieces are written in host byte order");
+
+// One array of an appended piece: its XML attributes, bytes per cell (0 for
+// a coordinate array) and how to fill one k-plane of interior cells.
+struct AppendedArray {
+  std::string attrs;
+  size_t bytes;
+};
+
+// The .vtr piece with the arrays of the ASCII piece (same names, types and
+// order) as raw little-endian binary in one appended block (VTK XML,
+// header_type UInt64: each array is preceded by its byte count). Values are
+// those the ASCII piece prints: grain ids through the VTR shuffle, cell
+// temperatures through an int, melted flags (1 in the plain realm); Euler
+// angles and coordinates keep full FP64 precision where the text has six
+// significant digits. Written one k-plane at a time.
+void write_piece_appended(const OutputView &v, const std::vector<int> &vars, const std::string &path) {
+  const int nxg = v.nx + 2, nyg = v.ny + 2, nzg = v.nz + 2;
+  const int64_t nxyg = (int64_t)nxg * nyg;
+  const int64_t plane = (int64_t)v.nx * v.ny, ncell = plane * v.nz;
+  std::vector<int> used;
+  std::vector<AppendedArray> arrays;
+  for (int var : vars) {
+    if (var == 0 && v.temperature) {
+      arrays.push_back({"type=\"Float64\" Name=\"cell_temperature\"", 8});
+    } else if (var == 2) {
+      arrays.push_back({"type=\"Int64\" Name=\"grain_id\"", 8});
+    } else if (var == 3) {
+      arrays.push_back({"type=\"Float64\" Name=\"grain_orientation\" NumberOfComponents=\"3\"", 24});
+    } else if (var == 6) {
+      arrays.push_back({"type=\"Int8\" Name=\"melted_flag\"", 1});
+    } else {
+      continue;
+    }
+    used.push_back(var);
+  }
+  std::ofstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot write " + path);
+  uint64_t offset = 0;
+  f << "<?xml version=\"1.0\"?>\n";
+  f << "<VTKFile type=\"RectilinearGrid\" version=\"0.1\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n";
+  f << W2 << "<RectilinearGrid WholeExtent=\"0 " << v.nx << " 0 " << v.ny << " 0 " << v.nz << "\">\n";
+  f << W3 << "<Piece Extent=\"0 " << v.nx << " 0 " << v.ny << " 0 " << v.nz << "\">\n";
+  f << W4 << "<CellData Scalars=\"grain_id\">\n";
+  for (const AppendedArray &a : arrays) {
+    f << W5 << "<DataArray " << a.attrs << " format=\"appended\" offset=\"" << offset << "\"/>\n";
+    offset += 8 + a.bytes * (uint64_t)ncell;
+  }
+  f << W4 << "</CellData>\n";
+  f << W4 << "<Coordinates>\n";
+  const char *nm[3] = {"X_Coordinates", "Y_Coordinates", "Z_Coordinates"};
+  const int npts[3] = {v.nx + 1, v.ny + 1, v.nz + 1};
+  for (int a = 0; a < 3; a++) {
+    f << W5 << "<DataArray type=\"Float64\" Name=\"" << nm[a] << "\" format=\"appended\" offset=\"" << offset
+      << "\"/>\n";
+    offset += 8 + 8 * (uint64_t)npts[a];
+  }
+  f << W4 << "</Coordinates>\n";
+  f << W3 << "</Piece>\n";
+  f << W2 << "</RectilinearGrid>\n";
+  f << W2 << "<AppendedData encoding=\"raw\">\n" << W3 << "_";
+  std::vector<char> buf;
+  for (size_t q = 0; q < used.size(); ++q) {
+    const int var = used[q];
+    const uint64_t nbytes = arrays[q].bytes * (uint64_t)ncell;
+    f.write((const char *)&nbytes, 8);
+    buf.resize((size_t)(arrays[q].bytes * plane));
+    for (int k = 1; k < nzg - 1; k++) {
+      char *o = buf.data();
+      for (int j = 1; j < nyg - 1; j++)
+        for (int i = 1; i < nxg - 1; i++) {
+          const int64_t c = k * nxyg + (int64_t)j * nxg + i;
+          if (var == 0) {
+            const double t = (double)(int)v.temperature[c];
+            memcpy(o, &t, 8);
+            o += 8;
+          } else if (var == 2) {
+            int val = v.orient[c];
+            if (val >= 0 && v.mapped_vtr) val = (*v.mapped_vtr)[val];
+            const int64_t w = val;
+            memcpy(o, &w, 8);
+            o += 8;
+          } else if (var == 3) {
+            const int val = v.orient[c];
+            double e[3] = {0.0, 0.0, 0.0};
+            if (val >= 0)
+              for (int a = 0; a < 3; a++) e[a] = v.euler[3 * (int64_t)val + a];
+            memcpy(o, e, 24);
+            o += 24;
+          } else {
+            *o++ = (char)(v.melted ? (int8_t)v.melted[c] : (int8_t)1);
+          }
+        }
+      f.write(buf.data(), (std::streamsize)buf.size());
+    }
+  }
+  const double org[3] = {v.x0, v.y0, v.z0};
+  for (int a = 0; a < 3; a++) {
+    std::vector<double> x((size_t)npts[a]);
+    for (int i = 0; i < npts[a]; i++) x[i] = org[a] + i * v.h;
+    const uint64_t nbytes = 8 * (uint64_t)npts[a];
+    f.write((const char *)&nbytes, 8);
+    f.write((const char *)x.data(), (std::streamsize)nbytes);
+  }
+  f << "\n" << W2 << "</AppendedData>\n";
+  f << "</VTKFile>\n";
+  if (!f) throw std::runtime_error("cannot write " + path);
 }
 
 }  // namespace
@@ -81,7 +192,9 @@ void VtrSeries::write(const OutputView &v, double time) {
   create_path(step_dir + "/" + pvd_name_);
   times_.emplace_back(num_output_, time);
   const int nxg = v.nx + 2, nyg = v.ny + 2, nzg = v.nz + 2, nxyg = nxg * nyg;
-  {
+  if (cfg_.appended) {
+    write_piece_appended(v, cfg_.variables, step_dir + "/" + pvd_name_ + padded(5, 0) + ".vtr");
+  } else {
     std::ofstream f(step_dir + "/" + pvd_name_ + padded(5, 0) + ".vtr");
     if (!f) throw std::runtime_error("cannot write " + step_dir);
     f << "<?xml version=\"1.0\"?>\n";

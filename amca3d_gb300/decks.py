@@ -45,6 +45,7 @@ class PlainCase:
     output_frequency: int = 0
     output_base: str = "./Results/Grains"
     output_variables: Sequence[str] = ("grain_ID",)
+    output_format: Optional[str] = None  # "appended": binary VTR pieces (a key the reference ignores)
     microstructure_file: Optional[str] = None
     shuffle_vtr: bool = False
     shuffle_vtk: Optional[bool] = None
@@ -88,6 +89,7 @@ class PlainCase:
         if self.time_step_factor_ca is not None:
             ti.append(f"      time_step_factor_ca: {_num(self.time_step_factor_ca)}")
         outv = "\n".join(f"        - {v}" for v in self.output_variables)
+        fmt = f"\n      output_format: {self.output_format}" if self.output_format else ""
         return f"""# {self.name} (seed {self.seed})
 simulations:
   - name: {self.name}
@@ -138,7 +140,7 @@ realms:
 
     output:
       output_data_base_name: {self.output_base}
-      output_frequency: {self.output_frequency}
+      output_frequency: {self.output_frequency}{fmt}
       output_variables:
 {outv}
 
@@ -269,6 +271,7 @@ class RemeltCase:
     output_base: str = "./Results/Grains"
     output_frequency: int = 100000
     output_variables: Sequence[str] = ("grain_orientation",)
+    output_format: Optional[str] = None  # "appended": binary VTR pieces (a key the reference ignores)
 
     @property
     def n_interior(self) -> int:
@@ -316,6 +319,7 @@ class RemeltCase:
         if self.time_step_factor_ca is not None:
             ti.append(f"      time_step_factor_ca: {_num(self.time_step_factor_ca)}")
         outv = "\n".join(f"        - {v}" for v in self.output_variables)
+        fmt = f"\n      output_format: {self.output_format}" if self.output_format else ""
         return f"""# {self.name} (seed {self.seed})
 simulations:
   - name: {self.name}
@@ -392,7 +396,7 @@ realms:
 
     output:
       output_data_base_name: {self.output_base}
-      output_frequency: {self.output_frequency}
+      output_frequency: {self.output_frequency}{fmt}
       output_variables:
 {outv}
 

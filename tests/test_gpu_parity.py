@@ -116,6 +116,50 @@ def test_gpu_outputs_byte_identical(amca):
             assert filecmp.cmp(a, b, shallow=False), rel
 
 
+def test_gpu_appended_vtr_carries_the_reference_values(amca):
+    """output_format: appended writes every VTR piece as raw binary: per
+    snapshot the same arrays as the reference's ASCII piece, grain ids
+    equal, Euler angles and coordinates equal to the text's six digits and,
+    at full precision, to the orientation table and x0 + i h; the PVTR and
+    PVD files stay byte-identical."""
+    import dataclasses
+
+    from amca3d_gb300.vtr import read_vtr
+
+    case = dataclasses.replace(cases.output_case(), output_format="appended")
+    ref_dir = os.path.join(GOLD, "outputs_tiny")
+    with tempfile.TemporaryDirectory() as wd:
+        r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed, write_outputs=True, workdir=wd)
+        r.initialize()
+        r.run()
+        r.write_outputs()
+        euler = r.orientations()
+        r.close()
+        ref_files = sorted(os.path.relpath(os.path.join(d, f), ref_dir) for d, _, fs in os.walk(ref_dir) for f in fs)
+        got_files = sorted(os.path.relpath(os.path.join(d, f), wd) for d, _, fs in os.walk(wd) for f in fs)
+        assert ref_files == got_files
+        nvtr = 0
+        for rel in ref_files:
+            a, b = os.path.join(ref_dir, rel), os.path.join(wd, rel)
+            if not rel.endswith(".vtr"):
+                assert filecmp.cmp(a, b, shallow=False), rel
+                continue
+            nvtr += 1
+            assert b"AppendedData" in open(b, "rb").read()
+            ra, rb = read_vtr(a), read_vtr(b)
+            assert list(ra) == list(rb), rel
+            assert rb["grain_id"].dtype == np.int64 and np.array_equal(ra["grain_id"], rb["grain_id"]), rel
+            ids = rb["grain_id"]
+            o = rb["grain_orientation"]
+            assert np.allclose(o, ra["grain_orientation"], rtol=5e-6, atol=1e-12), rel
+            assert np.array_equal(o[ids >= 0], euler[ids[ids >= 0]]) and (o[ids < 0] == 0).all(), rel
+            for ax, n, x0 in zip("XYZ", case.cells, case.origin):
+                c = rb[f"{ax}_Coordinates"]
+                assert np.allclose(c, ra[f"{ax}_Coordinates"], rtol=5e-6, atol=1e-12)
+                assert np.array_equal(c, x0 + np.arange(n + 1) * case.cell_size)
+        assert nvtr >= 3
+
+
 def test_gpu_deterministic_and_consistent(amca):
     case = [c for c in cases.small_cases() if c.name == "dense_20_s5"][0]
     a = run_gpu(amca, case)

@@ -152,6 +152,37 @@ def test_remelt_gpu_output_files_match_reference(amca, tmp_path):
     assert not bad, bad
 
 
+def test_remelt_gpu_appended_vtr_equals_ascii(amca, tmp_path):
+    """Binary VTR pieces of the coupled realm carry the values of its ASCII
+    pieces (which equal the reference's byte for byte): grain ids, melted
+    flags and the int-rounded temperatures exactly, Euler angles to the
+    text's six digits."""
+    import dataclasses
+
+    from amca3d_gb300.vtr import read_vtr
+
+    fx = remelt_cases.output_fixture()
+    got = {}
+    for fmt in ("ascii", "appended"):
+        wd = tmp_path / fmt
+        wd.mkdir()
+        fx2 = dataclasses.replace(fx, case=dataclasses.replace(fx.case, output_format=fmt))
+        M.prepare(fx2, str(wd))
+        r = amca.CellularAutomataRealm(fx2.case.to_yaml(), seed=fx.case.seed, workdir=str(wd), write_outputs=True)
+        r.initialize()
+        r.run()
+        r.close()
+        got[fmt] = {os.path.relpath(os.path.join(d, f), str(wd)): read_vtr(os.path.join(d, f))
+                    for d, _, fs in os.walk(str(wd)) for f in fs if f.endswith(".vtr")}
+    assert sorted(got["ascii"]) == sorted(got["appended"]) and len(got["ascii"]) >= 2
+    for rel, a in got["ascii"].items():
+        b = got["appended"][rel]
+        assert list(a) == list(b) and "cell_temperature" in b and "melted_flag" in b
+        for k in ("grain_id", "melted_flag", "cell_temperature"):
+            assert np.array_equal(a[k], b[k]), (rel, k)
+        assert np.allclose(a["grain_orientation"], b["grain_orientation"], rtol=5e-6, atol=1e-12), rel
+
+
 def test_cli_runs_the_deck_like_the_reference(amca, tmp_path):
     """amca3d -i Inputfile.i -o run.log in the deck's directory writes the
     reference's output files."""

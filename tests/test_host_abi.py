@@ -147,6 +147,43 @@ def test_missing_required_key_is_named(amca, key):
     assert e.value.code == -2 and key in str(e.value)
 
 
+def test_output_format_key(amca):
+    """output_format (a key of this library) accepts ascii / appended and
+    names itself on anything else; decks without it read as before."""
+    base = dataclasses.replace(cases.small_cases()[2], output_frequency=5)
+    for fmt in ("ascii", "appended"):
+        amca.CellularAutomataRealm(dataclasses.replace(base, output_format=fmt).to_yaml()).close()
+    with pytest.raises(amca.AmcaError) as e:
+        amca.CellularAutomataRealm(dataclasses.replace(base, output_format="hdf5").to_yaml())
+    assert e.value.code == -2 and "output_format" in str(e.value)
+
+
+def test_vtr_reader_on_reference_ascii_pieces(tmp_path):
+    """amca3d_gb300.vtr.read_vtr reads the reference's ASCII pieces and an
+    appended piece built here byte by byte."""
+    from amca3d_gb300.vtr import read_vtr
+
+    c = cases.output_case()
+    n = c.cells[0] * c.cells[1] * c.cells[2]
+    d = os.path.join(ROOT, "tests", "golden", "outputs_tiny", "Results", "grainsTimeStates", "timeStep_00007",
+                     "Grains00000.vtr")
+    a = read_vtr(d)
+    assert list(a) == ["grain_id", "grain_orientation", "X_Coordinates", "Y_Coordinates", "Z_Coordinates"]
+    assert a["grain_id"].shape == (n,) and a["grain_orientation"].shape == (n, 3)
+    assert np.allclose(a["X_Coordinates"], c.origin[0] + np.arange(c.cells[0] + 1) * c.cell_size, rtol=1e-5)
+    ids = np.array([3, -1, 7], np.int64)
+    xs = np.array([0.0, 0.5], np.float64)
+    head = ('<?xml version="1.0"?>\n<VTKFile type="RectilinearGrid" version="0.1" byte_order="LittleEndian" '
+            'header_type="UInt64">\n<CellData>\n<DataArray type="Int64" Name="grain_id" format="appended" '
+            'offset="0"/>\n</CellData>\n<Coordinates>\n<DataArray type="Float64" Name="X_Coordinates" '
+            'format="appended" offset="32"/>\n</Coordinates>\n<AppendedData encoding="raw">\n   _')
+    blob = np.uint64(24).tobytes() + ids.tobytes() + np.uint64(16).tobytes() + xs.tobytes()
+    p = tmp_path / "piece.vtr"
+    p.write_bytes(head.encode() + blob + b"\n</AppendedData>\n</VTKFile>\n")
+    b = read_vtr(str(p))
+    assert np.array_equal(b["grain_id"], ids) and np.array_equal(b["X_Coordinates"], xs)
+
+
 def test_problem_physics_type_checked(amca):
     deck = cases.small_cases()[2].to_yaml().replace("type: RappazGandin", "type: Other")
     with pytest.raises(amca.AmcaError):
