@@ -68,7 +68,8 @@ EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "am
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
            "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
-           "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_get_stats", "amca_batch_last_error",
+           "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_set_layout", "amca_batch_get_stats",
+           "amca_batch_last_error",
            "amca_batch_destroy", "amca_last_error", "amca_destroy")
 
 
@@ -89,11 +90,15 @@ class BatchStats(ctypes.Structure):
                 ("max_blocks", ctypes.c_int32), ("graph", ctypes.c_int32), ("n_tuned", ctypes.c_int32),
                 ("runs", ctypes.c_int64), ("last_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("cell_updates", ctypes.c_int64), ("tuned_team", ctypes.c_int32 * 8),
-                ("tuned_ms", ctypes.c_double * 8)]
+                ("tuned_ms", ctypes.c_double * 8), ("mixed_ms", ctypes.c_double), ("grid_blocks", ctypes.c_int32),
+                ("n_classes", ctypes.c_int32), ("class_team", ctypes.c_int32 * 8),
+                ("class_teams", ctypes.c_int32 * 8), ("class_realms", ctypes.c_int32 * 8)]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("tuned_")}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith(("tuned_", "class_"))}
         d["tuned"] = {int(self.tuned_team[i]): float(self.tuned_ms[i]) for i in range(self.n_tuned)}
+        d["classes"] = [{"team_size": int(self.class_team[i]), "teams": int(self.class_teams[i]),
+                         "realms": int(self.class_realms[i])} for i in range(self.n_classes)]
         return d
 
 
@@ -162,6 +167,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_batch_run.restype = i
     lib.amca_batch_tune.argtypes = [vp, i, ctypes.POINTER(ctypes.c_int)]
     lib.amca_batch_tune.restype = i
+    lib.amca_batch_set_layout.argtypes = [vp, i, vp, vp, vp]
+    lib.amca_batch_set_layout.restype = i
     lib.amca_batch_get_stats.argtypes = [vp, ctypes.POINTER(BatchStats)]
     lib.amca_batch_get_stats.restype = i
     lib.amca_batch_last_error.argtypes = [vp]
@@ -399,6 +406,18 @@ class Batch:
         ms = ctypes.c_double()
         self._check(self._lib.amca_batch_run(self._b, ctypes.byref(ms)))
         return ms.value
+
+    def set_layout(self, team_size, teams, realm_class) -> None:
+        """Class c = teams[c] teams of team_size[c] blocks; realm r runs in
+        class realm_class[r]."""
+        ts = np.ascontiguousarray(team_size, np.int32)
+        tn = np.ascontiguousarray(teams, np.int32)
+        rc = np.ascontiguousarray(realm_class, np.int32)
+        if len(ts) != len(tn) or len(rc) != len(self.realms):
+            raise ValueError("team_size and teams need one entry per class, realm_class one per realm")
+        self._check(self._lib.amca_batch_set_layout(self._b, len(ts), ts.ctypes.data_as(ctypes.c_void_p),
+                                                    tn.ctypes.data_as(ctypes.c_void_p),
+                                                    rc.ctypes.data_as(ctypes.c_void_p)))
 
     def tune(self, repeats: int = 1) -> int:
         t = ctypes.c_int()

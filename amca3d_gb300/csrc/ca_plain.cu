@@ -743,24 +743,29 @@ __global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *c
 
 // ---------------------------------------------------------------------------
 // Batched launch: many independent realms in one cooperative launch. The
-// grid is cut into teams of team_size consecutive blocks; the first block of
-// a team pulls the next queue position q and publishes order[q] in the team's
-// slot (by round parity); after a team barrier every block of the team runs
-// that realm with run_realm, the team standing in for the grid (its barriers
-// count team_size arrivals on the realm's own control words). A realm's
-// result does not depend on how many blocks run it, so the team size and the
-// queue order are free to tune.
+// grid is cut into teams of consecutive blocks (plan.blk gives each block
+// its team and rank, plan.tsize each team's size); teams of one class share
+// a queue over the class's slice of `order`. The first block of a team pulls
+// the next queue position and publishes the realm in the team's slot (by
+// round parity); after a team barrier every block of the team runs that
+// realm with run_realm, the team standing in for the grid (its barriers
+// count the team's arrivals on the realm's own control words). A realm's
+// result does not depend on how many blocks run it, so team sizes, classes
+// and queue order are free to tune.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock, kMinBlocks)
-    plain_batched_kernel(const PlainDevice *insts, const int *order, int ninst, int team_size, unsigned *queue,
+    plain_batched_kernel(const PlainDevice *insts, const int *order, int ninst, BatchPlanDev plan, unsigned *queues,
                          BatchTeam *teams, int *error, long long step_limit) {
   __shared__ unsigned long long smem[kWarps + 2];
   __shared__ PlainDevice sd;  // the descriptor of the realm this team runs
   __shared__ int s_idx;
-  const int team = blockIdx.x / team_size;
+  const int2 bt = plan.blk[blockIdx.x];
+  const int team = bt.x;
+  const int cls = plan.tclass[team];
+  const int2 range = plan.crange[cls];  // (first position in order, realms) of the class
   if (threadIdx.x == 0) {
-    t_nb = team_size;
-    t_b = blockIdx.x - team * team_size;
+    t_nb = plan.tsize[team];
+    t_b = bt.y;
   }
   __syncthreads();
   BatchTeam *tw = teams + team;
@@ -768,8 +773,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks)
     // the slot written here was last read in round - 2, before every block
     // of the team arrived at the barrier of round - 1
     if (t_b == 0 && threadIdx.x == 0) {
-      const unsigned q = atomicAdd(queue, 1u);
-      tw->slot[round & 1] = q < (unsigned)ninst ? order[q] : -1;
+      const unsigned q = atomicAdd(queues + cls, 1u);
+      tw->slot[round & 1] = q < (unsigned)range.y ? order[range.x + (int)q] : -1;
     }
     if (!team_barrier(&tw->count, &tw->gen, error)) break;
     if (threadIdx.x == 0) s_idx = ld_volatile(&tw->slot[round & 1]);
@@ -788,8 +793,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks)
 // Every realm of a batch back to its state right after initialize (site
 // flags, look-back words, control block, field), and the queue and team
 // words to zero. blockIdx.y is the realm.
-__global__ void batch_reset_kernel(const PlainDevice *insts, int ninst, unsigned *queue, BatchTeam *teams, int nteams,
-                                   int *error) {
+__global__ void batch_reset_kernel(const PlainDevice *insts, int ninst, unsigned *queues, int nclasses,
+                                   BatchTeam *teams, int nteams, int *error) {
   const int r = blockIdx.y;
   const PlainDevice &d = insts[r];
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -800,10 +805,8 @@ __global__ void batch_reset_kernel(const PlainDevice *insts, int ninst, unsigned
     *d.ctrl = c;
   }
   if (r == 0) {
-    if (tid == 0) {
-      *queue = 0u;
-      *error = 0;
-    }
+    if (tid == 0) *error = 0;
+    for (long long q = tid; q < nclasses; q += stride) queues[q] = 0u;
     for (long long t = tid; t < nteams; t += stride) teams[t] = BatchTeam{0u, 0u, {-1, -1}};
   }
   for (long long i = tid; i < d.nsites; i += stride) d.site_live[i] = 1;
@@ -1098,17 +1101,18 @@ int plain_batched_grid(int device) {
   return sms * per_sm;
 }
 
-cudaError_t plain_batch_reset(const PlainDevice *insts, int ninst, unsigned *queue, BatchTeam *teams, int nteams,
-                              int *error, cudaStream_t s) {
+cudaError_t plain_batch_reset(const PlainDevice *insts, int ninst, unsigned *queues, int nclasses, BatchTeam *teams,
+                              int nteams, int *error, cudaStream_t s) {
   if (ninst <= 0) return cudaSuccess;
-  batch_reset_kernel<<<dim3(64, ninst), 256, 0, s>>>(insts, ninst, queue, teams, nteams, error);
+  batch_reset_kernel<<<dim3(64, ninst), 256, 0, s>>>(insts, ninst, queues, nclasses, teams, nteams, error);
   return cudaGetLastError();
 }
 
-cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ninst, int team_size, int nteams,
-                              unsigned *queue, BatchTeam *teams, int *error, long long step_limit, cudaStream_t s) {
+cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ninst, const BatchPlanDev &plan,
+                              int grid_blocks, unsigned *queues, BatchTeam *teams, int *error, long long step_limit,
+                              cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(nteams * team_size);
+  cfg.gridDim = dim3(grid_blocks);
   cfg.blockDim = dim3(kBlock);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
@@ -1117,8 +1121,7 @@ cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ni
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, plain_batched_kernel, insts, order, ninst, team_size, queue, teams, error,
-                            step_limit);
+  return cudaLaunchKernelEx(&cfg, plain_batched_kernel, insts, order, ninst, plan, queues, teams, error, step_limit);
 }
 
 cudaError_t plain_batch_gather(const PlainDevice *insts, int ninst, PlainCtrl *out, cudaStream_t s) {

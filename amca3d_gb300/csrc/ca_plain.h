@@ -127,6 +127,16 @@ struct BatchTeam {
   int slot[2];
 };
 
+// Layout of a batched launch (device arrays): per block its team and rank
+// in the team; per team its size and class; per class the (first position,
+// count) of its realms in the launch's order array.
+struct BatchPlanDev {
+  const int2 *blk;
+  const int *tsize;
+  const int *tclass;
+  const int2 *crange;
+};
+
 // Fill the orientation field: -1 interior, 0 on the ghost layer
 // (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833),
 // and the solid bitmap to match.
@@ -146,18 +156,19 @@ cudaError_t plain_run_steps(const PlainDevice &d, long long step_limit, int grid
 int plain_batched_grid(int device);
 
 // Every realm of insts[0..ninst) (a device array) back to its state right
-// after initialize; the queue, the error word and the nteams team records
-// to zero.
-cudaError_t plain_batch_reset(const PlainDevice *insts, int ninst, unsigned *queue, BatchTeam *teams, int nteams,
-                              int *error, cudaStream_t s);
+// after initialize; the nclasses queues, the error word and the nteams team
+// records to zero.
+cudaError_t plain_batch_reset(const PlainDevice *insts, int ninst, unsigned *queues, int nclasses, BatchTeam *teams,
+                              int nteams, int *error, cudaStream_t s);
 
-// One cooperative launch of nteams * team_size blocks: each team of
-// team_size blocks takes realms order[0], order[1], ... from the queue and
-// runs each to solid, final_time or step_limit, as plain_run_steps would.
+// One cooperative launch of grid_blocks blocks laid out by `plan`: the teams
+// of each class take that class's realms, in order, from the class's queue
+// and run each to solid, final_time or step_limit, as plain_run_steps would.
 // A team barrier that ran out sets *error; a realm's own failures go to its
 // control block.
-cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ninst, int team_size, int nteams,
-                              unsigned *queue, BatchTeam *teams, int *error, long long step_limit, cudaStream_t s);
+cudaError_t plain_batched_run(const PlainDevice *insts, const int *order, int ninst, const BatchPlanDev &plan,
+                              int grid_blocks, unsigned *queues, BatchTeam *teams, int *error, long long step_limit,
+                              cudaStream_t s);
 
 // out[r] (device) = realm r's control block.
 cudaError_t plain_batch_gather(const PlainDevice *insts, int ninst, PlainCtrl *out, cudaStream_t s);

@@ -405,6 +405,18 @@ struct amca_t {
 
 // Many plain realms in one cooperative launch (amca_batch_*).
 struct amca_batch {
+  // One launch layout: teams (size, class) and, per class, its realms in
+  // queue order. A uniform layout has one class.
+  struct Plan {
+    std::vector<int> tsize, tclass;
+    std::vector<std::vector<int>> classes;
+    int blocks() const {
+      int n = 0;
+      for (int t : tsize) n += t;
+      return n;
+    }
+  };
+
   std::string err;
   std::vector<amca_t *> realms;
   int device = 0;
@@ -412,27 +424,31 @@ struct amca_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   PlainDevice *d_insts = nullptr;
   int *d_order = nullptr;
-  unsigned *d_queue = nullptr;
+  unsigned *d_queues = nullptr;
   BatchTeam *d_teams = nullptr;
   int *d_error = nullptr;
+  int2 *d_blk = nullptr, *d_crange = nullptr;
+  int *d_tsize = nullptr, *d_tclass = nullptr;
   PlainCtrl *d_ctrls = nullptr;
   PlainCtrl *h_ctrls = nullptr;  // pinned
   int *h_error = nullptr;        // pinned
-  int max_blocks = 0, team_size = 8, nteams = 0;
-  std::vector<int> order;
+  int max_blocks = 0;
+  Plan plan;
+  int grid = 0;
+  std::vector<int> order;  // realms by measured time, longest first
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = true;     // capture works on this device / driver
-  bool graph_stale = true;  // launch shape changed since the capture
+  bool graph_stale = true;  // launch layout changed since the capture
   int64_t runs = 0, cell_updates = 0;
-  double last_ms = 0.0, total_ms = 0.0;
+  double last_ms = 0.0, total_ms = 0.0, mixed_ms = 0.0;
   std::vector<std::pair<int, double>> tuned;
 
   ~amca_batch() {
     if (stream) cudaStreamSynchronize(stream);
     drop_graph();
-    for (void *p : {(void *)d_insts, (void *)d_order, (void *)d_queue, (void *)d_teams, (void *)d_error,
-                    (void *)d_ctrls})
+    for (void *p : {(void *)d_insts, (void *)d_order, (void *)d_queues, (void *)d_teams, (void *)d_error,
+                    (void *)d_blk, (void *)d_crange, (void *)d_tsize, (void *)d_tclass, (void *)d_ctrls})
       if (p) cudaFree(p);
     if (h_ctrls) cudaFreeHost(h_ctrls);
     if (h_error) cudaFreeHost(h_error);
@@ -462,37 +478,67 @@ struct amca_batch {
     for (int r = 0; r < nr; ++r) descs[r] = realms[r]->dev;
     CK(cudaMalloc(&d_insts, nr * sizeof(PlainDevice)));
     CK(cudaMalloc(&d_order, nr * sizeof(int)));
-    CK(cudaMalloc(&d_queue, sizeof(unsigned)));
+    CK(cudaMalloc(&d_queues, max_blocks * sizeof(unsigned)));
     CK(cudaMalloc(&d_teams, max_blocks * sizeof(BatchTeam)));
     CK(cudaMalloc(&d_error, sizeof(int)));
+    CK(cudaMalloc(&d_blk, max_blocks * sizeof(int2)));
+    CK(cudaMalloc(&d_crange, max_blocks * sizeof(int2)));
+    CK(cudaMalloc(&d_tsize, max_blocks * sizeof(int)));
+    CK(cudaMalloc(&d_tclass, max_blocks * sizeof(int)));
     CK(cudaMalloc(&d_ctrls, nr * sizeof(PlainCtrl)));
     CK(cudaMallocHost(&h_ctrls, nr * sizeof(PlainCtrl)));
     CK(cudaMallocHost(&h_error, sizeof(int)));
     CK(cudaMemcpyAsync(d_insts, descs.data(), nr * sizeof(PlainDevice), cudaMemcpyHostToDevice, stream));
     order.resize(nr);
     for (int r = 0; r < nr; ++r) order[r] = r;
-    upload_order();
     set_team(team > 0 ? team : 8);
   }
 
-  void upload_order() {
-    CK(cudaMemcpyAsync(d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
-  }
-
-  void set_team(int team) {
+  Plan uniform(int team) const {
     if (team < 1 || team > max_blocks)
       throw std::invalid_argument("team size must be between 1 and the co-resident blocks (" +
                                   std::to_string(max_blocks) + ")");
-    team_size = team;
-    nteams = std::min(max_blocks / team, n());
+    Plan p;
+    const int nt = std::min(max_blocks / team, n());
+    p.tsize.assign(nt, team);
+    p.tclass.assign(nt, 0);
+    p.classes.push_back(order);
+    return p;
+  }
+
+  void set_team(int team) { apply(uniform(team)); }
+
+  // Upload a layout; the next run captures a new graph.
+  void apply(const Plan &p) {
+    const int nt = (int)p.tsize.size(), nc = (int)p.classes.size();
+    if (nt < 1 || nc < 1 || p.blocks() > max_blocks) throw std::logic_error("batch layout does not fit");
+    std::vector<int2> blk;
+    for (int t = 0; t < nt; ++t)
+      for (int r = 0; r < p.tsize[t]; ++r) blk.push_back(make_int2(t, r));
+    std::vector<int> ord;
+    std::vector<int2> cr;
+    for (const auto &c : p.classes) {
+      cr.push_back(make_int2((int)ord.size(), (int)c.size()));
+      ord.insert(ord.end(), c.begin(), c.end());
+    }
+    if ((int)ord.size() != n()) throw std::logic_error("batch layout must list every realm once");
+    CK(cudaMemcpyAsync(d_blk, blk.data(), blk.size() * sizeof(int2), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_crange, cr.data(), cr.size() * sizeof(int2), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tsize, p.tsize.data(), nt * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tclass, p.tclass.data(), nt * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_order, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    plan = p;
+    grid = (int)blk.size();
     graph_stale = true;
   }
 
   void enqueue() {
     const int nr = n();
-    CK(plain_batch_reset(d_insts, nr, d_queue, d_teams, nteams, d_error, stream));
-    CK(plain_batched_run(d_insts, d_order, nr, team_size, nteams, d_queue, d_teams, d_error, 1ll << 60, stream));
+    const BatchPlanDev pd{d_blk, d_tsize, d_tclass, d_crange};
+    CK(plain_batch_reset(d_insts, nr, d_queues, (int)plan.classes.size(), d_teams, (int)plan.tsize.size(), d_error,
+                         stream));
+    CK(plain_batched_run(d_insts, d_order, nr, pd, grid, d_queues, d_teams, d_error, 1ll << 60, stream));
     CK(plain_batch_gather(d_insts, nr, d_ctrls, stream));
     CK(cudaMemcpyAsync(h_ctrls, d_ctrls, nr * sizeof(PlainCtrl), cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(h_error, d_error, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -554,32 +600,139 @@ struct amca_batch {
   }
 
   // Block 0 of a realm's team timed every phase of its run; their sum is the
-  // realm's time in the launch.
-  static double realm_ns(const PlainCtrl &c) {
-    return (double)(c.ns_nucleation + c.ns_claim + c.ns_resolve + c.ns_step_end);
+  // realm's time in the launch, ms.
+  static double realm_ms(const PlainCtrl &c) {
+    return 1e-6 * (double)(c.ns_nucleation + c.ns_claim + c.ns_resolve + c.ns_step_end);
   }
 
+  // Mixed layout from per-realm times t[s][r] measured at uniform team sizes
+  // sizes[s]: for a target makespan M each realm takes the team size with
+  // the least block time (size x time) among those that finish it within M;
+  // realms of one size share teams, counted by first-fit decreasing into
+  // bins of M. The smallest M whose teams fit is found by bisection; blocks
+  // left over then go, one team at a time, to the class with the largest
+  // time per team. Each class's queue runs longest realm first.
+  Plan mixed(const std::vector<int> &sizes, const std::vector<std::vector<double>> &t) const {
+    const int nr = n(), ns = (int)sizes.size();
+    auto choose = [&](double M, std::vector<int> &pick) {
+      for (int r = 0; r < nr; ++r) {
+        int best = -1;
+        for (int s = 0; s < ns; ++s)
+          if (t[s][r] <= M && (best < 0 || sizes[s] * t[s][r] < sizes[best] * t[best][r])) best = s;
+        if (best < 0) return false;
+        pick[r] = best;
+      }
+      return true;
+    };
+    auto teams_for = [&](double M, const std::vector<int> &pick, std::vector<int> &nteams) {
+      nteams.assign(ns, 0);
+      int blocks = 0;
+      for (int s = 0; s < ns; ++s) {
+        std::vector<double> items;
+        for (int r = 0; r < nr; ++r)
+          if (pick[r] == s) items.push_back(t[s][r]);
+        std::sort(items.rbegin(), items.rend());
+        std::vector<double> bins;
+        for (double x : items) {
+          bool placed = false;
+          for (double &b : bins)
+            if (b + x <= M) {
+              b += x;
+              placed = true;
+              break;
+            }
+          if (!placed) bins.push_back(x);
+        }
+        nteams[s] = (int)bins.size();
+        blocks += sizes[s] * nteams[s];
+      }
+      return blocks;
+    };
+    double lo = 0.0, hi = 0.0;
+    for (int r = 0; r < nr; ++r) {
+      double m = 1e300;
+      for (int s = 0; s < ns; ++s) m = std::min(m, t[s][r]);
+      lo = std::max(lo, m);
+      hi += t[0][r];
+    }
+    std::vector<int> pick((size_t)nr), nteams;
+    hi = std::max(hi, lo);
+    if (!choose(hi, pick) || teams_for(hi, pick, nteams) > max_blocks) return Plan();
+    for (int it = 0; it < 50; ++it) {
+      const double M = 0.5 * (lo + hi);
+      if (choose(M, pick) && teams_for(M, pick, nteams) <= max_blocks)
+        hi = M;
+      else
+        lo = M;
+    }
+    choose(hi, pick);
+    int blocks = teams_for(hi, pick, nteams);
+    std::vector<double> load((size_t)ns, 0.0);
+    for (int r = 0; r < nr; ++r) load[pick[r]] += t[pick[r]][r];
+    std::vector<int> members((size_t)ns, 0);
+    for (int r = 0; r < nr; ++r) members[pick[r]]++;
+    for (;;) {
+      int best = -1;
+      for (int s = 0; s < ns; ++s)
+        if (nteams[s] > 0 && nteams[s] < members[s] && blocks + sizes[s] <= max_blocks &&
+            (best < 0 || load[s] / nteams[s] > load[best] / nteams[best]))
+          best = s;
+      if (best < 0) break;
+      nteams[best]++;
+      blocks += sizes[best];
+    }
+    Plan p;
+    for (int s = ns - 1; s >= 0; --s) {
+      if (nteams[s] == 0) continue;
+      std::vector<int> rs;
+      for (int r = 0; r < nr; ++r)
+        if (pick[r] == s) rs.push_back(r);
+      std::stable_sort(rs.begin(), rs.end(), [&](int a, int b) { return t[s][a] > t[s][b]; });
+      const int cls = (int)p.classes.size();
+      p.classes.push_back(rs);
+      for (int k = 0; k < nteams[s]; ++k) {
+        p.tsize.push_back(sizes[s]);
+        p.tclass.push_back(cls);
+      }
+    }
+    return p;
+  }
+
+  // Returns the uniform team size kept, or 0 when the mixed layout won.
   int tune(int repeats) {
     repeats = std::max(repeats, 1);
+    set_team(plan.tsize.empty() ? 8 : plan.tsize[0]);
     run();
-    std::vector<double> t((size_t)n());
-    for (int r = 0; r < n(); ++r) t[r] = realm_ns(h_ctrls[r]);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return t[a] > t[b]; });
-    upload_order();
+    std::vector<double> t0((size_t)n());
+    for (int r = 0; r < n(); ++r) t0[r] = realm_ms(h_ctrls[r]);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return t0[a] > t0[b]; });
     tuned.clear();
-    int best = team_size;
-    double best_ms = 1e300;
+    mixed_ms = 0.0;
     std::vector<int> sizes;
-    for (int s = 1; s <= 64 && s <= max_blocks; s *= 2) sizes.push_back(s);
-    for (int s : sizes) {
-      set_team(s);
+    for (int s = 1; s <= 128 && s <= max_blocks; s *= 2) sizes.push_back(s);
+    std::vector<std::vector<double>> t(sizes.size(), std::vector<double>((size_t)n(), 1e300));
+    int best = 8;
+    double best_ms = 1e300;
+    for (size_t k = 0; k < sizes.size(); ++k) {
+      set_team(sizes[k]);
       double m = 1e300;
-      for (int k = 0; k < repeats; ++k) m = std::min(m, run());
-      tuned.emplace_back(s, m);
+      for (int q = 0; q < repeats; ++q) {
+        m = std::min(m, run());
+        for (int r = 0; r < n(); ++r) t[k][r] = std::min(t[k][r], realm_ms(h_ctrls[r]));
+      }
+      if (tuned.size() < 8) tuned.emplace_back(sizes[k], m);
       if (m < best_ms) {
         best_ms = m;
-        best = s;
+        best = sizes[k];
       }
+    }
+    Plan mp = mixed(sizes, t);
+    if (!mp.tsize.empty()) {
+      apply(mp);
+      double m = 1e300;
+      for (int q = 0; q < repeats; ++q) m = std::min(m, run());
+      mixed_ms = m;
+      if (m < best_ms) return 0;
     }
     set_team(best);
     return best;
@@ -986,13 +1139,55 @@ int amca_batch_tune(amca_batch *b, int repeats, int *team_size_out) {
   });
 }
 
+int amca_batch_set_layout(amca_batch *b, int nclasses, const int32_t *team_size, const int32_t *teams,
+                          const int32_t *realm_class) {
+  if (!b) return AMCA_ERR_ARG;
+  return guarded(b, [&] {
+    if (nclasses < 1 || nclasses > b->max_blocks || !team_size || !teams || !realm_class)
+      throw std::invalid_argument("amca_batch_set_layout: need 1 or more classes and three arrays");
+    amca_batch::Plan p;
+    p.classes.resize(nclasses);
+    long long blocks = 0;
+    for (int c = 0; c < nclasses; ++c) {
+      if (team_size[c] < 1 || teams[c] < 1)
+        throw std::invalid_argument("amca_batch_set_layout: every class needs at least one team of one block");
+      blocks += (long long)team_size[c] * teams[c];
+      if (blocks > b->max_blocks)
+        throw std::invalid_argument("amca_batch_set_layout: the teams need more blocks than fit on the device (" +
+                                    std::to_string(b->max_blocks) + ")");
+      for (int k = 0; k < teams[c]; ++k) {
+        p.tsize.push_back(team_size[c]);
+        p.tclass.push_back(c);
+      }
+    }
+    for (int r : b->order) {
+      const int c = realm_class[r];
+      if (c < 0 || c >= nclasses) throw std::invalid_argument("amca_batch_set_layout: realm class out of range");
+      p.classes[c].push_back(r);
+    }
+    b->apply(p);
+  });
+}
+
 int amca_batch_get_stats(const amca_batch *b, amca_batch_stats *s) {
   if (!b || !s) return AMCA_ERR_ARG;
   memset(s, 0, sizeof *s);
   s->realms = b->n();
-  s->team_size = b->team_size;
-  s->teams = b->nteams;
+  const amca_batch::Plan &p = b->plan;
+  s->teams = (int32_t)p.tsize.size();
+  s->team_size = p.classes.size() == 1 && !p.tsize.empty() ? p.tsize[0] : 0;
+  s->grid_blocks = b->grid;
   s->max_blocks = b->max_blocks;
+  s->n_classes = (int32_t)std::min<size_t>(p.classes.size(), 8);
+  for (int c = 0; c < s->n_classes; ++c) {
+    s->class_realms[c] = (int32_t)p.classes[c].size();
+    for (size_t t = 0; t < p.tsize.size(); ++t)
+      if (p.tclass[t] == c) {
+        s->class_team[c] = p.tsize[t];
+        s->class_teams[c]++;
+      }
+  }
+  s->mixed_ms = b->mixed_ms;
   s->graph = b->graph_ok ? 1 : 0;
   s->runs = b->runs;
   s->last_ms = b->last_ms;

@@ -305,15 +305,28 @@ int amca_batch_create(amca_t *const *realms, int n, int team_size, amca_batch **
  * ran out. */
 int amca_batch_run(amca_batch *b, double *device_ms);
 
-/* Autotuning: runs the batch once to measure each realm, orders the queue
- * longest realm first, then times team sizes 1, 2, 4, ... (up to 64, and
- * the largest that fits) `repeats` times each (at least 1) and keeps the
- * fastest. *team_size_out (may be NULL) = the size kept. */
+/* Autotuning: runs the batch once to measure each realm and orders the
+ * queue longest realm first; times every realm at uniform team sizes 1, 2,
+ * 4, ... (up to 128 and the largest that fits), `repeats` times each (at
+ * least 1); then builds a mixed layout from those per-realm times (each
+ * realm on the team size that spends the fewest block-milliseconds while
+ * finishing within the smallest makespan whose teams fit; teams of one size
+ * share a queue, longest realm first) and times it too. The fastest layout
+ * is kept. *team_size_out (may be NULL) = the uniform size kept, or 0 when
+ * the mixed layout was kept. */
 int amca_batch_tune(amca_batch *b, int repeats, int *team_size_out);
+
+/* Set the launch layout by hand: nclasses classes, class c made of
+ * teams[c] teams of team_size[c] blocks; realm r is run by a team of class
+ * realm_class[r]. Within a class realms are taken longest first once
+ * amca_batch_tune has measured them, else in handle order. The blocks of
+ * all teams must fit on the device (amca_batch_stats.max_blocks). */
+int amca_batch_set_layout(amca_batch *b, int nclasses, const int32_t *team_size, const int32_t *teams,
+                          const int32_t *realm_class);
 
 typedef struct {
   int32_t realms;
-  int32_t team_size;     /* blocks per realm */
+  int32_t team_size;     /* blocks per realm of a uniform layout; 0 for a mixed layout */
   int32_t teams;         /* teams in the launch */
   int32_t max_blocks;    /* co-resident blocks of the batched kernel on this device */
   int32_t graph;         /* 1: runs replay a CUDA graph; 0: plain launches (capture unavailable) */
@@ -323,7 +336,13 @@ typedef struct {
   double total_ms;
   int64_t cell_updates;  /* sum over realms of interior cells x CA steps, last run */
   int32_t tuned_team[8];
-  double tuned_ms[8];    /* best time of each team size tried */
+  double tuned_ms[8];    /* best time of each uniform team size tried */
+  double mixed_ms;       /* best time of the mixed layout tried (0: none) */
+  int32_t grid_blocks;   /* blocks of the launch */
+  int32_t n_classes;     /* team classes of the layout (at most 8 reported) */
+  int32_t class_team[8];    /* team size of each class */
+  int32_t class_teams[8];   /* teams of each class */
+  int32_t class_realms[8];  /* realms of each class */
 } amca_batch_stats;
 
 int amca_batch_get_stats(const amca_batch *b, amca_batch_stats *out);

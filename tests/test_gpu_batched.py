@@ -97,12 +97,27 @@ def test_batch_reads_like_single_runs(amca, small_batch):
         assert np.array_equal(s, r.field("site_undercooling"))
 
 
+@pytest.mark.parametrize("layout", [((1, 4, 16), (5, 3, 2)), ((2, 64), (4, 1)), ((3,), (1,))])
+def test_batch_mixed_layouts_match_reference(amca, small_batch, layout):
+    """Teams of several sizes in one launch (realm r in class r mod k), and a
+    single team that runs every realm in turn."""
+    decks_, realms = small_batch
+    sizes, teams = layout
+    with amca.Batch(realms) as b:
+        b.set_layout(sizes, teams, [r % len(sizes) for r in range(len(realms))])
+        st = b.stats()
+        assert st["grid_blocks"] == sum(s * t for s, t in zip(sizes, teams)) and st["n_classes"] == len(sizes)
+        b.run()
+        assert check_golden(realms, decks_, GOLDEN) == []
+
+
 def test_batch_autotune_keeps_results(amca, small_batch):
     decks_, realms = small_batch
     with amca.Batch(realms) as b:
         t = b.tune(repeats=1)
         st = b.stats()
-        assert t == st["team_size"] and t in st["tuned"] and len(st["tuned"]) >= 5
+        assert t == st["team_size"] and len(st["tuned"]) >= 5 and (t == 0 or t in st["tuned"])
+        assert st["mixed_ms"] > 0 or t != 0
         assert st["graph"] == 1, "the batched run is not replayed as a CUDA graph"
         b.run()
         assert check_golden(realms, decks_, GOLDEN) == []
@@ -114,6 +129,11 @@ def test_batch_rejects_bad_handles(amca, small_batch):
         amca.Batch([realms[0], realms[1], realms[0]])
     with pytest.raises(amca.AmcaError, match="team size"):
         amca.Batch(realms[:2], team_size=100000)
+    with amca.Batch(realms[:2]) as b:
+        with pytest.raises(amca.AmcaError, match="more blocks"):
+            b.set_layout([64], [100], [0, 0])
+        with pytest.raises(amca.AmcaError, match="out of range"):
+            b.set_layout([4], [2], [0, 1])
 
 
 def test_batched_64_full_size_matches_reference(amca):
@@ -128,6 +148,11 @@ def test_batched_64_full_size_matches_reference(amca):
     try:
         with amca.Batch(realms) as b:
             b.tune(repeats=1)
+            b.run()
+            assert check_golden(realms, decks_, golden) == []
+            # a mixed layout: the 8 largest realms on teams of 32, the rest on 2
+            big = set(np.argsort([-c.n_interior for c in decks_])[:8])
+            b.set_layout([32, 2], [8, 100], [0 if r in big else 1 for r in range(len(decks_))])
             b.run()
             assert check_golden(realms, decks_, golden) == []
     finally:
