@@ -68,7 +68,8 @@ EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "am
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
            "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
-           "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_set_layout", "amca_batch_get_stats",
+           "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_set_layout", "amca_batch_get_layout",
+           "amca_batch_get_stats",
            "amca_batch_last_error",
            "amca_batch_destroy", "amca_last_error", "amca_destroy")
 
@@ -167,8 +168,10 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_batch_run.restype = i
     lib.amca_batch_tune.argtypes = [vp, i, ctypes.POINTER(ctypes.c_int)]
     lib.amca_batch_tune.restype = i
-    lib.amca_batch_set_layout.argtypes = [vp, i, vp, vp, vp]
+    lib.amca_batch_set_layout.argtypes = [vp, i, vp, vp, vp, vp]
     lib.amca_batch_set_layout.restype = i
+    lib.amca_batch_get_layout.argtypes = [vp, i, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_int)]
+    lib.amca_batch_get_layout.restype = i
     lib.amca_batch_get_stats.argtypes = [vp, ctypes.POINTER(BatchStats)]
     lib.amca_batch_get_stats.restype = i
     lib.amca_batch_last_error.argtypes = [vp]
@@ -407,17 +410,35 @@ class Batch:
         self._check(self._lib.amca_batch_run(self._b, ctypes.byref(ms)))
         return ms.value
 
-    def set_layout(self, team_size, teams, realm_class) -> None:
+    def set_layout(self, team_size, teams, realm_class, queue_order=None) -> None:
         """Class c = teams[c] teams of team_size[c] blocks; realm r runs in
-        class realm_class[r]."""
+        class realm_class[r]; queue_order (optional) orders each class's
+        queue."""
+        vp = ctypes.c_void_p
         ts = np.ascontiguousarray(team_size, np.int32)
         tn = np.ascontiguousarray(teams, np.int32)
         rc = np.ascontiguousarray(realm_class, np.int32)
         if len(ts) != len(tn) or len(rc) != len(self.realms):
             raise ValueError("team_size and teams need one entry per class, realm_class one per realm")
-        self._check(self._lib.amca_batch_set_layout(self._b, len(ts), ts.ctypes.data_as(ctypes.c_void_p),
-                                                    tn.ctypes.data_as(ctypes.c_void_p),
-                                                    rc.ctypes.data_as(ctypes.c_void_p)))
+        qo = None if queue_order is None else np.ascontiguousarray(queue_order, np.int32)
+        if qo is not None and len(qo) != len(self.realms):
+            raise ValueError("queue_order needs one entry per realm")
+        self._check(self._lib.amca_batch_set_layout(self._b, len(ts), ts.ctypes.data_as(vp), tn.ctypes.data_as(vp),
+                                                    rc.ctypes.data_as(vp),
+                                                    None if qo is None else qo.ctypes.data_as(vp)))
+
+    def layout(self):
+        """(team_size, teams, realm_class, queue_order) of the current layout."""
+        vp = ctypes.c_void_p
+        nc = ctypes.c_int()
+        self._check(self._lib.amca_batch_get_layout(self._b, 0, None, None, None, None, ctypes.byref(nc)))
+        ts = np.zeros(nc.value, np.int32)
+        tn = np.zeros(nc.value, np.int32)
+        rc = np.zeros(len(self.realms), np.int32)
+        qo = np.zeros(len(self.realms), np.int32)
+        self._check(self._lib.amca_batch_get_layout(self._b, nc.value, ts.ctypes.data_as(vp), tn.ctypes.data_as(vp),
+                                                    rc.ctypes.data_as(vp), qo.ctypes.data_as(vp), ctypes.byref(nc)))
+        return ts, tn, rc, qo
 
     def tune(self, repeats: int = 1) -> int:
         t = ctypes.c_int()

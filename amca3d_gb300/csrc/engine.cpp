@@ -726,13 +726,36 @@ struct amca_batch {
         best = sizes[k];
       }
     }
-    Plan mp = mixed(sizes, t);
-    if (!mp.tsize.empty()) {
+    // Mixed layouts, refined: a realm's time on a small team measured with
+    // few busy blocks per SM is optimistic once every SM is full, so each
+    // round replaces the estimates of the sizes it used by the times the
+    // realms took inside that layout and plans again.
+    Plan best_mixed;
+    for (int round = 0; round < 4; ++round) {
+      Plan mp = mixed(sizes, t);
+      if (mp.tsize.empty()) break;
       apply(mp);
       double m = 1e300;
-      for (int q = 0; q < repeats; ++q) m = std::min(m, run());
-      mixed_ms = m;
-      if (m < best_ms) return 0;
+      std::vector<double> took((size_t)n(), 1e300);
+      for (int q = 0; q < repeats; ++q) {
+        m = std::min(m, run());
+        for (int r = 0; r < n(); ++r) took[r] = std::min(took[r], realm_ms(h_ctrls[r]));
+      }
+      if (mixed_ms == 0.0 || m < mixed_ms) {
+        mixed_ms = m;
+        best_mixed = mp;
+      }
+      for (size_t c = 0; c < mp.classes.size(); ++c) {
+        int size = 0;
+        for (size_t k = 0; k < mp.tsize.size(); ++k)
+          if (mp.tclass[k] == (int)c) size = mp.tsize[k];
+        const size_t si = std::find(sizes.begin(), sizes.end(), size) - sizes.begin();
+        for (int r : mp.classes[c]) t[si][r] = took[r];
+      }
+    }
+    if (mixed_ms > 0.0 && mixed_ms < best_ms) {
+      apply(best_mixed);
+      return 0;
     }
     set_team(best);
     return best;
@@ -1140,7 +1163,7 @@ int amca_batch_tune(amca_batch *b, int repeats, int *team_size_out) {
 }
 
 int amca_batch_set_layout(amca_batch *b, int nclasses, const int32_t *team_size, const int32_t *teams,
-                          const int32_t *realm_class) {
+                          const int32_t *realm_class, const int32_t *queue_order) {
   if (!b) return AMCA_ERR_ARG;
   return guarded(b, [&] {
     if (nclasses < 1 || nclasses > b->max_blocks || !team_size || !teams || !realm_class)
@@ -1160,13 +1183,50 @@ int amca_batch_set_layout(amca_batch *b, int nclasses, const int32_t *team_size,
         p.tclass.push_back(c);
       }
     }
-    for (int r : b->order) {
+    std::vector<int> q = b->order;
+    if (queue_order) {
+      q.assign(queue_order, queue_order + b->n());
+      std::vector<char> seen((size_t)b->n(), 0);
+      for (int r : q) {
+        if (r < 0 || r >= b->n() || seen[r])
+          throw std::invalid_argument("amca_batch_set_layout: queue_order is not a permutation of the realms");
+        seen[r] = 1;
+      }
+    }
+    for (int r : q) {
       const int c = realm_class[r];
       if (c < 0 || c >= nclasses) throw std::invalid_argument("amca_batch_set_layout: realm class out of range");
       p.classes[c].push_back(r);
     }
     b->apply(p);
+    if (queue_order) b->order = q;
   });
+}
+
+int amca_batch_get_layout(const amca_batch *b, int cap, int32_t *team_size, int32_t *teams, int32_t *realm_class,
+                          int32_t *queue_order, int *nclasses) {
+  if (!b) return AMCA_ERR_ARG;
+  const amca_batch::Plan &p = b->plan;
+  const int nc = (int)p.classes.size();
+  if (nclasses) *nclasses = nc;
+  for (int c = 0; c < nc && c < cap; ++c) {
+    int size = 0, count = 0;
+    for (size_t t = 0; t < p.tsize.size(); ++t)
+      if (p.tclass[t] == c) {
+        size = p.tsize[t];
+        ++count;
+      }
+    if (team_size) team_size[c] = size;
+    if (teams) teams[c] = count;
+  }
+  int k = 0;
+  for (int c = 0; c < nc; ++c)
+    for (int r : p.classes[c]) {
+      if (realm_class) realm_class[r] = c;
+      if (queue_order) queue_order[k] = r;
+      ++k;
+    }
+  return AMCA_OK;
 }
 
 int amca_batch_get_stats(const amca_batch *b, amca_batch_stats *s) {

@@ -611,7 +611,8 @@ def run_ours_batched(args, dist: Dist):
         r.initialize()
         realms.append(r)
     batch = A.Batch(realms)
-    team = batch.tune(repeats=2)
+    batch.tune(repeats=2)
+    layout = batch.layout()
     for _ in range(args.warmup):
         batch.run()
     clocks = ClockSampler(dev)
@@ -659,7 +660,8 @@ def run_ours_batched(args, dist: Dist):
             r = A.CellularAutomataRealm(c.to_yaml(), seed=c.seed, device=dev)
             r.initialize()
             rs.append(r)
-        with A.Batch(rs, team_size=team) as b:
+        with A.Batch(rs) as b:
+            b.set_layout(*layout)
             b.run()
             upd = b.stats()["cell_updates"]
         for r, p in zip(rs, pinned):
@@ -697,6 +699,8 @@ def run_ours_batched(args, dist: Dist):
                    "cell_updates_per_run": bs["cell_updates"], **gstats,
                    "team_size": bs["team_size"], "teams": bs["teams"], "max_blocks": bs["max_blocks"],
                    "cuda_graph": bool(bs["graph"]), "autotune_ms_by_team": bs["tuned"],
+                   "autotune_mixed_ms": bs["mixed_ms"], "layout_classes": bs["classes"],
+                   "grid_blocks": bs["grid_blocks"],
                    "sequential_plain_ms": seq, "sequential_plain_cell_updates_per_s": bs["cell_updates"] / (seq / 1e3),
                    "speedup_vs_sequential_plain": seq / ms, "sequential_fields_match": seq_same,
                    "e2e_fields_match": same, "parallelism": f"replicas x{args.gpus}",

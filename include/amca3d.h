@@ -318,11 +318,20 @@ int amca_batch_tune(amca_batch *b, int repeats, int *team_size_out);
 
 /* Set the launch layout by hand: nclasses classes, class c made of
  * teams[c] teams of team_size[c] blocks; realm r is run by a team of class
- * realm_class[r]. Within a class realms are taken longest first once
- * amca_batch_tune has measured them, else in handle order. The blocks of
- * all teams must fit on the device (amca_batch_stats.max_blocks). */
+ * realm_class[r]. Within a class realms are queued in the order they appear
+ * in queue_order (a permutation of the realm indices), or, when it is NULL,
+ * longest first once amca_batch_tune has measured them, else in handle
+ * order. The blocks of all teams must fit on the device
+ * (amca_batch_stats.max_blocks). */
 int amca_batch_set_layout(amca_batch *b, int nclasses, const int32_t *team_size, const int32_t *teams,
-                          const int32_t *realm_class);
+                          const int32_t *realm_class, const int32_t *queue_order);
+
+/* The current layout, in amca_batch_set_layout's terms: *nclasses classes
+ * (team_size and teams filled for the first `cap` of them), realm_class and
+ * queue_order (one entry per realm each; any array may be NULL). Setting it
+ * on another batch of the same decks reproduces the launch. */
+int amca_batch_get_layout(const amca_batch *b, int cap, int32_t *team_size, int32_t *teams, int32_t *realm_class,
+                          int32_t *queue_order, int *nclasses);
 
 typedef struct {
   int32_t realms;

@@ -121,6 +121,14 @@ def test_batch_autotune_keeps_results(amca, small_batch):
         assert st["graph"] == 1, "the batched run is not replayed as a CUDA graph"
         b.run()
         assert check_golden(realms, decks_, GOLDEN) == []
+        ts, tn, rc, qo = b.layout()
+        assert sorted(qo) == list(range(len(realms))) and int((ts * tn).sum()) == b.stats()["grid_blocks"]
+    # the tuned layout set on another batch of the same realms
+    with amca.Batch(realms) as b2:
+        b2.set_layout(ts, tn, rc, qo)
+        assert [list(x) for x in b2.layout()] == [list(x) for x in (ts, tn, rc, qo)]
+        b2.run()
+        assert check_golden(realms, decks_, GOLDEN) == []
 
 
 def test_batch_rejects_bad_handles(amca, small_batch):
@@ -134,6 +142,8 @@ def test_batch_rejects_bad_handles(amca, small_batch):
             b.set_layout([64], [100], [0, 0])
         with pytest.raises(amca.AmcaError, match="out of range"):
             b.set_layout([4], [2], [0, 1])
+        with pytest.raises(amca.AmcaError, match="permutation"):
+            b.set_layout([4], [2], [0, 0], [1, 1])
 
 
 def test_batched_64_full_size_matches_reference(amca):
