@@ -475,60 +475,46 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
 // ---------------------------------------------------------------------------
 // Resolve: captures, deactivation, child records, survivor compaction.
 // ---------------------------------------------------------------------------
-// Marking pass: per rank, the captured neighbours (final claim is its own)
-// and whether it stays active; written over the containment mask as
-// captures | survives << 31. Ranks are independent, so blocks take
-// dynamic batches as in the claim phase.
-__device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
+// Mark of one rank: the captured neighbours (final claim is its own) and
+// whether it stays active, as captures | survives << 31.
+__device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r, unsigned par, const EnvRec *cur) {
   const Grid &g = d.grid;
-  __shared__ long long s_batch;
-  long long batch = (n + 2ll * t_nb - 1) / (2ll * t_nb);
-  batch = (batch + 31) & ~31ll;
-  if (batch > kClaimBatch) batch = kClaimBatch;
-  if (batch < 32) batch = 32;
-  for (;;) {
-    if (threadIdx.x == 0) s_batch = (long long)atomicAdd(&d.ctrl->mark_next, (unsigned long long)batch);
-    __syncthreads();
-    const long long b = s_batch;
-    __syncthreads();
-    if (b >= n) break;
-    const long long e = b + batch < n ? b + batch : n;
-    for (long long r = b + threadIdx.x; r < e; r += kBlock) {
-      const uint32_t lm = d.liq[r], cm = d.con[r];
-      uint32_t cap = 0, surv = 0;
-      if (lm) {
-        const int cell = cur[r].cell;
-        const uint32_t mine = claim_word(par, (uint32_t)r);
-        // a liquid neighbour this envelope does not contain and nobody
-        // claimed keeps it active without a look at the cell field
-        const uint32_t other = lm & ~cm;
-        const uint32_t clm = neighbour_bits(d.claimed, g, cell);
-        surv = (other & ~clm) ? 1u : 0u;
-        // claim words are read for contained cells, and for claimed ones
-        // while survival is still open
-        const uint32_t need = cm | (surv ? 0u : (other & clm));
+  const uint32_t lm = d.liq[r], cm = d.con[r];
+  uint32_t cap = 0, surv = 0;
+  if (lm) {
+    const int cell = cur[r].cell;
+    const uint32_t mine = claim_word(par, (uint32_t)r);
+    // a liquid neighbour this envelope does not contain and nobody claimed
+    // keeps it active without a look at the cell field
+    const uint32_t other = lm & ~cm;
+    const uint32_t clm = neighbour_bits(d.claimed, g, cell);
+    surv = (other & ~clm) ? 1u : 0u;
+    // claim words are read for contained cells, and for claimed ones while
+    // survival is still open
+    const uint32_t need = cm | (surv ? 0u : (other & clm));
 #pragma unroll
-        for (int nb = 0; nb < 26; ++nb) {
-          if (!((need >> nb) & 1u)) continue;
-          int di, dj, dk;
-          const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
-          if ((cm >> nb) & 1u) {
-            cap |= (s == mine ? 1u : 0u) << nb;
-          } else if (s == kLiquid || (s & kRankMask) > (uint32_t)r) {
-            surv = 1;
-          }
-        }
+    for (int nb = 0; nb < 26; ++nb) {
+      if (!((need >> nb) & 1u)) continue;
+      int di, dj, dk;
+      const uint32_t s = d.orient[cell + nbr_delta(g, nb, di, dj, dk)];
+      if ((cm >> nb) & 1u) {
+        cap |= (s == mine ? 1u : 0u) << nb;
+      } else if (s == kLiquid || (s & kRankMask) > (uint32_t)r) {
+        surv = 1;
       }
-      d.con[r] = cap | (surv << 31);
     }
   }
+  return cap | (surv << 31);
 }
 
-// Scan pass: one look-back per block over its contiguous chunk of marks gives
-// new envelope ids (walk order), child records and the survivors' places in
-// the next active list.
-__device__ bool resolve_phase(const PlainDevice &d, long long n, long long step, const EnvRec *cur, EnvRec *next_act,
-                              unsigned long long *smem) {
+// Each block marks its contiguous chunk of ranks (the claim words are final
+// after the claim phase's barrier), then one look-back per block over the
+// chunk's marks gives new envelope ids (walk order), child records and the
+// survivors' places in the next active list. Marking reads only claim words,
+// the claimed bitmap and its own ranks' masks, none of which another block's
+// resolve writes, so no barrier separates the two passes.
+__device__ bool resolve_phase(const PlainDevice &d, long long n, long long step, unsigned par, const EnvRec *cur,
+                              EnvRec *next_act, unsigned long long *smem) {
   PlainCtrl *c = d.ctrl;
   long long *n_next = &c->n_active_next[step & 1];
   const long long base_grain = ld_volatile(&c->next_grain);
@@ -538,7 +524,8 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   block_chunk(n, b, e);
   unsigned long long acc = 0;
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
-    const uint32_t word = d.con[r];
+    const uint32_t word = mark_rank(d, r, par, cur);
+    d.con[r] = word;  // read back below by the same thread
     acc += ((unsigned long long)__popc(word & 0x03ffffffu) << 32) | (word >> 31);
   }
   unsigned long long agg;
@@ -639,8 +626,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         c->claim_next = 0ull;  // the next claim phase is two barriers away
       }
       t_work = threadIdx.x == 0 ? now_ns() : 0ull;
-      mark_phase(d, n, gen & 1u, list);
-      __syncthreads();
+      if (!(ok = resolve_phase(d, n, step, gen & 1u, list, next_act, smem))) break;
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
         atomicAdd(&c->ns_resolve_work_sum, w);
@@ -648,16 +634,11 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
-        c->mark_next = 0ull;  // the next marking pass is two barriers away
-        c->ns_resolve_work_max += c->phase_max_scratch[1];
-        c->phase_max_scratch[1] = 0ull;
-      }
-      if (!(ok = resolve_phase(d, n, step, list, next_act, smem))) break;
-      if (!(ok = grid_barrier(c))) break;
-      if (timer) {
         t_now = now_ns();
         c->ns_resolve += t_now - t_mark;
         t_mark = t_now;
+        c->ns_resolve_work_max += c->phase_max_scratch[1];
+        c->phase_max_scratch[1] = 0ull;
       }
       n = ld_volatile(&c->gen_n);
       lo = ld_volatile(&c->gen_lo);

@@ -74,7 +74,6 @@ struct PlainCtrl {
   unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
   unsigned long long phase_max_scratch[2];             // running max of the current phase
   unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase
-  unsigned long long mark_next;                        // next rank batch of the resolve marking pass
 };
 
 enum { kErrBarrier = 1, kErrLookback = 2 };
