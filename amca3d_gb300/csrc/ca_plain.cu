@@ -507,6 +507,31 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
   return cap | (surv << 31);
 }
 
+// Marking pass for large generations: blocks take dynamic batches of ranks,
+// as in the claim phase, and write each rank's mark over its containment
+// mask; a grid barrier then opens the scan.
+__device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
+  __shared__ long long s_batch;
+  long long batch = (n + 2ll * t_nb - 1) / (2ll * t_nb);
+  batch = (batch + 31) & ~31ll;
+  if (batch > kClaimBatch) batch = kClaimBatch;
+  if (batch < 32) batch = 32;
+  for (;;) {
+    if (threadIdx.x == 0) s_batch = (long long)atomicAdd(&d.ctrl->mark_next, (unsigned long long)batch);
+    __syncthreads();
+    const long long b = s_batch;
+    __syncthreads();
+    if (b >= n) break;
+    const long long e = b + batch < n ? b + batch : n;
+    for (long long r = b + threadIdx.x; r < e; r += kBlock) d.con[r] = mark_rank(d, r, par, cur);
+  }
+}
+
+// Whether a generation of n ranks is marked inside the resolve pass (at most
+// one rank per thread of the team: the barrier a separate pass needs would
+// cost more than the imbalance of static chunks).
+__device__ __forceinline__ bool mark_in_resolve(long long n) { return n <= (long long)kBlock * t_nb; }
+
 // Each block marks its contiguous chunk of ranks (the claim words are final
 // after the claim phase's barrier), then one look-back per block over the
 // chunk's marks gives new envelope ids (walk order), child records and the
@@ -523,9 +548,15 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   long long b, e;
   block_chunk(n, b, e);
   unsigned long long acc = 0;
+  const bool marking = mark_in_resolve(n);
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
-    const uint32_t word = mark_rank(d, r, par, cur);
-    d.con[r] = word;  // read back below by the same thread
+    uint32_t word;
+    if (marking) {
+      word = mark_rank(d, r, par, cur);
+      d.con[r] = word;  // read back below by the same thread
+    } else {
+      word = d.con[r];  // marked by mark_phase before the last barrier
+    }
     acc += ((unsigned long long)__popc(word & 0x03ffffffu) << 32) | (word >> 31);
   }
   unsigned long long agg;
@@ -626,9 +657,18 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         c->claim_next = 0ull;  // the next claim phase is two barriers away
       }
       t_work = threadIdx.x == 0 ? now_ns() : 0ull;
+      unsigned long long w_mark = 0;  // busy time of a separate marking pass (thread 0)
+      if (!mark_in_resolve(n)) {
+        mark_phase(d, n, gen & 1u, list);
+        __syncthreads();
+        if (threadIdx.x == 0) w_mark = now_ns() - t_work;
+        if (!(ok = grid_barrier(c))) break;
+        if (timer) c->mark_next = 0ull;  // the next marking pass is two barriers away
+        t_work = threadIdx.x == 0 ? now_ns() : 0ull;
+      }
       if (!(ok = resolve_phase(d, n, step, gen & 1u, list, next_act, smem))) break;
       if (threadIdx.x == 0) {
-        const unsigned long long w = now_ns() - t_work;
+        const unsigned long long w = now_ns() - t_work + w_mark;
         atomicAdd(&c->ns_resolve_work_sum, w);
         atomicMax(&c->phase_max_scratch[1], w);
       }

@@ -74,6 +74,7 @@ struct PlainCtrl {
   unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
   unsigned long long phase_max_scratch[2];             // running max of the current phase
   unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase
+  unsigned long long mark_next;                        // next rank batch of a separate marking pass
 };
 
 enum { kErrBarrier = 1, kErrLookback = 2 };
