@@ -222,6 +222,55 @@ __device__ __forceinline__ void block_chunk(long long n, long long &b, long long
   if (e > n) e = n;
 }
 
+// Dynamic schedule of a phase over n ranks: chunk q of a shared counter.
+// Chunks of `big` ranks first, then, over the last small * t_nb ranks,
+// chunks of `small` ranks (at most one per thread), so the blocks that finish
+// last are at most one short chunk behind. Small generations (whose
+// envelopes each build themselves in FP64) get 32-rank chunks spread over
+// every block.
+struct Chunks {
+  long long n, big, small, nbig, split;
+};
+
+__device__ __forceinline__ long long round32(long long x) { return (x + 31) & ~31ll; }
+
+__device__ __forceinline__ Chunks make_chunks(long long n) {
+  Chunks c;
+  c.n = n;
+  c.small = round32((n + t_nb - 1) / t_nb);
+  c.small = c.small < 32 ? 32 : (c.small > kBlock ? kBlock : c.small);
+  c.big = round32((n + 2ll * t_nb - 1) / (2ll * t_nb));
+  c.big = c.big < c.small ? c.small : (c.big > kClaimBatch ? kClaimBatch : c.big);
+  const long long head = n - c.small * t_nb;
+  c.nbig = head > 0 ? head / c.big : 0;
+  c.split = c.nbig * c.big;
+  return c;
+}
+
+// [b, e) of chunk q; false when q is past the end.
+__device__ __forceinline__ bool chunk_range(const Chunks &c, long long q, long long &b, long long &e) {
+  if (q < c.nbig) {
+    b = q * c.big;
+    e = b + c.big;
+  } else {
+    b = c.split + (q - c.nbig) * c.small;
+    e = b + c.small;
+  }
+  if (b >= c.n) return false;
+  if (e > c.n) e = c.n;
+  return true;
+}
+
+// Thread 0: take the next chunk of a phase over n ranks from *counter and
+// publish [b, e) in rng (b = -1 when none is left).
+__device__ __noinline__ void next_chunk(long long n, unsigned long long *counter, long long *rng) {
+  const Chunks c = make_chunks(n);
+  long long b, e;
+  if (!chunk_range(c, (long long)atomicAdd(counter, 1ull), b, e)) b = e = -1;
+  rng[0] = b;
+  rng[1] = e;
+}
+
 __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj, int &dk) {
   nbr_offset(n, di, dj, dk);
   return dk * g.nxyg + dj * g.nxg + di;
@@ -351,25 +400,18 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
                             double dt, double vel, EnvRec *cur, const EnvRec *prev, unsigned long long *stat_tests,
                             unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
-  __shared__ long long s_batch;
+  __shared__ long long s_rng[2];
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
   unsigned long long tests = 0, tests64 = 0;
-  // Claims need no order: blocks take batches of consecutive ranks from a
+  // Claims need no order: blocks take chunks of consecutive ranks from a
   // shared counter until none is left, so blocks that drew cheap envelopes
-  // (few liquid neighbours) take more batches. About two batches per block,
-  // 32..512 ranks each: small generations (whose envelopes each build
-  // themselves in FP64) still spread over every block.
-  long long batch = (n + 2ll * t_nb - 1) / (2ll * t_nb);
-  batch = (batch + 31) & ~31ll;
-  if (batch > kClaimBatch) batch = kClaimBatch;
-  if (batch < 32) batch = 32;
+  // (few liquid neighbours) take more chunks.
   for (;;) {
-    if (threadIdx.x == 0) s_batch = (long long)atomicAdd(&d.ctrl->claim_next, (unsigned long long)batch);
+    if (threadIdx.x == 0) next_chunk(n, &d.ctrl->claim_next, s_rng);
     __syncthreads();
-    const long long b = s_batch;
+    const long long b = s_rng[0], e = s_rng[1];
     __syncthreads();
-    if (b >= n) break;
-    const long long e = b + batch < n ? b + batch : n;
+    if (b < 0) break;
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
     EnvRec en;
     double gxd = 0, gyd = 0, gzd = 0;
@@ -511,18 +553,13 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
 // as in the claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
 __device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
-  __shared__ long long s_batch;
-  long long batch = (n + 2ll * t_nb - 1) / (2ll * t_nb);
-  batch = (batch + 31) & ~31ll;
-  if (batch > kClaimBatch) batch = kClaimBatch;
-  if (batch < 32) batch = 32;
+  __shared__ long long s_rng[2];
   for (;;) {
-    if (threadIdx.x == 0) s_batch = (long long)atomicAdd(&d.ctrl->mark_next, (unsigned long long)batch);
+    if (threadIdx.x == 0) next_chunk(n, &d.ctrl->mark_next, s_rng);
     __syncthreads();
-    const long long b = s_batch;
+    const long long b = s_rng[0], e = s_rng[1];
     __syncthreads();
-    if (b >= n) break;
-    const long long e = b + batch < n ? b + batch : n;
+    if (b < 0) break;
     for (long long r = b + threadIdx.x; r < e; r += kBlock) d.con[r] = mark_rank(d, r, par, cur);
   }
 }

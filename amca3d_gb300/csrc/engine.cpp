@@ -731,7 +731,7 @@ struct amca_batch {
     // round replaces the estimates of the sizes it used by the times the
     // realms took inside that layout and plans again.
     Plan best_mixed;
-    for (int round = 0; round < 4; ++round) {
+    for (int round = 0; round < 6; ++round) {
       Plan mp = mixed(sizes, t);
       if (mp.tsize.empty()) break;
       apply(mp);
