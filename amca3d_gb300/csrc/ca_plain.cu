@@ -222,54 +222,92 @@ __device__ __forceinline__ void block_chunk(long long n, long long &b, long long
   if (e > n) e = n;
 }
 
-// Dynamic schedule of a phase over n ranks: chunk q of a shared counter.
-// Chunks of `big` ranks first, then, over the last small * t_nb ranks,
-// chunks of `small` ranks (at most one per thread), so the blocks that finish
-// last are at most one short chunk behind. Small generations (whose
-// envelopes each build themselves in FP64) get 32-rank chunks spread over
-// every block.
-struct Chunks {
-  long long n, big, small, nbig, split;
-};
-
-__device__ __forceinline__ long long round32(long long x) { return (x + 31) & ~31ll; }
-
-__device__ __forceinline__ Chunks make_chunks(long long n) {
-  Chunks c;
-  c.n = n;
-  c.small = round32((n + t_nb - 1) / t_nb);
-  c.small = c.small < 32 ? 32 : (c.small > kBlock ? kBlock : c.small);
-  c.big = round32((n + 2ll * t_nb - 1) / (2ll * t_nb));
-  c.big = c.big < c.small ? c.small : (c.big > kClaimBatch ? kClaimBatch : c.big);
-  const long long head = n - c.small * t_nb;
-  c.nbig = head > 0 ? head / c.big : 0;
-  c.split = c.nbig * c.big;
-  return c;
-}
-
-// [b, e) of chunk q; false when q is past the end.
-__device__ __forceinline__ bool chunk_range(const Chunks &c, long long q, long long &b, long long &e) {
-  if (q < c.nbig) {
-    b = q * c.big;
-    e = b + c.big;
-  } else {
-    b = c.split + (q - c.nbig) * c.small;
-    e = b + c.small;
-  }
-  if (b >= c.n) return false;
-  if (e > c.n) e = c.n;
-  return true;
-}
-
-// Thread 0: take the next chunk of a phase over n ranks from *counter and
-// publish [b, e) in rng (b = -1 when none is left).
-__device__ __noinline__ void next_chunk(long long n, unsigned long long *counter, long long *rng) {
-  const Chunks c = make_chunks(n);
+// Dynamic schedule of a pass over n ranks, taken warp by warp from a shared
+// counter (warps never wait for each other inside the pass): chunks of up to
+// 256 ranks first, then, over the last 32 ranks per warp of the team, chunks
+// of 32 (one rank per lane), so the warps that finish last are at most one
+// short chunk behind. Lane 0 calls it; returns (b, e), or b = -1 when none
+// is left.
+__device__ __noinline__ longlong2 next_warp_chunk(long long n, unsigned long long *counter) {
+  const long long warps = (long long)t_nb * kWarps;
+  long long big = (((n + 2 * warps - 1) / (2 * warps)) + 31) & ~31ll;
+  big = big < 32 ? 32 : (big > 256 ? 256 : big);
+  const long long head = n - 32 * warps;
+  const long long nbig = head > 0 ? head / big : 0, split = nbig * big;
+  const long long q = (long long)atomicAdd(counter, 1ull);
   long long b, e;
-  if (!chunk_range(c, (long long)atomicAdd(counter, 1ull), b, e)) b = e = -1;
-  rng[0] = b;
-  rng[1] = e;
+  if (q < nbig) {
+    b = q * big;
+    e = b + big;
+  } else {
+    b = split + (q - nbig) * 32;
+    e = b + 32;
+  }
+  if (b >= n) return make_longlong2(-1, -1);
+  return make_longlong2(b, e < n ? e : n);
 }
+
+// The same for a whole block: chunks of up to kClaimBatch ranks, then, over
+// the last kBlock ranks per block of the team, chunks of at most one rank per
+// thread (32-rank chunks for generations too small to give every block one).
+// Thread 0 calls it.
+__device__ __noinline__ longlong2 next_block_chunk(long long n, unsigned long long *counter) {
+  long long small = (((n + t_nb - 1) / t_nb) + 31) & ~31ll;
+  small = small < 32 ? 32 : (small > kBlock ? kBlock : small);
+  long long big = (((n + 2ll * t_nb - 1) / (2ll * t_nb)) + 31) & ~31ll;
+  big = big < small ? small : (big > kClaimBatch ? kClaimBatch : big);
+  const long long head = n - small * t_nb;
+  const long long nbig = head > 0 ? head / big : 0, split = nbig * big;
+  const long long q = (long long)atomicAdd(counter, 1ull);
+  long long b, e;
+  if (q < nbig) {
+    b = q * big;
+    e = b + big;
+  } else {
+    b = split + (q - nbig) * small;
+    e = b + small;
+  }
+  if (b >= n) return make_longlong2(-1, -1);
+  return make_longlong2(b, e < n ? e : n);
+}
+
+__shared__ long long s_chunk[2];
+
+// Dynamic schedule of a pass over n ranks whose order does not matter.
+// Ranks are taken warp by warp (no block-wide waits inside the pass) by
+// teams of at most 64 blocks and, on larger teams, for generations of at most
+// four ranks per lane; large generations on large teams go block by block,
+// because the shared counter serialises its atomics (about 3 ns each on
+// GB300) and one warp chunk per warp of 600 blocks costs tens of us.
+// Every thread of the block calls next() until it returns false and visits
+// ranks first(), first() + stride(), ... below e.
+struct RankSched {
+  long long n;
+  unsigned long long *counter;
+  bool warp;
+  __device__ RankSched(long long n_, unsigned long long *c) : n(n_), counter(c), warp(t_nb <= 64 || n_ <= 1024ll * t_nb) {}
+  __device__ __forceinline__ bool next(long long &b, long long &e) {
+    if (warp) {
+      longlong2 c = make_longlong2(0, 0);
+      if ((threadIdx.x & 31) == 0) c = next_warp_chunk(n, counter);
+      b = __shfl_sync(0xffffffffu, c.x, 0);
+      e = __shfl_sync(0xffffffffu, c.y, 0);
+      return b >= 0;
+    }
+    if (threadIdx.x == 0) {
+      const longlong2 c = next_block_chunk(n, counter);
+      s_chunk[0] = c.x;
+      s_chunk[1] = c.y;
+    }
+    __syncthreads();
+    b = s_chunk[0];
+    e = s_chunk[1];
+    __syncthreads();
+    return b >= 0;
+  }
+  __device__ __forceinline__ int first() const { return warp ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
+  __device__ __forceinline__ int stride() const { return warp ? 32 : kBlock; }
+};
 
 __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj, int &dk) {
   nbr_offset(n, di, dj, dk);
@@ -400,19 +438,16 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
                             double dt, double vel, EnvRec *cur, const EnvRec *prev, unsigned long long *stat_tests,
                             unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
-  __shared__ long long s_rng[2];
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
   unsigned long long tests = 0, tests64 = 0;
-  // Claims need no order: blocks take chunks of consecutive ranks from a
-  // shared counter until none is left, so blocks that drew cheap envelopes
-  // (few liquid neighbours) take more chunks.
-  for (;;) {
-    if (threadIdx.x == 0) next_chunk(n, &d.ctrl->claim_next, s_rng);
-    __syncthreads();
-    const long long b = s_rng[0], e = s_rng[1];
-    __syncthreads();
-    if (b < 0) break;
-  for (long long r = b + threadIdx.x; r < e; r += kBlock) {
+  // Claims need no order: warps or blocks take chunks of consecutive ranks
+  // from a shared counter until none is left, so those that drew cheap
+  // envelopes (few liquid neighbours) take more chunks.
+  RankSched sched(n, &d.ctrl->claim_next);
+  const int first = sched.first(), stride = sched.stride();
+  long long b, e;
+  while (sched.next(b, e)) {
+  for (long long r = b + first; r < e; r += stride) {
     EnvRec en;
     double gxd = 0, gyd = 0, gzd = 0;
     bool have_centre = false;
@@ -549,19 +584,15 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
   return cap | (surv << 31);
 }
 
-// Marking pass for large generations: blocks take dynamic batches of ranks,
-// as in the claim phase, and write each rank's mark over its containment
+// Marking pass for large generations: dynamic chunks of ranks, as in the
+// claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
 __device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
-  __shared__ long long s_rng[2];
-  for (;;) {
-    if (threadIdx.x == 0) next_chunk(n, &d.ctrl->mark_next, s_rng);
-    __syncthreads();
-    const long long b = s_rng[0], e = s_rng[1];
-    __syncthreads();
-    if (b < 0) break;
-    for (long long r = b + threadIdx.x; r < e; r += kBlock) d.con[r] = mark_rank(d, r, par, cur);
-  }
+  RankSched sched(n, &d.ctrl->mark_next);
+  const int first = sched.first(), stride = sched.stride();
+  long long b, e;
+  while (sched.next(b, e))
+    for (long long r = b + first; r < e; r += stride) d.con[r] = mark_rank(d, r, par, cur);
 }
 
 // Whether a generation of n ranks is marked inside the resolve pass (at most
