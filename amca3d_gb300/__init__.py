@@ -55,11 +55,13 @@ class Stats(ctypes.Structure):
                 ("launches", ctypes.c_int64), ("sites_scanned", ctypes.c_int64), ("nucleations", ctypes.c_int64),
                 ("captures", ctypes.c_int64), ("active_grown", ctypes.c_int64),
                 ("grains_processed", ctypes.c_int64), ("algorithmic_bytes", ctypes.c_double),
-                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("phase_ms", ctypes.c_double * 9)]
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("phase_ms", ctypes.c_double * 9),
+                ("detail_ms", ctypes.c_double * 16)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["phase_ms"] = list(d["phase_ms"])
+        d["detail_ms"] = list(d["detail_ms"])
         return d
 
 

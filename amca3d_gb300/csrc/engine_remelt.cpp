@@ -702,6 +702,13 @@ void RemeltRealm::stats(amca_stats *s) const {
   for (int i = 0; i < 5; ++i) s->phase_ms[i] = c.ns_phase[i] * 1e-6;
   s->phase_ms[5] = c.ns_host * 1e-6;
   s->phase_ms[6] = c.ns_barrier * 1e-6;
+  const double nb = blocks_ > 0 ? (double)blocks_ : 1.0;
+  for (int i = 0; i < 6; ++i) {
+    s->detail_ms[i] = c.ns_work_sum[i] * 1e-6 / nb;
+    s->detail_ms[6 + i] = c.ns_work_max[i] * 1e-6;
+  }
+  s->detail_ms[12] = c.ns_newgrain * 1e-6;
+  s->detail_ms[13] = c.ns_nucleation * 1e-6;
 }
 
 int RemeltRealm::final_grain_count() {

@@ -38,6 +38,7 @@
 // New grain objects (cells without one) get ids in sweep order: events
 // (sweep position, neighbour index) are sorted by block 0 after the step.
 #include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
 #include <math.h>
 
 #include <algorithm>
@@ -67,12 +68,19 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
   return *(const volatile T *)p;
 }
 
+// When this block left its last grid barrier (thread 0).
+__shared__ unsigned long long s_left;
+
 // Sense-counting grid barrier bounded in time; false when a wait ran out or
-// another block reported an error.
-__device__ bool grid_barrier(RemeltCtrl *c) {
+// another block reported an error. `p` names the work it closes (see
+// RemeltCtrl::ns_work_sum) for the busy-time counters.
+__device__ bool grid_barrier(RemeltCtrl *c, int p) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned long long tb = blockIdx.x == 0 ? now_ns() : 0ull;
+    const unsigned long long tb = now_ns();
+    const unsigned long long w = tb - s_left;
+    atomicAdd(&c->ns_work_sum[p], w);
+    atomicMax(&c->work_scratch[p], w);
     const unsigned gen = ld_acquire(&c->bar_gen);
     __threadfence();
     const unsigned arrived = atomicAdd(&c->bar_count, 1u);
@@ -92,7 +100,14 @@ __device__ bool grid_barrier(RemeltCtrl *c) {
       }
     }
     __threadfence();
-    if (blockIdx.x == 0) c->ns_barrier += now_ns() - tb;
+    s_left = now_ns();
+    if (blockIdx.x == 0) {
+      c->ns_barrier += s_left - tb;
+      // every block's maximum for this work is in; the next one comes at
+      // least four barriers later
+      c->ns_work_max[p] += c->work_scratch[p];
+      c->work_scratch[p] = 0ull;
+    }
   }
   __syncthreads();
   return ld_volatile(&c->error) == 0;
@@ -132,6 +147,18 @@ __device__ __forceinline__ unsigned append_slot(unsigned *counter) {
   unsigned base = 0;
   if (grp.thread_rank() == 0) base = atomicAdd(counter, grp.size());
   return grp.shfl(base, 0) + grp.thread_rank();
+}
+
+// `cnt` consecutive list slots for each thread that reaches it together: one
+// atomicAdd per coalesced group, the group's counts placed by an inclusive
+// scan (order within a list is free).
+__device__ __forceinline__ unsigned append_slots(unsigned *counter, unsigned cnt) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group grp = cg::coalesced_threads();
+  const unsigned incl = cg::inclusive_scan(grp, cnt);
+  unsigned base = 0;
+  if (grp.thread_rank() == grp.size() - 1) base = atomicAdd(counter, incl);
+  return grp.shfl(base, grp.size() - 1) + incl - cnt;
 }
 
 // Order-preserving key of a double (for atomicMin); NaN never reaches it.
@@ -843,6 +870,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
   const int64_t nyzg = (int64_t)g.nyg * g.nzg;
   unsigned long long tests = 0, tests64 = 0, caps = 0, exactT = 0, melts = 0, visited = 0, eactive = 0;
   bool ok = true;
+  if (tid == 0) s_left = now_ns();
   for (;;) {
     const StepScalars S = read_scalars(c);
     // --- loop condition of time_integration_weak_coupling (CafeSolver.cpp:188) and launch limits ---
@@ -863,7 +891,9 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
 
     // ===== A: phase update + melted flags (Remelting.cpp:339-404, :484-517) =====
     if (blockIdx.x == 0) {
+      const unsigned long long tg = tid == 0 ? now_ns() : 0ull;
       assign_new_grains(d, c);
+      if (tid == 0) c->ns_newgrain += now_ns() - tg;
       if (tid == 0) {
         c->n_claim = 0;
         c->n_eact[par ^ 1] = 0;  // built in phase E for the next step; its last reader was the previous phase A
@@ -903,7 +933,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       atomicAdd(&c->ns_phase[0], t1 - t_phase);
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c))) break;
+    if (!(ok = grid_barrier(c, 0))) break;
 
     // ===== B: liquid-neighbour flags (Remelting.cpp:518-540) =====
     {
@@ -913,18 +943,32 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       } else {
         for (int64_t q = gtid; q < nl; q += nthr) {
           const int32_t cell = d.liq[q];
+          // all 26 neighbour states, then all flag updates, in flight at once
+          uint32_t solid = 0;
+#pragma unroll
           for (int n = 0; n < 26; ++n) {
             int di, dj, dk;
             nbr_offset(n, di, dj, dk);
+            solid |= (d.orient[cell + dk * g.nxyg + dj * g.nxg + di] > -1 ? 1u : 0u) << n;
+          }
+          uint32_t fresh = 0;
+#pragma unroll
+          for (int n = 0; n < 26; ++n) {
+            if (!((solid >> n) & 1u)) continue;
+            int di, dj, dk;
+            nbr_offset(n, di, dj, dk);
             const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
-            if (d.orient[nb] > -1) {
-              const unsigned bit = 1u << (nb & 31);
-              const unsigned old = atomicOr(&d.flagbits[nb >> 5], bit);
-              if (!(old & bit)) {
-                const unsigned slot = append_slot(&c->n_flag[par]);
-                if (slot < d.list_cap) d.flagged[par][slot] = nb;
-              }
-            }
+            const unsigned bit = 1u << (nb & 31);
+            if (!(atomicOr(&d.flagbits[nb >> 5], bit) & bit)) fresh |= 1u << n;
+          }
+          unsigned slot = append_slots(&c->n_flag[par], (unsigned)__popc(fresh));
+          while (fresh) {
+            const int n = __ffs(fresh) - 1;
+            fresh &= fresh - 1;
+            int di, dj, dk;
+            nbr_offset(n, di, dj, dk);
+            if (slot < d.list_cap) d.flagged[par][slot] = cell + dk * g.nxyg + dj * g.nxg + di;
+            ++slot;
           }
         }
       }
@@ -956,7 +1000,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       atomicAdd(&c->ns_phase[1], t1 - t_phase);
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c))) break;
+    if (!(ok = grid_barrier(c, 1))) break;
 
     // ===== C: nucleation (block 0) | cutoff + minimum temperature (Remelting.cpp:656-705) =====
     const unsigned nf = ld_volatile(&c->n_flag[par]);
@@ -964,6 +1008,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
     }
     if (blockIdx.x == 0 && d.nsites > 0) {
+      const unsigned long long tn = tid == 0 ? now_ns() : 0ull;
       // nucleate_at_nucleation_sites (Remelting.cpp:936-999): ascending sites,
       // orientation id = count so far, a grain object created where the cell has none
       unsigned done_o = 0, done_g = 0;
@@ -999,6 +1044,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
         c->n_orient = S.n_orient + done_o;
         c->n_grains = n_grains + done_g;
         c->nucleations += done_o;
+        c->ns_nucleation += now_ns() - tn;
       }
     }
     {
@@ -1044,7 +1090,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       atomicAdd(&c->ns_phase[2], t1 - t_phase);
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c))) break;
+    if (!(ok = grid_barrier(c, 2))) break;
 
     // ===== dt (Remelting.cpp:706-726, CafeSolver.cpp:195-199) =====
     const double minT = dkey_inv(ld_volatile(&c->minT_key));
@@ -1054,7 +1100,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       const unsigned nh = ld_volatile(&c->n_hard);
       if (nh > 0 || min_hard) {  // uniform: every block read the same counter and key
         if (blockIdx.x == 0 && !host_velocities(d, c, nh, min_hard, minT)) atomicCAS(&c->error, 0, kRemeltErrHost);
-        if (!(ok = grid_barrier(c))) break;
+        if (!(ok = grid_barrier(c, 5))) break;
         if (min_hard) vmin = ld_volatile(&c->vmin);
       }
     }
@@ -1082,15 +1128,25 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       float m32[9];
 #pragma unroll
       for (int qq = 0; qq < 9; ++qq) m32[qq] = d.omat32[9 * (int64_t)ori + qq];
+      // candidates: non-ghost liquid neighbours with material at or below Tm,
+      // from all 26 neighbour states loaded at once
+      uint32_t cand = 0;
+#pragma unroll
       for (int n = 0; n < 26; ++n) {
         int di, dj, dk;
         nbr_offset(n, di, dj, dk);
-        if (ghost(g, I + di, J + dj, K + dk)) continue;
         const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
-        if (d.orient[nb] > -1) continue;
-        const uint8_t cls = d.tcls[nb];  // the neighbour is liquid: its classes are this step's
-        if (!(cls & kTle)) continue;      // overhot (T > Tm)
-        if (!(cls & kTgtNull)) continue;  // no material
+        const bool in = !ghost(g, I + di, J + dj, K + dk);
+        const int32_t o = in ? d.orient[nb] : 0;
+        const uint8_t cls = in ? d.tcls[nb] : 0;  // a liquid neighbour's classes are this step's
+        cand |= (in && o <= -1 && (cls & kTle) && (cls & kTgtNull) ? 1u : 0u) << n;
+      }
+      while (cand) {
+        const int n = __ffs(cand) - 1;
+        cand &= cand - 1;
+        int di, dj, dk;
+        nbr_offset(n, di, dj, dk);
+        const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
         ++tests;
         int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg,
                              L32);
@@ -1116,7 +1172,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       atomicAdd(&c->ns_phase[3], t1 - t_phase);
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c))) break;
+    if (!(ok = grid_barrier(c, 3))) break;
 
     // ===== E: captures (Remelting.cpp:807-847) and the FE replay step (LoadDataFromFile.cpp:207-313) =====
     {
@@ -1274,7 +1330,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       const unsigned long long t1 = now_ns();
       atomicAdd(&c->ns_phase[4], t1 - t_phase);
     }
-    if (!(ok = grid_barrier(c))) break;
+    if (!(ok = grid_barrier(c, 4))) break;
     if (ld_volatile(&c->status) == kRemeltFramesEnd) break;
   }
   if (ok && blockIdx.x == 0) assign_new_grains(d, c);

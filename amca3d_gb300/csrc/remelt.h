@@ -70,6 +70,11 @@ struct RemeltCtrl {
   unsigned long long ns_phase[5];
   unsigned long long ns_host;  // block 0's wait for host velocity answers
   unsigned long long ns_barrier;  // block 0's time inside grid barriers
+  // per-block busy time between barriers, by the barrier that closes it
+  // (0 A, 1 B, 2 C, 3 D, 4 E, 5 host velocities): sum over blocks and the
+  // sum over steps of the slowest block; scratch holds the current step's max
+  unsigned long long ns_work_sum[6], ns_work_max[6], work_scratch[6];
+  unsigned long long ns_newgrain, ns_nucleation;  // block 0's new-grain ids (phase A) and nucleation (phase C)
   int fstat_frame[2];          // frame whose per-element extrema each slot holds (-1: none)
   int any_near;                // some element met a frame near the void threshold: rebuild every step
 };

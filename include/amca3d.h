@@ -193,6 +193,12 @@ typedef struct {
    * the barrier: [5] claim mean over blocks, [6] claim slowest block,
    * [7] resolve mean, [8] resolve slowest block (summed over phases) */
   double phase_ms[9];
+  /* Remelting realm only (zeros otherwise), ms summed over steps: per-block
+   * busy time between grid barriers, mean over blocks [0..5] and slowest
+   * block [6..11], for the work closed by the barrier after phase A, B, C,
+   * D, E and after the host velocity answers; block 0's new-grain ids [12]
+   * and nucleation [13]. */
+  double detail_ms[16];
 } amca_stats;
 /* For the FE-coupled remelting realm the fields mean: liquid_cells -1 (not
  * tracked), grains = grain objects, active = flagged (liquid-neighbour) cells
