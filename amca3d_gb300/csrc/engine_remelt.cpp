@@ -534,21 +534,44 @@ static double reference_velocity(const PlainConfig &c, double T) {
 }
 
 // Runs beside a kernel launch: answers the kernel's velocity requests.
-void RemeltRealm::serve_velocities(const volatile int *stop) {
+void RemeltRealm::serve_velocities(const volatile int *stop, int w, int workers, VelocityJob *job) {
   HostVelocity *hv = hostvel_;
-  unsigned last = __atomic_load_n(&hv->seq_done, __ATOMIC_ACQUIRE);
+  // worker 0 watches the device's request word and hands each request to all
+  // workers; every worker spins (yielding when idle for long) on the job word
+  unsigned last = w == 0 ? __atomic_load_n(&hv->seq_done, __ATOMIC_ACQUIRE) : job->seq.load(std::memory_order_acquire);
   unsigned idle = 0;
   while (!*stop) {
-    const unsigned r = __atomic_load_n(&hv->seq_req, __ATOMIC_ACQUIRE);
-    if (r == last) {
-      if (++idle > 4096) std::this_thread::yield();
-      continue;
+    unsigned r;
+    if (w == 0) {
+      r = __atomic_load_n(&hv->seq_req, __ATOMIC_ACQUIRE);
+      if (r != last) {
+        const unsigned n = std::min(__atomic_load_n(&hv->n, __ATOMIC_ACQUIRE), (unsigned)kHostVelCap);
+        // small requests are not worth waking the others
+        const int use = n >= 64u ? workers : 1;
+        job->n.store(n, std::memory_order_relaxed);
+        job->left.store((unsigned)use, std::memory_order_relaxed);
+        if (use > 1) job->seq.store(r, std::memory_order_release);
+        for (unsigned i = 0; i < n; i += (unsigned)use) hv->v[i] = reference_velocity(cfg_.ca, hv->T[i]);
+        if (job->left.fetch_sub(1, std::memory_order_acq_rel) != 1)
+          while (job->left.load(std::memory_order_acquire) != 0 && !*stop) {
+          }
+        __atomic_store_n(&hv->seq_done, r, __ATOMIC_RELEASE);
+        last = r;
+        idle = 0;
+        continue;
+      }
+    } else {
+      r = job->seq.load(std::memory_order_acquire);
+      if (r != last) {
+        const unsigned n = job->n.load(std::memory_order_relaxed);
+        for (unsigned i = (unsigned)w; i < n; i += (unsigned)workers) hv->v[i] = reference_velocity(cfg_.ca, hv->T[i]);
+        job->left.fetch_sub(1, std::memory_order_acq_rel);
+        last = r;
+        idle = 0;
+        continue;
+      }
     }
-    idle = 0;
-    const unsigned n = __atomic_load_n(&hv->n, __ATOMIC_ACQUIRE);
-    for (unsigned i = 0; i < n && i < (unsigned)kHostVelCap; ++i) hv->v[i] = reference_velocity(cfg_.ca, hv->T[i]);
-    __atomic_store_n(&hv->seq_done, r, __ATOMIC_RELEASE);
-    last = r;
+    if (++idle > 4096) std::this_thread::yield();
   }
 }
 
@@ -579,13 +602,20 @@ void RemeltRealm::launch(long long limit) {
     const int running = kRemeltRunning;
     h2d(&dev_.ctrl->status, &running, sizeof running);
     volatile int stop = 0;
-    std::thread server([&] { serve_velocities(&stop); });
+    // the hard velocities of one step (a few hundred glibc pow calls) are
+    // split over a few spinning host threads
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int workers = std::max(1, std::min(8, hw / 2));
+    VelocityJob job;
+    std::vector<std::thread> servers;
+    for (int w = 0; w < workers; ++w)
+      servers.emplace_back([&, w] { serve_velocities(&stop, w, workers, &job); });
     RCK(cudaEventRecord(ev0_, stream_));
     cudaError_t le = remelt_run_steps(dev_, limit, blocks_, stream_);
     if (le == cudaSuccess) le = cudaEventRecord(ev1_, stream_);
     if (le == cudaSuccess) le = cudaStreamSynchronize(stream_);
     stop = 1;
-    server.join();
+    for (std::thread &t : servers) t.join();
     if (le != cudaSuccess) throw CudaError(std::string("remelting kernel: ") + cudaGetErrorString(le));
     ++launches_;
     sync_ctrl();
@@ -709,6 +739,7 @@ void RemeltRealm::stats(amca_stats *s) const {
   }
   s->detail_ms[12] = c.ns_newgrain * 1e-6;
   s->detail_ms[13] = c.ns_nucleation * 1e-6;
+  s->detail_ms[14] = c.ns_flags_max * 1e-6;
 }
 
 int RemeltRealm::final_grain_count() {

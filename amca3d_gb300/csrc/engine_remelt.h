@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <memory>
 #include <string>
 #include <vector>
@@ -59,7 +60,14 @@ class RemeltRealm {
   void sync_ctrl();
   void extend_orientations();
   void upload_initial_state();
-  void serve_velocities(const volatile int *stop);
+  // Host side of the velocity requests: worker w of `workers` evaluates
+  // entries w, w + workers, ... of each request; the last to finish answers.
+  struct VelocityJob {
+    std::atomic<unsigned> seq{0};   // request being served
+    std::atomic<unsigned> n{0};     // its entry count
+    std::atomic<unsigned> left{0};  // workers still evaluating it
+  };
+  void serve_velocities(const volatile int *stop, int w, int workers, VelocityJob *job);
   void launch(long long limit);
   void write_snapshot();
   // host copies of the output fields of the current state

@@ -936,12 +936,22 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
     if (!(ok = grid_barrier(c, 0))) break;
 
     // ===== B: liquid-neighbour flags (Remelting.cpp:518-540) =====
+    if (tid == 0 && blockIdx.x == 0) {
+      c->ns_flags_max += c->flags_scratch;  // last step's maximum: every block added it before the A barrier
+      c->flags_scratch = 0ull;
+    }
+    const unsigned long long tfl = tid == 0 ? now_ns() : 0ull;
     {
       const unsigned nl = ld_volatile(&c->n_liq);
       if (nl > d.list_cap) {
         if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
       } else {
-        for (int64_t q = gtid; q < nl; q += nthr) {
+        // entries are dealt lane-major over the warps (q = lane * warps +
+        // warp): the list holds the cells of an element together, and their
+        // flag bits share bitmap words, so neighbouring entries go to
+        // different warps rather than into one warp's same-word atomics
+        const int64_t nw = nthr >> 5, wid = gtid >> 5, lane = tid & 31;
+        for (int64_t q = lane * nw + wid; q < nl; q += nthr) {
           const int32_t cell = d.liq[q];
           // all 26 neighbour states, then all flag updates, in flight at once
           uint32_t solid = 0;
@@ -973,25 +983,29 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
         }
       }
     }
+    __syncthreads();
+    if (tid == 0) atomicMax(&c->flags_scratch, now_ns() - tfl);
     // site conditions of nucleate_at_nucleation_sites (Remelting.cpp:946-960), all blocks
+    // (only a liquid, melted cell can nucleate: the temperatures are
+    // evaluated for those alone)
     for (int64_t sidx = gtid; sidx < d.nsites; sidx += nthr) {
       const int32_t cell = d.site_cell[sidx];
-      double T = -1.0;
-      const bool withMat = eval_T(d, th, cell, T);
-      bool cooling = false;
-      if (S.step > 0) {  // cooling_ of this step's phase update (Remelting.cpp:362-373)
-        double Told = -1.0;
-        eval_T(d, thp, cell, Told);
-        double rate = 410;
-        if (Told > 0) rate = (T - Told) / S.dt;
-        if (T <= 0) rate = 0;
-        cooling = withMat ? (rate < 0) : false;
-      }
       uint8_t f = 0;
-      const bool isLiquid = d.orient[cell] == -1;
-      if (cooling && isLiquid && d.melted[cell] && T > d.Tnuc) {
-        const double dT = d.Tm - T;
-        if (dT > d.site_dtc[sidx]) f = d.grain[cell] == -1 ? 2 : 1;
+      if (d.orient[cell] == -1 && d.melted[cell]) {
+        double T = -1.0, Told = -1.0;
+        const bool withMat = eval_T(d, th, cell, T);
+        bool cooling = false;
+        if (S.step > 0) {  // cooling_ of this step's phase update (Remelting.cpp:362-373)
+          eval_T(d, thp, cell, Told);
+          double rate = 410;
+          if (Told > 0) rate = (T - Told) / S.dt;
+          if (T <= 0) rate = 0;
+          cooling = withMat ? (rate < 0) : false;
+        }
+        if (cooling && T > d.Tnuc) {
+          const double dT = d.Tm - T;
+          if (dT > d.site_dtc[sidx]) f = d.grain[cell] == -1 ? 2 : 1;
+        }
       }
       d.snuc[sidx] = f;
     }

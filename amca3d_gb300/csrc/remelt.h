@@ -75,6 +75,7 @@ struct RemeltCtrl {
   // sum over steps of the slowest block; scratch holds the current step's max
   unsigned long long ns_work_sum[6], ns_work_max[6], work_scratch[6];
   unsigned long long ns_newgrain, ns_nucleation;  // block 0's new-grain ids (phase A) and nucleation (phase C)
+  unsigned long long ns_flags_max, flags_scratch;  // slowest block's liquid-neighbour flag pass (phase B)
   int fstat_frame[2];          // frame whose per-element extrema each slot holds (-1: none)
   int any_near;                // some element met a frame near the void threshold: rebuild every step
 };

@@ -511,6 +511,7 @@ def run_ours_pbf(args, dist: Dist):
                    "busy_ms_mean_A_B_C_D_E_host": [round(x, 3) for x in st["detail_ms"][:6]],
                    "busy_ms_slowest_A_B_C_D_E_host": [round(x, 3) for x in st["detail_ms"][6:12]],
                    "block0_newgrain_nucleation_ms": [round(x, 3) for x in st["detail_ms"][12:14]],
+                   "flag_pass_slowest_ms": round(st["detail_ms"][14], 3),
                    "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": load_traffic("remelt_persistent_pbf_500.json"),

@@ -197,7 +197,8 @@ typedef struct {
    * busy time between grid barriers, mean over blocks [0..5] and slowest
    * block [6..11], for the work closed by the barrier after phase A, B, C,
    * D, E and after the host velocity answers; block 0's new-grain ids [12]
-   * and nucleation [13]. */
+   * and nucleation [13]; the slowest block's liquid-neighbour flag pass in
+   * phase B [14]. */
   double detail_ms[16];
 } amca_stats;
 /* For the FE-coupled remelting realm the fields mean: liquid_cells -1 (not
