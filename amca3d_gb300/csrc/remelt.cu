@@ -767,12 +767,61 @@ __device__ void assign_new_grains(const RemeltDevice &d, RemeltCtrl *c) {
 // the per-cell part of checkup_liquid_cell_neigh_to_growth (:484-517) for one
 // interior cell. `count_all`: add every liquid cell to its element's count
 // (first step); otherwise only cells that melt now.
+// What the phase update needs of a cell's element, read once per element by
+// the warp that walks its cells: the nodal FP32 temperatures of this step and
+// their error bound, the void flag and whether the frame extrema keep every
+// solid cell of it unchanged.
+struct ElemView {
+  int32_t e;
+  bool void_;
+  bool quiet;
+  float t[8];
+  float err;
+};
+
+// Warp-collective: the view of element e (every lane gets it).
+__device__ __forceinline__ ElemView elem_view(const RemeltDevice &d, const float *th32, int32_t e) {
+  ElemView v;
+  v.e = e;
+  const int lane = threadIdx.x & 31;
+  int64_t nid[8];
+  elem_nodes(d.nn, e, nid);
+  int64_t mine = nid[0];
+#pragma unroll
+  for (int i = 1; i < 8; ++i)
+    if (lane == i) mine = nid[i];
+  const float tl = lane < 8 ? th32[mine] : 0.0f;
+  v.void_ = d.evoid[e] != 0;
+  v.quiet = d.emax[e] < d.Tm && d.emin[e] >= null_plus();
+  float mg = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    v.t[i] = __shfl_sync(0xffffffffu, tl, i);
+    mg = fmaxf(mg, fabsf(v.t[i]));
+  }
+  v.err = ldexpf(mg, -16) + 1.52587890625e-05f;
+  return v;
+}
+
+// eval_T32 with the element's nodal values already at hand (same operands,
+// same operation order, same result).
+__device__ __forceinline__ float eval_T32_view(const RemeltDevice &d, int64_t c, const ElemView &v, float &err) {
+  const float xi = d.pc32[3 * c], eta = d.pc32[3 * c + 1], zeta = d.pc32[3 * c + 2];
+  const float a0 = 1.0f - eta, a1 = 1.0f + eta, b0 = 1.0f - xi, b1 = 1.0f + xi, c0 = 1.0f - zeta, c1 = 1.0f + zeta;
+  const float *t = v.t;
+  err = v.err;
+  return 0.125f * (a0 * b0 * c0 * t[0] + a0 * b1 * c0 * t[1] + a1 * b1 * c0 * t[2] + a1 * b0 * c0 * t[3] +
+                   a0 * b0 * c1 * t[4] + a0 * b1 * c1 * t[5] + a1 * b1 * c1 * t[6] + a1 * b0 * c1 * t[7]);
+}
+
+// `ev`: the cell's element view when the caller walks an element's cells
+// (the cell's tag is then ev->e), or nullptr.
 __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell, const double *th,
                              const float *th32, const StepScalars &S, bool count_all, unsigned long long &exactT,
-                             unsigned long long &melts) {
+                             unsigned long long &melts, const ElemView *ev = nullptr) {
   int32_t o = d.orient[cell];
-  const int32_t e = d.tag[cell];
-  const bool withMat = e >= 0 && !d.evoid[e];
+  const int32_t e = ev ? ev->e : d.tag[cell];
+  const bool withMat = e >= 0 && !(ev ? ev->void_ : d.evoid[e] != 0);
   const double np = null_plus();
   // the FP32 estimate decides each comparison unless it is within its error
   // bound of the threshold; then the exact FP64 temperature decides them all
@@ -796,8 +845,8 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   if (o > -1) {
     if (withMat) {
       // certainly below the liquidus and above nullMatTemp_ + 0.01: nothing changes
-      if (d.emax[e] < d.Tm && d.emin[e] >= np) return;
-      T32 = eval_T32(d, th32, cell, e, err);
+      if (ev ? ev->quiet : (d.emax[e] < d.Tm && d.emin[e] >= np)) return;
+      T32 = ev ? eval_T32_view(d, cell, *ev, err) : eval_T32(d, th32, cell, e, err);
       have32 = true;
       int b = below(d.Tm);
       if (b < 0) {
@@ -828,7 +877,7 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   bool wm2, flags, le, gtn;
   bool decided = false;
   if (!exact) {
-    if (!have32) T32 = eval_T32(d, th32, cell, e, err);
+    if (!have32) T32 = ev ? eval_T32_view(d, cell, *ev, err) : eval_T32(d, th32, cell, e, err);
     const double lo = (double)T32 - (double)err, hi = (double)T32 + (double)err;
     const bool ok_np = hi < np || lo >= np, ok_tm = hi < d.Tm || lo > d.Tm, ok_nl = hi <= -1.0 || lo > -1.0;
     if (ok_np && ok_tm && ok_nl && T32 == T32) {
@@ -922,8 +971,9 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       for (int64_t w = gw; w < na; w += nw) {
         const int32_t e = d.eact[par][w];
         const int64_t b = d.ecell_start[e], en = d.ecell_start[e + 1];
+        const ElemView ev = elem_view(d, th32, e);
         for (int64_t k = b + lane; k < en; k += 32) {
-          phase_update(d, c, d.ecell[k], th, th32, S, false, exactT, melts);
+          phase_update(d, c, d.ecell[k], th, th32, S, false, exactT, melts, &ev);
           ++visited;
         }
       }
