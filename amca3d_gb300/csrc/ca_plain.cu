@@ -85,22 +85,30 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
   return *(const volatile T *)p;
 }
 
-// Sense-counting barrier of the t_nb blocks of the team over the words
-// (count, gen). Returns false (with *error set) when a wait ran out or
-// another block reported an error.
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Barrier of the t_nb blocks of the team on the adjacent words (count, gen),
+// read as one 64-bit word with the generation in the high half: an arrival
+// is one atomicAdd, and the last arrival resets the count and opens the next
+// generation with one more. Returns false (with *error set) when a wait ran
+// out or another block reported an error.
 __device__ bool team_barrier(unsigned *count, unsigned *gen_word, int *error) {
+  unsigned long long *w = (unsigned long long *)count;  // gen_word == count + 1
+  (void)gen_word;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned gen = ld_acquire(gen_word);
     __threadfence();
-    const unsigned arrived = atomicAdd(count, 1u);
-    if (arrived == t_nb - 1) {
-      atomicExch(count, 0u);
-      __threadfence();
-      atomicAdd(gen_word, 1u);
+    const unsigned long long old = atomicAdd(w, 1ull);
+    const unsigned gen = (unsigned)(old >> 32);
+    if ((unsigned)old == (unsigned)t_nb - 1u) {
+      atomicAdd(w, (1ull << 32) - (unsigned long long)t_nb);
     } else {
       const unsigned long long t0 = now_ns();
-      while (ld_acquire(gen_word) == gen) {
+      while ((unsigned)(ld_acquire64(w) >> 32) == gen) {
         if (ld_volatile(error) != 0) break;
         if (now_ns() - t0 > kWaitNs) {
           atomicCAS(error, 0, kErrBarrier);

@@ -23,6 +23,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "ca_math.h"
@@ -77,6 +78,11 @@ struct PlainCtrl {
   unsigned long long mark_next;                        // next rank batch of a separate marking pass
 };
 
+// The barrier reads (bar_count, bar_gen) as one 64-bit word, generation in
+// the high half.
+static_assert(offsetof(PlainCtrl, bar_count) == 0 && offsetof(PlainCtrl, bar_gen) == 4,
+              "barrier words must form one aligned 64-bit word");
+
 enum { kErrBarrier = 1, kErrLookback = 2 };
 
 // One envelope as the generation lists carry it: everything the neighbour
@@ -121,8 +127,8 @@ struct PlainDevice {
 
 // One team of the batched launch: its barrier words and the realm it runs in
 // the current round, by round parity (-1: none left).
-struct BatchTeam {
-  unsigned count;
+struct alignas(8) BatchTeam {
+  unsigned count;  // barrier arrivals; with gen one 64-bit word (gen in the high half)
   unsigned gen;
   int slot[2];
 };

@@ -58,6 +58,11 @@ __device__ __forceinline__ unsigned long long now_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -81,16 +86,18 @@ __device__ bool grid_barrier(RemeltCtrl *c, int p) {
     const unsigned long long w = tb - s_left;
     atomicAdd(&c->ns_work_sum[p], w);
     atomicMax(&c->work_scratch[p], w);
-    const unsigned gen = ld_acquire(&c->bar_gen);
+    // (bar_count, bar_gen) as one 64-bit word, generation in the high half:
+    // an arrival is one atomicAdd; the last one resets the count and opens
+    // the next generation with one more
+    unsigned long long *bw = (unsigned long long *)&c->bar_count;
     __threadfence();
-    const unsigned arrived = atomicAdd(&c->bar_count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&c->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
+    const unsigned long long old = atomicAdd(bw, 1ull);
+    const unsigned gen = (unsigned)(old >> 32);
+    if ((unsigned)old == gridDim.x - 1) {
+      atomicAdd(bw, (1ull << 32) - (unsigned long long)gridDim.x);
     } else {
       const unsigned long long t0 = now_ns();
-      while (ld_acquire(&c->bar_gen) == gen) {
+      while ((unsigned)(ld_acquire64(bw) >> 32) == gen) {
         if (ld_volatile(&c->error) != 0) break;
         if (now_ns() - t0 > kWaitNs) {
           atomicCAS(&c->error, 0, kRemeltErrBarrier);
@@ -159,6 +166,18 @@ __device__ __forceinline__ unsigned append_slots(unsigned *counter, unsigned cnt
   unsigned base = 0;
   if (grp.thread_rank() == grp.size() - 1) base = atomicAdd(counter, incl);
   return grp.shfl(base, grp.size() - 1) + incl - cnt;
+}
+
+// Short lists whose items carry FP64 work or long load chains are dealt
+// across blocks first: item q goes to block first_block + q % nb (thread
+// q / nb of it), so the work spreads over every SM instead of filling the
+// first few. Visit q = spread_begin(...), then q += spread_stride(...).
+__device__ __forceinline__ int64_t spread_begin(int first_block) {
+  const int64_t nb = gridDim.x - first_block;
+  return (int64_t)threadIdx.x * nb + (blockIdx.x - first_block);
+}
+__device__ __forceinline__ int64_t spread_stride(int first_block) {
+  return (int64_t)(gridDim.x - first_block) * blockDim.x;
 }
 
 // Order-preserving key of a double (for atomicMin); NaN never reaches it.
@@ -1038,7 +1057,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
     // site conditions of nucleate_at_nucleation_sites (Remelting.cpp:946-960), all blocks
     // (only a liquid, melted cell can nucleate: the temperatures are
     // evaluated for those alone)
-    for (int64_t sidx = gtid; sidx < d.nsites; sidx += nthr) {
+    for (int64_t sidx = spread_begin(0); sidx < d.nsites; sidx += spread_stride(0)) {
       const int32_t cell = d.site_cell[sidx];
       uint8_t f = 0;
       if (d.orient[cell] == -1 && d.melted[cell]) {
@@ -1113,8 +1132,8 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
     }
     {
       const bool solo = gridDim.x == 1;
-      const int64_t g0 = solo ? gtid : gtid - blockDim.x;
-      const int64_t gn = solo ? nthr : nthr - blockDim.x;
+      const int64_t g0 = spread_begin(solo ? 0 : 1);
+      const int64_t gn = spread_stride(solo ? 0 : 1);
       if (nf <= d.list_cap && (solo || blockIdx.x > 0)) {
         const unsigned long long key_tm = dkey(d.Tm);
         unsigned long long best = key_tm;
@@ -1158,8 +1177,17 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
 
     // ===== dt (Remelting.cpp:706-726, CafeSolver.cpp:195-199) =====
     const double minT = dkey_inv(ld_volatile(&c->minT_key));
-    bool min_hard = false;
-    double vmin = velocity(d, minT, min_hard);
+    // the same FP64 velocity for every thread: one thread per block computes it
+    __shared__ double s_vmin;
+    __shared__ int s_min_hard;
+    if (tid == 0) {
+      bool h = false;
+      s_vmin = velocity(d, minT, h);
+      s_min_hard = h ? 1 : 0;
+    }
+    __syncthreads();
+    const bool min_hard = s_min_hard != 0;
+    double vmin = s_vmin;
     {
       const unsigned nh = ld_volatile(&c->n_hard);
       if (nh > 0 || min_hard) {  // uniform: every block read the same counter and key
@@ -1174,7 +1202,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
     const double dT = (S.dT_FE < dtLoc) ? S.dT_FE : dtLoc;
 
     // ===== D: grow and claim (Remelting.cpp:545-622) =====
-    for (int64_t q = gtid; q < nf && nf <= d.list_cap; q += nthr) {
+    for (int64_t q = spread_begin(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
       const int32_t cell = d.flagged[par][q];
       int I, J, K;
       cell_ijk(g, cell, I, J, K);
@@ -1244,7 +1272,7 @@ __global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long 
       if (nc > d.list_cap) {
         if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
       } else {
-        for (int64_t q = gtid; q < nc; q += nthr) {
+        for (int64_t q = spread_begin(0); q < nc; q += spread_stride(0)) {
           const int32_t nb = d.claimed[q];
           const int32_t w = d.orient[nb] - INT_MIN;
           const int wi = (int)(w / nyzg), wj = (int)((w / g.nzg) % g.nyg), wk = (int)(w % g.nzg);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "ca_math.h"
@@ -40,7 +41,7 @@ struct HostVelocity {
 constexpr uint8_t kTlt = 1, kTle = 2, kTgtNull = 4, kTgeNullPlus = 8;
 
 struct RemeltCtrl {
-  unsigned int bar_count, bar_gen;
+  unsigned int bar_count, bar_gen;  // one 64-bit word for the grid barrier, generation in the high half
   int error;
   int status;
   // coupling scalars, published by block 0 at the end of every step
@@ -79,6 +80,9 @@ struct RemeltCtrl {
   int fstat_frame[2];          // frame whose per-element extrema each slot holds (-1: none)
   int any_near;                // some element met a frame near the void threshold: rebuild every step
 };
+
+static_assert(offsetof(RemeltCtrl, bar_count) == 0 && offsetof(RemeltCtrl, bar_gen) == 4,
+              "barrier words must form one aligned 64-bit word");
 
 struct RemeltDevice {
   Grid g;
