@@ -927,7 +927,10 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   }
 }
 
-__global__ void __launch_bounds__(kBlock, 1) remelt_kernel(RemeltDevice d, long long limit) {
+// Register budget of two blocks per SM (128 per thread), run with one block
+// per SM: on pbf_500 that is faster than the unconstrained 186 registers, two
+// blocks per SM, or 512-thread blocks (740 against 768, 793 and 801 ms per run).
+__global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long long limit) {
   __shared__ unsigned smem[kWarps + 2];
   RemeltCtrl *c = d.ctrl;
   const Grid &g = d.g;
