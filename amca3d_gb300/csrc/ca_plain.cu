@@ -255,66 +255,115 @@ __device__ __noinline__ longlong2 next_warp_chunk(long long n, unsigned long lon
   return make_longlong2(b, e < n ? e : n);
 }
 
-// The same for a whole block: chunks of up to kClaimBatch ranks, then, over
-// the last kBlock ranks per block of the team, chunks of at most one rank per
-// thread (32-rank chunks for generations too small to give every block one).
-// Thread 0 calls it.
-__device__ __noinline__ longlong2 next_block_chunk(long long n, unsigned long long *counter) {
+// Chunks of a pass over n ranks taken block by block: chunks of up to
+// kClaimBatch ranks, then, over the last kBlock ranks per block of the team,
+// chunks of at most one rank per thread (32-rank chunks for generations too
+// small to give every block one). s_chunks = (big, small, number of big
+// chunks, where the small ones start), set once per pass by thread 0.
+__shared__ long long s_chunks[4];
+
+__device__ __noinline__ void set_block_chunks(long long n) {
   long long small = (((n + t_nb - 1) / t_nb) + 31) & ~31ll;
   small = small < 32 ? 32 : (small > kBlock ? kBlock : small);
   long long big = (((n + 2ll * t_nb - 1) / (2ll * t_nb)) + 31) & ~31ll;
   big = big < small ? small : (big > kClaimBatch ? kClaimBatch : big);
   const long long head = n - small * t_nb;
-  const long long nbig = head > 0 ? head / big : 0, split = nbig * big;
-  const long long q = (long long)atomicAdd(counter, 1ull);
+  const long long nbig = head > 0 ? head / big : 0;
+  s_chunks[0] = big;
+  s_chunks[1] = small;
+  s_chunks[2] = nbig;
+  s_chunks[3] = nbig * big;
+}
+
+// Chunk q: (b, e), or b = -1 past the end.
+__device__ __forceinline__ longlong2 block_chunk_range(long long n, long long q) {
   long long b, e;
-  if (q < nbig) {
-    b = q * big;
-    e = b + big;
+  if (q < s_chunks[2]) {
+    b = q * s_chunks[0];
+    e = b + s_chunks[0];
   } else {
-    b = split + (q - nbig) * small;
-    e = b + small;
+    b = s_chunks[3] + (q - s_chunks[2]) * s_chunks[1];
+    e = b + s_chunks[1];
   }
   if (b >= n) return make_longlong2(-1, -1);
   return make_longlong2(b, e < n ? e : n);
 }
 
-__shared__ long long s_chunk[2];
+// The block's pool of the current chunk, handed to its warps 32 ranks at a
+// time: (chunk index << 32) | offset into the chunk.
+__shared__ unsigned long long s_pool;
 
-// Dynamic schedule of a pass over n ranks whose order does not matter.
-// Ranks are taken warp by warp (no block-wide waits inside the pass) by
-// teams of at most 64 blocks and, on larger teams, for generations of at most
-// four ranks per lane; large generations on large teams go block by block,
-// because the shared counter serialises its atomics (about 3 ns each on
-// GB300) and one warp chunk per warp of 600 blocks costs tens of us.
-// Every thread of the block calls next() until it returns false and visits
-// ranks first(), first() + stride(), ... below e.
+// Dynamic schedule of a pass over n ranks whose order does not matter, in
+// pieces of 32 ranks per warp (lane i takes rank b + i). Teams of at most 64
+// blocks, and small generations on larger teams, take their chunks warp by
+// warp from the shared counter. Large generations on large teams take them
+// block by block (one shared-counter atomic per block chunk: the counter
+// serialises its atomics, about 3 ns each on GB300, and one per warp chunk
+// of 600 blocks costs tens of us), and the block's warps share each chunk
+// through the pool: a shared-memory atomic gives a warp its piece, the warp
+// whose piece starts at the chunk's end takes the next chunk, and no warp
+// waits for the others except while the pool is refilled.
 struct RankSched {
   long long n;
   unsigned long long *counter;
+  int *error;
   bool warp;
-  __device__ RankSched(long long n_, unsigned long long *c) : n(n_), counter(c), warp(t_nb <= 64 || n_ <= 1024ll * t_nb) {}
+  __device__ RankSched(long long n_, unsigned long long *c, int *err)
+      : n(n_), counter(c), error(err), warp(t_nb <= 64 || n_ <= 1024ll * t_nb) {
+    if (!warp) {
+      if (threadIdx.x == 0) {
+        set_block_chunks(n);
+        s_pool = atomicAdd(counter, 1ull) << 32;
+      }
+      __syncthreads();
+    }
+  }
+  // The next piece [b, e) of this warp; false when none is left.
   __device__ __forceinline__ bool next(long long &b, long long &e) {
+    const int lane = threadIdx.x & 31;
     if (warp) {
       longlong2 c = make_longlong2(0, 0);
-      if ((threadIdx.x & 31) == 0) c = next_warp_chunk(n, counter);
+      if (lane == 0) c = next_warp_chunk(n, counter);
       b = __shfl_sync(0xffffffffu, c.x, 0);
       e = __shfl_sync(0xffffffffu, c.y, 0);
       return b >= 0;
     }
-    if (threadIdx.x == 0) {
-      const longlong2 c = next_block_chunk(n, counter);
-      s_chunk[0] = c.x;
-      s_chunk[1] = c.y;
+    const unsigned long long t0 = now_ns();
+    for (;;) {
+      unsigned long long old = 0;
+      if (lane == 0) old = atomicAdd(&s_pool, 32ull);
+      old = __shfl_sync(0xffffffffu, old, 0);
+      const long long q = (long long)(old >> 32), off = (long long)(old & 0xffffffffull);
+      const longlong2 ch = block_chunk_range(n, q);
+      if (ch.x < 0) return false;
+      const long long len = ch.y - ch.x;
+      if (off < len) {
+        b = ch.x + off;
+        e = b + 32 < ch.y ? b + 32 : ch.y;
+        return true;
+      }
+      if (off < len + 32) {  // this warp's piece starts at the chunk's end: it takes the next chunk
+        if (lane == 0) atomicExch(&s_pool, atomicAdd(counter, 1ull) << 32);
+        __syncwarp();
+        continue;
+      }
+      // another warp is taking the next chunk: wait until the pool moves on
+      int bail = 0;
+      if (lane == 0) {
+        while ((long long)(*(volatile unsigned long long *)&s_pool >> 32) == q) {
+          if (now_ns() - t0 > kWaitNs || ld_volatile(error) != 0) {
+            atomicCAS(error, 0, kErrBarrier);
+            bail = 1;
+            break;
+          }
+          __nanosleep(20);
+        }
+      }
+      if (__shfl_sync(0xffffffffu, bail, 0)) return false;
     }
-    __syncthreads();
-    b = s_chunk[0];
-    e = s_chunk[1];
-    __syncthreads();
-    return b >= 0;
   }
-  __device__ __forceinline__ int first() const { return warp ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
-  __device__ __forceinline__ int stride() const { return warp ? 32 : kBlock; }
+  __device__ __forceinline__ int first() const { return (int)(threadIdx.x & 31); }
+  __device__ __forceinline__ int stride() const { return 32; }
 };
 
 __device__ __forceinline__ int nbr_delta(const Grid &g, int n, int &di, int &dj, int &dk) {
@@ -451,7 +500,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
   // Claims need no order: warps or blocks take chunks of consecutive ranks
   // from a shared counter until none is left, so those that drew cheap
   // envelopes (few liquid neighbours) take more chunks.
-  RankSched sched(n, &d.ctrl->claim_next);
+  RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e)) {
@@ -596,7 +645,7 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
 // claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
 __device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
-  RankSched sched(n, &d.ctrl->mark_next);
+  RankSched sched(n, &d.ctrl->mark_next, &d.ctrl->error);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e))
