@@ -320,3 +320,21 @@ def test_cli_help_and_missing_deck(amca, tmp_path):
     (tmp_path / "bad.i").write_text("solvers: [nothing]\n")
     r = subprocess.run([cli, "-i", str(tmp_path / "bad.i")], capture_output=True, text=True)
     assert r.returncode == 1 and "parsing the deck" in r.stderr
+
+
+def test_batched_workload_decks_match_their_golden_runs():
+    """The 64 batched instances come from Python's Mersenne Twister random()
+    (fixed across versions); their grids, cooling rates and site densities
+    equal those the reference ran for batched_64_golden.json."""
+    import json
+
+    from amca3d_gb300 import decks
+
+    golden = json.load(open(os.path.join(ROOT, "tests", "golden", "batched_64_golden.json")))
+    b = decks.config_batched_64()
+    assert len(b) == 64 and sorted(c.name for c in b) == sorted(golden)
+    for c in b:
+        g = golden[c.name]
+        assert list(c.cells) == g["cells"] and c.t_dot == g["t_dot"] and c.bulk[0] == g["bulk_density"]
+        assert 32 <= c.cells[0] <= 128 and -200.0 <= c.t_dot <= -5.0 and c.seed == 0
+    assert 43e6 < sum(c.n_interior for c in b) < 45e6
