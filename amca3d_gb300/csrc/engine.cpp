@@ -77,6 +77,20 @@ struct amca_t {
     return (T *)p;
   }
 
+  // The realm's buffers carved out of one allocation (one cudaMalloc and one
+  // cudaFree per realm): a sizing pass, then the same sequence handing out
+  // 256-byte-aligned pointers.
+  struct Arena {
+    char *base = nullptr;
+    size_t off = 0;
+    template <typename T>
+    T *take(size_t n) {
+      const size_t at = (off + 255) & ~(size_t)255;
+      off = at + std::max<size_t>(n, 1) * sizeof(T);
+      return base ? (T *)(base + at) : nullptr;
+    }
+  };
+
   std::string path(const std::string &p) const {
     if (p.empty() || p[0] == '/' || workdir.empty()) return p;
     return workdir + "/" + p;
@@ -158,34 +172,44 @@ struct amca_t {
     d.ncells = (int64_t)g.nxyg * g.nzg;
     d.nsites = nsites;
     d.gcap = (int64_t)c.nx * c.ny * c.nz;
-    d.orient = alloc<uint32_t>(d.ncells);
-    int32_t *site_cell = alloc<int32_t>(nsites);
-    double *site_dtc = alloc<double>(nsites);
-    d.site_live = alloc<uint8_t>(nsites);
-    double *omat = alloc<double>(nsites * 9);
-    float *omat32 = alloc<float>(nsites * 9);
+    const int64_t ntA = 2 * kStatusWords, ntB = kStatusWords;
+    int32_t *site_cell = nullptr;
+    double *site_dtc = nullptr, *omat = nullptr;
+    float *omat32 = nullptr;
+    auto layout = [&](Arena &a) {
+      d.orient = a.take<uint32_t>(d.ncells);
+      site_cell = a.take<int32_t>(nsites);
+      site_dtc = a.take<double>(nsites);
+      d.site_live = a.take<uint8_t>(nsites);
+      omat = a.take<double>(nsites * 9);
+      omat32 = a.take<float>(nsites * 9);
+      d.gx = a.take<double>(d.gcap);
+      d.gy = a.take<double>(d.gcap);
+      d.gz = a.take<double>(d.gcap);
+      d.gori = a.take<int32_t>(d.gcap);
+      d.gcell = a.take<int32_t>(d.gcap);
+      d.act0 = a.take<EnvRec>(d.gcap);
+      d.act1 = a.take<EnvRec>(d.gcap);
+      d.gen0 = a.take<EnvRec>(d.gcap);
+      d.gen1 = a.take<EnvRec>(d.gcap);
+      d.liq = a.take<uint32_t>(d.gcap);
+      d.con = a.take<uint32_t>(d.gcap);
+      d.child = a.take<uint32_t>(d.gcap);
+      d.solid = a.take<uint32_t>(solid_words(d.ncells));
+      d.claimed = a.take<uint32_t>(solid_words(d.ncells));
+      d.scanA = a.take<unsigned long long>(ntA);
+      d.scanB = a.take<unsigned long long>(ntB);
+      d.ctrl = a.take<PlainCtrl>(1);
+    };
+    Arena sizing;
+    layout(sizing);
+    Arena arena;
+    arena.base = alloc<char>(sizing.off);
+    layout(arena);
     d.site_cell = site_cell;
     d.site_dtc = site_dtc;
     d.omat = omat;
     d.omat32 = omat32;
-    d.gx = alloc<double>(d.gcap);
-    d.gy = alloc<double>(d.gcap);
-    d.gz = alloc<double>(d.gcap);
-    d.gori = alloc<int32_t>(d.gcap);
-    d.gcell = alloc<int32_t>(d.gcap);
-    d.act0 = alloc<EnvRec>(d.gcap);
-    d.act1 = alloc<EnvRec>(d.gcap);
-    d.gen0 = alloc<EnvRec>(d.gcap);
-    d.gen1 = alloc<EnvRec>(d.gcap);
-    d.liq = alloc<uint32_t>(d.gcap);
-    d.con = alloc<uint32_t>(d.gcap);
-    d.child = alloc<uint32_t>(d.gcap);
-    d.solid = alloc<uint32_t>(solid_words(d.ncells));
-    d.claimed = alloc<uint32_t>(solid_words(d.ncells));
-    const int64_t ntA = 2 * kStatusWords, ntB = kStatusWords;
-    d.scanA = alloc<unsigned long long>(ntA);
-    d.scanB = alloc<unsigned long long>(ntB);
-    d.ctrl = alloc<PlainCtrl>(1);
     ntA_ = ntA;
     ntB_ = ntB;
     if (nsites) {

@@ -28,69 +28,96 @@ int GlibcRand::next() {
 SiteSet make_sites(const PlainConfig &c, GlibcRand &rng) {
   const int nxg = c.nx + 2, nyg = c.ny + 2, nzg = c.nz + 2;
   const int64_t nxyg = (int64_t)nxg * nyg, ncells = nxyg * nzg;
-  std::unordered_map<int32_t, double> dtc_of;  // cellNucleationDT_ of the cells that hold a site
-  std::vector<int32_t> sites;
+  // every draw in draw order: (cell, dTc, population); a cell keeps the
+  // smallest dTc of its draws and counts for the population of its first
+  // draw (create_nucleation_sites' map of chosen cells, shared by both
+  // populations)
+  struct Draw {
+    int32_t cell;
+    int32_t pop;  // 0 surface, 1 bulk
+    double dtc;
+  };
+  std::vector<Draw> draws;
   SiteSet out;
   auto population = [&](double density, double mean, double sigma, bool surface) {
-    std::vector<int32_t> ids;
+    // Surface list (CA/src/CellularAutomataManager_3D.cpp:958-1000): ascending
+    // ghost-inclusive id, a face cell listed once per face it lies on (z, x,
+    // y faces). Rows with J == nx+1 are skipped: the reference tests
+    // locGhostJ against nxLocGhost_-1. A row that touches a z or y face lists
+    // all its cells, the others only their two x ends. Entry q is found from
+    // per-row counts instead of materialising the list.
+    std::vector<int64_t> row_end;  // cumulative entry count after each (K, J) row, K outer
     int64_t numCells64 = 0;
-    if (surface) {
-      // Ascending ghost-inclusive id; a face cell is listed once per face it
-      // lies on (bottom/top, then left/right, then front/rear). Rows with
-      // J == nx+1 are skipped: the reference tests locGhostJ against
-      // nxLocGhost_-1. Ghost rows never qualify, so only interior rows are
-      // walked, and of rows that touch no y/z face only their two x ends.
+    auto row_base = [&](int K, int J) { return (K == 1 || K == c.nz ? 1 : 0) + (J == 1 || J == c.ny ? 1 : 0); };
+    if (surface && density != 0.0) {  // a zero density draws no site whatever the list holds
+      row_end.reserve((size_t)c.nz * c.ny);
       for (int K = 1; K <= c.nz; ++K)
         for (int J = 1; J <= c.ny; ++J) {
-          if (J == nxg - 1) continue;
-          const bool full = K == 1 || K == c.nz || J == 1 || J == c.ny;
-          for (int I = 1; I <= c.nx; I = (full || I == c.nx) ? I + 1 : c.nx) {
-            const int32_t id = (int32_t)(K * nxyg + (int64_t)J * nxg + I);
-            if (K == 1 || K == c.nz) ids.push_back(id);
-            if (I == 1 || I == c.nx) ids.push_back(id);
-            if (J == 1 || J == c.ny) ids.push_back(id);
+          int64_t m = 0;
+          if (J != nxg - 1) {
+            const int bb = row_base(K, J);
+            m = bb > 0 ? (int64_t)bb * c.nx + (c.nx == 1 ? 1 : 2) : (c.nx == 1 ? 1 : 2);
           }
+          numCells64 += m;
+          row_end.push_back(numCells64);
         }
-      numCells64 = (int64_t)ids.size();
-    } else {
+    } else if (!surface) {
       // the bulk list is every interior cell in k, j, i order; entry q is
       // computed instead of stored
       numCells64 = (int64_t)c.nx * c.ny * c.nz;
     }
+    auto surface_cell = [&](int64_t q) {
+      const int64_t r = std::upper_bound(row_end.begin(), row_end.end(), q) - row_end.begin();
+      const int K = (int)(r / c.ny) + 1, J = (int)(r % c.ny) + 1;
+      const int64_t p = q - (r > 0 ? row_end[r - 1] : 0);
+      const int bb = row_base(K, J);
+      int I;
+      if (bb == 0 || c.nx == 1) {
+        I = (p == 0 || c.nx == 1) ? 1 : c.nx;  // the two x ends (one cell when nx == 1)
+      } else if (p < bb + 1) {
+        I = 1;  // bb + 1 entries at I = 1
+      } else if (p - (bb + 1) < (int64_t)bb * (c.nx - 2)) {
+        I = 2 + (int)((p - (bb + 1)) / bb);  // bb entries at each inner I
+      } else {
+        I = c.nx;
+      }
+      return (int32_t)(K * nxyg + (int64_t)J * nxg + I);
+    };
     auto bulk_cell = [&](int64_t q) {
       const int64_t k = q / ((int64_t)c.nx * c.ny) + 1, j = (q / c.nx) % c.ny + 1, i = q % c.nx + 1;
       return (int32_t)(k * nxyg + j * nxg + i);
     };
     const double per_cell = surface ? c.h * c.h : c.h * c.h * c.h;
     const int numCells = (int)numCells64;
-    const int numSites = round(per_cell * density * numCells) + 0.5;
+    const int numSites = density == 0.0 ? 0 : (int)(round(per_cell * density * numCells) + 0.5);
     std::default_random_engine generator;
     std::normal_distribution<double> distribution(mean, sigma);
-    int64_t generated = 0;
     if (numSites > 0 && numCells == 0) throw std::runtime_error("nucleation sites requested on an empty cell set");
+    draws.reserve(draws.size() + (size_t)std::max(numSites, 0));
     for (int s = 0; s < numSites; ++s) {
       const int q = rng.next() % numCells;
-      const int32_t cell = surface ? ids[q] : bulk_cell(q);
+      const int32_t cell = surface ? surface_cell(q) : bulk_cell(q);
       double dT = distribution(generator);
       dT = (dT < 0) ? 0 : dT;
-      auto it = dtc_of.find(cell);
-      if (it == dtc_of.end()) {
-        sites.push_back(cell);
-        dtc_of.emplace(cell, dT);
-        ++generated;
-      } else if (dT < it->second) {
-        it->second = dT;
-      }
+      draws.push_back(Draw{cell, surface ? 0 : 1, dT});
     }
-    std::sort(sites.begin(), sites.end());
-    (surface ? out.surface_sites : out.bulk_sites) = generated;
   };
   (void)ncells;
   population(c.ns, c.mu_s, c.sigma_s, true);
   population(c.nv, c.mu_v, c.sigma_v, false);
-  out.cell = sites;
-  out.dtc.resize(sites.size());
-  for (size_t i = 0; i < sites.size(); ++i) out.dtc[i] = dtc_of.at(sites[i]);
+  // ascending cell id; within a cell, draw order
+  std::stable_sort(draws.begin(), draws.end(), [](const Draw &a, const Draw &b) { return a.cell < b.cell; });
+  out.surface_sites = 0;
+  out.bulk_sites = 0;
+  for (size_t i = 0; i < draws.size();) {
+    size_t j = i + 1;
+    double dtc = draws[i].dtc;
+    for (; j < draws.size() && draws[j].cell == draws[i].cell; ++j) dtc = std::min(dtc, draws[j].dtc);
+    out.cell.push_back(draws[i].cell);
+    out.dtc.push_back(dtc);
+    (draws[i].pop == 0 ? out.surface_sites : out.bulk_sites) += 1;
+    i = j;
+  }
   return out;
 }
 
@@ -128,8 +155,10 @@ namespace {
 // Run body(lo, hi) over [0, n) on up to hardware_concurrency threads.
 template <typename F>
 void parallel_ranges(int64_t n, F body) {
+  // one thread per 2048 items at most: the per-item work (glibc libm
+  // trigonometry) is a few hundred ns, a thread start a few tens of us
   unsigned nt = std::max(1u, std::thread::hardware_concurrency());
-  if (n < 65536) nt = 1;
+  nt = (unsigned)std::min<int64_t>(nt, std::max<int64_t>(1, n / 2048));
   nt = (unsigned)std::min<int64_t>(nt, 64);
   std::vector<std::thread> th;
   const int64_t chunk = (n + nt - 1) / nt;
