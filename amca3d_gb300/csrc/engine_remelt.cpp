@@ -129,34 +129,29 @@ void RemeltRealm::prepare() {
   orient0_.assign((size_t)N, -1);
   grain0_.assign((size_t)N, -1);
   melted0_.assign((size_t)N, cfg_.initial_melted ? 1 : 0);
-  rec0_.assign(4 * (size_t)N, 0.0);
   gori0_.assign((size_t)N, -1);
   site_field_.assign((size_t)N, -1.0);
   grain_cell_.clear();
   grain_ori0_.clear();
-  auto centre = [&](int64_t cell, double out[3]) {
-    const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
-    out[0] = centre_coord(c.x0, c.h, I);
-    out[1] = centre_coord(c.y0, c.h, J);
-    out[2] = centre_coord(c.z0, c.h, K);
-  };
   if (cfg_.random_micro && !micro_) {
     // random_microstructure_information (CellularAutomataManager_3D.cpp:1929-1984):
     // one orientation and one grain per interior cell, in cell order
     const int64_t M = (int64_t)c.nx * c.ny * c.nz;
     otab_ = make_orientations(M, *rng_);
     int64_t q = 0;
-    for (int64_t cell = 0; cell < N; ++cell) {
-      const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
-      if (is_ghost(I, J, K, nxg, nyg, nzg)) continue;
-      orient0_[cell] = (int32_t)q;
-      grain0_[cell] = (int32_t)q;
-      gori0_[cell] = (int32_t)q;
-      centre(cell, &rec0_[4 * cell]);
-      grain_cell_.push_back((int32_t)cell);
-      grain_ori0_.push_back((int32_t)q);
-      ++q;
-    }
+    grain_cell_.reserve((size_t)M);
+    grain_ori0_.reserve((size_t)M);
+    for (int K = 1; K < nzg - 1; ++K)
+      for (int J = 1; J < nyg - 1; ++J)
+        for (int I = 1; I < nxg - 1; ++I) {
+          const int64_t cell = K * nxyg + (int64_t)J * nxg + I;
+          orient0_[cell] = (int32_t)q;
+          grain0_[cell] = (int32_t)q;
+          gori0_[cell] = (int32_t)q;
+          grain_cell_.push_back((int32_t)cell);
+          grain_ori0_.push_back((int32_t)q);
+          ++q;
+        }
     n_init_orient_ = M;
     n_init_grains_ = M;
     if (c.shuffle_vtr) mapped_vtr_ = make_mapped_ids(N, true, *rng_);
@@ -164,7 +159,9 @@ void RemeltRealm::prepare() {
   } else {
     // load_microstructure_information + retrieve_grain_information_before_simulation
     // (CellularAutomataManager_3DRemelting.cpp:164-332)
-    RestartData r = micro_ ? *micro_ : read_restart(path(cfg_.micro_file));
+    RestartData loaded;
+    if (!micro_) loaded = read_restart(path(cfg_.micro_file));
+    const RestartData &r = micro_ ? *micro_ : loaded;
     if (r.ncells != N)
       throw std::runtime_error("Error : microstructure information file is not fit the current domain size");
     if (!cfg_.nucleation && c.shuffle_vtr) mapped_vtr_ = make_mapped_ids(r.expected, true, *rng_);
@@ -175,25 +172,28 @@ void RemeltRealm::prepare() {
     grain_cell_ = r.gcell;
     grain_ori0_ = r.gori;
     std::vector<uint8_t> owned((size_t)r.ngrains, 0);
-    for (int64_t cell = 0; cell < N; ++cell) {
-      const int K = (int)(cell / nxyg), J = (int)((cell % nxyg) / nxg), I = (int)((cell % nxyg) % nxg);
-      if (is_ghost(I, J, K, nxg, nyg, nzg)) {
-        orient0_[cell] = -1;
-        continue;
-      }
-      const int32_t g = grain0_[cell];
-      if (g >= 0) {
-        if (g >= r.ngrains) throw std::runtime_error("restart cell refers to a grain that is not listed");
-        if (owned[g] || r.gcell[g] != cell)
-          throw std::runtime_error("restart grains must each belong to the one interior cell that refers to them");
-        owned[g] = 1;
-        centre(cell, &rec0_[4 * cell]);  // grain centre reset to its cell centre, length 0 (:289-296)
-        gori0_[cell] = r.gori[g];
-      }
-      if (orient0_[cell] > -1) continue;
-      if (g < 0) throw std::runtime_error("restart cell has neither an orientation nor a grain");
-      orient0_[cell] = r.gori[g];
-    }
+    for (int K = 0; K < nzg; ++K)
+      for (int J = 0; J < nyg; ++J)
+        for (int I = 0; I < nxg; ++I) {
+          const int64_t cell = K * nxyg + (int64_t)J * nxg + I;
+          if (is_ghost(I, J, K, nxg, nyg, nzg)) {
+            orient0_[cell] = -1;
+            continue;
+          }
+          const int32_t g = grain0_[cell];
+          if (g >= 0) {
+            if (g >= r.ngrains) throw std::runtime_error("restart cell refers to a grain that is not listed");
+            if (owned[g] || r.gcell[g] != cell)
+              throw std::runtime_error("restart grains must each belong to the one interior cell that refers to them");
+            owned[g] = 1;
+            // the grain's centre is reset to its cell centre, length 0
+            // (:289-296): remelt_init_records on the device
+            gori0_[cell] = r.gori[g];
+          }
+          if (orient0_[cell] > -1) continue;
+          if (g < 0) throw std::runtime_error("restart cell has neither an orientation nor a grain");
+          orient0_[cell] = r.gori[g];
+        }
     n_init_orient_ = r.norient;
     n_init_grains_ = r.ngrains;
     expected_grains_ = r.expected;
@@ -223,17 +223,7 @@ void RemeltRealm::upload_initial_state() {
   h2d(dev_.orient, orient0_.data(), N * 4);
   h2d(dev_.grain, grain0_.data(), N * 4);
   h2d(dev_.melted, melted0_.data(), N);
-  std::vector<double> x((size_t)N), y((size_t)N), z((size_t)N), l((size_t)N);
-  for (int64_t i = 0; i < N; ++i) {
-    x[i] = rec0_[4 * i];
-    y[i] = rec0_[4 * i + 1];
-    z[i] = rec0_[4 * i + 2];
-    l[i] = rec0_[4 * i + 3];
-  }
-  h2d(dev_.gx, x.data(), N * 8);
-  h2d(dev_.gy, y.data(), N * 8);
-  h2d(dev_.gz, z.data(), N * 8);
-  h2d(dev_.glen, l.data(), N * 8);
+  RCK(remelt_init_records(dev_, stream_));  // from the grain field just uploaded
   h2d(dev_.gori, gori0_.data(), N * 4);
   RCK(cudaMemsetAsync(dev_.gdx, 0, N * 4, stream_));
   RCK(cudaMemsetAsync(dev_.gdy, 0, N * 4, stream_));

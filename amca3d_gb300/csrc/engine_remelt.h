@@ -102,7 +102,6 @@ class RemeltRealm {
   std::vector<int32_t> mapped_vtr_;
   std::vector<int32_t> orient0_, grain0_;  // initial cell fields
   std::vector<uint8_t> melted0_;
-  std::vector<double> rec0_;       // initial grain records per cell: x, y, z, length
   std::vector<int32_t> gori0_;
   std::vector<int32_t> grain_cell_;  // grain id -> owning cell (restart + created)
   std::vector<int32_t> grain_ori0_;  // grain id -> initial orientation

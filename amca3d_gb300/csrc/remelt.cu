@@ -701,6 +701,30 @@ cudaError_t remelt_round_coords(const double *pc, float *pc32, int64_t n, cudaSt
   return cudaGetLastError();
 }
 
+// Initial grain records: an interior cell that holds a grain gets its
+// cell's centre and length 0 (the record of a freshly read or random
+// microstructure), every other cell zeros.
+__global__ void init_records_kernel(RemeltDevice d) {
+  const Grid &g = d.g;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < d.ncells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int I, J, K;
+    cell_ijk(g, c, I, J, K);
+    const bool has = !ghost(g, I, J, K) && d.grain[c] >= 0;
+    d.gx[c] = has ? centre_coord(g.x0, g.h, I) : 0.0;
+    d.gy[c] = has ? centre_coord(g.y0, g.h, J) : 0.0;
+    d.gz[c] = has ? centre_coord(g.z0, g.h, K) : 0.0;
+    d.glen[c] = 0.0;
+  }
+}
+
+cudaError_t remelt_init_records(const RemeltDevice &d, cudaStream_t s) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  init_records_kernel<<<sms > 0 ? 4 * sms : 256, 256, 0, s>>>(d);
+  return cudaGetLastError();
+}
+
 cudaError_t remelt_init_theta(const RemeltDevice &d, cudaStream_t s) {
   const int64_t n = std::max<int64_t>(d.nnodes, d.nelem);
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);

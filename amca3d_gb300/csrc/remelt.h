@@ -181,6 +181,11 @@ cudaError_t remelt_round_coords(const double *pc, float *pc32, int64_t n, cudaSt
 // Frame-0 node temperatures and element bounds before the first step.
 cudaError_t remelt_init_theta(const RemeltDevice &d, cudaStream_t s);
 
+// Grain records (centre, half-diagonal) of the initial microstructure from
+// the grain field already on the device: cell centre and length 0 for every
+// interior cell that holds a grain, zeros elsewhere.
+cudaError_t remelt_init_records(const RemeltDevice &d, cudaStream_t s);
+
 // Grid size for the persistent kernel: per_sm co-resident blocks per SM (at
 // most what fits).
 int remelt_persistent_grid(int device, int per_sm);
