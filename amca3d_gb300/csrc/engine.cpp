@@ -931,10 +931,7 @@ int amca_set_microstructure(amca_t *h, const int32_t *grain, const int32_t *orie
       r.melted.assign(melted, melted + N);
     else
       r.melted.assign((size_t)N, 0);
-    if (dtc)
-      r.dtc.assign(dtc, dtc + N);
-    else
-      r.dtc.assign((size_t)N, -1.0);
+    if (dtc) r.dtc.assign(dtc, dtc + N);  // kept for completeness: the realm draws its own sites
     r.euler.assign(euler, euler + 3 * norient);
     r.gcell.assign(grain_cell, grain_cell + ngrains);
     r.gori.assign(grain_orient, grain_orient + ngrains);
