@@ -63,11 +63,6 @@ __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long l
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 template <typename T>
 __device__ __forceinline__ T ld_volatile(const T *p) {
   return *(const volatile T *)p;
