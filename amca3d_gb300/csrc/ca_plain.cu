@@ -236,13 +236,19 @@ __device__ __forceinline__ void block_chunk(long long n, long long &b, long long
 // of 32 (one rank per lane), so the warps that finish last are at most one
 // short chunk behind. Lane 0 calls it; returns (b, e), or b = -1 when none
 // is left.
-__device__ __noinline__ longlong2 next_warp_chunk(long long n, unsigned long long *counter) {
+// A warp's first chunk is its own, numbered across blocks first (warp w of
+// block b takes chunk w * blocks + b, so a small generation spreads over
+// every SM) and taken without an atomic (a generation smaller than one chunk
+// per warp costs no counter traffic); later ones come from the counter,
+// numbered after those.
+__device__ __noinline__ longlong2 next_warp_chunk(long long n, unsigned long long *counter, bool first) {
   const long long warps = (long long)t_nb * kWarps;
   long long big = (((n + 2 * warps - 1) / (2 * warps)) + 31) & ~31ll;
   big = big < 32 ? 32 : (big > 256 ? 256 : big);
   const long long head = n - 32 * warps;
   const long long nbig = head > 0 ? head / big : 0, split = nbig * big;
-  const long long q = (long long)atomicAdd(counter, 1ull);
+  const long long q =
+      first ? (long long)(threadIdx.x >> 5) * t_nb + t_b : warps + (long long)atomicAdd(counter, 1ull);
   long long b, e;
   if (q < nbig) {
     b = q * big;
@@ -308,12 +314,13 @@ struct RankSched {
   unsigned long long *counter;
   int *error;
   bool warp;
+  bool own_chunk = true;  // warp mode: the first chunk is the warp's own
   __device__ RankSched(long long n_, unsigned long long *c, int *err)
       : n(n_), counter(c), error(err), warp(t_nb <= 64 || n_ <= 1024ll * t_nb) {
     if (!warp) {
       if (threadIdx.x == 0) {
         set_block_chunks(n);
-        s_pool = atomicAdd(counter, 1ull) << 32;
+        s_pool = (unsigned long long)t_b << 32;  // the block's first chunk is its own index
       }
       __syncthreads();
     }
@@ -323,7 +330,8 @@ struct RankSched {
     const int lane = threadIdx.x & 31;
     if (warp) {
       longlong2 c = make_longlong2(0, 0);
-      if (lane == 0) c = next_warp_chunk(n, counter);
+      if (lane == 0) c = next_warp_chunk(n, counter, own_chunk);
+      own_chunk = false;
       b = __shfl_sync(0xffffffffu, c.x, 0);
       e = __shfl_sync(0xffffffffu, c.y, 0);
       return b >= 0;
@@ -343,7 +351,7 @@ struct RankSched {
         return true;
       }
       if (off < len + 32) {  // this warp's piece starts at the chunk's end: it takes the next chunk
-        if (lane == 0) atomicExch(&s_pool, atomicAdd(counter, 1ull) << 32);
+        if (lane == 0) atomicExch(&s_pool, ((unsigned long long)t_nb + atomicAdd(counter, 1ull)) << 32);
         __syncwarp();
         continue;
       }
