@@ -746,6 +746,10 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   bool ok = true;
   const bool timer = t_b == 0 && threadIdx.x == 0;
   unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
+  // per-block busy time (thread 0), added to the control block once per
+  // launch; the per-phase maximum is raised only by a block that exceeds it
+  // (same-address atomics from every block serialise)
+  unsigned long long claim_busy = 0, resolve_busy = 0;
   while (!done && time < d.final_time && step < step_limit) {
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
     EnvRec *act = cur ? d.act1 : d.act0;
@@ -776,8 +780,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
-        atomicAdd(&c->ns_claim_work_sum, w);
-        atomicMax(&c->phase_max_scratch[0], w);
+        claim_busy += w;
+        if (w > ld_volatile(&c->phase_max_scratch[0])) atomicMax(&c->phase_max_scratch[0], w);
       }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
@@ -802,8 +806,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       if (!(ok = resolve_phase(d, n, step, gen & 1u, list, next_act, smem))) break;
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work + w_mark;
-        atomicAdd(&c->ns_resolve_work_sum, w);
-        atomicMax(&c->phase_max_scratch[1], w);
+        resolve_busy += w;
+        if (w > ld_volatile(&c->phase_max_scratch[1])) atomicMax(&c->phase_max_scratch[1], w);
       }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
@@ -853,6 +857,10 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     live += __shfl_down_sync(0xffffffffu, live, o);
   }
   if ((threadIdx.x & 31) == 0) {
+    if (threadIdx.x == 0) {
+      if (claim_busy) atomicAdd(&c->ns_claim_work_sum, claim_busy);
+      if (resolve_busy) atomicAdd(&c->ns_resolve_work_sum, resolve_busy);
+    }
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);
     if (live) atomicAdd(&c->sites_scanned, live);
