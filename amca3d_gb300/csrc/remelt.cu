@@ -68,8 +68,11 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
   return *(const volatile T *)p;
 }
 
-// When this block left its last grid barrier (thread 0).
+// When this block left its last grid barrier (thread 0), and its busy time
+// per barrier kind, added to the control block once per launch
+// (same-address atomics from every block at every barrier would serialise).
 __shared__ unsigned long long s_left;
+__shared__ unsigned long long s_busy[6];
 
 // Sense-counting grid barrier bounded in time; false when a wait ran out or
 // another block reported an error. `p` names the work it closes (see
@@ -79,8 +82,8 @@ __device__ bool grid_barrier(RemeltCtrl *c, int p) {
   if (threadIdx.x == 0) {
     const unsigned long long tb = now_ns();
     const unsigned long long w = tb - s_left;
-    atomicAdd(&c->ns_work_sum[p], w);
-    atomicMax(&c->work_scratch[p], w);
+    s_busy[p] += w;
+    if (w > ld_volatile(&c->work_scratch[p])) atomicMax(&c->work_scratch[p], w);
     // (bar_count, bar_gen) as one 64-bit word, generation in the high half:
     // an arrival is one atomicAdd; the last one resets the count and opens
     // the next generation with one more
@@ -960,7 +963,10 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
   const int64_t nyzg = (int64_t)g.nyg * g.nzg;
   unsigned long long tests = 0, tests64 = 0, caps = 0, exactT = 0, melts = 0, visited = 0, eactive = 0;
   bool ok = true;
-  if (tid == 0) s_left = now_ns();
+  if (tid == 0) {
+    s_left = now_ns();
+    for (int i = 0; i < 6; ++i) s_busy[i] = 0ull;
+  }
   for (;;) {
     const StepScalars S = read_scalars(c);
     // --- loop condition of time_integration_weak_coupling (CafeSolver.cpp:188) and launch limits ---
@@ -1075,7 +1081,10 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
       }
     }
     __syncthreads();
-    if (tid == 0) atomicMax(&c->flags_scratch, now_ns() - tfl);
+    if (tid == 0) {
+      const unsigned long long w = now_ns() - tfl;
+      if (w > ld_volatile(&c->flags_scratch)) atomicMax(&c->flags_scratch, w);
+    }
     // site conditions of nucleate_at_nucleation_sites (Remelting.cpp:946-960), all blocks
     // (only a liquid, melted cell can nucleate: the temperatures are
     // evaluated for those alone)
@@ -1187,7 +1196,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
             best = k < best ? k : best;
           }
         }
-        if (best < key_tm) atomicMin(&c->minT_key, best);
+        if (best < key_tm && best < ld_volatile(&c->minT_key)) atomicMin(&c->minT_key, best);
       }
     }
     if (gtid == 0) {
@@ -1448,6 +1457,9 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     if (ld_volatile(&c->status) == kRemeltFramesEnd) break;
   }
   if (ok && blockIdx.x == 0) assign_new_grains(d, c);
+  if (tid == 0)
+    for (int i = 0; i < 6; ++i)
+      if (s_busy[i]) atomicAdd(&c->ns_work_sum[i], s_busy[i]);
   if (tests) atomicAdd(&c->tests, tests);
   if (tests64) atomicAdd(&c->tests64, tests64);
   if (caps) atomicAdd(&c->captures, caps);
