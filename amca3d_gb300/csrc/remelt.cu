@@ -154,6 +154,38 @@ __device__ __forceinline__ unsigned append_slot(unsigned *counter) {
   return grp.shfl(base, 0) + grp.thread_rank();
 }
 
+// Block-staged list appends: entries go to a shared-memory buffer (shared
+// atomic), and the block moves the buffer to the global list with one
+// global atomicAdd when the phase ends (stage_flush, every thread) — one
+// same-address global atomic per block instead of one per warp and
+// iteration. Entries beyond the buffer go to the global list directly.
+constexpr unsigned kStage = 1024;
+__shared__ unsigned s_stage_n;
+__shared__ int32_t s_stage[kStage];
+
+__device__ __forceinline__ void stage_push(int32_t v, unsigned *count, int32_t *list, unsigned cap) {
+  const unsigned k = atomicAdd(&s_stage_n, 1u);
+  if (k < kStage) {
+    s_stage[k] = v;
+  } else {
+    const unsigned slot = atomicAdd(count, 1u);
+    if (slot < cap) list[slot] = v;
+  }
+}
+
+__device__ void stage_flush(unsigned *count, int32_t *list, unsigned cap) {
+  __shared__ unsigned s_base;
+  __syncthreads();
+  const unsigned n = min(s_stage_n, kStage);
+  if (threadIdx.x == 0) s_base = n ? atomicAdd(count, n) : 0u;
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < n; i += blockDim.x)
+    if (s_base + i < cap) list[s_base + i] = s_stage[i];
+  __syncthreads();
+  if (threadIdx.x == 0) s_stage_n = 0u;
+  __syncthreads();
+}
+
 // `cnt` consecutive list slots for each thread that reaches it together: one
 // atomicAdd per coalesced group, the group's counts placed by an inclusive
 // scan (order within a list is free).
@@ -943,10 +975,7 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   if (!wm2) m1 = 0;
   if (m1 != m0) d.melted[cell] = m1;
   d.tcls[cell] = (uint8_t)((flags ? kTlt : 0) | (le ? kTle : 0) | (gtn ? kTgtNull : 0) | (wm2 ? kTgeNullPlus : 0));
-  if (wm2 && flags) {  // the cell flags its solid neighbours
-    const unsigned slot = append_slot(&c->n_liq);
-    if (slot < d.list_cap) d.liq[slot] = (int32_t)cell;
-  }
+  if (wm2 && flags) stage_push((int32_t)cell, &c->n_liq, d.liq, d.list_cap);  // the cell flags its solid neighbours
 }
 
 // Register budget of two blocks per SM (128 per thread), run with one block
@@ -966,6 +995,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
   if (tid == 0) {
     s_left = now_ns();
     for (int i = 0; i < 6; ++i) s_busy[i] = 0ull;
+    s_stage_n = 0u;
   }
   for (;;) {
     const StepScalars S = read_scalars(c);
@@ -1025,6 +1055,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         }
       }
     }
+    stage_flush(&c->n_liq, d.liq, d.list_cap);
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
       atomicAdd(&c->ns_phase[0], t1 - t_phase);
