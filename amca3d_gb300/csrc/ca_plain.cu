@@ -247,6 +247,8 @@ __device__ __noinline__ longlong2 next_warp_chunk(long long n, unsigned long lon
   big = big < 32 ? 32 : (big > 256 ? 256 : big);
   const long long head = n - 32 * warps;
   const long long nbig = head > 0 ? head / big : 0, split = nbig * big;
+  // when every chunk is some warp's own, the counter has none to give
+  if (!first && nbig + (n - split + 31) / 32 <= warps) return make_longlong2(-1, -1);
   const long long q =
       first ? (long long)(threadIdx.x >> 5) * t_nb + t_b : warps + (long long)atomicAdd(counter, 1ull);
   long long b, e;
