@@ -406,16 +406,50 @@ __device__ __forceinline__ uint32_t liquid_neighbours(const uint32_t *solid, con
   return ~neighbour_bits(solid, g, cell) & 0x03ffffffu;
 }
 
+// Nucleus number r (in site order) of this step on `cell`: orientation,
+// envelope table entry and active-list record (CellularAutomataManager.cpp:262-290).
+__device__ __forceinline__ void place_nucleus(const PlainDevice &d, EnvRec *act, long long base_act,
+                                              long long base_orient, long long base_grain, long long r, int cell) {
+  const int oid = (int)(base_orient + r);
+  const long long gid = base_grain + r;
+  int I, J, K;
+  cell_ijk(d.grid, cell, I, J, K);
+  d.orient[cell] = (uint32_t)oid;
+  set_solid(d.solid, cell);
+  d.gx[gid] = centre_coord(d.grid.x0, d.grid.h, I);
+  d.gy[gid] = centre_coord(d.grid.y0, d.grid.h, J);
+  d.gz[gid] = centre_coord(d.grid.z0, d.grid.h, K);
+  d.gori[gid] = oid;
+  d.gcell[gid] = cell;
+  EnvRec en;  // a nucleus: length 0, centred on its cell
+  en.L = 0.0;
+  en.dx = en.dy = en.dz = 0.f;
+  en.cell = cell;
+  en.ori = oid;
+  en.id = (int32_t)gid;
+  act[base_act + r] = en;
+}
+
+// Sites are held as tiles of kBlock, one per block, when they fit: tile t =
+// sites [t*kBlock, (t+1)*kBlock), thread i of block t owns site t*kBlock + i
+// for the whole launch and keeps its cell (-1 once removed) and dTc in shared
+// memory.
+__device__ __forceinline__ bool site_tiles(const PlainDevice &d) { return d.nsites <= (long long)kBlock * t_nb; }
+
 // ---------------------------------------------------------------------------
 // Nucleation (CellularAutomataManager.cpp:219-297) in site order.
-// Pass 1 marks sites (2 = nucleates now, 0 = removed), pass 2 hands out
-// orientation / envelope ids in site order.
+// Tiled sites: one pass, nucleus ranks from one block scan plus the look-back
+// over the site tiles. Otherwise pass 1 marks sites (2 = nucleates now, 0 =
+// removed) and pass 2 hands out orientation / envelope ids in site order.
+// The counts that every block tracks itself (orientations, envelope ids,
+// liquid cells) are not read here; the last site tile publishes the active
+// count in the step's parity slot (a step without envelopes has no barrier
+// before the next nucleation), which every block reads after the barrier.
 // ---------------------------------------------------------------------------
 __device__ bool nucleation_phase(const PlainDevice &d, double time, long long step, long long base_act,
-                                 EnvRec *act, unsigned long long *smem, unsigned long long *stat_live) {
+                                 long long base_orient, long long base_grain, EnvRec *act, int *s_cell,
+                                 double *s_dtc, unsigned long long *smem, unsigned long long *stat_live) {
   PlainCtrl *c = d.ctrl;
-  const long long base_orient = ld_volatile(&c->n_orient);
-  const long long base_grain = ld_volatile(&c->next_grain);
   unsigned long long *scan = d.scanA + (step & 1) * kStatusWords;
   const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
   const double dTu = d.Tm - T;
@@ -435,7 +469,31 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
     c->dt_active[step & 1] = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
     c->dt_none[step & 1] = (d.max_dt < b) ? d.max_dt : b;
   }
-  __threadfence();
+  if (site_tiles(d)) {
+    const long long ntiles = (d.nsites + kBlock - 1) / kBlock;
+    if (t_b >= ntiles) {  // no sites in this block
+      if (ntiles == 0 && t_b == 0 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_act;
+      return true;
+    }
+    const int cell = s_cell[threadIdx.x];
+    unsigned nuc = 0;
+    if (cell >= 0) {
+      ++*stat_live;
+      const bool liquid = d.orient[cell] == kLiquid;
+      nuc = liquid && dTu > s_dtc[threadIdx.x];
+      if (!liquid || nuc) {  // removed from the site list
+        s_cell[threadIdx.x] = -1;
+        d.site_live[(long long)t_b * kBlock + threadIdx.x] = 0;
+      }
+    }
+    unsigned long long agg;
+    const unsigned long long ex = block_exclusive_scan(nuc, smem, &agg);
+    const unsigned long long pre = block_prefix(scan, agg, smem, c);
+    if (pre == ~0ull) return false;
+    if (nuc) place_nucleus(d, act, base_act, base_orient, base_grain, (long long)(pre + ex), cell);
+    if (t_b == ntiles - 1 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_act + (long long)(pre + agg);
+    return true;
+  }
   long long b, e;
   block_chunk(d.nsites, b, e);
   unsigned long long count = 0;
@@ -463,37 +521,10 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
     }
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan(nuc, smem, &tot);
-    if (nuc) {
-      const long long r = (long long)(run + ex);
-      const int oid = (int)(base_orient + r);
-      const long long gid = base_grain + r;
-      int I, J, K;
-      cell_ijk(d.grid, cell, I, J, K);
-      d.orient[cell] = (uint32_t)oid;
-      set_solid(d.solid, cell);
-      d.gx[gid] = centre_coord(d.grid.x0, d.grid.h, I);
-      d.gy[gid] = centre_coord(d.grid.y0, d.grid.h, J);
-      d.gz[gid] = centre_coord(d.grid.z0, d.grid.h, K);
-      d.gori[gid] = oid;
-      d.gcell[gid] = cell;
-      EnvRec en;  // a nucleus: length 0, centred on its cell
-      en.L = 0.0;
-      en.dx = en.dy = en.dz = 0.f;
-      en.cell = cell;
-      en.ori = oid;
-      en.id = (int32_t)gid;
-      act[base_act + r] = en;
-    }
+    if (nuc) place_nucleus(d, act, base_act, base_orient, base_grain, (long long)(run + ex), cell);
     run += tot;
   }
-  if (t_b == t_nb - 1 && threadIdx.x == 0) {
-    const long long total = (long long)(pre + agg);
-    c->n_orient = base_orient + total;
-    c->next_grain = base_grain + total;
-    c->n_active = base_act + total;
-    c->liquid -= total;
-    c->nucleations += (unsigned long long)total;
-  }
+  if (t_b == t_nb - 1 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_act + (long long)(pre + agg);
   return true;
 }
 
@@ -673,13 +704,12 @@ __device__ __forceinline__ bool mark_in_resolve(long long n) { return n <= (long
 // survivors' places in the next active list. Marking reads only claim words,
 // the claimed bitmap and its own ranks' masks, none of which another block's
 // resolve writes, so no barrier separates the two passes.
+// base_next = survivors placed by this step's earlier generations; the last
+// block publishes the generation's capture count and the new survivor count,
+// which every block reads after the barrier.
 __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step, unsigned par, const EnvRec *cur,
-                              EnvRec *next_act, unsigned long long *smem) {
+                              EnvRec *next_act, long long base_next, unsigned long long *smem) {
   PlainCtrl *c = d.ctrl;
-  long long *n_next = &c->n_active_next[step & 1];
-  const long long base_grain = ld_volatile(&c->next_grain);
-  const long long base_next = ld_volatile(n_next);
-  __threadfence();
   long long b, e;
   block_chunk(n, b, e);
   unsigned long long acc = 0;
@@ -723,13 +753,8 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   }
   if (t_b == t_nb - 1 && threadIdx.x == 0) {
     const unsigned long long total = pre + agg;
-    const long long caps = (long long)(total >> 32), survs = (long long)(total & 0xffffffffull);
-    c->gen_lo = base_grain;
-    c->gen_n = caps;
-    c->next_grain = base_grain + caps;
-    *n_next = base_next + survs;
-    c->liquid -= caps;
-    c->captures += (unsigned long long)caps;
+    c->gen_n = (long long)(total >> 32);
+    c->n_active_next[step & 1] = base_next + (long long)(total & 0xffffffffull);
   }
   return true;
 }
@@ -737,41 +762,61 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
 // Whole CA steps of one realm by the current team, until it is solid, its
 // termination time, or step_limit.
 __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned long long *smem) {
+  // block 0's phase clock and step counters (its thread 0 only), added to
+  // the control block once per launch
+  enum { kNuc, kClaim, kClaim0, kResolve, kClaimMax, kResolveMax, kGens, kGrown, kProc, kCaps, kNucs, kClk };
+  __shared__ unsigned long long s_clk[kClk];
+  // this block's tile of sites when they are tiled (cell -1: removed, or no site)
+  __shared__ int s_cell[kBlock];
+  __shared__ double s_dtc[kBlock];
   PlainCtrl *c = d.ctrl;
   unsigned long long tests = 0, tests64 = 0, live = 0;
-  // per-step state, identical in every thread (read once, then advanced locally)
+  // per-step state, identical in every thread (read once, then advanced
+  // locally from the counts that the last block of a phase publishes)
   long long step = ld_volatile(&c->step);
   double time = ld_volatile(&c->time), dt = ld_volatile(&c->dt);
   long long n_act = ld_volatile(&c->n_active);
+  long long n_orient = ld_volatile(&c->n_orient), grain = ld_volatile(&c->next_grain);
+  long long liquid = ld_volatile(&c->liquid);
   int cur = ld_volatile(&c->cur_list);
   bool done = ld_volatile(&c->done) != 0;
   bool ok = true;
+  if (site_tiles(d)) {
+    const long long i = (long long)t_b * kBlock + threadIdx.x;
+    const bool on = i < d.nsites && d.site_live[i] != 0;
+    s_cell[threadIdx.x] = on ? d.site_cell[i] : -1;
+    s_dtc[threadIdx.x] = on ? d.site_dtc[i] : 0.0;
+  }
   const bool timer = t_b == 0 && threadIdx.x == 0;
+  if (timer)
+    for (int k = 0; k < kClk; ++k) s_clk[k] = 0ull;
   unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
   // per-block busy time (thread 0), added to the control block once per
-  // launch; the per-phase maximum is raised only by a block that exceeds it
-  // (same-address atomics from every block serialise)
+  // launch; with phase_detail the per-phase maximum is raised only by a block
+  // that exceeds it (same-address atomics from every block serialise)
   unsigned long long claim_busy = 0, resolve_busy = 0;
   while (!done && time < d.final_time && step < step_limit) {
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
     EnvRec *act = cur ? d.act1 : d.act0;
     EnvRec *next_act = cur ? d.act0 : d.act1;
-    if (!(ok = nucleation_phase(d, time, step, n_act, act, smem, &live))) break;
+    if (!(ok = nucleation_phase(d, time, step, n_act, n_orient, grain, act, s_cell, s_dtc, smem, &live))) break;
     if (!(ok = grid_barrier(c))) break;
     if (timer) {
       t_now = now_ns();
-      c->ns_nucleation += t_now - t_mark;
+      s_clk[kNuc] += t_now - t_mark;
       t_mark = t_now;
-      // next step's survivor count starts at zero; every block read it last
-      // at the end of the previous step, before this barrier
-      c->n_active_next[(step + 1) & 1] = 0;
     }
-    const long long nA = ld_volatile(&c->n_active);
+    const long long nA = ld_volatile(&c->n_active_nuc[step & 1]);
     const double vel = ld_volatile(&c->vel[step & 1]);
     dt = nA > 0 ? ld_volatile(&c->dt_active[step & 1]) : ld_volatile(&c->dt_none[step & 1]);
+    const long long nucs = nA - n_act;  // nuclei of this step
+    n_orient += nucs;
+    grain += nucs;
+    liquid -= nucs;
+    if (timer) s_clk[kNucs] += (unsigned long long)nucs;
 
     // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
-    long long n = nA, lo = 0, processed = 0;
+    long long n = nA, lo = 0, processed = 0, n_next = 0;
     int kind = 0;
     unsigned gen = 0;
     EnvRec *list = act, *parents = nullptr;  // records of this generation / of its parents
@@ -783,16 +828,18 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
         claim_busy += w;
-        if (w > ld_volatile(&c->phase_max_scratch[0])) atomicMax(&c->phase_max_scratch[0], w);
+        if (d.phase_detail && w > ld_volatile(&c->phase_max_scratch[0])) atomicMax(&c->phase_max_scratch[0], w);
       }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
         t_now = now_ns();
-        c->ns_claim += t_now - t_mark;
-        if (gen == 0) c->ns_claim_gen0 += t_now - t_mark;
+        s_clk[kClaim] += t_now - t_mark;
+        if (gen == 0) s_clk[kClaim0] += t_now - t_mark;
         t_mark = t_now;
-        c->ns_claim_work_max += c->phase_max_scratch[0];
-        c->phase_max_scratch[0] = 0ull;
+        if (d.phase_detail) {
+          s_clk[kClaimMax] += ld_volatile(&c->phase_max_scratch[0]);
+          c->phase_max_scratch[0] = 0ull;
+        }
         c->claim_next = 0ull;  // the next claim phase is two barriers away
       }
       t_work = threadIdx.x == 0 ? now_ns() : 0ull;
@@ -805,22 +852,29 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         if (timer) c->mark_next = 0ull;  // the next marking pass is two barriers away
         t_work = threadIdx.x == 0 ? now_ns() : 0ull;
       }
-      if (!(ok = resolve_phase(d, n, step, gen & 1u, list, next_act, smem))) break;
+      if (!(ok = resolve_phase(d, n, step, gen & 1u, list, next_act, n_next, smem))) break;
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work + w_mark;
         resolve_busy += w;
-        if (w > ld_volatile(&c->phase_max_scratch[1])) atomicMax(&c->phase_max_scratch[1], w);
+        if (d.phase_detail && w > ld_volatile(&c->phase_max_scratch[1])) atomicMax(&c->phase_max_scratch[1], w);
       }
       if (!(ok = grid_barrier(c))) break;
       if (timer) {
         t_now = now_ns();
-        c->ns_resolve += t_now - t_mark;
+        s_clk[kResolve] += t_now - t_mark;
         t_mark = t_now;
-        c->ns_resolve_work_max += c->phase_max_scratch[1];
-        c->phase_max_scratch[1] = 0ull;
+        if (d.phase_detail) {
+          s_clk[kResolveMax] += ld_volatile(&c->phase_max_scratch[1]);
+          c->phase_max_scratch[1] = 0ull;
+        }
       }
-      n = ld_volatile(&c->gen_n);
-      lo = ld_volatile(&c->gen_lo);
+      const long long caps = ld_volatile(&c->gen_n);  // envelopes of the next generation
+      n_next = ld_volatile(&c->n_active_next[step & 1]);
+      lo = grain;  // their ids follow on
+      grain += caps;
+      liquid -= caps;
+      if (timer) s_clk[kCaps] += (unsigned long long)caps;
+      n = caps;
       kind = 1;
       ++gen;
       parents = list;
@@ -828,17 +882,16 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     }
     if (!ok) break;
     // step end (CellularAutomataManager_3D.cpp:653-659): every block advances
-    // the same locals; the survivors' count was published before the last
-    // barrier, so no further barrier is needed
-    n_act = ld_volatile(&c->n_active_next[step & 1]);
+    // the same locals, so no further barrier is needed
+    n_act = n_next;
     cur ^= 1;
     time = time + dt;
     ++step;
-    done = ld_volatile(&c->liquid) == 0;
+    done = liquid == 0;
     if (timer) {
-      c->gens += gen;
-      c->active_grown += (unsigned long long)nA;
-      c->grains_processed += (unsigned long long)processed;
+      s_clk[kGens] += gen;
+      s_clk[kGrown] += (unsigned long long)nA;
+      s_clk[kProc] += (unsigned long long)processed;
     }
   }
   if (ok && timer) {
@@ -847,8 +900,22 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     c->time = time;
     c->dt = dt;
     c->n_active = n_act;
+    c->n_orient = n_orient;
+    c->next_grain = grain;
+    c->liquid = liquid;
     c->cur_list = cur;
     c->done = done ? 1 : 0;
+    c->ns_nucleation += s_clk[kNuc];
+    c->ns_claim += s_clk[kClaim];
+    c->ns_claim_gen0 += s_clk[kClaim0];
+    c->ns_resolve += s_clk[kResolve];
+    c->ns_claim_work_max += s_clk[kClaimMax];
+    c->ns_resolve_work_max += s_clk[kResolveMax];
+    c->gens += s_clk[kGens];
+    c->active_grown += s_clk[kGrown];
+    c->grains_processed += s_clk[kProc];
+    c->captures += s_clk[kCaps];
+    c->nucleations += s_clk[kNucs];
     c->ns_step_end += now_ns() - t_mark;
   }
   // statistics: one atomic per warp

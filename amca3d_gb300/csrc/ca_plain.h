@@ -46,11 +46,11 @@ struct PlainCtrl {
   int cur_list;     // which act[] holds the current active list
   long long n_orient;
   long long next_grain;
-  long long n_active;          // active envelopes (between launches; after nucleation inside one)
+  long long n_active;          // active envelopes between launches
   long long n_active_next[2];  // survivors of the step, by step parity
+  long long n_active_nuc[2];   // active envelopes after the step's nucleation, by step parity
   long long liquid;
-  long long gen_lo;
-  long long gen_n;
+  long long gen_n;  // captures of the last resolved generation
   long long step;
   double time;
   double dt;
@@ -103,6 +103,7 @@ struct PlainDevice {
   double max_dt, final_time, tsf, trunc;
   float h32;
   float coord_err;  // bound on FP64 cell-centre rounding, per component
+  int phase_detail; // nonzero: also gather the slowest block's busy time per phase
   // arrays
   uint32_t *orient;
   uint32_t *solid;    // 1 bit per cell: solid at the start of the current generation (ghosts included)

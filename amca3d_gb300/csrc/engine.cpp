@@ -5,6 +5,7 @@
 // parse the deck, draw sites and the orientation stream with the reference's
 // libraries, move tables to HBM, run the persistent step kernel, write outputs.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -169,6 +170,10 @@ struct amca_t {
     const int nn[3] = {g.nxg, g.nyg, g.nzg};
     for (int a = 0; a < 3; ++a) cmax = std::max(cmax, std::fabs(o[a]) + (nn[a] + 1) * c.h);
     d.coord_err = (float)(std::ldexp(cmax, -49) + 1e-30);
+    // the slowest block's busy time per phase costs a global load per block
+    // and phase, so it is gathered only on request
+    const char *detail = getenv("AMCA_PHASE_DETAIL");
+    d.phase_detail = detail && detail[0] && detail[0] != '0' ? 1 : 0;
     d.ncells = (int64_t)g.nxyg * g.nzg;
     d.nsites = nsites;
     d.gcap = (int64_t)c.nx * c.ny * c.nz;

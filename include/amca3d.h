@@ -191,7 +191,10 @@ typedef struct {
    * [1] claim, [2] resolve, [3] step end (each up to the grid barrier that
    * closes it), [4] the generation-0 part of [1]; per-block busy time before
    * the barrier: [5] claim mean over blocks, [6] claim slowest block,
-   * [7] resolve mean, [8] resolve slowest block (summed over phases) */
+   * [7] resolve mean, [8] resolve slowest block (summed over phases); [6]
+   * and [8] are gathered only when the environment variable
+   * AMCA_PHASE_DETAIL is set to a nonzero value when the handle is
+   * initialized (zero otherwise: it adds a global load per block and phase) */
   double phase_ms[9];
   /* Remelting realm only (zeros otherwise), ms summed over steps: per-block
    * busy time between grid barriers, mean over blocks [0..5] and slowest
