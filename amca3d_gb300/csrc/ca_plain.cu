@@ -91,36 +91,54 @@ __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long l
   return v;
 }
 
+// Thread 0's verdict on the block's last barrier.
+__shared__ int s_bar_ok;
+
 // Barrier of the t_nb blocks of the team on the adjacent words (count, gen),
 // read as one 64-bit word with the generation in the high half: an arrival
 // is one atomicAdd, and the last arrival resets the count and opens the next
-// generation with one more. Returns false (with *error set) when a wait ran
-// out or another block reported an error.
-__device__ bool team_barrier(unsigned *count, unsigned *gen_word, int *error) {
-  unsigned long long *w = (unsigned long long *)count;  // gen_word == count + 1
-  (void)gen_word;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned long long old = atomicAdd(w, 1ull);
-    const unsigned gen = (unsigned)(old >> 32);
-    if ((unsigned)old == (unsigned)t_nb - 1u) {
-      atomicAdd(w, (1ull << 32) - (unsigned long long)t_nb);
-    } else {
-      const unsigned long long t0 = now_ns();
-      while ((unsigned)(ld_acquire64(w) >> 32) == gen) {
-        if (ld_volatile(error) != 0) break;
-        if (now_ns() - t0 > kWaitNs) {
-          atomicCAS(error, 0, kErrBarrier);
-          break;
-        }
-        __nanosleep(32);
+// generation with one more. Returns false when a wait ran out or thread 0
+// saw the error word set: sampled as it arrives (its latency hides behind
+// the arrival) and while it waits. An error raised in this block before the
+// barrier is always seen; one raised elsewhere at the latest at the next
+// barrier, where every block still running waits on the blocks that stopped.
+// The verdict reaches the block through shared memory (no global read after
+// the release).
+// Thread 0's part: arrive and wait; the verdict goes to s_bar_ok. Not
+// inlined: one copy instead of one per barrier site keeps the step loop's
+// register allocation free of it.
+__device__ __noinline__ void barrier_arrive_wait(unsigned long long *w, int *error) {
+  __threadfence();
+  const int seen = ld_volatile(error);
+  const unsigned long long old = atomicAdd(w, 1ull);
+  const unsigned gen = (unsigned)(old >> 32);
+  bool ok = true;
+  if ((unsigned)old == (unsigned)t_nb - 1u) {
+    atomicAdd(w, (1ull << 32) - (unsigned long long)t_nb);
+  } else {
+    const unsigned long long t0 = now_ns();
+    while ((unsigned)(ld_acquire64(w) >> 32) == gen) {
+      if (ld_volatile(error) != 0) {
+        ok = false;
+        break;
       }
+      if (now_ns() - t0 > kWaitNs) {
+        atomicCAS(error, 0, kErrBarrier);
+        ok = false;
+        break;
+      }
+      __nanosleep(32);
     }
-    __threadfence();
   }
+  __threadfence();
+  s_bar_ok = ok && seen == 0;
+}
+__device__ __forceinline__ bool team_barrier(unsigned *count, unsigned *gen_word, int *error) {
+  (void)gen_word;  // == count + 1
   __syncthreads();
-  return ld_volatile(error) == 0;
+  if (threadIdx.x == 0) barrier_arrive_wait((unsigned long long *)count, error);
+  __syncthreads();
+  return s_bar_ok != 0;
 }
 
 // Barrier over the blocks that run the realm; false when it failed.

@@ -328,6 +328,12 @@ void RemeltRealm::initialize() {
           "Error: a proc has no corrsponding FEM mesh!! Maybe decrease the number of multi-core parallel can help.");
     d.force_exact = counts[1] ? 1 : 0;
   }
+  {
+    // the slowest block's busy time per barrier costs a global load per block
+    // and barrier, so it is gathered only on request
+    const char *detail = getenv("AMCA_PHASE_DETAIL");
+    d.detail = detail && detail[0] && detail[0] != '0' ? 1 : 0;
+  }
   d.tag = tag;
   d.pc = pc;
   {

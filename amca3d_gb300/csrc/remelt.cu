@@ -73,32 +73,64 @@ __device__ __forceinline__ T ld_volatile(const T *p) {
 // (same-address atomics from every block at every barrier would serialise).
 __shared__ unsigned long long s_left;
 __shared__ unsigned long long s_busy[6];
+// Block 0's clocks and host round trips (its thread 0), added to the control
+// block once per launch: a read-modify-write of the control block after a
+// barrier would hold up block 0 by a global round trip.
+enum {
+  kClkPhase = 0,  // [0..4] phases A..E
+  kClkBarrier = 5,
+  kClkHost,
+  kClkHostCalls,
+  kClkHostVel,
+  kClkNewgrain,
+  kClkNucleation,
+  kClkFlagsMax,
+  kClkWorkMax,  // [kClkWorkMax + p], p = 0..5
+  kClkN = kClkWorkMax + 6
+};
+__shared__ unsigned long long s_clk[kClkN];
+__shared__ unsigned s_host_seq;  // block 0: requests posted to the host so far
+__shared__ int s_bar_ok;         // thread 0's verdict on the block's last barrier
 
 // Sense-counting grid barrier bounded in time; false when a wait ran out or
-// another block reported an error. `p` names the work it closes (see
-// RemeltCtrl::ns_work_sum) for the busy-time counters.
-__device__ bool grid_barrier(RemeltCtrl *c, int p) {
+// thread 0 saw the error word set: sampled as it arrives (the load's latency
+// hides behind the arrival) and while it waits. An error raised in this
+// block before the barrier is always seen; one raised elsewhere at the latest
+// at the next barrier, where every block still running waits on those that
+// stopped (every list append is bounds-checked, so the phase between is
+// safe). The verdict reaches the block through shared memory. `p` names the
+// work it closes (see RemeltCtrl::ns_work_sum) for the busy-time counters;
+// the slowest block's time is gathered only with d.detail (a global load per
+// block and barrier).
+__device__ bool grid_barrier(const RemeltDevice &d, int p) {
+  RemeltCtrl *c = d.ctrl;
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned long long tb = now_ns();
     const unsigned long long w = tb - s_left;
     s_busy[p] += w;
-    if (w > ld_volatile(&c->work_scratch[p])) atomicMax(&c->work_scratch[p], w);
+    if (d.detail && w > ld_volatile(&c->work_scratch[p])) atomicMax(&c->work_scratch[p], w);
     // (bar_count, bar_gen) as one 64-bit word, generation in the high half:
     // an arrival is one atomicAdd; the last one resets the count and opens
     // the next generation with one more
     unsigned long long *bw = (unsigned long long *)&c->bar_count;
     __threadfence();
+    const int seen = ld_volatile(&c->error);
     const unsigned long long old = atomicAdd(bw, 1ull);
     const unsigned gen = (unsigned)(old >> 32);
+    bool ok = true;
     if ((unsigned)old == gridDim.x - 1) {
       atomicAdd(bw, (1ull << 32) - (unsigned long long)gridDim.x);
     } else {
       const unsigned long long t0 = now_ns();
       while ((unsigned)(ld_acquire64(bw) >> 32) == gen) {
-        if (ld_volatile(&c->error) != 0) break;
+        if (ld_volatile(&c->error) != 0) {
+          ok = false;
+          break;
+        }
         if (now_ns() - t0 > kWaitNs) {
           atomicCAS(&c->error, 0, kRemeltErrBarrier);
+          ok = false;
           break;
         }
         __nanosleep(32);
@@ -106,16 +138,19 @@ __device__ bool grid_barrier(RemeltCtrl *c, int p) {
     }
     __threadfence();
     s_left = now_ns();
+    s_bar_ok = ok && seen == 0;
     if (blockIdx.x == 0) {
-      c->ns_barrier += s_left - tb;
-      // every block's maximum for this work is in; the next one comes at
-      // least four barriers later
-      c->ns_work_max[p] += c->work_scratch[p];
-      c->work_scratch[p] = 0ull;
+      s_clk[kClkBarrier] += s_left - tb;
+      if (d.detail) {
+        // every block's maximum for this work is in; the next one comes at
+        // least four barriers later
+        s_clk[kClkWorkMax + p] += ld_volatile(&c->work_scratch[p]);
+        c->work_scratch[p] = 0ull;
+      }
     }
   }
   __syncthreads();
-  return ld_volatile(&c->error) == 0;
+  return s_bar_ok != 0;
 }
 
 __device__ unsigned block_exclusive_scan(unsigned v, unsigned *smem, unsigned *total) {
@@ -294,8 +329,8 @@ __device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned n
     __syncthreads();
     if (threadIdx.x == 0) {
       const unsigned long long h0 = now_ns();
-      const unsigned seq = c->host_seq + 1;
-      c->host_seq = seq;
+      const unsigned seq = s_host_seq + 1;
+      s_host_seq = seq;
       d.host->n = cnt;
       __threadfence_system();
       st_release_sys(&d.host->seq_req, seq);
@@ -308,9 +343,9 @@ __device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned n
         }
         __nanosleep(64);
       }
-      c->host_calls += 1;
-      c->host_vel += cnt;
-      c->ns_host += now_ns() - h0;
+      s_clk[kClkHostCalls] += 1;
+      s_clk[kClkHostVel] += cnt;
+      s_clk[kClkHost] += now_ns() - h0;
     }
     __syncthreads();
     if (!s_ok) break;
@@ -996,6 +1031,8 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     s_left = now_ns();
     for (int i = 0; i < 6; ++i) s_busy[i] = 0ull;
     s_stage_n = 0u;
+    for (int i = 0; i < kClkN; ++i) s_clk[i] = 0ull;
+    s_host_seq = ld_volatile(&c->host_seq);
   }
   for (;;) {
     const StepScalars S = read_scalars(c);
@@ -1019,7 +1056,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     if (blockIdx.x == 0) {
       const unsigned long long tg = tid == 0 ? now_ns() : 0ull;
       assign_new_grains(d, c);
-      if (tid == 0) c->ns_newgrain += now_ns() - tg;
+      if (tid == 0) s_clk[kClkNewgrain] += now_ns() - tg;
       if (tid == 0) {
         c->n_claim = 0;
         c->n_eact[par ^ 1] = 0;  // built in phase E for the next step; its last reader was the previous phase A
@@ -1058,14 +1095,14 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     stage_flush(&c->n_liq, d.liq, d.list_cap);
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
-      atomicAdd(&c->ns_phase[0], t1 - t_phase);
+      s_clk[kClkPhase + 0] += t1 - t_phase;
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c, 0))) break;
+    if (!(ok = grid_barrier(d, 0))) break;
 
     // ===== B: liquid-neighbour flags (Remelting.cpp:518-540) =====
-    if (tid == 0 && blockIdx.x == 0) {
-      c->ns_flags_max += c->flags_scratch;  // last step's maximum: every block added it before the A barrier
+    if (tid == 0 && blockIdx.x == 0 && d.detail) {
+      s_clk[kClkFlagsMax] += ld_volatile(&c->flags_scratch);  // last step's maximum: every block added it before the A barrier
       c->flags_scratch = 0ull;
     }
     const unsigned long long tfl = tid == 0 ? now_ns() : 0ull;
@@ -1114,7 +1151,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     __syncthreads();
     if (tid == 0) {
       const unsigned long long w = now_ns() - tfl;
-      if (w > ld_volatile(&c->flags_scratch)) atomicMax(&c->flags_scratch, w);
+      if (d.detail && w > ld_volatile(&c->flags_scratch)) atomicMax(&c->flags_scratch, w);
     }
     // site conditions of nucleate_at_nucleation_sites (Remelting.cpp:946-960), all blocks
     // (only a liquid, melted cell can nucleate: the temperatures are
@@ -1142,10 +1179,10 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     }
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
-      atomicAdd(&c->ns_phase[1], t1 - t_phase);
+      s_clk[kClkPhase + 1] += t1 - t_phase;
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c, 1))) break;
+    if (!(ok = grid_barrier(d, 1))) break;
 
     // ===== C: nucleation (block 0) | cutoff + minimum temperature (Remelting.cpp:656-705) =====
     const unsigned nf = ld_volatile(&c->n_flag[par]);
@@ -1189,7 +1226,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         c->n_orient = S.n_orient + done_o;
         c->n_grains = n_grains + done_g;
         c->nucleations += done_o;
-        c->ns_nucleation += now_ns() - tn;
+        s_clk[kClkNucleation] += now_ns() - tn;
       }
     }
     {
@@ -1232,10 +1269,10 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     }
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
-      atomicAdd(&c->ns_phase[2], t1 - t_phase);
+      s_clk[kClkPhase + 2] += t1 - t_phase;
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c, 2))) break;
+    if (!(ok = grid_barrier(d, 2))) break;
 
     // ===== dt (Remelting.cpp:706-726, CafeSolver.cpp:195-199) =====
     const double minT = dkey_inv(ld_volatile(&c->minT_key));
@@ -1254,7 +1291,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
       const unsigned nh = ld_volatile(&c->n_hard);
       if (nh > 0 || min_hard) {  // uniform: every block read the same counter and key
         if (blockIdx.x == 0 && !host_velocities(d, c, nh, min_hard, minT)) atomicCAS(&c->error, 0, kRemeltErrHost);
-        if (!(ok = grid_barrier(c, 5))) break;
+        if (!(ok = grid_barrier(d, 5))) break;
         if (min_hard) vmin = ld_volatile(&c->vmin);
       }
     }
@@ -1323,10 +1360,10 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     }
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
-      atomicAdd(&c->ns_phase[3], t1 - t_phase);
+      s_clk[kClkPhase + 3] += t1 - t_phase;
       t_phase = t1;
     }
-    if (!(ok = grid_barrier(c, 3))) break;
+    if (!(ok = grid_barrier(d, 3))) break;
 
     // ===== E: captures (Remelting.cpp:807-847) and the FE replay step (LoadDataFromFile.cpp:207-313) =====
     {
@@ -1482,15 +1519,27 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
       c->flagged += nf;
       if (exhausted) c->status = kRemeltFramesEnd;
       const unsigned long long t1 = now_ns();
-      atomicAdd(&c->ns_phase[4], t1 - t_phase);
+      s_clk[kClkPhase + 4] += t1 - t_phase;
     }
-    if (!(ok = grid_barrier(c, 4))) break;
-    if (ld_volatile(&c->status) == kRemeltFramesEnd) break;
+    if (!(ok = grid_barrier(d, 4))) break;
+    if (exhausted) break;  // uniform; block 0 recorded kRemeltFramesEnd
   }
   if (ok && blockIdx.x == 0) assign_new_grains(d, c);
   if (tid == 0)
     for (int i = 0; i < 6; ++i)
       if (s_busy[i]) atomicAdd(&c->ns_work_sum[i], s_busy[i]);
+  if (tid == 0 && blockIdx.x == 0) {
+    for (int k = 0; k < 5; ++k) c->ns_phase[k] += s_clk[kClkPhase + k];
+    for (int k = 0; k < 6; ++k) c->ns_work_max[k] += s_clk[kClkWorkMax + k];
+    c->ns_barrier += s_clk[kClkBarrier];
+    c->ns_host += s_clk[kClkHost];
+    c->host_calls += s_clk[kClkHostCalls];
+    c->host_vel += s_clk[kClkHostVel];
+    c->ns_newgrain += s_clk[kClkNewgrain];
+    c->ns_nucleation += s_clk[kClkNucleation];
+    c->ns_flags_max += s_clk[kClkFlagsMax];
+    c->host_seq = s_host_seq;
+  }
   if (tests) atomicAdd(&c->tests, tests);
   if (tests64) atomicAdd(&c->tests64, tests64);
   if (caps) atomicAdd(&c->captures, caps);

@@ -124,6 +124,7 @@ struct RemeltDevice {
   float *theta32[3];         // the same, rounded to float
   double *emax, *emin;       // per element bounds on the interpolated temperature (current step)
   int force_exact;           // some parametric coordinate is not finite: no bound shortcuts
+  int detail;                // nonzero: also gather the slowest block's busy time per barrier
   uint8_t *evoid;            // per element: some node below void_temperature + 1e-5
   int32_t *eliq;             // per element: interior liquid cells it holds
   double *fmax[2], *fmin[2]; // per element: node extrema of a frame (slot = frame index & 1)
