@@ -174,13 +174,20 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   const double third = perp / 3;
   double pA[3];
   for (int i = 0; i < 3; i++) pA[i] = pC[i] + (face_normal(quad, i) > 0 ? third : -third);
-  double dist[3] = {0.0, 0.0, 0.0};
+  // dist[i] = ((0 + d0^2) + d1^2) + d2^2 with d_j = pA[j] - corner_j * length.
+  // A corner has one non-zero axis a (corner_a = +-1): d_a = pA[a] -+ length;
+  // on the others d_j = pA[j] - (+0) = pA[j] exactly, and 0 + d0^2 = d0^2
+  // (d0^2 is +0 or positive), so the sums below are bit-identical.
+  const double sq[3] = {pA[0] * pA[0], pA[1] * pA[1], pA[2] * pA[2]};
+  double dist[3];
   for (int i = 0; i < 3; i++) {
     const int id = face_corner(quad, i);
-    for (int j = 0; j < 3; j++) {
-      const double d = pA[j] - corner_unit(id, j) * length;
-      dist[i] += d * d;
-    }
+    const int a = id < 4 ? (id & 1) : 2;  // +x +y -x -y +z -z
+    const double da = pA[a] - corner_unit(id, a) * length;
+    const double t0 = a == 0 ? da * da : sq[0];
+    const double t1 = a == 1 ? da * da : sq[1];
+    const double t2 = a == 2 ? da * da : sq[2];
+    dist[i] = (t0 + t1) + t2;
   }
   int cid0 = face_corner(quad, 0), cid1, cid2;
   double mind = dist[0];
@@ -200,7 +207,10 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   } else {
     cid2 = face_corner(quad, 2);
   }
-  double n12 = 0.0, n13 = 0.0, d12 = 0.0, d13 = 0.0;
+  // |S1S2|^2 and |S1S3|^2: the three corners of a face lie on three
+  // different axes, so each edge vector is +-length on two axes and +0 on
+  // the third, and both sums are exactly fl(L*L) + fl(L*L): one serves both.
+  double n12 = 0.0, d12 = 0.0, d13 = 0.0;
   for (int i = 0; i < 3; i++) {
     const double c1 = corner_unit(cid0, i) * length;
     const double s1a = pA[i] - c1;
@@ -208,11 +218,10 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
     n12 += s1s2 * s1s2;
     d12 += s1a * s1s2;
     const double s1s3 = corner_unit(cid2, i) * length - c1;
-    n13 += s1s3 * s1s3;
     d13 += s1a * s1s3;
   }
   n12 = (double)sqrtf((float)n12);
-  n13 = (double)sqrtf((float)n13);
+  const double n13 = n12;
   double I0 = d12 / n12, I1 = n12 - I0;
   const double J0 = d13 / n13, J1 = n13 - J0;
   const double tv = trunc_coeff * h;

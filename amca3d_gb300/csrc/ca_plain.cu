@@ -551,7 +551,7 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
 // neighbour tests, atomicMin claims.
 // ---------------------------------------------------------------------------
 __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par, bool grow,
-                            double dt, double vel, EnvRec *cur, const EnvRec *prev, unsigned long long *stat_tests,
+                            double dv, EnvRec *cur, const EnvRec *prev, unsigned long long *stat_tests,
                             unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
@@ -572,7 +572,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
       en = cur[r];
       liq = liquid_neighbours(d.solid, g, en.cell);
       if (grow) {
-        en.L += dt * vel;  // Grain::grow (Grain.h:27)
+        en.L += dv;  // Grain::grow (Grain.h:27): L + dt * vel, the product rounded once per step
         cur[r].L = en.L;
       }
     } else {
@@ -613,7 +613,9 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
     const int cell = en.cell, ori = en.ori, id = en.id;
     const double L = en.L;
     uint32_t con = 0;
-    if (liq && L != 0) {  // cell_is_captured is false for a zero half-diagonal
+    // cell_is_captured is false for a zero half-diagonal (tested on the bits:
+    // an integer compare instead of one on the narrow FP64 pipe)
+    if (liq && (__double_as_longlong(L) << 1) != 0) {
       int I, J, K;
       cell_ijk(g, cell, I, J, K);
       const float dxf = en.dx, dyf = en.dy, dzf = en.dz;
@@ -827,6 +829,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     const long long nA = ld_volatile(&c->n_active_nuc[step & 1]);
     const double vel = ld_volatile(&c->vel[step & 1]);
     dt = nA > 0 ? ld_volatile(&c->dt_active[step & 1]) : ld_volatile(&c->dt_none[step & 1]);
+    const double dv = dt * vel;  // every envelope's growth this step
     const long long nucs = nA - n_act;  // nuclei of this step
     n_orient += nucs;
     grain += nucs;
@@ -841,7 +844,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     while (n > 0) {
       processed += n;
       unsigned long long t_work = threadIdx.x == 0 ? now_ns() : 0ull;
-      claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dt, vel, list, parents, &tests, &tests64);
+      claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dv, list, parents, &tests, &tests64);
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
