@@ -25,6 +25,7 @@
 #endif
 
 #include <math.h>
+#include <string.h>
 
 namespace amca {
 
@@ -136,18 +137,48 @@ AMCA_HD double corner_unit(int c, int j) {
     default: return j == 2 ? -1.0 : 0.0;
   }
 }
+// Axis of corner c (+x +y -x -y +z -z).
+AMCA_HD int corner_axis(int c) { return c < 4 ? (c & 1) : 2; }
 AMCA_HD double dmin_ref(double a, double b) { return (b < a) ? b : a; }  // std::min
 AMCA_HD double dmax_ref(double a, double b) { return (a < b) ? b : a; }  // std::max
 
 // Octahedron::capture_cell: the new, decentred envelope for a captured cell.
 // gc = cell centre - parent centre (FP64). Writes the new centre offset
 // (global frame) into out[0..2] and the new half-diagonal into out[3].
+// Helpers that keep exact FP64 bookkeeping off the narrow FP64 pipe.
+AMCA_HD long long f64_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return __double_as_longlong(x);
+#else
+  long long b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+// plus_zero(x) == x + 0.0 (a zero of either sign becomes +0).
+AMCA_HD double plus_zero(double x) {
+  const long long b = f64_bits(x);
+  return b == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+// nonneg(x) == (x >= 0) for x not NaN (-0 included).
+AMCA_HD bool nonneg(double x) {
+  const long long b = f64_bits(x);
+  return b >= 0 || b == (long long)0x8000000000000000ull;
+}
+// corner_unit(c, corner_axis(c)) * length: +-length (exact: a sign flip).
+AMCA_HD double corner_length(int c, double length) { return (c == 2 || c == 3 || c == 5) ? -length : length; }
+
+// Octahedron::capture decentring (CA/src/Octahedron.cpp) in the reference's
+// operation order. Where a term is a product with a corner coordinate (+-1 on
+// one axis, 0 on the others) the zero terms are dropped and the +-1 products
+// taken as sign flips; every such rewrite is bit-identical: a sum accumulated
+// from +0.0 does not depend on the signs of its zero terms (+0 + -0 = +0,
+// x + -0 = x), and squares and products of zeros are zeros.
 AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, double length, double h,
                          double trunc_coeff, double out[4]) {
-  double cx = 0, cy = 0, cz = 0;
-  cx += gcx * l2g[0];
-  cy += gcx * l2g[1];
-  cz += gcx * l2g[2];
+  double cx = plus_zero(gcx * l2g[0]);  // 0 + p
+  double cy = plus_zero(gcx * l2g[1]);
+  double cz = plus_zero(gcx * l2g[2]);
   cx += gcy * l2g[3];
   cy += gcy * l2g[4];
   cz += gcy * l2g[5];
@@ -156,15 +187,16 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   cz += gcz * l2g[8];
   const double interception = fabs(cx) + fabs(cy) + fabs(cz);
   int quad = 0;
-  if (cz >= 0) {
-    if (cx >= 0 && cy >= 0) quad = 0;
-    else if (cx >= 0 && cy < 0) quad = 3;
-    else if (cx < 0 && cy >= 0) quad = 1;
+  const bool px = nonneg(cx), py = nonneg(cy);
+  if (nonneg(cz)) {
+    if (px && py) quad = 0;
+    else if (px && !py) quad = 3;
+    else if (!px && py) quad = 1;
     else quad = 2;
   } else {
-    if (cx >= 0 && cy >= 0) quad = 4;
-    else if (cx >= 0 && cy < 0) quad = 7;
-    else if (cx < 0 && cy >= 0) quad = 5;
+    if (px && py) quad = 4;
+    else if (px && !py) quad = 7;
+    else if (!px && py) quad = 5;
     else quad = 6;
   }
   const double pC[3] = {cx, cy, cz};
@@ -174,51 +206,57 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   const double third = perp / 3;
   double pA[3];
   for (int i = 0; i < 3; i++) pA[i] = pC[i] + (face_normal(quad, i) > 0 ? third : -third);
-  // dist[i] = ((0 + d0^2) + d1^2) + d2^2 with d_j = pA[j] - corner_j * length.
-  // A corner has one non-zero axis a (corner_a = +-1): d_a = pA[a] -+ length;
-  // on the others d_j = pA[j] - (+0) = pA[j] exactly, and 0 + d0^2 = d0^2
-  // (d0^2 is +0 or positive), so the sums below are bit-identical.
+  // dist[i] = ((0 + d0^2) + d1^2) + d2^2 with d_j = pA[j] - corner_j * length:
+  // on corner i's axis a, d_a = pA[a] -+ length; elsewhere d_j = pA[j]
   const double sq[3] = {pA[0] * pA[0], pA[1] * pA[1], pA[2] * pA[2]};
   double dist[3];
   for (int i = 0; i < 3; i++) {
     const int id = face_corner(quad, i);
-    const int a = id < 4 ? (id & 1) : 2;  // +x +y -x -y +z -z
-    const double da = pA[a] - corner_unit(id, a) * length;
+    const int a = corner_axis(id);
+    const double da = pA[a] - corner_length(id, length);
     const double t0 = a == 0 ? da * da : sq[0];
     const double t1 = a == 1 ? da * da : sq[1];
     const double t2 = a == 2 ? da * da : sq[2];
     dist[i] = (t0 + t1) + t2;
   }
+  // distances are +0 or positive: their order is the order of their bits
+  const long long b1 = f64_bits(dist[1]), b2 = f64_bits(dist[2]);
   int cid0 = face_corner(quad, 0), cid1, cid2;
-  double mind = dist[0];
+  long long mind = f64_bits(dist[0]);
   // i = 1
-  if (mind > dist[1]) {
-    mind = dist[1];
+  if (mind > b1) {
+    mind = b1;
     cid1 = cid0;
     cid0 = face_corner(quad, 1);
   } else {
     cid1 = face_corner(quad, 1);
   }
   // i = 2
-  if (mind > dist[2]) {
-    mind = dist[2];
+  if (mind > b2) {
+    mind = b2;
     cid2 = cid0;
     cid0 = face_corner(quad, 2);
   } else {
     cid2 = face_corner(quad, 2);
   }
-  // |S1S2|^2 and |S1S3|^2: the three corners of a face lie on three
-  // different axes, so each edge vector is +-length on two axes and +0 on
-  // the third, and both sums are exactly fl(L*L) + fl(L*L): one serves both.
-  double n12 = 0.0, d12 = 0.0, d13 = 0.0;
+  // |S1S2|^2 = |S1S3|^2: the three corners of a face lie on three different
+  // axes, so each edge vector is +-length on two axes and +0 on the third and
+  // both sums are exactly fl(L*L) + fl(L*L). S1A . S1S2 and S1A . S1S3 keep
+  // their two non-zero terms, in order.
+  const int a0 = corner_axis(cid0), a1 = corner_axis(cid1), a2 = corner_axis(cid2);
+  const double c1v = corner_length(cid0, length);  // S1 on its axis
+  const double e1 = corner_length(cid1, length);   // S2 on its axis
+  const double e2 = corner_length(cid2, length);   // S3 on its axis
+  const double ll = length * length;
+  double n12 = ll + ll;
+  double d12 = 0.0, d13 = 0.0;
   for (int i = 0; i < 3; i++) {
-    const double c1 = corner_unit(cid0, i) * length;
-    const double s1a = pA[i] - c1;
-    const double s1s2 = corner_unit(cid1, i) * length - c1;
-    n12 += s1s2 * s1s2;
-    d12 += s1a * s1s2;
-    const double s1s3 = corner_unit(cid2, i) * length - c1;
-    d13 += s1a * s1s3;
+    const double s1a = i == a0 ? pA[i] - c1v : pA[i];
+    // S2 - S1 (and S3 - S1) on axis i: +e on S2's axis, -c1 on S1's, +0 elsewhere
+    if (i == a1) d12 += s1a * e1;
+    else if (i == a0) d12 += s1a * (0.0 - c1v);
+    if (i == a2) d13 += s1a * e2;
+    else if (i == a0) d13 += s1a * (0.0 - c1v);
   }
   n12 = (double)sqrtf((float)n12);
   const double n13 = n12;
@@ -233,20 +271,12 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   const double L2 = 0.5 * (dmin_ref(J0, tv) + dmin_ref(J1, tv));
   const double Lnew = (double)sqrtf(2.0f) * (dmax_ref(L1, L2));
   const double mag = (length - Lnew);
-  // (mag * c_i) / (length * T) for the corner S1 = c: only its axis component
-  // is non-zero; the others are (mag * +0) / positive = zero with mag's sign
-  const double zero = mag < 0 ? -0.0 : 0.0;
-  double o0 = 0.0, o1 = 0.0, o2 = 0.0;
-  for (int i = 0; i < 3; i++) {
-    const double c = corner_unit(cid0, i);
-    const double comp = c != 0 ? mag * (c * length) / (length * kTheodorus) : zero;
-    o0 += comp * l2g[i + 0];
-    o1 += comp * l2g[i + 3];
-    o2 += comp * l2g[i + 6];
-  }
-  out[0] = o0;
-  out[1] = o1;
-  out[2] = o2;
+  // (mag * c_i) / (length * T) for the corner S1 = c: non-zero on S1's axis
+  // only; the rotated offset o_k = sum_i comp_i * l2g[i + 3k] is that term + 0
+  const double comp = mag * c1v / (length * kTheodorus);
+  out[0] = plus_zero(comp * l2g[a0 + 0]);
+  out[1] = plus_zero(comp * l2g[a0 + 3]);
+  out[2] = plus_zero(comp * l2g[a0 + 6]);
   out[3] = Lnew;
 }
 
