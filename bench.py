@@ -45,6 +45,9 @@ from amca3d_gb300 import decks  # noqa: E402
 
 METRIC = "cell-updates/s on 1 GB300, plain vs surrogate/batched, at matched grain stats"
 UNIT = "cell-updates/s"
+# AMCA_PHASE_DETAIL=1 makes the kernels also gather the slowest block's busy
+# time per phase (a global load per block and barrier); reported only then
+PHASE_DETAIL = os.environ.get("AMCA_PHASE_DETAIL", "0") not in ("", "0")
 
 
 def workload():
@@ -328,7 +331,13 @@ def run_ours(args, dist: Dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_block({"ca_steps_per_run": ca_steps[-1], "envelopes": st["grains"], **gstats,
                                 "generations_per_run": st["generations"], "tests_per_run": st["tests"],
-                                "phase_ms_nucleation_claim_resolve_end": [round(x, 3) for x in st["phase_ms"]],
+                                "phase_ms_nucleation_claim_resolve_end": [round(x, 3) for x in st["phase_ms"][:4]],
+                                "phase_ms_claim_gen0": round(st["phase_ms"][4], 3),
+                                "busy_ms_mean_claim_resolve": [round(st["phase_ms"][5], 3),
+                                                               round(st["phase_ms"][7], 3)],
+                                **({"busy_ms_slowest_claim_resolve": [round(st["phase_ms"][6], 3),
+                                                                      round(st["phase_ms"][8], 3)]}
+                                   if PHASE_DETAIL else {}),
                                 "fp64_tests_per_run": st["tests_fp64"],
                                 "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same}, case),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -509,9 +518,9 @@ def run_ours_pbf(args, dist: Dist):
                    "host_velocity_wait_ms": round(st["phase_ms"][5], 3),
                    "grid_barrier_ms": round(st["phase_ms"][6], 3),
                    "busy_ms_mean_A_B_C_D_E_host": [round(x, 3) for x in st["detail_ms"][:6]],
-                   "busy_ms_slowest_A_B_C_D_E_host": [round(x, 3) for x in st["detail_ms"][6:12]],
+                   **({"busy_ms_slowest_A_B_C_D_E_host": [round(x, 3) for x in st["detail_ms"][6:12]],
+                       "flag_pass_slowest_ms": round(st["detail_ms"][14], 3)} if PHASE_DETAIL else {}),
                    "block0_newgrain_nucleation_ms": [round(x, 3) for x in st["detail_ms"][12:14]],
-                   "flag_pass_slowest_ms": round(st["detail_ms"][14], 3),
                    "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": load_traffic("remelt_persistent_pbf_500.json"),
