@@ -69,7 +69,7 @@ class Stats(ctypes.Structure):
 EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
-           "amca_plain_run_noalloc", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
+           "amca_plain_run_noalloc", "amca_selftest_barrier", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
            "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_set_layout", "amca_batch_get_layout",
            "amca_batch_get_stats",
            "amca_batch_last_error",
@@ -147,6 +147,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.amca_envelope_eval.argtypes = [i, ctypes.c_size_t, vp, vp, vp, ctypes.c_double, vp, vp, vp, vp]
     lib.amca_envelope_eval.restype = i
+    lib.amca_selftest_barrier.argtypes = [i, i, i, ctypes.c_int64, ctypes.c_int32, vp, vp]
+    lib.amca_selftest_barrier.restype = i
     lib.amca_final_grain_count.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
     lib.amca_final_grain_count.restype = i
     lib.amca_reset.argtypes = [vp]
@@ -237,6 +239,20 @@ def envelope_eval(l2g: np.ndarray, gc: np.ndarray, length: np.ndarray, h: float,
     if rc != AMCA_OK:
         raise AmcaError(rc, lib.amca_last_error(None).decode())
     return cap, fast, info
+
+
+def selftest_barrier(blocks: int, parties: int, wait_ns: int, preset_error: int = 0, device: int = 0):
+    """Run the step kernels' bounded grid barrier once on `blocks` blocks
+    expecting `parties` arrivals (amca_selftest_barrier). Returns (error word
+    afterwards, per-block verdicts: 1 = the barrier returned success)."""
+    lib = load_library()
+    err = ctypes.c_int32(0)
+    verdicts = np.zeros(blocks, np.int32)
+    rc = lib.amca_selftest_barrier(device, blocks, parties, int(wait_ns), int(preset_error), ctypes.byref(err),
+                                   verdicts.ctypes.data_as(ctypes.c_void_p))
+    if rc != AMCA_OK:
+        raise AmcaError(rc, lib.amca_last_error(None).decode())
+    return int(err.value), verdicts
 
 
 class CellularAutomataRealm:

@@ -107,7 +107,7 @@ __shared__ int s_bar_ok;
 // Thread 0's part: arrive and wait; the verdict goes to s_bar_ok. Not
 // inlined: one copy instead of one per barrier site keeps the step loop's
 // register allocation free of it.
-__device__ __noinline__ void barrier_arrive_wait(unsigned long long *w, int *error) {
+__device__ __noinline__ void barrier_arrive_wait(unsigned long long *w, int *error, unsigned long long wait_ns) {
   __threadfence();
   const int seen = ld_volatile(error);
   const unsigned long long old = atomicAdd(w, 1ull);
@@ -122,7 +122,7 @@ __device__ __noinline__ void barrier_arrive_wait(unsigned long long *w, int *err
         ok = false;
         break;
       }
-      if (now_ns() - t0 > kWaitNs) {
+      if (now_ns() - t0 > wait_ns) {
         atomicCAS(error, 0, kErrBarrier);
         ok = false;
         break;
@@ -133,10 +133,11 @@ __device__ __noinline__ void barrier_arrive_wait(unsigned long long *w, int *err
   __threadfence();
   s_bar_ok = ok && seen == 0;
 }
-__device__ __forceinline__ bool team_barrier(unsigned *count, unsigned *gen_word, int *error) {
+__device__ __forceinline__ bool team_barrier(unsigned *count, unsigned *gen_word, int *error,
+                                             unsigned long long wait_ns = kWaitNs) {
   (void)gen_word;  // == count + 1
   __syncthreads();
-  if (threadIdx.x == 0) barrier_arrive_wait((unsigned long long *)count, error);
+  if (threadIdx.x == 0) barrier_arrive_wait((unsigned long long *)count, error, wait_ns);
   __syncthreads();
   return s_bar_ok != 0;
 }
@@ -1322,6 +1323,46 @@ cudaError_t plain_envelope_eval(long long n, const double *l2g, const double *gc
                                 const double *trunc, int32_t *cap64, int32_t *capfast, double *info, cudaStream_t s) {
   envelope_eval_kernel<<<256, 128, 0, s>>>(n, l2g, gc, len, h, trunc, cap64, capfast, info);
   return cudaGetLastError();
+}
+
+namespace {
+// Self-test of the bounded barrier: `parties` arrivals expected from the
+// launch's blocks (parties > blocks: one never comes and every wait must run
+// out), with the error word preset to `preset`. verdict[b] = what block b's
+// barrier returned.
+__global__ void barrier_selftest_kernel(unsigned long long *word, int *error, int parties, unsigned long long wait_ns,
+                                        int *verdict) {
+  if (threadIdx.x == 0) {
+    t_nb = parties;
+    t_b = blockIdx.x;
+  }
+  __syncthreads();
+  const bool ok = team_barrier((unsigned *)word, (unsigned *)word + 1, error, wait_ns);
+  if (threadIdx.x == 0) verdict[blockIdx.x] = ok ? 1 : 0;
+}
+}  // namespace
+
+cudaError_t plain_barrier_selftest(int blocks, int parties, long long wait_ns, int preset, int *error_out,
+                                   int *verdicts) {
+  unsigned long long *word = nullptr;
+  int *dev = nullptr;
+  cudaError_t e = cudaMalloc(&word, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&dev, sizeof(int) * (size_t)(blocks + 1));
+  if (e == cudaSuccess) e = cudaMemset(word, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, sizeof(int) * (size_t)(blocks + 1));
+  if (e == cudaSuccess) e = cudaMemcpy(dev, &preset, sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    int *error = dev, *verdict = dev + 1;
+    unsigned long long w = (unsigned long long)wait_ns;
+    void *args[] = {&word, &error, &parties, &w, &verdict};
+    e = cudaLaunchCooperativeKernel((const void *)barrier_selftest_kernel, dim3(blocks), dim3(kBlock), args, 0, 0);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(error_out, dev, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(verdicts, dev + 1, sizeof(int) * (size_t)blocks, cudaMemcpyDeviceToHost);
+  if (word) cudaFree(word);
+  if (dev) cudaFree(dev);
+  return e;
 }
 
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s) {

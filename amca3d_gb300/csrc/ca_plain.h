@@ -144,6 +144,13 @@ struct BatchPlanDev {
   const int2 *crange;
 };
 
+// Self-test of the bounded grid barrier with `blocks` blocks (cooperative)
+// expecting `parties` arrivals, every wait limited to wait_ns, the error word
+// preset to `preset`: *error_out = the error word afterwards, verdicts[b] =
+// 1 when block b's barrier returned true.
+cudaError_t plain_barrier_selftest(int blocks, int parties, long long wait_ns, int preset, int *error_out,
+                                   int *verdicts);
+
 // Fill the orientation field: -1 interior, 0 on the ghost layer
 // (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833),
 // and the solid bitmap to match.

@@ -1136,6 +1136,23 @@ int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc
   return rc;
 }
 
+int amca_selftest_barrier(int device, int blocks, int parties, int64_t wait_ns, int32_t preset_error,
+                          int32_t *error_out, int32_t *verdicts) {
+  if (!error_out || !verdicts || blocks < 1 || blocks > 64 || parties < 1 || wait_ns < 1000 ||
+      wait_ns > 2000000000ll) {
+    g_create_error = "amca_selftest_barrier: bad argument (1 <= blocks <= 64, 1 us <= wait_ns <= 2 s)";
+    return AMCA_ERR_ARG;
+  }
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = plain_barrier_selftest(blocks, parties, (long long)wait_ns, preset_error, error_out,
+                                                   verdicts);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("amca_selftest_barrier: ") + cudaGetErrorString(e);
+    return AMCA_ERR_CUDA;
+  }
+  return AMCA_OK;
+}
+
 int amca_batch_create(amca_t *const *realms, int n, int team_size, amca_batch **out) {
   if (!out || !realms || n < 1 || n > 65535) {
     g_create_error = "amca_batch_create: null argument, or not 1 to 65535 realms";

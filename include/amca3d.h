@@ -242,6 +242,19 @@ int amca_host_free(void *p);
 int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc, const double *length, double h,
                        const double *trunc, int32_t *captured, int32_t *captured_fast, double *info);
 
+/* Self-test of the device-side failure detection: one cooperative launch of
+ * `blocks` blocks (1..64) through the grid barrier the step kernels use,
+ * which here expects `parties` arrivals and bounds every wait by wait_ns
+ * (1 us..2 s), with the error word preset to preset_error. With parties >
+ * blocks one arrival never comes: every wait runs out, the error word reads
+ * 1 (barrier wait timed out) and every verdict 0, and the context stays
+ * usable; with parties == blocks and preset_error != 0 the barrier completes
+ * and every block reports the error it saw. *error_out = the error word
+ * afterwards, verdicts[b] = 1 when block b's barrier returned success. No
+ * counterpart in the reference, whose errors abort the run. */
+int amca_selftest_barrier(int device, int blocks, int parties, int64_t wait_ns, int32_t preset_error,
+                          int32_t *error_out, int32_t *verdicts);
+
 /* Plain-realm parameters as plain numbers (what amca_create reads from a deck). */
 typedef struct {
   int32_t nx, ny, nz;                 /* interior cells per axis */
