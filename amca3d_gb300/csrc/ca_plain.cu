@@ -26,9 +26,10 @@
 //             gives the new envelope ids (walk order), the child records
 //             (parent id, neighbour index) and the order-preserving
 //             compaction of survivors into the next active list.
-// Each block owns one contiguous chunk of every phase's index range, so a
-// block's envelopes are neighbours in id order (and mostly in space), and the
-// look-back runs once per block and phase. Every phase boundary is a grid
+// The resolve pass gives each block one contiguous chunk of the generation
+// (its look-back runs once per block); claims and a separate marking pass
+// need no order and hand out rank pieces dynamically (RankSched); nucleation
+// sites sit one tile per block when they fit. Every phase boundary is a grid
 // barrier; every wait is bounded in time and reports through an error flag.
 //
 // Loads use the default (L1-cached) path: a phase only reads values written
