@@ -69,7 +69,7 @@ class Stats(ctypes.Structure):
 EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
-           "amca_plain_run_noalloc", "amca_selftest_barrier", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
+           "amca_plain_run_noalloc", "amca_selftest_barrier", "amca_release_cached_memory", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
            "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_set_layout", "amca_batch_get_layout",
            "amca_batch_get_stats",
            "amca_batch_last_error",
@@ -149,6 +149,8 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_envelope_eval.restype = i
     lib.amca_selftest_barrier.argtypes = [i, i, i, ctypes.c_int64, ctypes.c_int32, vp, vp]
     lib.amca_selftest_barrier.restype = i
+    lib.amca_release_cached_memory.argtypes = [i]
+    lib.amca_release_cached_memory.restype = i
     lib.amca_final_grain_count.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
     lib.amca_final_grain_count.restype = i
     lib.amca_reset.argtypes = [vp]
@@ -239,6 +241,14 @@ def envelope_eval(l2g: np.ndarray, gc: np.ndarray, length: np.ndarray, h: float,
     if rc != AMCA_OK:
         raise AmcaError(rc, lib.amca_last_error(None).decode())
     return cap, fast, info
+
+
+def release_cached_memory(device: int = -1) -> None:
+    """Free the device arena kept from destroyed realms (amca_release_cached_memory)."""
+    lib = load_library()
+    rc = lib.amca_release_cached_memory(device)
+    if rc != AMCA_OK:
+        raise AmcaError(rc, lib.amca_last_error(None).decode())
 
 
 def selftest_barrier(blocks: int, parties: int, wait_ns: int, preset_error: int = 0, device: int = 0):

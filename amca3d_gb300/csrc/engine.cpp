@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -34,6 +35,66 @@ namespace {
   } while (0)
 
 thread_local std::string g_create_error;
+
+// Realm arenas kept for reuse after amca_destroy: at most one per device, the
+// larger one. Allocating and freeing a realm's multi-GB arena costs about a
+// millisecond each; a realm created after another one reuses its memory. An
+// arena is only given back once its stream is idle, and every buffer in it
+// is initialized (or written before it is read) as for a fresh allocation.
+// The cache is never destroyed: the driver reclaims the memory at exit.
+struct ArenaCache {
+  std::mutex m;
+  std::vector<std::pair<void *, size_t>> slot;  // by device
+};
+ArenaCache &arena_cache() {
+  static ArenaCache *c = new ArenaCache();
+  return *c;
+}
+
+// An arena of at least `bytes` on `device` (the current device): the cached
+// one when it fits without wasting more than half of it, else a new one.
+void *arena_take(int device, size_t bytes, size_t *got) {
+  ArenaCache &c = arena_cache();
+  {
+    std::lock_guard<std::mutex> g(c.m);
+    if (device >= 0 && (size_t)device < c.slot.size()) {
+      auto &s = c.slot[(size_t)device];
+      if (s.first && s.second >= bytes && s.second / 2 <= bytes) {
+        void *p = s.first;
+        *got = s.second;
+        s = {nullptr, 0};
+        return p;
+      }
+    }
+  }
+  void *p = nullptr;
+  CK(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
+  *got = std::max<size_t>(bytes, 1);
+  return p;
+}
+
+void arena_give(int device, void *p, size_t bytes) {
+  ArenaCache &c = arena_cache();
+  void *drop = nullptr;
+  {
+    std::lock_guard<std::mutex> g(c.m);
+    if (device < 0) {
+      drop = p;
+    } else {
+      if ((size_t)device >= c.slot.size()) c.slot.resize((size_t)device + 1, {nullptr, 0});
+      auto &s = c.slot[(size_t)device];
+      if (!s.first) {
+        s = {p, bytes};
+      } else if (s.second < bytes) {
+        drop = s.first;
+        s = {p, bytes};
+      } else {
+        drop = p;
+      }
+    }
+  }
+  if (drop) cudaFree(drop);
+}
 
 }  // namespace
 
@@ -64,6 +125,7 @@ struct amca_t {
 
   ~amca_t() {
     if (stream) cudaStreamSynchronize(stream);
+    if (arena_ptr) arena_give(device, arena_ptr, arena_bytes);
     for (void *p : allocs) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -209,7 +271,8 @@ struct amca_t {
     Arena sizing;
     layout(sizing);
     Arena arena;
-    arena.base = alloc<char>(sizing.off);
+    arena_ptr = arena_take(device, sizing.off, &arena_bytes);
+    arena.base = (char *)arena_ptr;
     layout(arena);
     d.site_cell = site_cell;
     d.site_dtc = site_dtc;
@@ -234,6 +297,8 @@ struct amca_t {
   }
 
   int64_t ntA_ = 0, ntB_ = 0;
+  void *arena_ptr = nullptr;  // the realm's buffers, from and back to the arena cache
+  size_t arena_bytes = 0;
 
   // Device state right after initialize: liquid field with the ghost layer,
   // live sites, cleared scan words, zeroed control block.
@@ -1134,6 +1199,25 @@ int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc
   }
   for (void *p : bufs) cudaFree(p);
   return rc;
+}
+
+int amca_release_cached_memory(int device) {
+  ArenaCache &c = arena_cache();
+  std::vector<void *> drop;
+  {
+    std::lock_guard<std::mutex> g(c.m);
+    for (size_t d = 0; d < c.slot.size(); ++d)
+      if ((device < 0 || (size_t)device == d) && c.slot[d].first) {
+        drop.push_back(c.slot[d].first);
+        c.slot[d] = {nullptr, 0};
+      }
+  }
+  for (void *p : drop)
+    if (cudaFree(p) != cudaSuccess) {
+      g_create_error = "amca_release_cached_memory: cudaFree failed";
+      return AMCA_ERR_CUDA;
+    }
+  return AMCA_OK;
 }
 
 int amca_selftest_barrier(int device, int blocks, int parties, int64_t wait_ns, int32_t preset_error,

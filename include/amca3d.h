@@ -242,6 +242,12 @@ int amca_host_free(void *p);
 int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc, const double *length, double h,
                        const double *trunc, int32_t *captured, int32_t *captured_fast, double *info);
 
+/* A destroyed plain realm's device arena (its one allocation) is kept for
+ * the next realm created on the same device (at most one per device, reused
+ * when it is at most twice the size needed). This frees the kept arena of
+ * `device` (every device when device < 0). */
+int amca_release_cached_memory(int device);
+
 /* Self-test of the device-side failure detection: one cooperative launch of
  * `blocks` blocks (1..64) through the grid barrier the step kernels use,
  * which here expects `parties` arrivals and bounds every wait by wait_ns

@@ -201,3 +201,25 @@ def test_gpu_errors_are_status_codes(amca):
     with pytest.raises(amca.AmcaError):
         r.initialize()
     r.close()
+
+
+def test_reused_arena_gives_the_same_fields(amca):
+    """A realm created after another one was destroyed runs in its kept arena
+    (stale contents included) and still matches the reference bit for bit;
+    so does one after the cache was released."""
+    golden = json.load(open(os.path.join(GOLD, "plain_golden.json")))
+    cs = cases.small_cases()[:3]
+    for rnd in range(3):
+        if rnd == 2:
+            amca.release_cached_memory(-1)
+        for c in cs:
+            r = amca.CellularAutomataRealm(c.to_yaml(), seed=c.seed)
+            try:
+                r.initialize()
+                r.run()
+                o = np.ascontiguousarray(r.field("orientation_id"), dtype="<i4")
+                g = np.ascontiguousarray(r.field("grain_id"), dtype="<i4")
+                assert hashlib.sha256(o.tobytes()).hexdigest() == golden[c.name]["orient_sha256"], (rnd, c.name)
+                assert hashlib.sha256(g.tobytes()).hexdigest() == golden[c.name]["grain_sha256"], (rnd, c.name)
+            finally:
+                r.close()

@@ -67,3 +67,4 @@ def test_selftest_rejects_bad_arguments(amca):
         amca.selftest_barrier(0, 1, wait_ns=1_000_000)
     with pytest.raises(amca.AmcaError, match="bad argument"):
         amca.selftest_barrier(4, 5, wait_ns=10_000_000_000)
+

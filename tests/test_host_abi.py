@@ -45,6 +45,12 @@ def test_library_exports_every_declared_symbol(amca):
     assert sorted(amca.EXPORTS) == names
 
 
+def test_release_cached_memory_without_a_cached_arena(amca):
+    """Nothing is kept before a realm was destroyed: releasing is a no-op."""
+    amca.release_cached_memory(-1)
+    amca.release_cached_memory(0)
+
+
 @pytest.mark.parametrize("case", cases.small_cases() + cases.large_cases(), ids=lambda c: c.name)
 def test_deck_grid(amca, case):
     r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
