@@ -7,6 +7,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstdint>
 #include <atomic>
 #include <cmath>
 #include <stdexcept>
@@ -126,14 +128,14 @@ void RemeltRealm::prepare() {
   rng_.reset(new GlibcRand(opts_.seed));  // srand in the CA manager's constructor (CellularAutomataManager_3D.cpp:40)
   const int nxg = c.nx + 2, nyg = c.ny + 2, nzg = c.nz + 2;
   const int64_t nxyg = (int64_t)nxg * nyg, N = nxyg * nzg;
-  orient0_.assign((size_t)N, -1);
-  grain0_.assign((size_t)N, -1);
-  melted0_.assign((size_t)N, cfg_.initial_melted ? 1 : 0);
-  gori0_.assign((size_t)N, -1);
-  site_field_.assign((size_t)N, -1.0);
+  site_field_.clear();  // built on first use (site_field())
   grain_cell_.clear();
   grain_ori0_.clear();
   if (cfg_.random_micro && !micro_) {
+    orient0_.assign((size_t)N, -1);
+    grain0_.assign((size_t)N, -1);
+    melted0_.assign((size_t)N, cfg_.initial_melted ? 1 : 0);
+    gori0_.assign((size_t)N, -1);
     // random_microstructure_information (CellularAutomataManager_3D.cpp:1929-1984):
     // one orientation and one grain per interior cell, in cell order
     const int64_t M = (int64_t)c.nx * c.ny * c.nz;
@@ -161,47 +163,78 @@ void RemeltRealm::prepare() {
     // (CellularAutomataManager_3DRemelting.cpp:164-332)
     RestartData loaded;
     if (!micro_) loaded = read_restart(path(cfg_.micro_file));
-    const RestartData &r = micro_ ? *micro_ : loaded;
+    RestartData &r = micro_ ? *micro_ : loaded;  // consumed here: its arrays move into the initial state
     if (r.ncells != N)
       throw std::runtime_error("Error : microstructure information file is not fit the current domain size");
     if (!cfg_.nucleation && c.shuffle_vtr) mapped_vtr_ = make_mapped_ids(r.expected, true, *rng_);
     otab_ = orientations_from_euler(r.euler);
-    orient0_ = r.orient;
-    grain0_ = r.grain;
-    melted0_ = r.melted;
-    grain_cell_ = r.gcell;
-    grain_ori0_ = r.gori;
-    std::vector<uint8_t> owned((size_t)r.ngrains, 0);
-    for (int K = 0; K < nzg; ++K)
-      for (int J = 0; J < nyg; ++J)
-        for (int I = 0; I < nxg; ++I) {
-          const int64_t cell = K * nxyg + (int64_t)J * nxg + I;
-          if (is_ghost(I, J, K, nxg, nyg, nzg)) {
-            orient0_[cell] = -1;
-            continue;
-          }
-          const int32_t g = grain0_[cell];
-          if (g >= 0) {
-            if (g >= r.ngrains) throw std::runtime_error("restart cell refers to a grain that is not listed");
-            if (owned[g] || r.gcell[g] != cell)
-              throw std::runtime_error("restart grains must each belong to the one interior cell that refers to them");
-            owned[g] = 1;
-            // the grain's centre is reset to its cell centre, length 0
-            // (:289-296): remelt_init_records on the device
-            gori0_[cell] = r.gori[g];
-          }
-          if (orient0_[cell] > -1) continue;
-          if (g < 0) throw std::runtime_error("restart cell has neither an orientation nor a grain");
-          orient0_[cell] = r.gori[g];
-        }
+    orient0_ = std::move(r.orient);
+    grain0_ = std::move(r.grain);
+    melted0_ = std::move(r.melted);
+    grain_cell_ = std::move(r.gcell);
+    grain_ori0_ = std::move(r.gori);
     n_init_orient_ = r.norient;
     n_init_grains_ = r.ngrains;
     expected_grains_ = r.expected;
+    micro_.reset();
+    gori0_.assign((size_t)N, -1);
+    // per cell, in parallel over z slabs: a grain belongs to the one interior
+    // cell its record names (a second cell naming it fails that test), and a
+    // cell without an orientation takes its grain's; the error reported is
+    // that of the first offending cell in cell order, as a serial pass would
+    const int64_t ngr = n_init_grains_;
+    const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<int64_t> bad_cell((size_t)nt, INT64_MAX);
+    std::vector<int> bad_kind((size_t)nt, 0);
+    std::vector<std::thread> th;
+    auto slab = [&](int t) {
+      const int k0 = (int)((int64_t)nzg * t / nt), k1 = (int)((int64_t)nzg * (t + 1) / nt);
+      for (int K = k0; K < k1; ++K)
+        for (int J = 0; J < nyg; ++J)
+          for (int I = 0; I < nxg; ++I) {
+            const int64_t cell = K * nxyg + (int64_t)J * nxg + I;
+            if (is_ghost(I, J, K, nxg, nyg, nzg)) {
+              orient0_[cell] = -1;
+              continue;
+            }
+            const int32_t g = grain0_[cell];
+            int kind = 0;
+            if (g >= 0) {
+              if (g >= ngr) {
+                kind = 1;
+              } else if (grain_cell_[g] != cell) {
+                kind = 2;
+              } else {
+                // the grain's centre is reset to its cell centre, length 0
+                // (:289-296): remelt_init_records on the device
+                gori0_[cell] = grain_ori0_[g];
+              }
+            }
+            if (!kind && orient0_[cell] <= -1) {
+              if (g < 0) kind = 3;
+              else orient0_[cell] = grain_ori0_[g];
+            }
+            if (kind) {
+              bad_cell[t] = cell;
+              bad_kind[t] = kind;
+              return;
+            }
+          }
+    };
+    for (int t = 1; t < nt; ++t) th.emplace_back(slab, t);
+    slab(0);
+    for (auto &x : th) x.join();
+    for (int t = 0; t < nt; ++t) {
+      if (bad_cell[t] == INT64_MAX) continue;
+      if (bad_kind[t] == 1) throw std::runtime_error("restart cell refers to a grain that is not listed");
+      if (bad_kind[t] == 2)
+        throw std::runtime_error("restart grains must each belong to the one interior cell that refers to them");
+      throw std::runtime_error("restart cell has neither an orientation nor a grain");
+    }
   }
   init_draws_ = rng_->draws();
   if (cfg_.nucleation) {
     sites_ = make_sites(c, *rng_);
-    for (size_t i = 0; i < sites_.cell.size(); ++i) site_field_[sites_.cell[i]] = sites_.dtc[i];
     if (c.shuffle_vtr) {  // global_mapped_grain_ID_plus (CellularAutomataManager_3DRemelting.cpp:873-931)
       const int64_t surf = ((int64_t)c.nx * c.ny + (int64_t)c.nx * (c.nz - 2) + (int64_t)(c.ny - 2) * (c.nz - 2)) * 2;
       const int64_t bulk = (int64_t)c.nx * c.ny * c.nz;
@@ -216,6 +249,14 @@ void RemeltRealm::prepare() {
     append_orientations(otab_, make_orientations(K, *rng_));
   }
   prepared_ = true;
+}
+
+const std::vector<double> &RemeltRealm::site_field() {
+  if (site_field_.empty()) {
+    site_field_.assign((size_t)dev_.ncells > 0 ? (size_t)dev_.ncells : orient0_.size(), -1.0);
+    for (size_t i = 0; i < sites_.cell.size(); ++i) site_field_[sites_.cell[i]] = sites_.dtc[i];
+  }
+  return site_field_;
 }
 
 void RemeltRealm::upload_initial_state() {
@@ -345,18 +386,66 @@ void RemeltRealm::initialize() {
     std::vector<int32_t> htag((size_t)N);
     d2h(htag.data(), tag, N * 4);
     RCK(cudaStreamSynchronize(stream_));
-    std::vector<int64_t> start((size_t)d.nelem + 1, 0);
-    auto interior = [&](int64_t cell) {
-      const int K = (int)(cell / g.nxyg), J = (int)((cell % g.nxyg) / g.nxg), I = (int)((cell % g.nxyg) % g.nxg);
-      return I > 0 && I < g.nxg - 1 && J > 0 && J < g.nyg - 1 && K > 0 && K < g.nzg - 1;
+    // counts per element and thread over z slabs of the interior, then each
+    // thread fills its slab's cells: every element's list stays in ascending
+    // cell order, as a serial pass gives
+    const int64_t ne = d.nelem;
+    int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if ((int64_t)nt * (ne + 1) > (64ll << 20)) nt = 1;  // bound the per-thread count arrays
+    const int kz = g.nzg - 2;
+    nt = std::max(1, std::min(nt, kz));
+    std::vector<std::vector<int32_t>> cnt((size_t)nt, std::vector<int32_t>((size_t)ne, 0));
+    auto slab_of = [&](int t, int &k0, int &k1) {
+      k0 = 1 + (int)((int64_t)kz * t / nt);
+      k1 = 1 + (int)((int64_t)kz * (t + 1) / nt);
     };
-    for (int64_t cell = 0; cell < N; ++cell)
-      if (htag[cell] >= 0 && interior(cell)) start[htag[cell] + 1]++;
-    for (int64_t e = 0; e < d.nelem; ++e) start[e + 1] += start[e];
-    std::vector<int32_t> list((size_t)std::max<int64_t>(start[d.nelem], 1));
-    std::vector<int64_t> fill(start.begin(), start.end() - 1);
-    for (int64_t cell = 0; cell < N; ++cell)
-      if (htag[cell] >= 0 && interior(cell)) list[fill[htag[cell]]++] = (int32_t)cell;
+    auto run_threads = [&](auto body) {
+      std::vector<std::thread> th;
+      for (int t = 1; t < nt; ++t) th.emplace_back(body, t);
+      body(0);
+      for (auto &x : th) x.join();
+    };
+    run_threads([&](int t) {
+      int k0, k1;
+      slab_of(t, k0, k1);
+      int32_t *ct = cnt[(size_t)t].data();
+      for (int K = k0; K < k1; ++K)
+        for (int J = 1; J < g.nyg - 1; ++J) {
+          const int32_t *row = htag.data() + (int64_t)K * g.nxyg + (int64_t)J * g.nxg;
+          for (int I = 1; I < g.nxg - 1; ++I)
+            if (row[I] >= 0) ++ct[row[I]];
+        }
+    });
+    std::vector<int64_t> start((size_t)ne + 1, 0);
+    for (int64_t e = 0; e < ne; ++e) {
+      int64_t sum = 0;
+      for (int t = 0; t < nt; ++t) sum += cnt[(size_t)t][(size_t)e];
+      start[(size_t)e + 1] = start[(size_t)e] + sum;
+    }
+    std::vector<int32_t> list((size_t)std::max<int64_t>(start[(size_t)ne], 1));
+    // thread t's first slot of element e: start[e] plus the counts of the slabs before it
+    for (int64_t e = 0; e < ne; ++e) {
+      int64_t at = start[(size_t)e];
+      for (int t = 0; t < nt; ++t) {
+        const int32_t n_te = cnt[(size_t)t][(size_t)e];
+        cnt[(size_t)t][(size_t)e] = (int32_t)(at - start[(size_t)e]);
+        at += n_te;
+      }
+    }
+    run_threads([&](int t) {
+      int k0, k1;
+      slab_of(t, k0, k1);
+      int32_t *ct = cnt[(size_t)t].data();
+      for (int K = k0; K < k1; ++K)
+        for (int J = 1; J < g.nyg - 1; ++J) {
+          const int64_t base = (int64_t)K * g.nxyg + (int64_t)J * g.nxg;
+          const int32_t *row = htag.data() + base;
+          for (int I = 1; I < g.nxg - 1; ++I) {
+            const int32_t e = row[I];
+            if (e >= 0) list[(size_t)(start[(size_t)e] + ct[e]++)] = (int32_t)(base + I);
+          }
+        }
+    });
     int64_t *es = alloc<int64_t>(start.size());
     int32_t *el = alloc<int32_t>(list.size());
     h2d(es, start.data(), start.size() * 8);
@@ -640,7 +729,7 @@ void RemeltRealm::get_field(int field, void *dst, size_t bytes) {
       return;
     case AMCA_FIELD_SITE_UNDERCOOLING:
       need(N * 8);
-      memcpy(dst, site_field_.data(), N * 8);
+      memcpy(dst, site_field().data(), N * 8);
       return;
     case AMCA_FIELD_MELTED:
       need(N);
@@ -845,7 +934,7 @@ void RemeltRealm::write_outputs() {
       }
     }
     v.grain = f.grain.data();
-    v.site_dtc = site_field_.data();
+    v.site_dtc = site_field().data();
     v.n_grains = ng;
     v.gx = gx.data();
     v.gy = gy.data();

@@ -106,7 +106,8 @@ class RemeltRealm {
   std::vector<int32_t> grain_cell_;  // grain id -> owning cell (restart + created)
   std::vector<int32_t> grain_ori0_;  // grain id -> initial orientation
   int64_t init_draws_ = 0;           // glibc rand() values consumed before the nucleation stream
-  std::vector<double> site_field_;   // cellNucleationDT_
+  std::vector<double> site_field_;   // cellNucleationDT_, built on first use
+  const std::vector<double> &site_field();
   int64_t expected_grains_ = 0;
   int64_t restart_sites_ = 0;
   // device
