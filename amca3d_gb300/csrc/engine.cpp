@@ -36,64 +36,73 @@ namespace {
 
 thread_local std::string g_create_error;
 
-// Realm arenas kept for reuse after amca_destroy: at most one per device, the
-// larger one. Allocating and freeing a realm's multi-GB arena costs about a
-// millisecond each; a realm created after another one reuses its memory. An
-// arena is only given back once its stream is idle, and every buffer in it
-// is initialized (or written before it is read) as for a fresh allocation.
-// The cache is never destroyed: the driver reclaims the memory at exit.
+// Realm arenas kept for reuse after amca_destroy, per device, up to
+// kArenaCacheBytes in all (the larger ones kept first). Allocating and
+// freeing a realm's arena costs up to a few milliseconds each; a realm
+// created after others were destroyed (the next deck of a sweep, the next
+// pass of a batch) reuses their memory. An arena is only given back once its
+// stream is idle, and every buffer in it is initialized (or written before
+// it is read) as for a fresh allocation. The cache is never destroyed: the
+// driver reclaims the memory at exit.
+constexpr size_t kArenaCacheBytes = 32ull << 30;
 struct ArenaCache {
   std::mutex m;
-  std::vector<std::pair<void *, size_t>> slot;  // by device
+  std::vector<std::vector<std::pair<void *, size_t>>> slot;  // by device
 };
 ArenaCache &arena_cache() {
   static ArenaCache *c = new ArenaCache();
   return *c;
 }
 
-// An arena of at least `bytes` on `device` (the current device): the cached
-// one when it fits without wasting more than half of it, else a new one.
+// An arena of at least `bytes` on `device` (the current device): the
+// smallest kept one that fits without wasting more than half of it, else a
+// new one.
 void *arena_take(int device, size_t bytes, size_t *got) {
+  bytes = std::max<size_t>(bytes, 1);
   ArenaCache &c = arena_cache();
   {
     std::lock_guard<std::mutex> g(c.m);
     if (device >= 0 && (size_t)device < c.slot.size()) {
-      auto &s = c.slot[(size_t)device];
-      if (s.first && s.second >= bytes && s.second / 2 <= bytes) {
-        void *p = s.first;
-        *got = s.second;
-        s = {nullptr, 0};
+      auto &v = c.slot[(size_t)device];
+      size_t best = v.size();
+      for (size_t i = 0; i < v.size(); ++i)
+        if (v[i].second >= bytes && v[i].second / 2 <= bytes && (best == v.size() || v[i].second < v[best].second))
+          best = i;
+      if (best < v.size()) {
+        void *p = v[best].first;
+        *got = v[best].second;
+        v.erase(v.begin() + (long)best);
         return p;
       }
     }
   }
   void *p = nullptr;
-  CK(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
-  *got = std::max<size_t>(bytes, 1);
+  CK(cudaMalloc(&p, bytes));
+  *got = bytes;
   return p;
 }
 
 void arena_give(int device, void *p, size_t bytes) {
   ArenaCache &c = arena_cache();
-  void *drop = nullptr;
+  std::vector<void *> drop;
   {
     std::lock_guard<std::mutex> g(c.m);
     if (device < 0) {
-      drop = p;
+      drop.push_back(p);
     } else {
-      if ((size_t)device >= c.slot.size()) c.slot.resize((size_t)device + 1, {nullptr, 0});
-      auto &s = c.slot[(size_t)device];
-      if (!s.first) {
-        s = {p, bytes};
-      } else if (s.second < bytes) {
-        drop = s.first;
-        s = {p, bytes};
-      } else {
-        drop = p;
-      }
+      if ((size_t)device >= c.slot.size()) c.slot.resize((size_t)device + 1);
+      auto &v = c.slot[(size_t)device];
+      v.emplace_back(p, bytes);
+      std::sort(v.begin(), v.end(), [](const std::pair<void *, size_t> &a, const std::pair<void *, size_t> &b) {
+        return a.second > b.second;
+      });
+      size_t total = 0, keep = 0;
+      for (; keep < v.size() && total + v[keep].second <= kArenaCacheBytes; ++keep) total += v[keep].second;
+      for (size_t i = keep; i < v.size(); ++i) drop.push_back(v[i].first);
+      v.resize(keep);
     }
   }
-  if (drop) cudaFree(drop);
+  for (void *q : drop) cudaFree(q);
 }
 
 }  // namespace
@@ -1207,9 +1216,9 @@ int amca_release_cached_memory(int device) {
   {
     std::lock_guard<std::mutex> g(c.m);
     for (size_t d = 0; d < c.slot.size(); ++d)
-      if ((device < 0 || (size_t)device == d) && c.slot[d].first) {
-        drop.push_back(c.slot[d].first);
-        c.slot[d] = {nullptr, 0};
+      if (device < 0 || (size_t)device == d) {
+        for (auto &a : c.slot[d]) drop.push_back(a.first);
+        c.slot[d].clear();
       }
   }
   for (void *p : drop)

@@ -243,8 +243,9 @@ int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc
                        const double *trunc, int32_t *captured, int32_t *captured_fast, double *info);
 
 /* A destroyed plain realm's device arena (its one allocation) is kept for
- * the next realm created on the same device (at most one per device, reused
- * when it is at most twice the size needed). This frees the kept arena of
+ * the realms created after it on the same device (up to 32 GiB of arenas per
+ * device, the larger ones kept first; a realm takes the smallest kept arena
+ * that is at most twice the size it needs). This frees the kept arenas of
  * `device` (every device when device < 0). */
 int amca_release_cached_memory(int device);
 
