@@ -45,6 +45,9 @@ thread_local std::string g_create_error;
 // it is read) as for a fresh allocation. The cache is never destroyed: the
 // driver reclaims the memory at exit.
 constexpr size_t kArenaCacheBytes = 32ull << 30;
+// Interior cells up to which a plain realm runs 3 blocks per SM instead of
+// the kernel's full occupancy (see initialize).
+constexpr long long kSmallRealmCells = 4ll << 20;
 struct ArenaCache {
   std::mutex m;
   std::vector<std::vector<std::pair<void *, size_t>>> slot;  // by device
@@ -297,6 +300,20 @@ struct amca_t {
     }
     reset_device();
     grid_blocks = plain_persistent_grid(device);
+    {
+      // Blocks per SM of the persistent launch: a small realm's generations
+      // are short, so its steps are set by barrier and look-back latency,
+      // which fall with the number of blocks (128^3 on GB300: 19.06 ms at 4
+      // blocks per SM, 18.04 at 3; 200^3 equal; 320^3 94.7 at 4, 100.1 at 3).
+      // AMCA_PLAIN_BLOCKS_PER_SM overrides the choice.
+      int per_sm = (long long)c.nx * c.ny * c.nz <= kSmallRealmCells ? 3 : 0;
+      if (const char *e = getenv("AMCA_PLAIN_BLOCKS_PER_SM")) per_sm = std::max(1, atoi(e));
+      if (per_sm > 0) {
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        grid_blocks = std::min(grid_blocks, sms * per_sm);
+      }
+    }
     if (grid_blocks <= 0) throw CudaError("no co-resident blocks for the persistent CA kernel");
     CK(cudaStreamSynchronize(stream));
     // VtrManager::initialize
