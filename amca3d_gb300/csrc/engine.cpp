@@ -19,6 +19,7 @@
 #include "../../include/amca3d.h"
 #include "ca_plain.h"
 #include "deck.h"
+#include "device_cache.h"
 #include "engine_remelt.h"
 #include "errors.h"
 #include "host_init.h"
@@ -36,77 +37,9 @@ namespace {
 
 thread_local std::string g_create_error;
 
-// Realm arenas kept for reuse after amca_destroy, per device, up to
-// kArenaCacheBytes in all (the larger ones kept first). Allocating and
-// freeing a realm's arena costs up to a few milliseconds each; a realm
-// created after others were destroyed (the next deck of a sweep, the next
-// pass of a batch) reuses their memory. An arena is only given back once its
-// stream is idle, and every buffer in it is initialized (or written before
-// it is read) as for a fresh allocation. The cache is never destroyed: the
-// driver reclaims the memory at exit.
-constexpr size_t kArenaCacheBytes = 32ull << 30;
 // Interior cells up to which a plain realm runs 3 blocks per SM instead of
 // the kernel's full occupancy (see initialize).
 constexpr long long kSmallRealmCells = 4ll << 20;
-struct ArenaCache {
-  std::mutex m;
-  std::vector<std::vector<std::pair<void *, size_t>>> slot;  // by device
-};
-ArenaCache &arena_cache() {
-  static ArenaCache *c = new ArenaCache();
-  return *c;
-}
-
-// An arena of at least `bytes` on `device` (the current device): the
-// smallest kept one that fits without wasting more than half of it, else a
-// new one.
-void *arena_take(int device, size_t bytes, size_t *got) {
-  bytes = std::max<size_t>(bytes, 1);
-  ArenaCache &c = arena_cache();
-  {
-    std::lock_guard<std::mutex> g(c.m);
-    if (device >= 0 && (size_t)device < c.slot.size()) {
-      auto &v = c.slot[(size_t)device];
-      size_t best = v.size();
-      for (size_t i = 0; i < v.size(); ++i)
-        if (v[i].second >= bytes && v[i].second / 2 <= bytes && (best == v.size() || v[i].second < v[best].second))
-          best = i;
-      if (best < v.size()) {
-        void *p = v[best].first;
-        *got = v[best].second;
-        v.erase(v.begin() + (long)best);
-        return p;
-      }
-    }
-  }
-  void *p = nullptr;
-  CK(cudaMalloc(&p, bytes));
-  *got = bytes;
-  return p;
-}
-
-void arena_give(int device, void *p, size_t bytes) {
-  ArenaCache &c = arena_cache();
-  std::vector<void *> drop;
-  {
-    std::lock_guard<std::mutex> g(c.m);
-    if (device < 0) {
-      drop.push_back(p);
-    } else {
-      if ((size_t)device >= c.slot.size()) c.slot.resize((size_t)device + 1);
-      auto &v = c.slot[(size_t)device];
-      v.emplace_back(p, bytes);
-      std::sort(v.begin(), v.end(), [](const std::pair<void *, size_t> &a, const std::pair<void *, size_t> &b) {
-        return a.second > b.second;
-      });
-      size_t total = 0, keep = 0;
-      for (; keep < v.size() && total + v[keep].second <= kArenaCacheBytes; ++keep) total += v[keep].second;
-      for (size_t i = keep; i < v.size(); ++i) drop.push_back(v[i].first);
-      v.resize(keep);
-    }
-  }
-  for (void *q : drop) cudaFree(q);
-}
 
 }  // namespace
 
@@ -137,7 +70,7 @@ struct amca_t {
 
   ~amca_t() {
     if (stream) cudaStreamSynchronize(stream);
-    if (arena_ptr) arena_give(device, arena_ptr, arena_bytes);
+    if (arena_ptr) cache_give(device, arena_ptr, arena_bytes);
     for (void *p : allocs) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -283,7 +216,8 @@ struct amca_t {
     Arena sizing;
     layout(sizing);
     Arena arena;
-    arena_ptr = arena_take(device, sizing.off, &arena_bytes);
+    arena_ptr = cache_take(device, sizing.off, &arena_bytes);
+    if (!arena_ptr) throw CudaError("cudaMalloc of the realm arena failed");
     arena.base = (char *)arena_ptr;
     layout(arena);
     d.site_cell = site_cell;
@@ -1228,21 +1162,10 @@ int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc
 }
 
 int amca_release_cached_memory(int device) {
-  ArenaCache &c = arena_cache();
-  std::vector<void *> drop;
-  {
-    std::lock_guard<std::mutex> g(c.m);
-    for (size_t d = 0; d < c.slot.size(); ++d)
-      if (device < 0 || (size_t)device == d) {
-        for (auto &a : c.slot[d]) drop.push_back(a.first);
-        c.slot[d].clear();
-      }
+  if (!cache_release(device)) {
+    g_create_error = "amca_release_cached_memory: cudaFree failed";
+    return AMCA_ERR_CUDA;
   }
-  for (void *p : drop)
-    if (cudaFree(p) != cudaSuccess) {
-      g_create_error = "amca_release_cached_memory: cudaFree failed";
-      return AMCA_ERR_CUDA;
-    }
   return AMCA_OK;
 }
 

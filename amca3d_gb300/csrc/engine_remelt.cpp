@@ -1,6 +1,7 @@
 // engine_remelt.cpp — see engine_remelt.h.
 #include "engine_remelt.h"
 
+#include "device_cache.h"
 #include "errors.h"
 
 #include <stdlib.h>
@@ -44,7 +45,7 @@ RemeltRealm::RemeltRealm(RemeltConfig cfg, const amca_opts &opts, std::string wo
 
 RemeltRealm::~RemeltRealm() {
   if (stream_) cudaStreamSynchronize(stream_);
-  for (void *p : allocs_) cudaFree(p);
+  for (const auto &a : allocs_) cache_give(device_, a.first, a.second);
   if (hostvel_) cudaFreeHost(hostvel_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
@@ -53,9 +54,10 @@ RemeltRealm::~RemeltRealm() {
 
 template <typename T>
 T *RemeltRealm::alloc(size_t n) {
-  void *p = nullptr;
-  RCK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
-  allocs_.push_back(p);
+  size_t got = 0;
+  void *p = cache_take(device_, std::max<size_t>(n, 1) * sizeof(T), &got);
+  if (!p) throw CudaError("cudaMalloc failed for a remelting realm buffer");
+  allocs_.emplace_back(p, got);
   return (T *)p;
 }
 

@@ -12,6 +12,7 @@
 #include <atomic>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/amca3d.h"
@@ -114,7 +115,7 @@ class RemeltRealm {
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
-  std::vector<void *> allocs_;
+  std::vector<std::pair<void *, size_t>> allocs_;  // device buffers and sizes, back to the device cache at the end
   RemeltDevice dev_{};
   RemeltCtrl ctrl_{};
   RemeltCtrl ctrl0_{};

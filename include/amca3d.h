@@ -242,11 +242,11 @@ int amca_host_free(void *p);
 int amca_envelope_eval(int device, size_t n, const double *l2g, const double *gc, const double *length, double h,
                        const double *trunc, int32_t *captured, int32_t *captured_fast, double *info);
 
-/* A destroyed plain realm's device arena (its one allocation) is kept for
- * the realms created after it on the same device (up to 32 GiB of arenas per
- * device, the larger ones kept first; a realm takes the smallest kept arena
- * that is at most twice the size it needs). This frees the kept arenas of
- * `device` (every device when device < 0). */
+/* A destroyed realm's device buffers (the plain realm's one arena, the
+ * remelting realm's arrays) are kept for the realms created after it on the
+ * same device (up to 32 GiB per device, the larger ones kept first; a buffer
+ * is reused when it is at most twice the size asked for). This frees the
+ * kept buffers of `device` (every device when device < 0). */
 int amca_release_cached_memory(int device);
 
 /* Self-test of the device-side failure detection: one cooperative launch of
