@@ -9,11 +9,13 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/amca3d.h"
@@ -955,18 +957,38 @@ int amca_set_microstructure(amca_t *h, const int32_t *grain, const int32_t *orie
     r.norient = norient;
     r.ngrains = ngrains;
     r.expected = expected;
-    r.grain.assign(grain, grain + N);
-    r.orient.assign(orient, orient + N);
-    if (melted)
-      r.melted.assign(melted, melted + N);
-    else
-      r.melted.assign((size_t)N, 0);
+    // the per-cell and per-grain arrays are copied in parallel chunks (a
+    // pbf_500 microstructure is about 220 MB)
+    r.grain.resize((size_t)N);
+    r.orient.resize((size_t)N);
+    r.melted.resize((size_t)N);  // zeros unless given
+    r.gcell.resize((size_t)ngrains);
+    r.gori.resize((size_t)ngrains);
+    std::vector<std::pair<void *, const void *>> dst_src = {{r.grain.data(), grain}, {r.orient.data(), orient},
+                                                            {r.gcell.data(), grain_cell}, {r.gori.data(), grain_orient}};
+    const size_t sizes[4] = {(size_t)N * 4, (size_t)N * 4, (size_t)ngrains * 4, (size_t)ngrains * 4};
+    if (melted) {
+      dst_src.emplace_back(r.melted.data(), melted);
+    }
     if (dtc) r.dtc.assign(dtc, dtc + N);  // kept for completeness: the realm draws its own sites
     r.euler.assign(euler, euler + 3 * norient);
-    r.gcell.assign(grain_cell, grain_cell + ngrains);
-    r.gori.assign(grain_orient, grain_orient + ngrains);
-    for (int64_t g = 0; g < ngrains; ++g)
-      if (r.gori[g] < 0 || r.gori[g] >= norient) throw std::invalid_argument("grain orientation out of range");
+    const int nt = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    std::atomic<int> bad{0};
+    auto part = [&](int t) {
+      for (size_t a = 0; a < dst_src.size(); ++a) {
+        const size_t bytes = a < 4 ? sizes[a] : (size_t)N;
+        const size_t lo = bytes * t / nt, hi = bytes * (t + 1) / nt;
+        if (hi > lo) memcpy((char *)dst_src[a].first + lo, (const char *)dst_src[a].second + lo, hi - lo);
+      }
+      const int64_t g0 = ngrains * t / nt, g1 = ngrains * (t + 1) / nt;
+      for (int64_t g = g0; g < g1; ++g)
+        if (grain_orient[g] < 0 || grain_orient[g] >= norient) bad.store(1, std::memory_order_relaxed);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(part, t);
+    part(0);
+    for (auto &x : th) x.join();
+    if (bad.load()) throw std::invalid_argument("grain orientation out of range");
     h->rm->set_microstructure(std::move(r));
   });
 }
