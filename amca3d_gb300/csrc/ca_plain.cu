@@ -1121,7 +1121,10 @@ __global__ void envelope_eval_kernel(long long n, const double *l2g, const doubl
 
 // Set-up of the no-allocation entry point: clear the control block and the
 // look-back words, mark every site live, round the orientation matrices to float.
-__global__ void noalloc_setup_kernel(PlainDevice d, long long liquid) {
+// `bad` (preset to all ones) receives the smallest index of a site whose cell
+// is not an interior cell or does not follow the previous site's cell; the
+// host reads it before any kernel indexes the field with a site cell.
+__global__ void noalloc_setup_kernel(PlainDevice d, long long liquid, unsigned long long *bad) {
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
   if (tid == 0) {
@@ -1129,7 +1132,17 @@ __global__ void noalloc_setup_kernel(PlainDevice d, long long liquid) {
     c.liquid = liquid;
     *d.ctrl = c;
   }
-  for (long long i = tid; i < d.nsites; i += stride) d.site_live[i] = 1;
+  const Grid g = d.grid;
+  for (long long i = tid; i < d.nsites; i += stride) {
+    d.site_live[i] = 1;
+    const long long c = d.site_cell[i];
+    bool ok = c >= 0 && c < d.ncells && (i == 0 || d.site_cell[i - 1] < c);
+    if (ok) {
+      const long long k = c / g.nxyg, r = c - k * g.nxyg, j = r / g.nxg, ii = r - j * g.nxg;
+      ok = ii >= 1 && ii <= g.nx && j >= 1 && j <= g.ny && k >= 1 && k <= g.nz;
+    }
+    if (!ok) atomicMin(bad, (unsigned long long)i);
+  }
   float *m32 = const_cast<float *>(d.omat32);
   for (long long i = tid; i < 9 * d.nsites; i += stride) m32[i] = (float)d.omat[i];
   for (long long i = tid; i < kStatusWords; i += stride) {
@@ -1160,9 +1173,10 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
-  size_t ctrl, live, omat32, scanA, gx, gy, gz, gori, gcell, act0, act1, gen0, gen1, liq, con, child, solid, claimed,
-      scanB, total;
-  // n interior cells, s sites, `cells` ghost-inclusive cells
+  size_t ctrl, check, live, omat32, scanA, gx, gy, gz, gori, gcell, act0, act1, gen0, gen1, liq, con, child, solid,
+      claimed, scanB, total;
+  // n interior cells, s sites, `cells` ghost-inclusive cells; the caller
+  // bounds all three (see kNoAllocMaxCells) so that no size below wraps
   NoAllocLayout(long long n, long long s, long long cells) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -1171,6 +1185,7 @@ struct NoAllocLayout {
       return at;
     };
     ctrl = take(sizeof(PlainCtrl));
+    check = take(sizeof(unsigned long long));
     live = take((size_t)s);
     omat32 = take((size_t)s * 9 * sizeof(float));
     scanA = take((size_t)2 * kStatusWords * 8);
@@ -1193,10 +1208,29 @@ struct NoAllocLayout {
   }
 };
 
+// Largest grid edge and cell count the entry point considers. The edge bound
+// keeps (nx+2)(ny+2)(nz+2) inside 63 bits; the cell bound (the scratch size
+// in bytes: every interior cell takes more than a byte of scratch) keeps
+// every buffer size of NoAllocLayout far from wrapping. Grids that pass both
+// may still be rejected by the scratch size itself.
+constexpr long long kNoAllocMaxEdge = 1ll << 20;
+constexpr long long kNoAllocMaxCells = (long long)kNoAllocScratchBytes;
+
 int noalloc_fail(char *err, size_t errlen, int code, const char *what, const char *detail) {
   if (err && errlen) snprintf(err, errlen, "amca_plain_run_noalloc: %s%s%s", what, detail ? ": " : "", detail ? detail : "");
   return code;
 }
+
+// Puts the caller's current device back on every return path.
+struct DeviceRestore {
+  int dev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  }
+  ~DeviceRestore() {
+    if (dev >= 0) cudaSetDevice(dev);
+  }
+};
 }  // namespace
 
 }  // namespace amca
@@ -1213,7 +1247,13 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
     return noalloc_fail(err, errlen, AMCA_ERR_ARG, "grid dimensions and cell size must be positive", nullptr);
   if (device < 0 || device >= kNoAllocMaxDevices)
     return noalloc_fail(err, errlen, AMCA_ERR_ARG, "device ordinal out of range", nullptr);
-  const long long n = (long long)p->nx * p->ny * p->nz;
+  if (p->nx > kNoAllocMaxEdge || p->ny > kNoAllocMaxEdge || p->nz > kNoAllocMaxEdge)
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "grid too large for the static scratch", "an edge exceeds 2^20 cells");
+  const long long n = (long long)p->nx * p->ny * p->nz;  // < 2^60: no overflow
+  if (n > kNoAllocMaxCells)
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "grid too large for the static scratch", "too many interior cells");
+  if (nsites > n)
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "more sites than interior cells", nullptr);
   const NoAllocLayout lay(n, nsites, (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2));
   if (lay.total > kNoAllocScratchBytes) {
     char detail[160];
@@ -1221,6 +1261,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
              lay.total, n, (long long)nsites, kNoAllocScratchBytes);
     return noalloc_fail(err, errlen, AMCA_ERR_ARG, "grid too large for the static scratch", detail);
   }
+  DeviceRestore restore;
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "cudaSetDevice", cudaGetErrorString(e));
   {
@@ -1295,9 +1336,22 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.scanB = (unsigned long long *)(base + lay.scanB);
   // everything that must start at zero is cleared here: the array keeps the
   // previous call's contents
-  noalloc_setup_kernel<<<256, 256, 0, s>>>(d, n);
+  unsigned long long *check = (unsigned long long *)(base + lay.check);
+  if ((e = cudaMemsetAsync(check, 0xff, sizeof *check, s)) != cudaSuccess)
+    return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "set-up", cudaGetErrorString(e));
+  noalloc_setup_kernel<<<256, 256, 0, s>>>(d, n, check);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "set-up launch", cudaGetErrorString(e));
+  unsigned long long first_bad = 0;
+  if ((e = cudaMemcpyAsync(&first_bad, check, sizeof first_bad, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "checking the site list", cudaGetErrorString(e));
+  if (first_bad != ~0ull) {
+    char detail[160];
+    snprintf(detail, sizeof detail, "site %llu: its cell is not an interior cell of the grid or does not follow "
+             "the previous site's cell", first_bad);
+    return noalloc_fail(err, errlen, AMCA_ERR_ARG, "bad site list", detail);
+  }
   if ((e = plain_init_field(d, s)) != cudaSuccess)
     return noalloc_fail(err, errlen, AMCA_ERR_CUDA, "field launch", cudaGetErrorString(e));
   const int blocks = plain_persistent_grid(device);

@@ -297,9 +297,16 @@ typedef struct {
  * 172 bytes per interior cell plus 37 per site and 100 KB, i.e. roughly
  * 190,000 interior cells) are rejected with AMCA_ERR_ARG and a message.
  *
+ * The site list is checked on the GPU before the run (every site cell an
+ * interior cell, ids strictly ascending, at most one site per interior cell);
+ * a bad list is rejected with AMCA_ERR_ARG naming the first bad site. The
+ * caller's current device is the same after the call as before it.
+ *
  * The first call on a device looks up the array's device address (the host
- * name of the array is not a device address); make that first call before
- * any stream capture. Every call shares the one array and clears what must
+ * name of the array is not a device address) and keeps it for later calls;
+ * make that first call before any stream capture, and do not reset the
+ * device (cudaDeviceReset) between calls: the kept address would then be
+ * stale. Every call shares the one array and clears what must
  * start at zero; calls that overlap on the GPU (two host threads, or two
  * streams) race and corrupt each other. Runs until solid, final_time or
  * max_steps (< 0: no limit) on `stream` (NULL: default stream) and waits for

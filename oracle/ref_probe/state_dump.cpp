@@ -126,9 +126,25 @@ static void dump_state(CellularAutomataManager_3D *ca, FILE *f) {
   if (nn) put(f, fe->thetaArray_, 8 * (size_t)nn);
 }
 
+/* Which calls to record. By default every call. For runs too large to record
+ * every step, AMCA_DUMP_EVERY=N keeps only the CA steps that are multiples of
+ * N and AMCA_DUMP_FINAL=1 keeps the call that output_last_step_result makes
+ * at the end (VtrManager::execute(0, time) once the realm has stepped,
+ * CellularAutomataManager_3D.cpp:1990-1993); with either set, only the
+ * selected calls are recorded. */
+static bool selected(CellularAutomataManager_3D *ca, int numStep) {
+  const char *every = getenv("AMCA_DUMP_EVERY");
+  const char *fin = getenv("AMCA_DUMP_FINAL");
+  const long n = every ? atol(every) : 0;
+  const bool want_final = fin && *fin == '1';
+  if (n <= 0 && !want_final) return true;
+  if (numStep == 0 && ca->iStep_ > 0) return want_final;
+  return n > 0 && ca->iStep_ % n == 0;
+}
+
 extern "C" bool __wrap__ZN10VtrManager7executeEid(VtrManager *self, int numStep, double time) {
   const char *path = getenv("AMCA_DUMP");
-  if (path && *path) {
+  if (path && *path && selected(self->caManager_, numStep)) {
     FILE *f = fopen(path, "ab");
     if (!f) {
       fprintf(stderr, "state_dump: cannot open %s\n", path);
