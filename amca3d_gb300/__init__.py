@@ -70,6 +70,10 @@ EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "am
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
            "amca_plain_run_noalloc", "amca_selftest_barrier", "amca_release_cached_memory", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
+           "amca_set_scan_frames", "amca_set_thermal_frames", "amca_get_frame_stats", "amca_thermal_create",
+           "amca_thermal_train", "amca_thermal_eval", "amca_thermal_gradients", "amca_thermal_param_count",
+           "amca_thermal_get_params", "amca_thermal_set_params", "amca_thermal_get_encoding", "amca_thermal_frames",
+           "amca_thermal_last_error", "amca_thermal_destroy",
            "amca_batch_create", "amca_batch_run", "amca_batch_tune", "amca_batch_set_layout", "amca_batch_get_layout",
            "amca_batch_get_stats",
            "amca_batch_last_error",
@@ -85,6 +89,47 @@ class Rosenthal(ctypes.Structure):
                 ("diffusivity", ctypes.c_double), ("t0", ctypes.c_double), ("t_cap", ctypes.c_double),
                 ("x_start", ctypes.c_double), ("y_line", ctypes.c_double), ("z_top", ctypes.c_double),
                 ("void_above_set", ctypes.c_int32), ("void_above", ctypes.c_double), ("t_void", ctypes.c_double)]
+
+
+class Scan(ctypes.Structure):
+    """amca_scan of include/amca3d.h: frames of a raster scan (FE field or model)."""
+    _fields_ = [("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double), ("nodes", ctypes.c_int32 * 3),
+                ("frames", ctypes.c_int32), ("length_scale", ctypes.c_double), ("frame_dt", ctypes.c_double),
+                ("time_scale", ctypes.c_double), ("time_offset", ctypes.c_double), ("power", ctypes.c_double),
+                ("absorptivity", ctypes.c_double), ("speed", ctypes.c_double), ("conductivity", ctypes.c_double),
+                ("diffusivity", ctypes.c_double), ("t0", ctypes.c_double), ("t_cap", ctypes.c_double),
+                ("x_start", ctypes.c_double), ("x_turn", ctypes.c_double), ("y_line", ctypes.c_double),
+                ("z_top", ctypes.c_double), ("hatch", ctypes.c_double), ("track_time", ctypes.c_double),
+                ("ntracks", ctypes.c_int32)]
+
+    @classmethod
+    def of(cls, **kw) -> "Scan":
+        s = cls()
+        for k, v in kw.items():
+            if k in ("origin", "nodes"):
+                for a in range(3):
+                    getattr(s, k)[a] = v[a]
+            else:
+                setattr(s, k, v)
+        return s
+
+
+class ThermalSpec(ctypes.Structure):
+    """amca_thermal_spec of include/amca3d.h."""
+    _fields_ = [("power_lo", ctypes.c_double), ("power_hi", ctypes.c_double), ("speed_lo", ctypes.c_double),
+                ("speed_hi", ctypes.c_double), ("absorptivity", ctypes.c_double), ("conductivity", ctypes.c_double),
+                ("diffusivity", ctypes.c_double), ("t0", ctypes.c_double), ("t_cap", ctypes.c_double),
+                ("window_lo", ctypes.c_double * 3), ("window_hi", ctypes.c_double * 3),
+                ("near_lo", ctypes.c_double * 3), ("near_hi", ctypes.c_double * 3), ("near_fraction", ctypes.c_double),
+                ("shell_lo", ctypes.c_double), ("shell_hi", ctypes.c_double), ("shell_fraction", ctypes.c_double),
+                ("fourier_sigma", ctypes.c_double), ("fourier_sigma_pv", ctypes.c_double),
+                ("log_output", ctypes.c_int32), ("t_shift", ctypes.c_double), ("t_scale", ctypes.c_double),
+                ("seed", ctypes.c_uint64)]
+
+
+class ThermalTrainStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int64), ("samples_seen", ctypes.c_int64), ("first_loss", ctypes.c_double),
+                ("last_loss", ctypes.c_double), ("ms", ctypes.c_double)]
 
 
 class BatchStats(ctypes.Structure):
@@ -188,6 +233,37 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]
     lib.amca_destroy.restype = None
+    lib.amca_set_scan_frames.argtypes = [vp, ctypes.POINTER(Scan)]
+    lib.amca_set_scan_frames.restype = i
+    lib.amca_set_thermal_frames.argtypes = [vp, vp, ctypes.POINTER(Scan), ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double]
+    lib.amca_set_thermal_frames.restype = i
+    lib.amca_get_frame_stats.argtypes = [vp, vp]
+    lib.amca_get_frame_stats.restype = i
+    lib.amca_thermal_create.argtypes = [i, ctypes.POINTER(ThermalSpec), ctypes.POINTER(vp)]
+    lib.amca_thermal_create.restype = i
+    lib.amca_thermal_train.argtypes = [vp, i64, i, i, ctypes.c_double, ctypes.c_double,
+                                       ctypes.POINTER(ThermalTrainStats)]
+    lib.amca_thermal_train.restype = i
+    lib.amca_thermal_eval.argtypes = [vp, vp, i64, vp, vp]
+    lib.amca_thermal_eval.restype = i
+    lib.amca_thermal_gradients.argtypes = [vp, vp, vp, i64, vp, vp]
+    lib.amca_thermal_gradients.restype = i
+    lib.amca_thermal_param_count.argtypes = []
+    lib.amca_thermal_param_count.restype = i64
+    lib.amca_thermal_get_params.argtypes = [vp, vp]
+    lib.amca_thermal_get_params.restype = i
+    lib.amca_thermal_set_params.argtypes = [vp, vp]
+    lib.amca_thermal_set_params.restype = i
+    lib.amca_thermal_get_encoding.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    lib.amca_thermal_get_encoding.restype = i
+    lib.amca_thermal_frames.argtypes = [vp, ctypes.POINTER(Scan), ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, vp, vp, vp]
+    lib.amca_thermal_frames.restype = i
+    lib.amca_thermal_last_error.argtypes = [vp]
+    lib.amca_thermal_last_error.restype = cp
+    lib.amca_thermal_destroy.argtypes = [vp]
+    lib.amca_thermal_destroy.restype = None
     for name in ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "amca_initialize", "amca_step",
                  "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats"):
         getattr(lib, name).restype = i
@@ -359,6 +435,27 @@ class CellularAutomataRealm:
                 setattr(r, k, v)
         self._check(self._lib.amca_set_rosenthal_frames(self._h, ctypes.byref(r)))
 
+    def set_scan_frames(self, **kw) -> None:
+        """FE-coupled decks: frames of a raster scan's FE field (fields of
+        amca_scan), produced on the GPU a window at a time."""
+        self._scan = Scan.of(**kw)
+        self._check(self._lib.amca_set_scan_frames(self._h, ctypes.byref(self._scan)))
+
+    def set_thermal_frames(self, model: "ThermalModel", t_liq: float, band: float, thresh: float, **kw) -> None:
+        """FE-coupled decks: frames of a raster scan from a trained thermal
+        model, with the FE field where the model's error estimate exceeds
+        thresh within band of t_liq (K). The model must outlive the realm."""
+        self._scan = Scan.of(**kw)
+        self._model = model
+        self._check(self._lib.amca_set_thermal_frames(self._h, model.handle, ctypes.byref(self._scan), float(t_liq),
+                                                      float(band), float(thresh)))
+
+    def frame_stats(self) -> dict:
+        out = np.zeros(5, np.int64)
+        self._check(self._lib.amca_get_frame_stats(self._h, out.ctypes.data_as(ctypes.c_void_p)))
+        return dict(frames=int(out[0]), fills=int(out[1]), model_nodes=int(out[2]), near_liquidus=int(out[3]),
+                    fallbacks=int(out[4]))
+
     def field(self, name: str = "orientation_id", out: Optional[np.ndarray] = None) -> np.ndarray:
         fid = FIELD_IDS[name]
         n = self.cells_with_ghosts
@@ -494,3 +591,111 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class ThermalModel:
+    """The learned thermal model (amca_thermal_* of include/amca3d.h): a
+    Fourier-feature MLP trained on the GPU by the library's tensor-core
+    kernels to stand in for the FE nodal temperatures of a scanning laser."""
+
+    def __init__(self, device: int = 0, **spec):
+        self._lib = load_library()
+        s = ThermalSpec()
+        for k, v in spec.items():
+            if k in ("window_lo", "window_hi", "near_lo", "near_hi"):
+                for a in range(3):
+                    getattr(s, k)[a] = v[a]
+            else:
+                setattr(s, k, v)
+        self.spec = spec
+        self._h = ctypes.c_void_p()
+        rc = self._lib.amca_thermal_create(int(device), ctypes.byref(s), ctypes.byref(self._h))
+        if rc != AMCA_OK:
+            raise AmcaError(rc, "amca_thermal_create failed (check the spec ranges)")
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def _check(self, rc: int) -> None:
+        if rc != AMCA_OK:
+            raise AmcaError(rc, self._lib.amca_thermal_last_error(self._h).decode())
+
+    @staticmethod
+    def param_count() -> int:
+        return int(load_library().amca_thermal_param_count())
+
+    def train(self, samples: int, steps: int, batch: int, lr_max: float = 1e-3, lr_min: float = 1e-5) -> dict:
+        st = ThermalTrainStats()
+        self._check(self._lib.amca_thermal_train(self._h, int(samples), int(steps), int(batch), float(lr_max),
+                                                 float(lr_min), ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def eval(self, raw: np.ndarray):
+        """(T, error estimate) in K for raw inputs [n x 5]."""
+        raw = np.ascontiguousarray(raw, np.float32).reshape(-1, 5)
+        n = raw.shape[0]
+        T = np.zeros(n, np.float32)
+        e = np.zeros(n, np.float32)
+        vp = ctypes.c_void_p
+        self._check(self._lib.amca_thermal_eval(self._h, raw.ctypes.data_as(vp), n, T.ctypes.data_as(vp),
+                                                e.ctypes.data_as(vp)))
+        return T, e
+
+    def gradients(self, raw: np.ndarray, target: np.ndarray):
+        """(gradient vector, [n x 2] outputs mu, s) of one batch; no update."""
+        raw = np.ascontiguousarray(raw, np.float32).reshape(-1, 5)
+        y = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(self.param_count(), np.float32)
+        pred = np.zeros((raw.shape[0], 2), np.float32)
+        vp = ctypes.c_void_p
+        self._check(self._lib.amca_thermal_gradients(self._h, raw.ctypes.data_as(vp), y.ctypes.data_as(vp),
+                                                     raw.shape[0], g.ctypes.data_as(vp), pred.ctypes.data_as(vp)))
+        return g, pred
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        self._check(self._lib.amca_thermal_get_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.param_count():
+            raise ValueError("wrong parameter count")
+        self._check(self._lib.amca_thermal_set_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
+
+    def encoding(self) -> dict:
+        f = np.zeros(64 * 5, np.float32)
+        sh = np.zeros(5, np.float32)
+        sc = np.zeros(5, np.float32)
+        ts, tsc, lo = ctypes.c_float(), ctypes.c_float(), ctypes.c_int32()
+        vp = ctypes.c_void_p
+        self._check(self._lib.amca_thermal_get_encoding(self._h, f.ctypes.data_as(vp), sh.ctypes.data_as(vp),
+                                                        sc.ctypes.data_as(vp), ctypes.byref(ts), ctypes.byref(tsc),
+                                                        ctypes.byref(lo)))
+        return dict(fourier=f.reshape(64, 5), in_shift=sh, in_scale=sc, t_shift=ts.value, t_scale=tsc.value,
+                    log_output=int(lo.value))
+
+    def frames(self, scan: Scan, f0: int, nf: int, t_liq: float, band: float, thresh: float, with_fe: bool = False):
+        """(model frames [nf x nodes], FE frames or None, counts: evaluated, near the liquidus, fallbacks)."""
+        nn = scan.nodes[0] * scan.nodes[1] * scan.nodes[2]
+        out = np.zeros((nf, nn), np.float64)
+        fe = np.zeros((nf, nn), np.float64) if with_fe else None
+        counts = np.zeros(3, np.int64)
+        vp = ctypes.c_void_p
+        self._check(self._lib.amca_thermal_frames(self._h, ctypes.byref(scan), int(f0), int(nf), float(t_liq),
+                                                  float(band), float(thresh), out.ctypes.data_as(vp),
+                                                  None if fe is None else fe.ctypes.data_as(vp),
+                                                  counts.ctypes.data_as(vp)))
+        return out, fe, counts
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.amca_thermal_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1023,6 +1023,32 @@ int amca_set_rosenthal_frames(amca_t *h, const amca_rosenthal *p) {
   });
 }
 
+int amca_set_scan_frames(amca_t *h, const amca_scan *p) {
+  if (!h || !p) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_set_scan_frames needs an FE-coupled deck");
+    h->rm->set_scan(*p, nullptr, 0.0, 0.0, 0.0);
+  });
+}
+
+int amca_set_thermal_frames(amca_t *h, amca_thermal *m, const amca_scan *p, double t_liq, double band,
+                            double thresh) {
+  if (!h || !m || !p) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_set_thermal_frames needs an FE-coupled deck");
+    if (!(band >= 0) || !(thresh >= 0)) throw std::invalid_argument("band and thresh must be >= 0");
+    h->rm->set_scan(*p, thermal_model_of(m), t_liq, band, thresh);
+  });
+}
+
+int amca_get_frame_stats(amca_t *h, int64_t out[5]) {
+  if (!h || !out) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_get_frame_stats needs an FE-coupled deck");
+    h->rm->frame_stats(out);
+  });
+}
+
 int amca_get_field(amca_t *h, int field, void *dst, size_t bytes) {
   if (!h || !dst) return AMCA_ERR_ARG;
   if (h->rm) return guarded(h, [&] { h->rm->get_field(field, dst, bytes); });

@@ -92,27 +92,73 @@ void RemeltRealm::set_rosenthal(const RosenthalParams &p, int nframes, double ti
   ros_ = p;
   ros_nframes_ = nframes;
   ros_toff_ = time_offset;
-  // node coordinates and frame times exactly as the text reader would hold them
+  const int32_t nodes[3] = {p.nodes[0], p.nodes[1], p.nodes[2]};
+  synthetic_grid(p.origin, p.spacing, nodes, nframes, p.frame_dt, time_offset);
+  frames_src_ = 2;
+}
+
+// Node coordinates and frame times of generated frames, exactly as the text
+// reader would hold them for the same file.
+void RemeltRealm::synthetic_grid(const double origin[3], double spacing, const int32_t nodes[3], int nframes,
+                                 double frame_dt, double time_offset) {
   FeFrames fr;
-  for (int a = 0; a < 3; ++a) fr.nn[a] = p.nodes[a];
-  fr.nnodes = (int64_t)p.nodes[0] * p.nodes[1] * p.nodes[2];
+  for (int a = 0; a < 3; ++a) fr.nn[a] = nodes[a];
+  fr.nnodes = (int64_t)nodes[0] * nodes[1] * nodes[2];
   fr.coord.resize(3 * (size_t)fr.nnodes);
   for (int64_t n = 0; n < fr.nnodes; ++n) {
-    const int64_t I[3] = {n % p.nodes[0], (n / p.nodes[0]) % p.nodes[1], n / ((int64_t)p.nodes[0] * p.nodes[1])};
+    const int64_t I[3] = {n % nodes[0], (n / nodes[0]) % nodes[1], n / ((int64_t)nodes[0] * nodes[1])};
     for (int d = 0; d < 3; ++d) {
-      double x = p.origin[d] + p.spacing * (double)I[d];
+      double x = origin[d] + spacing * (double)I[d];
       x += cfg_.fe.offset[d];
       x *= cfg_.fe.length_scale;
       fr.coord[3 * n + d] = x;
     }
   }
   fr.times.resize((size_t)nframes);
-  const double t0 = time_offset + 0 * p.frame_dt;
+  const double t0 = time_offset + 0 * frame_dt;
   fr.times[0] = 0.0;
-  for (int f = 1; f < nframes; ++f) fr.times[f] = ((time_offset + f * p.frame_dt) - t0) * cfg_.fe.time_scale;
+  for (int f = 1; f < nframes; ++f) fr.times[f] = ((time_offset + f * frame_dt) - t0) * cfg_.fe.time_scale;
   fr.nframes = nframes;
   frames_ = std::move(fr);
-  frames_src_ = 2;
+}
+
+void RemeltRealm::set_scan(const amca_scan &scan, ThermalModel *model, double t_liq, double band, double thresh) {
+  if (initialized_) throw StateError("frames must be set before amca_initialize");
+  if (scan.frames < 2) throw std::invalid_argument("at least two frames");
+  for (int a = 0; a < 3; ++a)
+    if (scan.nodes[a] < 2) throw std::invalid_argument("at least 2 nodes per axis");
+  if (!(scan.spacing > 0) || !(scan.length_scale > 0) || !(scan.frame_dt > 0) || !(scan.time_scale > 0))
+    throw std::invalid_argument("scan: spacing, length_scale, frame_dt and time_scale must be positive");
+  if (scan.ntracks > 1 && !(scan.track_time > 0)) throw std::invalid_argument("scan: track_time must be positive");
+  scan_ = scan;
+  model_ = model;
+  t_liq_ = t_liq;
+  band_ = band;
+  thresh_ = thresh;
+  synthetic_grid(scan.origin, scan.spacing, scan.nodes, scan.frames, scan.frame_dt, scan.time_offset);
+  frames_src_ = 3;
+}
+
+// Frames avail_ .. upto - 1 into the ring (source 3).
+void RemeltRealm::fill_frames(int upto) {
+  upto = std::min<int>(upto, (int)nframes_);
+  if (upto <= avail_) return;
+  fill_scan_frames(&scan_, model_, t_liq_, band_, thresh_, avail_, upto - avail_, ring_, slots_, fcount_, stream_);
+  produced_ += upto - avail_;
+  ++fills_;
+  avail_ = upto;
+  dev_.frames_avail = avail_;
+}
+
+void RemeltRealm::frame_stats(int64_t out[5]) {
+  out[0] = produced_;
+  out[1] = fills_;
+  unsigned long long c[4] = {0, 0, 0, 0};
+  if (fcount_) {
+    RCK(cudaMemcpyAsync(c, fcount_, sizeof c, cudaMemcpyDeviceToHost, stream_));
+    RCK(cudaStreamSynchronize(stream_));
+  }
+  for (int i = 0; i < 3; ++i) out[2 + i] = (int64_t)c[i];
 }
 
 void RemeltRealm::set_microstructure(RestartData r) {
@@ -457,17 +503,33 @@ void RemeltRealm::initialize() {
     d.ecell = el;
   }
   // --- frames ---
-  double *frames = alloc<double>((size_t)nframes_ * d.nnodes);
-  if (frames_src_ == 2) {
-    RCK(remelt_rosenthal_frames(ros_, (int)nframes_, frames, stream_));
-  } else {
-    h2d(frames, frames_.theta.data(), frames_.theta.size() * 8);
-  }
   double *ftime = alloc<double>(nframes_);
   h2d(ftime, frames_.times.data(), nframes_ * 8);
-  d.frames = frames;
   d.frame_time = ftime;
   d.nframes = (int)nframes_;
+  if (frames_src_ == 3) {
+    // a ring of window + 4 slots, refilled a window at a time as the run reaches its end
+    window_ = 32;
+    if (const char *e = getenv("AMCA_FRAME_WINDOW")) window_ = std::max(2, atoi(e));
+    slots_ = (int)std::min<int64_t>(nframes_, window_ + 4);
+    ring_ = alloc<double>((size_t)slots_ * d.nnodes);
+    fcount_ = alloc<unsigned long long>(4);
+    RCK(cudaMemsetAsync(fcount_, 0, 4 * sizeof(unsigned long long), stream_));
+    d.frames = ring_;
+    d.frame_slots = slots_;
+    avail_ = 0;
+    fill_frames(window_ + 2);  // sets d.frames_avail (d is dev_)
+  } else {
+    double *frames = alloc<double>((size_t)nframes_ * d.nnodes);
+    if (frames_src_ == 2) {
+      RCK(remelt_rosenthal_frames(ros_, (int)nframes_, frames, stream_));
+    } else {
+      h2d(frames, frames_.theta.data(), frames_.theta.size() * 8);
+    }
+    d.frames = frames;
+    d.frame_slots = (int)nframes_;
+    d.frames_avail = (int)nframes_;
+  }
   d.bad_frame = (int)frames_.bad_frame;
   for (int i = 0; i < 3; ++i) {
     d.theta[i] = alloc<double>(d.nnodes);
@@ -564,6 +626,11 @@ void RemeltRealm::initialize() {
 
 void RemeltRealm::reset() {
   if (!initialized_) throw StateError("amca_reset before amca_initialize");
+  if (frames_src_ == 3 && avail_ > window_ + 2) {  // the ring has moved on: produce the first window again
+    avail_ = 0;
+    dev_.frames_avail = 0;
+    fill_frames(window_ + 2);
+  }
   upload_initial_state();
   kernel_ms_ = 0.0;
   launches_ = 0;
@@ -581,9 +648,10 @@ void RemeltRealm::sync_ctrl() {
                                 "more new grain objects in one step than the library supports (16384)",
                                 "time ratio error: timeRatio is less then 0",
                                 "work list overflow",
-                                "the host did not answer a velocity request in time"};
+                                "the host did not answer a velocity request in time",
+                                "a frame was needed before it was loaded"};
     const int e = ctrl_.error;
-    throw DeviceError(std::string("remelting kernel stopped: ") + (e > 0 && e < 7 ? msg[e] : "unknown error"));
+    throw DeviceError(std::string("remelting kernel stopped: ") + (e > 0 && e < 8 ? msg[e] : "unknown error"));
   }
 }
 
@@ -678,6 +746,10 @@ void RemeltRealm::run(long long max_steps) {
     launch(limit);
     if (ctrl_.status == kRemeltNeedOrient) {
       extend_orientations();
+      continue;
+    }
+    if (ctrl_.status == kRemeltNeedFrames) {
+      fill_frames(avail_ + window_);
       continue;
     }
     if (opts_.write_outputs && ctrl_.step != before && vtr_.due((int)ctrl_.step, ctrl_.time)) write_snapshot();

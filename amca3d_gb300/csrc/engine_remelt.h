@@ -20,6 +20,7 @@
 #include "fe_input.h"
 #include "host_init.h"
 #include "remelt.h"
+#include "surrogate.h"
 #include "writers.h"
 
 namespace amca {
@@ -34,6 +35,12 @@ class RemeltRealm {
   void set_frames(const int32_t nodes[3], const double *coords, int64_t nframes, const double *times,
                   const double *theta);
   void set_rosenthal(const RosenthalParams &p, int nframes, double time_offset);
+  // frames of a raster scan produced on the GPU a window at a time: the FE
+  // field (model == nullptr) or a thermal model with its fallback rule
+  void set_scan(const amca_scan &scan, ThermalModel *model, double t_liq, double band, double thresh);
+  // frames produced so far, window fills, and (model frames) nodes evaluated,
+  // nodes near the liquidus, fallbacks
+  void frame_stats(int64_t out[5]);
   // restart microstructure from memory (before prepare)
   void set_microstructure(RestartData r);
 
@@ -87,12 +94,23 @@ class RemeltRealm {
   std::string workdir_;
   bool prepared_ = false, initialized_ = false;
   // frame source
-  int frames_src_ = 0;  // 0 deck file, 1 arrays, 2 Rosenthal generator
+  int frames_src_ = 0;  // 0 deck file, 1 arrays, 2 Rosenthal generator, 3 scan (FE field or model), on a ring
   FeFrames frames_;
   RosenthalParams ros_{};
   int ros_nframes_ = 0;
   double ros_toff_ = 0.0;
   int64_t nframes_ = 0;
+  // frame ring of source 3
+  amca_scan scan_{};
+  ThermalModel *model_ = nullptr;
+  double t_liq_ = 0, band_ = 0, thresh_ = 0;
+  double *ring_ = nullptr;
+  int slots_ = 0, window_ = 0, avail_ = 0;
+  int64_t fills_ = 0, produced_ = 0;
+  unsigned long long *fcount_ = nullptr;  // device: model nodes evaluated, near the liquidus, fallbacks
+  void synthetic_grid(const double origin[3], double spacing, const int32_t nodes[3], int nframes, double frame_dt,
+                      double time_offset);
+  void fill_frames(int upto);
   std::unique_ptr<RestartData> micro_;  // set_microstructure
   // host tables
   std::unique_ptr<GlibcRand> rng_;

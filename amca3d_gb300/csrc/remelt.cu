@@ -480,7 +480,7 @@ __device__ void frame_extrema(const RemeltDevice &d, const int64_t nid[8], int f
     near = d.fnear[sl][e] != 0;
     return;
   }
-  const double *fr = d.frames + (int64_t)f * d.nnodes;
+  const double *fr = d.frames + (int64_t)(f % d.frame_slots) * d.nnodes;
   const double V = d.void_t + 0.00001;
   mx = -INFINITY;
   mn = INFINITY;
@@ -1041,6 +1041,9 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     if (!(S.time < d.final_time)) stop = kRemeltFinalTime;
     else if (S.step >= limit) stop = kRemeltStepLimit;
     else if (d.nsites > 0 && S.n_orient + d.nsites > d.orient_cap) stop = kRemeltNeedOrient;
+    // the step's frame replay reads frame f_next (and f_next + 1 when two frames share a time): both loaded,
+    // unless the frames end before them
+    else if (S.f_next + 1 >= d.frames_avail && d.frames_avail < d.nframes) stop = kRemeltNeedFrames;
     if (stop != kRemeltRunning) {
       if (gtid == 0) c->status = stop;
       break;
@@ -1419,10 +1422,16 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     if (fe_time == 0) fe_time = ts1;
     fe_time += dT;
     bool exhausted = false, bad = false;
+    bool unloaded = false;
     while (fe_time >= ts0) {
       if (f_next >= d.nframes) {
         exhausted = true;
         bad = (d.bad_frame == f_next);
+        break;
+      }
+      if (f_next >= d.frames_avail) {  // cannot happen after the check at the step's start
+        unloaded = true;
+        exhausted = true;
         break;
       }
       ts1 = ts0;
@@ -1434,8 +1443,8 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     if (!exhausted) {
       ratio = (fe_time - ts1) / (ts0 - ts1);
       if (ratio < 0.0 && gtid == 0) atomicCAS(&c->error, 0, kRemeltErrRatio);
-      const double *f0 = d.frames + (int64_t)f_new * d.nnodes;
-      const double *f1 = f0 - d.nnodes;
+      const double *f0 = d.frames + (int64_t)(f_new % d.frame_slots) * d.nnodes;
+      const double *f1 = d.frames + (int64_t)((f_new - 1) % d.frame_slots) * d.nnodes;
       double *tn = d.theta[(S.step + 1) % 3];
       float *tn32 = d.theta32[(S.step + 1) % 3];
       for (int64_t n = gtid; n < d.nnodes; n += nthr) {
@@ -1494,6 +1503,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     }
     if (gtid == 0) {
       if (bad) atomicCAS(&c->error, 0, kRemeltErrFrame);
+      if (unloaded) atomicCAS(&c->error, 0, kRemeltErrRing);
       if (!exhausted) {
         c->fstat_frame[f_new & 1] = f_new;
         c->fstat_frame[(f_new - 1) & 1] = f_new - 1;

@@ -18,10 +18,10 @@ namespace amca {
 constexpr int32_t kPendingGrain = 0x7fffffff;  // grain created this step, id assigned after the step
 constexpr int kNewGrainCap = 16384;            // new grain objects one step may create
 constexpr int kRemeltErrBarrier = 1, kRemeltErrFrame = 2, kRemeltErrNewGrains = 3, kRemeltErrRatio = 4,
-              kRemeltErrList = 5, kRemeltErrHost = 6;
+              kRemeltErrList = 5, kRemeltErrHost = 6, kRemeltErrRing = 7;
 // why a launch returned
 constexpr int kRemeltRunning = 0, kRemeltFinalTime = 1, kRemeltFramesEnd = 2, kRemeltNeedOrient = 3,
-              kRemeltStepLimit = 4;
+              kRemeltStepLimit = 4, kRemeltNeedFrames = 5;
 
 // Growth velocities whose glibc pow() rounding cannot be decided on the GPU
 // (an integer power within 0.02 ulp of a rounding midpoint; glibc's pow errs
@@ -116,9 +116,11 @@ struct RemeltDevice {
   // FE replay
   int nn[3];
   int64_t nnodes, nelem;
-  const double *frames;      // nframes x nnodes
-  const double *frame_time;  // per frame, scaled
-  int nframes;
+  const double *frames;      // ring of frame_slots frames (frame f in slot f % frame_slots), nnodes each
+  const double *frame_time;  // per frame, scaled (every frame)
+  int nframes;               // frames in all
+  int frame_slots;           // slots of the ring (nframes when every frame is resident)
+  int frames_avail;          // frames 0 .. frames_avail - 1 have been loaded (the last frame_slots of them are held)
   int bad_frame;             // index of a malformed frame, or -1
   double *theta[3];          // node temperatures by CA step (mod 3)
   float *theta32[3];         // the same, rounded to float

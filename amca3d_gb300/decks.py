@@ -636,3 +636,75 @@ def pbf_frames(cells, cell_size: float, nframes: int) -> FrameSpec:
     src = Rosenthal(power=200.0, absorptivity=0.4, speed=1.0, conductivity=20.0, diffusivity=5.0e-6, t0=300.0,
                     t_cap=3000.0, x_start=-5.0e-5, y_line=0.5 * ny * cell_size, z_top=nz * cell_size)
     return FrameSpec(origin=(-sp, -sp, -sp), spacing=sp, nodes=nodes, frame_dt=1.0e-6, frames=nframes, source=src)
+
+
+# ---------------------------------------------------------------------------
+# Thermal model workload: a multi-track raster scan over a large block, with
+# the FE field or the learned model as the frame source.
+# ---------------------------------------------------------------------------
+def thermal_spec(seed: int = 4, fourier_sigma: float = 0.5, fourier_sigma_pv: float = 0.1, log_output: int = 0,
+                 near_fraction: float = 0.3, shell_fraction: float = 0.4) -> dict:
+    """amca_thermal_spec of the learned thermal model: laser power 150-350 W,
+    scan speed 0.5-1.5 m/s, the PBF physics (A = 0.4, k = 20 W/(m K),
+    alpha = 5e-6 m^2/s, T0 = 300 K, cap 3000 K), a window from 1.2 mm behind
+    to 0.15 mm ahead of the source, +-0.25 mm across and 0.3 mm deep; of the
+    samples, near_fraction from the melt-pool box (the region where the field
+    exceeds 1450 K anywhere in the power and speed ranges) and shell_fraction
+    from that box until the field lies between 1450 and 1950 K (around the
+    1600-1700 K mushy zone); T = 300 K + 1000 K * output, or
+    299 K + 100 K * exp(output) with log_output."""
+    return dict(power_lo=150.0, power_hi=350.0, speed_lo=0.5, speed_hi=1.5, absorptivity=0.4, conductivity=20.0,
+                diffusivity=5.0e-6, t0=300.0, t_cap=3000.0,
+                window_lo=(-1.2e-3, -0.25e-3, -0.02e-3), window_hi=(0.15e-3, 0.25e-3, 0.3e-3),
+                near_lo=(-1.05e-3, -0.14e-3, -0.01e-3), near_hi=(0.06e-3, 0.14e-3, 0.14e-3),
+                near_fraction=near_fraction, shell_lo=1450.0, shell_hi=1950.0, shell_fraction=shell_fraction,
+                fourier_sigma=fourier_sigma, fourier_sigma_pv=fourier_sigma_pv, log_output=log_output,
+                t_shift=299.0 if log_output else 300.0, t_scale=100.0 if log_output else 1000.0, seed=seed)
+
+
+# Training schedule of the learned thermal model: 50M samples (seed 4), Adam
+# 1e-3 -> 1e-5 on a cosine schedule, 20,000 steps of 32,768.
+THERMAL_TRAIN = dict(samples=50_000_000, steps=20_000, batch=32_768, lr_max=1.0e-3, lr_min=1.0e-5)
+
+
+def scan_of(cells, cell_size: float, tracks: int, hatch: float, power: float = 200.0, speed: float = 1.0,
+            margin_start: float = 5.0e-5, margin_end: float = 5.0e-4, frame_dt: float = 1.0e-6) -> dict:
+    """amca_scan fields of a raster of `tracks` passes along x over a block of
+    `cells`: 10 um FE nodes from -10 um to one node past the block, tracks
+    centred across y with `hatch` spacing on the top surface, alternating
+    direction; each pass runs from margin_start before the block to margin_end
+    past it (the melt-pool tail leaves the block) at `speed`, frames every
+    frame_dt for the whole scan."""
+    nx, ny, nz = cells
+    sp = 1.0e-5
+    nodes = tuple(int(math.ceil(n * cell_size / sp)) + 3 for n in (nx, ny, nz))
+    length = nx * cell_size
+    track_time = (margin_start + length + margin_end) / speed
+    y0 = 0.5 * ny * cell_size - 0.5 * (tracks - 1) * hatch
+    frames = int(math.ceil(tracks * track_time / frame_dt)) + 2
+    return dict(origin=(-sp, -sp, -sp), spacing=sp, nodes=nodes, frames=frames, length_scale=1.0,
+                frame_dt=frame_dt, time_scale=1.0, time_offset=0.0, power=power, absorptivity=0.4, speed=speed,
+                conductivity=20.0, diffusivity=5.0e-6, t0=300.0, t_cap=3000.0, x_start=-margin_start,
+                x_turn=length + margin_start, y_line=y0, z_top=nz * cell_size, hatch=hatch, track_time=track_time,
+                ntracks=tracks)
+
+
+def config_thermal_block(name: str, cells, tracks: int, hatch: float, grains: int, seed: int = 4):
+    """A raster-scan workload on a columnar baseplate with the PBF physics:
+    liquidus 1700 K, solidus 1600 K, bulk sites 1e13 m^-3 (8 K, 2 K), KGT
+    a2 = 2.03e-4, 2 um cells, 200 W at 1 m/s. Returns (deck, scan fields,
+    microstructure arrays)."""
+    case = RemeltCase(name=name, cells=tuple(cells), cell_size=2.0e-6, nucleation=True, seed=seed,
+                      bulk=(1.0e13, 8.0, 2.0), surface=(0.0, 0.5, 0.1), melting_temperature=1700.0,
+                      solidus_temperature=1600.0, a=(0.0, 2.03e-4, 0.0), microstructure="baseplate.txt",
+                      termination_time=1.0, time_step=1.0e-6, time_step_factor=0.4)
+    scan = scan_of(cells, case.cell_size, tracks=tracks, hatch=hatch)
+    micro = columnar_microstructure(cells, case.cell_size, case.origin, grains, seed)
+    return case, scan, micro
+
+
+def config_thermal_1024():
+    """The learned-model workload: a 5-track raster (100 um hatch, alternating
+    direction, 200 W, 1 m/s) over 1024 x 512 x 256 cells of 2 um (134M) on a
+    columnar baseplate of 8,000 grains (seed 4)."""
+    return config_thermal_block("thermal_1024", (1024, 512, 256), tracks=5, hatch=1.0e-4, grains=8000)

@@ -142,6 +142,121 @@ typedef struct {
 } amca_rosenthal;
 int amca_set_rosenthal_frames(amca_t *h, const amca_rosenthal *p);
 
+/* Synthetic FE frames of a raster scan, generated on the GPU: ntracks
+ * passes along x with alternating direction (even tracks from x_start in +x,
+ * odd tracks from x_turn in -x), track k on y = y_line + k * hatch, each
+ * track_time seconds long; every frame holds the Rosenthal field of the
+ * current pass (the amca_rosenthal formula with xi measured along the
+ * direction of travel). Node grid, units and frame times as in
+ * amca_rosenthal. With ntracks = 1 the frames are amca_set_rosenthal_frames'
+ * bit for bit. The frames are produced a window at a time into a ring of
+ * device slots as the run reaches them, so device memory does not grow with
+ * the frame count. Before amca_initialize. Stands in for the frame file of
+ * FiniteElementManager (CA/src/LoadDataFromFile.cpp:21-191). */
+typedef struct amca_scan_s {
+  double origin[3];
+  double spacing;
+  int32_t nodes[3];
+  int32_t frames;
+  double length_scale, frame_dt, time_scale, time_offset;
+  double power, absorptivity, speed, conductivity, diffusivity, t0, t_cap;
+  double x_start, x_turn, y_line, z_top, hatch, track_time;
+  int32_t ntracks;
+} amca_scan;
+int amca_set_scan_frames(amca_t *h, const amca_scan *p);
+
+/* ---- Thermal model: a learned stand-in for the FE nodal temperatures ----
+ * No counterpart in the reference, which reads FE frames from text files
+ * (CA/src/LoadDataFromFile.cpp:21-191) and interpolates them at every CA
+ * step (CA/src/MapVoxelManager.cpp:746-799). The model maps (along-track
+ * offset from the laser, lateral offset, depth below the top surface, power,
+ * speed) to a temperature and an error estimate: 64 Fourier features, four
+ * hidden layers of 256 with SiLU (bf16 tensor-core GEMMs, FP32 accumulation),
+ * an FP32 head. It is trained on the GPU by this library's own forward and
+ * backward kernels on samples of the FE field of a scanning source
+ * (amca_scan's formula) and can then produce a realm's frames, falling back
+ * to the FE field at nodes near the liquidus whose error estimate is above a
+ * threshold. One model per handle; calls on a handle are not thread-safe. */
+typedef struct amca_thermal amca_thermal;
+
+typedef struct {
+  double power_lo, power_hi;                 /* training range of the laser power (W) */
+  double speed_lo, speed_hi;                 /* training range of the scan speed (m/s) */
+  double absorptivity, conductivity, diffusivity, t0, t_cap;  /* FE field physics */
+  double window_lo[3], window_hi[3];         /* offsets from the source the model covers (m):
+                                                along-track, lateral, depth */
+  double near_lo[3], near_hi[3];             /* melt-pool box sampled more densely (m) */
+  double near_fraction;                      /* share of the training samples from that box */
+  double shell_lo, shell_hi;                 /* temperature band (K) sampled more densely ... */
+  double shell_fraction;                     /* ... this share of the samples: points of the melt-pool
+                                                box redrawn (up to 64 times) until their FE temperature
+                                                lies in the band */
+  double fourier_sigma;                      /* spread of the Fourier frequencies along the three offsets
+                                                (turns per window half-width) */
+  double fourier_sigma_pv;                   /* the same along power and speed (turns per range half-width) */
+  int32_t log_output;                        /* 0: T = t_shift + t_scale * mu;
+                                                1: T = t_shift + t_scale * exp(mu) (t_shift below t0) */
+  double t_shift, t_scale;                   /* output map (K) */
+  uint64_t seed;
+} amca_thermal_spec;
+
+typedef struct {
+  int64_t steps, samples_seen;
+  double first_loss, last_loss; /* mean 0.5 (mu - y)^2 (normalised units) over the first and last 5% of steps */
+  double ms;                    /* wall time of the training loop */
+} amca_thermal_train_stats;
+
+int amca_thermal_create(int device, const amca_thermal_spec *spec, amca_thermal **out);
+/* Adam on `samples` training samples generated on the GPU from the spec's
+ * seed: `steps` steps of `batch` samples (a multiple of 128), learning rate
+ * from lr_max to lr_min on a cosine schedule after a short warm-up. */
+int amca_thermal_train(amca_thermal *m, int64_t samples, int steps, int batch, double lr_max, double lr_min,
+                       amca_thermal_train_stats *st);
+/* Temperatures and error estimates (K) of n points given as raw inputs
+ * (5 floats each: along-track offset, lateral offset, depth (m), power (W),
+ * speed (m/s)); host buffers. Runs the fused inference kernel. */
+int amca_thermal_eval(amca_thermal *m, const float *raw, int64_t n, float *T, float *err);
+/* Gradients of the training loss of one batch (n a multiple of 128; raw
+ * inputs and normalised targets in host memory) with respect to every
+ * parameter, without updating them, and the network outputs (mu, s per
+ * sample). For checking the training kernels. */
+int amca_thermal_gradients(amca_thermal *m, const float *raw, const float *target, int64_t n, float *grad,
+                           float *pred);
+/* Parameter vector (FP32 masters): per hidden layer l its weights [256][in]
+ * (in = 128 for l = 0, else 256) then its 256 biases, then the head weights
+ * [2][256] and its 2 biases. */
+int64_t amca_thermal_param_count(void);
+int amca_thermal_get_params(amca_thermal *m, float *params);
+int amca_thermal_set_params(amca_thermal *m, const float *params);
+/* The fixed encoding: Fourier matrix [64][5], u = (raw - shift) * scale, and
+ * the output map (t_shift, t_scale, log_output of the spec). */
+int amca_thermal_get_encoding(amca_thermal *m, float *fourier, float *in_shift, float *in_scale, float *t_shift,
+                              float *t_scale, int32_t *log_output);
+/* Frames f0 .. f0 + nf - 1 of a scan from the model into host memory
+ * (nf x nodes): nodes inside the model's window around the source take the
+ * model's temperature, the others t0; a node whose model temperature lies
+ * within band (K) of t_liq and whose error estimate exceeds thresh (K) takes
+ * the FE field instead. counts[0..2] (may be NULL) = nodes evaluated, near the
+ * liquidus, fallbacks. fe = NULL, or nf x nodes doubles receiving the FE
+ * field of the same frames (amca_set_scan_frames' values) for comparison. */
+int amca_thermal_frames(amca_thermal *m, const amca_scan *scan, int32_t f0, int32_t nf, double t_liq, double band,
+                        double thresh, double *frames, double *fe, int64_t *counts);
+const char *amca_thermal_last_error(const amca_thermal *m);
+void amca_thermal_destroy(amca_thermal *m);
+
+/* Frames of a scan from a trained model instead of the FE field (the realm
+ * keeps a reference to the model, which must outlive it): as
+ * amca_thermal_frames, produced a window at a time into a ring of device
+ * slots while the run reaches them. Before amca_initialize. */
+int amca_set_thermal_frames(amca_t *h, amca_thermal *m, const amca_scan *p, double t_liq, double band,
+                            double thresh);
+
+/* Frame production of a realm whose frames come from amca_set_scan_frames or
+ * amca_set_thermal_frames: out[0] frames produced, out[1] window fills,
+ * out[2..4] (model frames) nodes the model evaluated, nodes near the
+ * liquidus, fallbacks to the FE field. No counterpart in the reference. */
+int amca_get_frame_stats(amca_t *h, int64_t out[5]);
+
 /* Restart microstructure from memory instead of the deck's
  * load_microstructure_information file (same content as grainInfo<rank>.txt,
  * CellularAutomataManager_3DRemelting::load_microstructure_information,

@@ -201,3 +201,45 @@ def test_cli_runs_the_deck_like_the_reference(amca, tmp_path):
     got.pop("cli.log", None)
     assert got == golden["files"]
     assert f"Time Step Count: {golden['steps']}" in (tmp_path / "cli.log").read_text()
+
+
+def scan_kwargs_of(fs):
+    """amca_scan fields of a one-track FrameSpec (the Rosenthal frames' source)."""
+    r = fs.rosenthal_kwargs()
+    assert not r.pop("void_above_set")
+    for k in ("void_above", "t_void"):
+        r.pop(k)
+    r.update(x_turn=0.0, hatch=0.0, track_time=0.0, ntracks=1)
+    return r
+
+
+@pytest.mark.parametrize("window", ["2", "5"])
+@pytest.mark.parametrize("name", ["remelt_nucleation", "remelt_new_grains"])
+def test_remelt_gpu_frames_streamed_through_a_ring(amca, tmp_path, monkeypatch, name, window):
+    """Frames produced on the GPU a few at a time into a ring of window + 4
+    slots (the kernel stops when it needs a frame not yet produced) give the
+    reference's run bit for bit, after a reset too."""
+    monkeypatch.setenv("AMCA_FRAME_WINDOW", window)
+    fx = FIX[name]
+    M.prepare(fx, str(tmp_path))
+    r = amca.CellularAutomataRealm(fx.case.to_yaml(), seed=fx.case.seed, workdir=str(tmp_path))
+    r.set_scan_frames(**scan_kwargs_of(fx.frames))
+    r.initialize()
+    g = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    fields = [str(f) for f in g["fields"]]
+    for i in range(40):  # step by step through the first refills
+        dt = r.single_integration_step()
+        assert r.stats()["time"] == g["time"][i] and dt == g["dt"][i], f"step {i + 1}"
+        d = digests(r)
+        assert all(d[k] == g["digests"][i][fields.index(k)] for k in STATE), f"step {i + 1}"
+    r.run()
+    st = r.stats()
+    assert st["step"] == len(g["digests"]) and st["time"] == g["time"][-1]
+    for k in ("orient", "grain", "melted", "cooling", "flag"):
+        assert np.array_equal(r.field(FIELD_OF[k]).astype(g[k].dtype), g[k]), k
+    fs = r.frame_stats()
+    assert fs["fills"] > 3 and fs["frames"] <= fx.frames.frames
+    r.reset()
+    r.run()
+    assert np.array_equal(r.field("orientation_id"), g["orient"])
+    r.close()
