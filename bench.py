@@ -733,6 +733,138 @@ def run_ours_batched(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# Learned thermal model (thermal_1024): plain FE frames vs model frames
+# ----------------------------------------------------------------------------
+THERMAL_TEXT = ("thermal_1024: FE-coupled remelting realm, 1024x512x256 cells of 2 um (134M) on a columnar baseplate "
+                "of 8,000 grains (seed 4); a 5-track raster (100 um hatch, alternating direction, 200 W, 1 m/s), "
+                "frames every 1 us on 10 um FE nodes, produced on the GPU a window at a time: the FE field "
+                "(Rosenthal of the current pass, the plain run) or the learned thermal model (Fourier-feature MLP, "
+                "4x256 SiLU, bf16 tensor cores, trained on the GPU on 50M FE-field samples, seed 4) with the FE "
+                "field where its error estimate exceeds 5 K within 100 K of the 1700 K liquidus; liquidus 1700 K, "
+                "solidus 1600 K, bulk sites 1e13 m^-3 (8 K, 2 K), KGT a2=2.03e-4; every CA step to the end of the "
+                "frames")
+# FLOPs of one training sample (forward GEMMs, weight gradients, input gradients of layers 1-3)
+TRAIN_FLOP_PER_SAMPLE = 2 * (2 * (128 * 256 + 3 * 256 * 256)) + 2 * 3 * 256 * 256
+INFER_FLOP_PER_QUERY = 2 * (128 * 256 + 3 * 256 * 256 + 2 * 256)
+
+
+def thermal_accuracy(model, scan, frames, t_liq=1700.0, band=100.0, thresh=5.0) -> dict:
+    """Model frames against the FE field's frames at a few frames spread over
+    the scan: temperature error (K) over nodes whose FE temperature lies in
+    the mushy zone (1600-1700 K), from the network alone and after the
+    fallback rule."""
+    import amca3d_gb300 as A
+
+    sc = A.Scan.of(**scan)
+    errs_net, errs_fb, near, fb, ev = [], [], 0, 0, 0
+    for frac in (0.12, 0.31, 0.5, 0.69, 0.88):
+        f0 = int(frac * (frames - 2))
+        net, fe, c_net = model.frames(sc, f0, 2, t_liq, band, 1e30, with_fe=True)
+        out, _, c_fb = model.frames(sc, f0, 2, t_liq, band, thresh)
+        mushy = (fe >= 1600.0) & (fe <= 1700.0)
+        errs_net.append(np.abs(net[mushy] - fe[mushy]))
+        errs_fb.append(np.abs(out[mushy] - fe[mushy]))
+        ev += int(c_fb[0])
+        near += int(c_fb[1])
+        fb += int(c_fb[2])
+    en, ef = np.concatenate(errs_net), np.concatenate(errs_fb)
+
+    def summ(e):
+        return {"median": float(np.median(e)), "p95": float(np.percentile(e, 95)), "max": float(e.max()),
+                "mean": float(e.mean())} if e.size else {}
+    return {"mushy_nodes": int(en.size), "network_K": summ(en), "after_fallback_K": summ(ef),
+            "nodes_evaluated": ev, "near_liquidus": near, "fallbacks": fb}
+
+
+def run_ours_thermal(args, dist: Dist):
+    import amca3d_gb300 as A
+    from amca3d_gb300.grainstats import grain_stats as gs
+
+    dev = dist.local_rank
+    if args.thermal_block:
+        cells = tuple(int(v) for v in args.thermal_block.split(","))
+        case, scan, m = decks.config_thermal_block("thermal_block", cells, tracks=args.thermal_tracks,
+                                                   hatch=1.0e-4, grains=max(60, cells[0] * cells[1] // 65))
+    else:
+        case, scan, m = decks.config_thermal_1024()
+    deck = case.to_yaml()
+    spec = decks.thermal_spec()
+    tr = dict(decks.THERMAL_TRAIN)
+    if args.thermal_train_steps:
+        tr["steps"] = args.thermal_train_steps
+    model = A.ThermalModel(device=dev, **spec)
+    t0 = time.perf_counter()
+    st_train = model.train(**tr)
+    train_wall = time.perf_counter() - t0
+    acc = thermal_accuracy(model, scan, scan["frames"])
+
+    def make(kind):
+        r = A.CellularAutomataRealm(deck, seed=case.seed, device=dev)
+        r.set_microstructure(m["grain"], m["orient"], m["euler"], m["grain_cell"], m["grain_orient"],
+                             expected=m["expected"])
+        if kind == "fe":
+            r.set_scan_frames(**scan)
+        else:
+            r.set_thermal_frames(model, 1700.0, 100.0, 5.0, **scan)
+        r.initialize()
+        return r
+
+    res = {}
+    clocks = ClockSampler(dev)
+    clocks.start()
+    for kind in ("fe", "model"):
+        r = make(kind)
+        for _ in range(args.warmup):
+            r.reset()
+            r.run()
+        wall = []
+        for _ in range(args.steps):
+            r.reset()
+            t = time.perf_counter()
+            r.run()
+            wall.append(time.perf_counter() - t)
+        st = r.stats()
+        res[kind] = dict(stats=st, wall=wall, frames=r.frame_stats(),
+                         grains=gs(r.field("orientation_id"), r.orientations(), case.cells))
+        r.close()
+    clk = clocks.stop()
+    model.close()
+    if dist.rank != 0:
+        return
+    upd = {k: v["stats"]["cells"] * v["stats"]["step"] for k, v in res.items()}
+    rate = {k: upd[k] / (sum(v["wall"]) / len(v["wall"])) for k, v in res.items()}
+    g_fe, g_mod = res["fe"]["grains"], res["model"]["grains"]
+    line = {
+        "metric": METRIC, "value": rate["model"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(res["model"]["wall"]) / len(res["model"]["wall"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 CA, bf16 tensor-core model",
+        "data": "synthetic",
+        "config": {"workload": THERMAL_TEXT if not args.thermal_block else
+                   f"thermal_block {args.thermal_block}, {args.thermal_tracks} tracks: the thermal_1024 physics on "
+                   f"another block (profiling case, not the workload)", "cells": case.n_interior,
+                   "frames": scan["frames"], "fe_nodes": int(np.prod(scan["nodes"])),
+                   "plain_fe_frames_cell_updates_per_s": rate["fe"], "model_frames_cell_updates_per_s": rate["model"],
+                   "model_vs_plain": rate["model"] / rate["fe"],
+                   "ca_steps": {k: v["stats"]["step"] for k, v in res.items()},
+                   "run_ms": {k: 1e3 * sum(v["wall"]) / len(v["wall"]) for k, v in res.items()},
+                   "ca_kernel_ms": {k: v["stats"]["kernel_ms"] for k, v in res.items()},
+                   "grain_stats_plain": g_fe, "grain_stats_model": g_mod,
+                   "grain_stats_rel_diff": {"grains": abs(g_mod["grains"] - g_fe["grains"]) / max(g_fe["grains"], 1),
+                                            "mean_size": abs(g_mod["mean_size_cells"] - g_fe["mean_size_cells"])
+                                            / max(g_fe["mean_size_cells"], 1e-30),
+                                            "frac_100z_abs": abs(g_mod["frac_100z"] - g_fe["frac_100z"])},
+                   "model_frames": res["model"]["frames"], "temperature_error": acc,
+                   "training": {**st_train, "wall_s": train_wall,
+                                "samples_per_s": st_train["samples_seen"] / (st_train["ms"] / 1e3),
+                                "tflops": st_train["samples_seen"] * TRAIN_FLOP_PER_SAMPLE / (st_train["ms"] / 1e3)
+                                / 1e12, **tr},
+                   "model_flop_per_query": INFER_FLOP_PER_QUERY},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -742,7 +874,12 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=128, help="edge of the CPU-baseline sample block")
     ap.add_argument("--ref-sample", type=int, default=96, help="edge of each reference-arm sample block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["uniform_320", "pbf_500", "batched_64"], default="uniform_320")
+    ap.add_argument("--workload", choices=["uniform_320", "pbf_500", "batched_64", "thermal_1024"],
+                    default="uniform_320")
+    ap.add_argument("--thermal-block", default="", help="X,Y,Z cells: run the thermal_1024 physics on another block "
+                                                        "(profiling only, not the workload)")
+    ap.add_argument("--thermal-tracks", type=int, default=5)
+    ap.add_argument("--thermal-train-steps", type=int, default=0, help="override the training steps")
     ap.add_argument("--cpu-pbf-steps", type=int, default=40, help="CA steps of the pbf_500 CPU-baseline sample")
     ap.add_argument("--ref-pbf-steps", type=int, default=20, help="CA steps of each pbf_500 reference-arm sample")
     ap.add_argument("--pbf-block", default="", help="X,Y,Z cells: run the pbf_500 physics on another block "
@@ -754,7 +891,13 @@ def main():
     args = ap.parse_args()
     dist = Dist()
     try:
-        if args.workload == "pbf_500":
+        if args.workload == "thermal_1024":
+            if args.impl == "reference":
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned thermal model; "
+                                  "its CPU path of this workload's physics is the pbf_500 reference arm"}))
+            else:
+                run_ours_thermal(args, dist)
+        elif args.workload == "pbf_500":
             (run_reference_arm_pbf if args.impl == "reference" else run_ours_pbf)(args, dist)
         elif args.workload == "batched_64":
             (run_reference_arm_batched if args.impl == "reference" else run_ours_batched)(args, dist)
