@@ -70,6 +70,7 @@ EXPORTS = ("amca_create", "amca_get_grid", "amca_prepare", "amca_get_sites", "am
            "amca_run", "amca_get_field", "amca_get_orientations", "amca_write_outputs", "amca_get_stats",
            "amca_final_grain_count", "amca_reset", "amca_host_alloc", "amca_host_free", "amca_envelope_eval",
            "amca_plain_run_noalloc", "amca_selftest_barrier", "amca_release_cached_memory", "amca_set_fe_frames", "amca_set_rosenthal_frames", "amca_set_microstructure",
+           "amca_step_coupled", "amca_run_until", "amca_set_nodal_temperatures",
            "amca_set_scan_frames", "amca_set_thermal_frames", "amca_get_frame_stats", "amca_thermal_create",
            "amca_thermal_train", "amca_thermal_eval", "amca_thermal_gradients", "amca_thermal_param_count",
            "amca_thermal_get_params", "amca_thermal_set_params", "amca_thermal_get_encoding", "amca_thermal_frames",
@@ -233,6 +234,12 @@ def load_library(path: Optional[str] = None) -> ctypes.CDLL:
     lib.amca_last_error.restype = cp
     lib.amca_destroy.argtypes = [vp]
     lib.amca_destroy.restype = None
+    lib.amca_step_coupled.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    lib.amca_step_coupled.restype = i
+    lib.amca_run_until.argtypes = [vp, ctypes.c_double]
+    lib.amca_run_until.restype = i
+    lib.amca_set_nodal_temperatures.argtypes = [vp, vp, i64]
+    lib.amca_set_nodal_temperatures.restype = i
     lib.amca_set_scan_frames.argtypes = [vp, ctypes.POINTER(Scan)]
     lib.amca_set_scan_frames.restype = i
     lib.amca_set_thermal_frames.argtypes = [vp, vp, ctypes.POINTER(Scan), ctypes.c_double, ctypes.c_double,
@@ -390,6 +397,22 @@ class CellularAutomataRealm:
 
     def run(self, max_steps: int = -1) -> None:
         self._check(self._lib.amca_run(self._h, int(max_steps)))
+
+    def step_coupled(self, dt_cap: float) -> float:
+        """One step with dt also bounded by dt_cap (setup_time_step_for_coupling)."""
+        dt = ctypes.c_double()
+        self._check(self._lib.amca_step_coupled(self._h, float(dt_cap), ctypes.byref(dt)))
+        return dt.value
+
+    def run_until(self, t_end: float) -> None:
+        """Steps while time < t_end."""
+        self._check(self._lib.amca_run_until(self._h, float(t_end)))
+
+    def set_nodal_temperatures(self, theta: np.ndarray) -> None:
+        """FE-coupled decks: node temperatures the next step interpolates (an
+        external FE solver's thetaArray_); the realm stops replaying frames."""
+        t = np.ascontiguousarray(theta, np.float64)
+        self._check(self._lib.amca_set_nodal_temperatures(self._h, t.ctypes.data_as(ctypes.c_void_p), t.size))
 
     time_integration = run
 

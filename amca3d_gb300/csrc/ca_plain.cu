@@ -486,8 +486,14 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
     const double maxV = vel > 1e-10 ? vel : 1e-10;
     const double a = d.tsf * d.grid.h / maxV, b = d.tsf * d.grid.h / 1e-10;
     c->vel[step & 1] = vel;
-    c->dt_active[step & 1] = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
-    c->dt_none[step & 1] = (d.max_dt < b) ? d.max_dt : b;
+    double da = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
+    double dn = (d.max_dt < b) ? d.max_dt : b;
+    if (d.dt_cap > 0) {  // setup_time_step_for_coupling of an external solver
+      da = (d.dt_cap < da) ? d.dt_cap : da;
+      dn = (d.dt_cap < dn) ? d.dt_cap : dn;
+    }
+    c->dt_active[step & 1] = da;
+    c->dt_none[step & 1] = dn;
   }
   if (site_tiles(d)) {
     const long long ntiles = (d.nsites + kBlock - 1) / kBlock;
@@ -817,7 +823,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   // launch; with phase_detail the per-phase maximum is raised only by a block
   // that exceeds it (same-address atomics from every block serialise)
   unsigned long long claim_busy = 0, resolve_busy = 0;
-  while (!done && time < d.final_time && step < step_limit) {
+  const double t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
+  while (!done && time < t_end && step < step_limit) {
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
     EnvRec *act = cur ? d.act1 : d.act0;
     EnvRec *next_act = cur ? d.act0 : d.act1;

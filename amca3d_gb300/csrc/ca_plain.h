@@ -101,6 +101,9 @@ struct PlainDevice {
   // physics
   double T0, Tm, Tdot, a1, a2, a3;
   double max_dt, final_time, tsf, trunc;
+  // coupling with an external solver; 0 (the zero-initialised default) means none
+  double dt_cap;  // extra upper bound on dt
+  double t_stop;  // no step starts at time >= t_stop
   float h32;
   float coord_err;  // bound on FP64 cell-centre rounding, per component
   int phase_detail; // nonzero: also gather the slowest block's busy time per phase

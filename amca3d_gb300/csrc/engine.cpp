@@ -299,6 +299,30 @@ struct amca_t {
 
   bool finished() const { return ctrl.done || !(ctrl.time < cfg.final_time); }
 
+  // One step with dt also capped by dt_cap (<= 0: no cap).
+  void step_coupled(double dt_cap) {
+    dev.dt_cap = dt_cap > 0 ? dt_cap : 0.0;
+    try {
+      run(1);
+    } catch (...) {
+      dev.dt_cap = 0.0;
+      throw;
+    }
+    dev.dt_cap = 0.0;
+  }
+  // Steps while time < t_end.
+  void run_until(double t_end) {
+    if (!(t_end > 0)) return;  // time starts at 0: no step starts before t_end
+    dev.t_stop = t_end;
+    try {
+      run(-1);
+    } catch (...) {
+      dev.t_stop = 0.0;
+      throw;
+    }
+    dev.t_stop = 0.0;
+  }
+
   // Run up to `limit` (absolute step count) in one launch.
   void segment(long long limit) {
     CK(cudaEventRecord(ev0, stream));
@@ -924,6 +948,37 @@ int amca_step(amca_t *h, double *dt_out) {
   return guarded(h, [&] {
     h->run(1);
     if (dt_out) *dt_out = h->ctrl.dt;
+  });
+}
+
+int amca_step_coupled(amca_t *h, double dt_cap, double *dt_out) {
+  if (!h) return AMCA_ERR_ARG;
+  if (h->rm)
+    return guarded(h, [&] {
+      h->rm->step_coupled(dt_cap);
+      if (dt_out) *dt_out = h->rm->ctrl().dt;
+    });
+  return guarded(h, [&] {
+    if (!h->initialized) throw StateError("amca_step before amca_initialize");
+    h->step_coupled(dt_cap);
+    if (dt_out) *dt_out = h->ctrl.dt;
+  });
+}
+
+int amca_run_until(amca_t *h, double t_end) {
+  if (!h) return AMCA_ERR_ARG;
+  if (h->rm) return guarded(h, [&] { h->rm->run_until(t_end); });
+  return guarded(h, [&] {
+    if (!h->initialized) throw StateError("amca_run before amca_initialize");
+    h->run_until(t_end);
+  });
+}
+
+int amca_set_nodal_temperatures(amca_t *h, const double *theta, int64_t n) {
+  if (!h || !theta || n <= 0) return AMCA_ERR_ARG;
+  return guarded(h, [&] {
+    if (!h->rm) throw std::invalid_argument("amca_set_nodal_temperatures needs an FE-coupled deck");
+    h->rm->set_nodal_temperatures(theta, n);
   });
 }
 

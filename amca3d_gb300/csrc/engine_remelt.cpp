@@ -507,6 +507,9 @@ void RemeltRealm::initialize() {
   h2d(ftime, frames_.times.data(), nframes_ * 8);
   d.frame_time = ftime;
   d.nframes = (int)nframes_;
+  d.dt_cap = INFINITY;
+  d.t_stop = INFINITY;
+  d.external = 0;
   if (frames_src_ == 3) {
     // a ring of window + 4 slots, refilled a window at a time as the run reaches its end
     window_ = 32;
@@ -631,6 +634,10 @@ void RemeltRealm::reset() {
     dev_.frames_avail = 0;
     fill_frames(window_ + 2);
   }
+  dev_.external = 0;
+  dev_.dt_cap = INFINITY;
+  dev_.t_stop = INFINITY;
+  ext_ready_ = false;
   upload_initial_state();
   kernel_ms_ = 0.0;
   launches_ = 0;
@@ -730,11 +737,62 @@ void RemeltRealm::serve_velocities(const volatile int *stop, int w, int workers,
   }
 }
 
+void RemeltRealm::set_nodal_temperatures(const double *theta, int64_t n) {
+  if (!initialized_) throw StateError("amca_set_nodal_temperatures before amca_initialize");
+  if (n != dev_.nnodes)
+    throw std::invalid_argument("amca_set_nodal_temperatures: " + std::to_string(dev_.nnodes) + " node values needed");
+  if (!ext_theta_) ext_theta_ = alloc<double>((size_t)dev_.nnodes);
+  h2d(ext_theta_, theta, (size_t)n * 8);
+  const int par = (int)(ctrl_.step & 1);
+  RCK(cudaMemsetAsync(&dev_.ctrl->n_eact[par], 0, sizeof(unsigned), stream_));
+  RCK(remelt_external_theta(dev_, ctrl_.step, ext_theta_, stream_));
+  RCK(cudaStreamSynchronize(stream_));
+  dev_.external = 1;
+  ext_ready_ = true;
+}
+
+void RemeltRealm::step_coupled(double dt_cap) {
+  if (!initialized_) throw StateError("amca_step before amca_initialize");
+  const double cap = dt_cap > 0 ? dt_cap : INFINITY;
+  if (dev_.external) {
+    // the external solver's step is the FE time step of the coupling (dT_FE and the CA's maxTimestep_)
+    h2d(&dev_.ctrl->dT_FE, &cap, sizeof cap);
+    h2d(&dev_.ctrl->max_ts, &cap, sizeof cap);
+  }
+  dev_.dt_cap = cap;
+  try {
+    run(1);
+  } catch (...) {
+    dev_.dt_cap = INFINITY;
+    throw;
+  }
+  dev_.dt_cap = INFINITY;
+}
+
+void RemeltRealm::run_until(double t_end) {
+  if (!initialized_) throw StateError("amca_run before amca_initialize");
+  if (dev_.external) throw StateError("node temperatures come from the caller: advance step by step");
+  dev_.t_stop = t_end;
+  try {
+    run(-1);
+  } catch (...) {
+    dev_.t_stop = INFINITY;
+    throw;
+  }
+  dev_.t_stop = INFINITY;
+}
+
 void RemeltRealm::run(long long max_steps) {
   if (!initialized_) throw StateError("amca_run before amca_initialize");
+  if (dev_.external) {
+    if (!ext_ready_) throw StateError("call amca_set_nodal_temperatures before each step");
+    if (max_steps != 1) throw StateError("node temperatures come from the caller: advance step by step");
+  }
+  if (ctrl_.status == kRemeltTimeStop) ctrl_.status = kRemeltRunning;
   const long long target = max_steps < 0 ? (1ll << 60) : ctrl_.step + max_steps;
   const OutputConfig &oc = cfg_.ca.output;
-  while (ctrl_.status != kRemeltFinalTime && ctrl_.status != kRemeltFramesEnd && ctrl_.step < target) {
+  while (ctrl_.status != kRemeltFinalTime && ctrl_.status != kRemeltFramesEnd && ctrl_.status != kRemeltTimeStop &&
+         ctrl_.step < target) {
     long long limit = target;
     if (opts_.write_outputs) {  // VtrManager::execute after every step (Remelting.cpp:640)
       if (oc.frequency >= 1)
@@ -754,6 +812,7 @@ void RemeltRealm::run(long long max_steps) {
     }
     if (opts_.write_outputs && ctrl_.step != before && vtr_.due((int)ctrl_.step, ctrl_.time)) write_snapshot();
   }
+  if (dev_.external) ext_ready_ = false;  // the handed-in node temperatures are used up
 }
 
 void RemeltRealm::launch(long long limit) {

@@ -48,6 +48,11 @@ class RemeltRealm {
   void initialize();  // device state, frames, FE -> CA map
   void reset();       // back to the state right after initialize
   void run(long long max_steps);
+  // coupling with an external solver: one step with dt also capped by dt_cap;
+  // steps while time < t_end; node temperatures for the next step
+  void step_coupled(double dt_cap);
+  void run_until(double t_end);
+  void set_nodal_temperatures(const double *theta, int64_t n);
   bool prepared() const { return prepared_; }
   bool initialized() const { return initialized_; }
 
@@ -111,6 +116,8 @@ class RemeltRealm {
   void synthetic_grid(const double origin[3], double spacing, const int32_t nodes[3], int nframes, double frame_dt,
                       double time_offset);
   void fill_frames(int upto);
+  double *ext_theta_ = nullptr;  // device copy of the host's node temperatures
+  bool ext_ready_ = false;       // node temperatures handed in for the next step
   std::unique_ptr<RestartData> micro_;  // set_microstructure
   // host tables
   std::unique_ptr<GlibcRand> rng_;

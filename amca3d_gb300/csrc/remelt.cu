@@ -744,7 +744,44 @@ __global__ void init_theta_kernel(RemeltDevice d) {
   }
 }
 
+// Node temperatures of step `step` handed in by the host (external FE
+// solver): the step's node arrays, element bounds and void flags, and its
+// list of elements to visit (the rebuild of phase E, from these values).
+__global__ void external_theta_kernel(RemeltDevice d, long long step, const double *theta) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int par = (int)(step & 1);
+  double *tn = d.theta[step % 3];
+  float *tn32 = d.theta32[step % 3];
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.nnodes; n += stride) {
+    tn[n] = theta[n];
+    tn32[n] = (float)theta[n];
+  }
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.nelem; e += stride) {
+    int64_t nid[8];
+    elem_nodes(d.nn, e, nid);
+    double t[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t[i] = theta[nid[i]];
+    const uint8_t void_before = d.evoid[e];
+    element_bounds(d, e, t);
+    const bool v = d.evoid[e] != 0;
+    const bool active = (!v && !(d.emax[e] < d.Tm && d.emin[e] >= null_plus())) || (v != (void_before != 0)) ||
+                        (!v && d.eliq[e] > 0);
+    if (active) {
+      const unsigned slot = atomicAdd(&d.ctrl->n_eact[par], 1u);
+      if (slot < (unsigned)d.nelem) d.eact[par][slot] = (int32_t)e;
+    }
+  }
+}
+
 }  // namespace
+
+cudaError_t remelt_external_theta(const RemeltDevice &d, long long step, const double *theta, cudaStream_t s) {
+  const int64_t n = d.nnodes > d.nelem ? d.nnodes : d.nelem;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  external_theta_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(d, step, theta);
+  return cudaGetLastError();
+}
 
 cudaError_t remelt_rosenthal_frames(const RosenthalParams &p, int nframes, double *frames, cudaStream_t s) {
   const int64_t total = (int64_t)p.nodes[0] * p.nodes[1] * p.nodes[2] * nframes;
@@ -1039,11 +1076,12 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     // --- loop condition of time_integration_weak_coupling (CafeSolver.cpp:188) and launch limits ---
     int stop = kRemeltRunning;
     if (!(S.time < d.final_time)) stop = kRemeltFinalTime;
+    else if (!(S.time < d.t_stop)) stop = kRemeltTimeStop;
     else if (S.step >= limit) stop = kRemeltStepLimit;
     else if (d.nsites > 0 && S.n_orient + d.nsites > d.orient_cap) stop = kRemeltNeedOrient;
     // the step's frame replay reads frame f_next (and f_next + 1 when two frames share a time): both loaded,
     // unless the frames end before them
-    else if (S.f_next + 1 >= d.frames_avail && d.frames_avail < d.nframes) stop = kRemeltNeedFrames;
+    else if (!d.external && S.f_next + 1 >= d.frames_avail && d.frames_avail < d.nframes) stop = kRemeltNeedFrames;
     if (stop != kRemeltRunning) {
       if (gtid == 0) c->status = stop;
       break;
@@ -1301,7 +1339,8 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     const double maxV = vmin > 0 ? vmin : 0;
     const double a = d.tsf_ca * d.h / maxV;
     const double dtLoc = (S.max_ts < a) ? S.max_ts : a;
-    const double dT = (S.dT_FE < dtLoc) ? S.dT_FE : dtLoc;
+    const double dT_ = (S.dT_FE < dtLoc) ? S.dT_FE : dtLoc;
+    const double dT = (d.dt_cap < dT_) ? d.dt_cap : dT_;  // setup_time_step_for_coupling of an external solver
 
     // ===== D: grow and claim (Remelting.cpp:545-622) =====
     for (int64_t q = spread_begin(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
@@ -1419,107 +1458,112 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     // FE replay (uniform in every thread)
     double fe_time = S.fe_time, ts0 = S.ts0, ts1 = S.ts1;
     int f_new = S.f_new, f_next = S.f_next;
-    if (fe_time == 0) fe_time = ts1;
-    fe_time += dT;
-    bool exhausted = false, bad = false;
-    bool unloaded = false;
-    while (fe_time >= ts0) {
-      if (f_next >= d.nframes) {
-        exhausted = true;
-        bad = (d.bad_frame == f_next);
-        break;
-      }
-      if (f_next >= d.frames_avail) {  // cannot happen after the check at the step's start
-        unloaded = true;
-        exhausted = true;
-        break;
-      }
-      ts1 = ts0;
-      ts0 = d.frame_time[f_next];
-      f_new = f_next;
-      f_next++;
-    }
+    bool exhausted = false, bad = false, unloaded = false;
     double ratio = 0.0;
-    if (!exhausted) {
-      ratio = (fe_time - ts1) / (ts0 - ts1);
-      if (ratio < 0.0 && gtid == 0) atomicCAS(&c->error, 0, kRemeltErrRatio);
-      const double *f0 = d.frames + (int64_t)(f_new % d.frame_slots) * d.nnodes;
-      const double *f1 = d.frames + (int64_t)((f_new - 1) % d.frame_slots) * d.nnodes;
-      double *tn = d.theta[(S.step + 1) % 3];
-      float *tn32 = d.theta32[(S.step + 1) % 3];
-      for (int64_t n = gtid; n < d.nnodes; n += nthr) {
-        const double v = lerp_node(f0[n], f1[n], ratio, d.void_t);
-        tn[n] = v;
-        tn32[n] = (float)v;
-      }
-      // Element bounds depend on the frame pair only (every interpolated node value lies between
-      // its two frame values), so the active list is rebuilt when the pair changes; elements near
-      // the void threshold need the exact interpolation and force a rebuild every step.
-      const bool rebuild = S.step == 0 || f_new != S.f_new || ld_volatile(&c->any_near) || d.force_exact;
-      if (!rebuild) {
-        const unsigned na = ld_volatile(&c->n_eact[par]);
-        for (int64_t q = gtid; q < na; q += nthr) d.eact[par ^ 1][q] = d.eact[par][q];
-        if (gtid == 0) {
-          c->n_eact[par ^ 1] = na;
-          eactive += na;
+    // an external FE solver hands in the next node temperatures and element bounds between
+    // steps (amca_set_nodal_temperatures): no replay then
+    if (!d.external) {
+      if (fe_time == 0) fe_time = ts1;
+      fe_time += dT;
+      while (fe_time >= ts0) {
+        if (f_next >= d.nframes) {
+          exhausted = true;
+          bad = (d.bad_frame == f_next);
+          break;
         }
-      }
-      const bool st0 = ld_volatile(&c->fstat_frame[f_new & 1]) == f_new;
-      const bool st1 = ld_volatile(&c->fstat_frame[(f_new - 1) & 1]) == f_new - 1;
-      for (int64_t e = gtid; e < d.nelem && rebuild; e += nthr) {
-        int64_t nid[8];
-        elem_nodes(d.nn, e, nid);
-        const uint8_t void_before = d.evoid[e];
-        double mx0, mn0, mx1, mn1;
-        bool near0, near1;
-        frame_extrema(d, nid, f_new, e, st0, mx0, mn0, near0);
-        frame_extrema(d, nid, f_new - 1, e, st1, mx1, mn1, near1);
-        if (near0 || near1 || d.force_exact) {
-          if (!ld_volatile(&c->any_near)) atomicOr(&c->any_near, 1);
-          double t[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) t[i] = lerp_node(f0[nid[i]], f1[nid[i]], ratio, d.void_t);
-          element_bounds(d, e, t);
-        } else {
-          const double mx = mx0 > mx1 ? mx0 : mx1, mn = mn0 < mn1 ? mn0 : mn1;
-          const double mg = fmax(fabs(mx), fabs(mn));
-          d.evoid[e] = 0;
-          d.emax[e] = mx + ldexp(mg, -44);
-          d.emin[e] = mn - ldexp(mg, -44);
+        if (f_next >= d.frames_avail) {  // cannot happen after the check at the step's start
+          unloaded = true;
+          exhausted = true;
+          break;
         }
-        // the next phase update visits this element's cells when some may change: hot enough to
-        // melt or below nullMatTemp_ + 0.01, void status changed, or holding liquid with material
-        // (cells of a cold element are solid except those counted in eliq; a void element's cells
-        // are all liquid without material once it has been visited)
-        const bool v = d.evoid[e] != 0;
-        const bool active = (!v && !(d.emax[e] < d.Tm && d.emin[e] >= null_plus())) || (v != (void_before != 0)) ||
-                            (!v && ld_volatile(&d.eliq[e]) > 0);
-        if (active) {
-          const unsigned slot = append_slot(&c->n_eact[par ^ 1]);
-          if (slot < (unsigned)d.nelem) d.eact[par ^ 1][slot] = (int32_t)e;
-          ++eactive;
+        ts1 = ts0;
+        ts0 = d.frame_time[f_next];
+        f_new = f_next;
+        f_next++;
+      }
+      if (!exhausted) {
+        ratio = (fe_time - ts1) / (ts0 - ts1);
+        if (ratio < 0.0 && gtid == 0) atomicCAS(&c->error, 0, kRemeltErrRatio);
+        const double *f0 = d.frames + (int64_t)(f_new % d.frame_slots) * d.nnodes;
+        const double *f1 = d.frames + (int64_t)((f_new - 1) % d.frame_slots) * d.nnodes;
+        double *tn = d.theta[(S.step + 1) % 3];
+        float *tn32 = d.theta32[(S.step + 1) % 3];
+        for (int64_t n = gtid; n < d.nnodes; n += nthr) {
+          const double v = lerp_node(f0[n], f1[n], ratio, d.void_t);
+          tn[n] = v;
+          tn32[n] = (float)v;
+        }
+        // Element bounds depend on the frame pair only (every interpolated node value lies between
+        // its two frame values), so the active list is rebuilt when the pair changes; elements near
+        // the void threshold need the exact interpolation and force a rebuild every step.
+        const bool rebuild = S.step == 0 || f_new != S.f_new || ld_volatile(&c->any_near) || d.force_exact;
+        if (!rebuild) {
+          const unsigned na = ld_volatile(&c->n_eact[par]);
+          for (int64_t q = gtid; q < na; q += nthr) d.eact[par ^ 1][q] = d.eact[par][q];
+          if (gtid == 0) {
+            c->n_eact[par ^ 1] = na;
+            eactive += na;
+          }
+        }
+        const bool st0 = ld_volatile(&c->fstat_frame[f_new & 1]) == f_new;
+        const bool st1 = ld_volatile(&c->fstat_frame[(f_new - 1) & 1]) == f_new - 1;
+        for (int64_t e = gtid; e < d.nelem && rebuild; e += nthr) {
+          int64_t nid[8];
+          elem_nodes(d.nn, e, nid);
+          const uint8_t void_before = d.evoid[e];
+          double mx0, mn0, mx1, mn1;
+          bool near0, near1;
+          frame_extrema(d, nid, f_new, e, st0, mx0, mn0, near0);
+          frame_extrema(d, nid, f_new - 1, e, st1, mx1, mn1, near1);
+          if (near0 || near1 || d.force_exact) {
+            if (!ld_volatile(&c->any_near)) atomicOr(&c->any_near, 1);
+            double t[8];
+  #pragma unroll
+            for (int i = 0; i < 8; ++i) t[i] = lerp_node(f0[nid[i]], f1[nid[i]], ratio, d.void_t);
+            element_bounds(d, e, t);
+          } else {
+            const double mx = mx0 > mx1 ? mx0 : mx1, mn = mn0 < mn1 ? mn0 : mn1;
+            const double mg = fmax(fabs(mx), fabs(mn));
+            d.evoid[e] = 0;
+            d.emax[e] = mx + ldexp(mg, -44);
+            d.emin[e] = mn - ldexp(mg, -44);
+          }
+          // the next phase update visits this element's cells when some may change: hot enough to
+          // melt or below nullMatTemp_ + 0.01, void status changed, or holding liquid with material
+          // (cells of a cold element are solid except those counted in eliq; a void element's cells
+          // are all liquid without material once it has been visited)
+          const bool v = d.evoid[e] != 0;
+          const bool active = (!v && !(d.emax[e] < d.Tm && d.emin[e] >= null_plus())) || (v != (void_before != 0)) ||
+                              (!v && ld_volatile(&d.eliq[e]) > 0);
+          if (active) {
+            const unsigned slot = append_slot(&c->n_eact[par ^ 1]);
+            if (slot < (unsigned)d.nelem) d.eact[par ^ 1][slot] = (int32_t)e;
+            ++eactive;
+          }
         }
       }
     }
     if (gtid == 0) {
       if (bad) atomicCAS(&c->error, 0, kRemeltErrFrame);
       if (unloaded) atomicCAS(&c->error, 0, kRemeltErrRing);
-      if (!exhausted) {
-        c->fstat_frame[f_new & 1] = f_new;
-        c->fstat_frame[(f_new - 1) & 1] = f_new - 1;
+      if (!d.external) {
+        if (!exhausted) {
+          c->fstat_frame[f_new & 1] = f_new;
+          c->fstat_frame[(f_new - 1) & 1] = f_new - 1;
+        }
+        c->fe_time = fe_time;
+        c->ts0 = ts0;
+        c->ts1 = ts1;
+        c->f_new = f_new;
+        c->f_next = f_next;
+        c->ratio = ratio;
+        c->dT_FE = ts0 - fe_time;
+        c->max_ts = ts0 - fe_time;
       }
       c->step = S.step + 1;
       c->time = S.time + dT;
       c->dt_prev = S.dt;
       c->dt = dT;
-      c->fe_time = fe_time;
-      c->ts0 = ts0;
-      c->ts1 = ts1;
-      c->f_new = f_new;
-      c->f_next = f_next;
-      c->ratio = ratio;
-      c->dT_FE = ts0 - fe_time;
-      c->max_ts = ts0 - fe_time;
       c->theta_init = 0;
       c->liquid += ld_volatile(&c->n_liq);
       c->n_liq = 0;

@@ -21,7 +21,7 @@ constexpr int kRemeltErrBarrier = 1, kRemeltErrFrame = 2, kRemeltErrNewGrains = 
               kRemeltErrList = 5, kRemeltErrHost = 6, kRemeltErrRing = 7;
 // why a launch returned
 constexpr int kRemeltRunning = 0, kRemeltFinalTime = 1, kRemeltFramesEnd = 2, kRemeltNeedOrient = 3,
-              kRemeltStepLimit = 4, kRemeltNeedFrames = 5;
+              kRemeltStepLimit = 4, kRemeltNeedFrames = 5, kRemeltTimeStop = 6;
 
 // Growth velocities whose glibc pow() rounding cannot be decided on the GPU
 // (an integer power within 0.02 ulp of a rounding midpoint; glibc's pow errs
@@ -122,6 +122,10 @@ struct RemeltDevice {
   int frame_slots;           // slots of the ring (nframes when every frame is resident)
   int frames_avail;          // frames 0 .. frames_avail - 1 have been loaded (the last frame_slots of them are held)
   int bad_frame;             // index of a malformed frame, or -1
+  // coupling with an external solver (amca_step_coupled, amca_run_until, amca_set_nodal_temperatures)
+  double dt_cap;             // extra upper bound on dt (+inf: none)
+  double t_stop;             // the launch stops before a step that starts at time >= t_stop (+inf: none)
+  int external;              // node temperatures come from the host between steps: no frame replay
   double *theta[3];          // node temperatures by CA step (mod 3)
   float *theta32[3];         // the same, rounded to float
   double *emax, *emin;       // per element bounds on the interpolated temperature (current step)
@@ -196,6 +200,12 @@ int remelt_persistent_grid(int device, int per_sm);
 // Run CA steps until `limit` steps in total, the final time, the end of the
 // frames, or an orientation stream shorter than a step may need.
 cudaError_t remelt_run_steps(const RemeltDevice &d, long long limit, int blocks, cudaStream_t s);
+
+// Node temperatures of the next step (`step` = steps completed so far) from
+// the host's theta (device copy, nnodes doubles): the node arrays of that
+// step, each element's bounds and void flag, and the list of elements whose
+// cells the step's phase update visits (an external solver's frame).
+cudaError_t remelt_external_theta(const RemeltDevice &d, long long step, const double *theta, cudaStream_t s);
 
 // Every cell's temperature and cooling flag of the last completed step (the
 // values the reference holds in cellTemperature_ / cooling_), plus the

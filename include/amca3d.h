@@ -79,6 +79,35 @@ int amca_step(amca_t *h, double *dt_out);
  * Replaces CellularAutomataManager::time_integration (CA/src/CellularAutomataManager.cpp:134-147). */
 int amca_run(amca_t *h, int max_steps);
 
+/* ---- Coupling with a solver that advances beside the realm ----
+ * One step whose dt is also bounded by dt_cap (the coupled solver's time
+ * step; dt_cap <= 0 or +inf: no bound): dt = min(dt of amca_step, dt_cap).
+ * Replaces CellularAutomataManager::setup_time_step_for_coupling
+ * (CA/include/CellularAutomataManager.h:42) as CafeSolver applies it,
+ * dT = min(dT_FE, dT_CA) (CA/src/CafeSolver.cpp:190-206). For an FE-coupled
+ * realm whose node temperatures come from amca_set_nodal_temperatures, dt_cap
+ * is the FE time step itself (the reference's dT_FE and the CA's
+ * maxTimestep_, CA/src/CafeSolver.cpp:183-184,213-216). dt_out may be NULL. */
+int amca_step_coupled(amca_t *h, double dt_cap, double *dt_out);
+
+/* Steps while time < t_end (and the realm's own end conditions allow):
+ * the loop of CafeSolver::time_integration_weak_coupling and
+ * CellularAutomataManager::time_integration with the final time t_end
+ * (CA/src/CafeSolver.cpp:188, CA/src/CellularAutomataManager.cpp:134-147).
+ * The last step may end past t_end, as in the reference. */
+int amca_run_until(amca_t *h, double t_end);
+
+/* FE-coupled realms: the node temperatures (n = node count, in the node order
+ * of the frames, x fastest) that the next step interpolates, handed in by an
+ * FE solver that advances beside the realm: the FE realm's thetaArray_ after
+ * its own solve (CA/src/CafeSolver.cpp:207-216 with solveProblemMyself_),
+ * which MapVoxelManager::evaluate_temperature reads
+ * (CA/src/MapVoxelManager.cpp:746-799). From the first call on, the realm
+ * stops replaying its frames: before every step the caller hands in that
+ * step's node temperatures and advances it with amca_step_coupled (its dt_cap
+ * the FE time step). After amca_initialize; amca_reset returns to the frames. */
+int amca_set_nodal_temperatures(amca_t *h, const double *theta, int64_t n);
+
 enum {
   AMCA_FIELD_ORIENTATION_ID = 0, /* int32, ghost-inclusive grid: cellOrientationID_ (the output "grain_id") */
   AMCA_FIELD_GRAIN_ID = 1,       /* int32, ghost-inclusive grid: cellGrainID_ (envelope index per cell) */
