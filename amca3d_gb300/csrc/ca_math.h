@@ -280,6 +280,40 @@ AMCA_HD void capture_f64(const double *l2g, double gcx, double gcy, double gcz, 
   out[3] = Lnew;
 }
 
+// Hexahedral (8-node) interpolation of MapVoxelManager::evaluate_temperature
+// (CA/src/MapVoxelManager.cpp:746-799) in FP64: the shape functions in the
+// reference's factor order, summed from 0 in node order.
+AMCA_HD double hex8_interp64(const double t[8], double xi, double eta, double zeta) {
+  double s[8];
+  s[0] = 0.125 * (1.0 - eta) * (1.0 - xi) * (1.0 - zeta);
+  s[1] = 0.125 * (1.0 - eta) * (1.0 + xi) * (1.0 - zeta);
+  s[2] = 0.125 * (1.0 + eta) * (1.0 + xi) * (1.0 - zeta);
+  s[3] = 0.125 * (1.0 + eta) * (1.0 - xi) * (1.0 - zeta);
+  s[4] = 0.125 * (1.0 - eta) * (1.0 - xi) * (1.0 + zeta);
+  s[5] = 0.125 * (1.0 - eta) * (1.0 + xi) * (1.0 + zeta);
+  s[6] = 0.125 * (1.0 + eta) * (1.0 + xi) * (1.0 + zeta);
+  s[7] = 0.125 * (1.0 + eta) * (1.0 - xi) * (1.0 + zeta);
+  double v = 0.0;
+  for (int i = 0; i < 8; i++) v += s[i] * t[i];
+  return v;
+}
+
+// FP32 estimate of hex8_interp64 from the node values and parametric
+// coordinates rounded to float. The shape functions are convex weights
+// (coordinates in [-1, 1]), so its error stays below 2e-6 of the largest node
+// magnitude; hex8_err32 gives the bound the kernels decide with: 2^-16 of that
+// magnitude plus 2^-16 absolute.
+AMCA_HD float hex8_interp32(const float t[8], float xi, float eta, float zeta) {
+  const float a0 = 1.0f - eta, a1 = 1.0f + eta, b0 = 1.0f - xi, b1 = 1.0f + xi, c0 = 1.0f - zeta, c1 = 1.0f + zeta;
+  return 0.125f * (a0 * b0 * c0 * t[0] + a0 * b1 * c0 * t[1] + a1 * b1 * c0 * t[2] + a1 * b0 * c0 * t[3] +
+                   a0 * b0 * c1 * t[4] + a0 * b1 * c1 * t[5] + a1 * b1 * c1 * t[6] + a1 * b0 * c1 * t[7]);
+}
+AMCA_HD float hex8_err32(const float t[8]) {
+  float mg = 0.0f;
+  for (int i = 0; i < 8; ++i) mg = fmaxf(mg, fabsf(t[i]));
+  return ldexpf(mg, -16) + 1.52587890625e-05f;
+}
+
 // ProblemPhysics_RappazGandin1993::compute_growth_velocity for a uniform field
 AMCA_HD double kgt_velocity(double Tm, double T, double a1, double a2, double a3) {
   const double dT = Tm - T;

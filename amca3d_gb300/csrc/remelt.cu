@@ -389,20 +389,7 @@ __device__ bool eval_T(const RemeltDevice &d, const double *th, int64_t c, doubl
     t[i] = th[nid[i]];
     if (t[i] < nullMat) return false;
   }
-  const double xi = d.pc[3 * c], eta = d.pc[3 * c + 1], zeta = d.pc[3 * c + 2];
-  double s[8];
-  s[0] = 0.125 * (1.0 - eta) * (1.0 - xi) * (1.0 - zeta);
-  s[1] = 0.125 * (1.0 - eta) * (1.0 + xi) * (1.0 - zeta);
-  s[2] = 0.125 * (1.0 + eta) * (1.0 + xi) * (1.0 - zeta);
-  s[3] = 0.125 * (1.0 + eta) * (1.0 - xi) * (1.0 - zeta);
-  s[4] = 0.125 * (1.0 - eta) * (1.0 - xi) * (1.0 + zeta);
-  s[5] = 0.125 * (1.0 - eta) * (1.0 + xi) * (1.0 + zeta);
-  s[6] = 0.125 * (1.0 + eta) * (1.0 + xi) * (1.0 + zeta);
-  s[7] = 0.125 * (1.0 + eta) * (1.0 - xi) * (1.0 + zeta);
-  double v = 0.0;
-#pragma unroll
-  for (int i = 0; i < 8; i++) v += s[i] * t[i];
-  T = v;
+  T = hex8_interp64(t, d.pc[3 * c], d.pc[3 * c + 1], d.pc[3 * c + 2]);
   return true;
 }
 
@@ -415,19 +402,11 @@ __device__ bool eval_T(const RemeltDevice &d, const double *th, int64_t c, doubl
 __device__ float eval_T32(const RemeltDevice &d, const float *th32, int64_t c, int32_t e, float &err) {
   int64_t nid[8];
   elem_nodes(d.nn, e, nid);
-  const float xi = d.pc32[3 * c], eta = d.pc32[3 * c + 1], zeta = d.pc32[3 * c + 2];
-  const float a0 = 1.0f - eta, a1 = 1.0f + eta, b0 = 1.0f - xi, b1 = 1.0f + xi, c0 = 1.0f - zeta, c1 = 1.0f + zeta;
   float t[8];
-  float mg = 0.0f;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    t[i] = th32[nid[i]];
-    mg = fmaxf(mg, fabsf(t[i]));
-  }
-  const float v = 0.125f * (a0 * b0 * c0 * t[0] + a0 * b1 * c0 * t[1] + a1 * b1 * c0 * t[2] + a1 * b0 * c0 * t[3] +
-                            a0 * b0 * c1 * t[4] + a0 * b1 * c1 * t[5] + a1 * b1 * c1 * t[6] + a1 * b0 * c1 * t[7]);
-  err = ldexpf(mg, -16) + 1.52587890625e-05f;
-  return v;
+  for (int i = 0; i < 8; ++i) t[i] = th32[nid[i]];
+  err = hex8_err32(t);
+  return hex8_interp32(t, d.pc32[3 * c], d.pc32[3 * c + 1], d.pc32[3 * c + 2]);
 }
 
 // thetaArray_ update of pseudo_single_integration_step (LoadDataFromFile.cpp:281-290)
@@ -938,25 +917,17 @@ __device__ __forceinline__ ElemView elem_view(const RemeltDevice &d, const float
   const float tl = lane < 8 ? th32[mine] : 0.0f;
   v.void_ = d.evoid[e] != 0;
   v.quiet = d.emax[e] < d.Tm && d.emin[e] >= null_plus();
-  float mg = 0.0f;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    v.t[i] = __shfl_sync(0xffffffffu, tl, i);
-    mg = fmaxf(mg, fabsf(v.t[i]));
-  }
-  v.err = ldexpf(mg, -16) + 1.52587890625e-05f;
+  for (int i = 0; i < 8; ++i) v.t[i] = __shfl_sync(0xffffffffu, tl, i);
+  v.err = hex8_err32(v.t);
   return v;
 }
 
 // eval_T32 with the element's nodal values already at hand (same operands,
 // same operation order, same result).
 __device__ __forceinline__ float eval_T32_view(const RemeltDevice &d, int64_t c, const ElemView &v, float &err) {
-  const float xi = d.pc32[3 * c], eta = d.pc32[3 * c + 1], zeta = d.pc32[3 * c + 2];
-  const float a0 = 1.0f - eta, a1 = 1.0f + eta, b0 = 1.0f - xi, b1 = 1.0f + xi, c0 = 1.0f - zeta, c1 = 1.0f + zeta;
-  const float *t = v.t;
   err = v.err;
-  return 0.125f * (a0 * b0 * c0 * t[0] + a0 * b1 * c0 * t[1] + a1 * b1 * c0 * t[2] + a1 * b0 * c0 * t[3] +
-                   a0 * b0 * c1 * t[4] + a0 * b1 * c1 * t[5] + a1 * b1 * c1 * t[6] + a1 * b0 * c1 * t[7]);
+  return hex8_interp32(v.t, d.pc32[3 * c], d.pc32[3 * c + 1], d.pc32[3 * c + 2]);
 }
 
 // `ev`: the cell's element view when the caller walks an element's cells
