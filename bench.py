@@ -2,14 +2,19 @@
 with --workload pbf_500 the FE-coupled remelting realm on a laser track
 (500 x 250 x 100 cells, Rosenthal frames, columnar baseplate); with
 --workload batched_64 64 independent plain instances (edges 32..128) in one
-graph-replayed launch, beside the same instances as 64 sequential launches.
+graph-replayed launch, beside the same instances as 64 sequential launches;
+with --workload thermal_1024 the 134M-cell 5-track raster on frames of the
+FE field and on frames of the learned thermal model (trained first).
 
 One bench step = one full run of the deck from its initial state to its end
 (full solidification, or the end of the frames), every CA step of it, on one
-GPU; cell-updates/s = interior cells x CA steps / time.
+GPU; cell-updates/s = interior cells x CA steps / time. The default line
+(uniform_320, one GPU) also carries the pbf_500 and batched_64 results under
+those keys, each measured with its own warm-up, timed runs, clocks and
+roofline (--no-extra leaves them out).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload uniform_320|pbf_500|batched_64]
+                  [--workload uniform_320|pbf_500|batched_64|thermal_1024]
 
 ours (default): the CUDA path. `value` is device time (CUDA events around
   the persistent step kernel on its stream) with the realm's tables resident
@@ -352,7 +357,7 @@ def run_ours(args, dist: Dist):
     }
     if args.gpus == 1 and dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ----------------------------------------------------------------------------
@@ -534,7 +539,7 @@ def run_ours_pbf(args, dist: Dist):
     }
     if args.gpus == 1 and dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_pbf(args.cpu_pbf_steps)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ----------------------------------------------------------------------------
@@ -730,7 +735,7 @@ def run_ours_batched(args, dist: Dist):
     }
     if args.gpus == 1 and dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_batched()
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ----------------------------------------------------------------------------
@@ -865,6 +870,11 @@ def run_ours_thermal(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def emit(line) -> None:
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -874,6 +884,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=128, help="edge of the CPU-baseline sample block")
     ap.add_argument("--ref-sample", type=int, default=96, help="edge of each reference-arm sample block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="uniform_320 only: leave out the pbf_500 and batched_64 results of the default line")
+    ap.add_argument("--extra-steps", type=int, default=3, help="timed runs of each extra workload")
+    ap.add_argument("--extra-warmup", type=int, default=3, help="warm-up runs of each extra workload (>= 3)")
     ap.add_argument("--workload", choices=["uniform_320", "pbf_500", "batched_64", "thermal_1024"],
                     default="uniform_320")
     ap.add_argument("--thermal-block", default="", help="X,Y,Z cells: run the thermal_1024 physics on another block "
@@ -898,13 +912,31 @@ def main():
             else:
                 run_ours_thermal(args, dist)
         elif args.workload == "pbf_500":
-            (run_reference_arm_pbf if args.impl == "reference" else run_ours_pbf)(args, dist)
+            if args.impl == "reference":
+                run_reference_arm_pbf(args, dist)
+            else:
+                emit(run_ours_pbf(args, dist))
         elif args.workload == "batched_64":
-            (run_reference_arm_batched if args.impl == "reference" else run_ours_batched)(args, dist)
+            if args.impl == "reference":
+                run_reference_arm_batched(args, dist)
+            else:
+                emit(run_ours_batched(args, dist))
         elif args.impl == "reference":
             run_reference_arm(args, dist)
         else:
-            run_ours(args, dist)
+            line = run_ours(args, dist)
+            if line is not None and args.gpus == 1 and not args.no_extra and args.cells == 320:
+                # the other two workloads of the metric ride along on one GPU, each with its own
+                # timing, clocks and roofline (K and W of their own, kept short)
+                sub = argparse.Namespace(**vars(args))
+                sub.steps, sub.warmup = args.extra_steps, max(3, args.extra_warmup)
+                for key, fn in (("pbf_500", run_ours_pbf), ("batched_64", run_ours_batched)):
+                    extra = fn(sub, dist)
+                    if extra is not None:
+                        line[key] = {k: v for k, v in extra.items()
+                                     if k not in ("metric", "unit", "n_gpus", "higher_is_better", "scaling",
+                                                  "vs_baseline", "data")}
+            emit(line)
     finally:
         dist.close()
 
