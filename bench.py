@@ -24,8 +24,11 @@ ours (default): the CUDA path. `value` is device time (CUDA events around
 reference: the CPU implementation of the path (the C restatement of the
   reference, one process per host core, each on a bounded sample of the
   workload), same metric.
-For N > 1 (torchrun) each rank runs an independent replica ("replicas only":
-the single-domain CA does not shard); the value is the sum of cell updates
+For N > 1 (torchrun) each rank of uniform_320 and pbf_500 runs an independent
+replica (a single domain does not shard under bit-exactness); batched_64
+partitions its 64 instances over the ranks (longest first, no collective on
+the data path; the per-instance field digests are gathered and checked
+against the instances' reference runs). The value is the sum of cell updates
 over ranks divided by the slowest rank's time.
 """
 from __future__ import annotations
@@ -97,6 +100,14 @@ class Dist:
         t = torch.tensor([x], dtype=torch.float64)
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
         return float(t.item())
+
+    def gather(self, obj) -> list:
+        """Every rank's object, in rank order, on every rank."""
+        if not self.pg:
+            return [obj]
+        out = [None] * self.world
+        self.pg.all_gather_object(out, obj)
+        return out
 
     def close(self):
         if self.pg:
@@ -621,8 +632,13 @@ def _batch_grain_stats(realms, decks_) -> dict:
 def run_ours_batched(args, dist: Dist):
     import amca3d_gb300 as A
 
+    from amca3d_gb300 import shard
+
     dev = dist.local_rank
-    decks_ = decks.config_batched_64()
+    all_decks = decks.config_batched_64()
+    # N GPUs: the 64 instances partitioned over the ranks (longest first), each rank one batch of its share
+    mine = shard.partition(all_decks, dist.world)[dist.rank]
+    decks_ = [all_decks[i] for i in mine]
     realms = []
     for c in decks_:
         r = A.CellularAutomataRealm(c.to_yaml(), seed=c.seed, device=dev)
@@ -650,6 +666,13 @@ def run_ours_batched(args, dist: Dist):
     per = [r.stats() for r in realms]
     gstats = _batch_grain_stats(realms, decks_)
     orient_last = [r.field("orientation_id") for r in realms[:4]]
+    # every instance's result against its own reference run (digests gathered from all ranks)
+    local = {c.name: (shard.field_digest(r.field("orientation_id")), r.stats()["step"]) for c, r in zip(decks_, realms)}
+    gathered = {}
+    for part in dist.gather(local):
+        gathered.update(part)
+    golden = json.load(open(os.path.join(ROOT, "tests", "golden", "batched_64_golden.json")))
+    match = all(gathered.get(k, ("", -1)) == (v["orient_sha256"], v["steps"]) for k, v in golden.items())
     batch.close()
 
     # the same 64 instances as 64 sequential plain launches (one persistent
@@ -710,9 +733,10 @@ def run_ours_batched(args, dist: Dist):
     steps_all = [p_["step"] for p_ in per]
     line = {
         "metric": METRIC, "value": upd_total / t_dev, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "strong" if dist.world > 1 else "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": BATCH_TEXT, "instances": len(decks_), "cells": sum(c.n_interior for c in decks_),
+        "config": {"workload": BATCH_TEXT, "instances": len(all_decks), "cells": sum(c.n_interior for c in all_decks),
                    "ca_steps_min_mean_max": [min(steps_all), float(np.mean(steps_all)), max(steps_all)],
                    "cell_updates_per_run": bs["cell_updates"], **gstats,
                    "team_size": bs["team_size"], "teams": bs["teams"], "max_blocks": bs["max_blocks"],
@@ -721,7 +745,9 @@ def run_ours_batched(args, dist: Dist):
                    "grid_blocks": bs["grid_blocks"],
                    "sequential_plain_ms": seq, "sequential_plain_cell_updates_per_s": bs["cell_updates"] / (seq / 1e3),
                    "speedup_vs_sequential_plain": seq / ms, "sequential_fields_match": seq_same,
-                   "e2e_fields_match": same, "parallelism": f"replicas x{args.gpus}",
+                   "e2e_fields_match": same, "all_instances_match_reference": match,
+                   "ranks": dist.world, "instances_rank0": len(decks_),
+                   "parallelism": "instances partitioned over ranks, longest first" if dist.world > 1 else "1 GPU",
                    "l2": "inputs larger than L2: 64 orientation fields 183 MB + envelope tables 1.9 GB per run"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": load_traffic("ca_batched_64.json"), "peak_kind": f"{peak_kind} burst copy",

@@ -65,3 +65,75 @@ def test_reference_arm_prints_only_on_rank_zero(capsys):
     bench.run_reference_arm_pbf(Args(), FakeDist())
     bench.run_reference_arm_batched(Args(), FakeDist())
     assert capsys.readouterr().out == ""
+
+
+def test_batched_instances_partition_over_ranks():
+    """Every instance goes to exactly one rank, longest first, loads balanced."""
+    sys.path.insert(0, ROOT)
+    from amca3d_gb300 import decks, shard
+
+    cases = decks.config_batched_64()
+    for world in (1, 2, 4, 8):
+        parts = shard.partition(cases, world)
+        flat = sorted(i for p in parts for i in p)
+        assert flat == list(range(len(cases)))
+        loads = [sum(shard.instance_work(cases[i]) for i in p) for p in parts]
+        assert max(loads) <= 1.1 * (sum(loads) / world) + max(shard.instance_work(c) for c in cases)
+        # the heaviest instance goes to rank 0 first
+        heaviest = max(range(len(cases)), key=lambda i: shard.instance_work(cases[i]))
+        assert parts[0][0] == heaviest
+
+
+def _instance_rank(rank: int, world: int, port: int, names, out):
+    """One gloo rank: runs its share of the given instances on the C oracle
+    (standing in for its GPU) and gathers the field digests like the bench."""
+    os.environ.update(RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amca_oracle
+
+    import bench
+    from amca3d_gb300 import decks, shard
+
+    cases = [c for c in decks.config_batched_64() if c.name in names]
+    d = bench.Dist()
+    mine = shard.partition(cases, d.world)[d.rank]
+    local = {}
+    for i in mine:
+        r = amca_oracle.run_plain(cases[i])
+        local[cases[i].name] = (shard.field_digest(r["orient"]), int(r["steps"]))
+    gathered = {}
+    for part in d.gather(local):
+        gathered.update(part)
+    out.put((rank, len(mine), gathered))
+    d.close()
+
+
+def test_two_ranks_gather_instance_digests_that_match_the_reference(oracle):
+    """The N-GPU batched leg's plumbing on two gloo ranks: the smallest four
+    instances of batched_64 split over the ranks, each rank's digests
+    gathered on every rank and equal to the instances' reference runs."""
+    pytest.importorskip("torch")
+    import json
+    import multiprocessing as mp
+
+    from amca3d_gb300 import decks
+
+    golden = json.load(open(os.path.join(ROOT, "tests", "golden", "batched_64_golden.json")))
+    names = [c.name for c in sorted(decks.config_batched_64(), key=lambda c: c.n_interior)[:4]]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_instance_rank, args=(r, 2, port, names, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][1] + res[1][1] == 4 and res[0][1] > 0 and res[1][1] > 0
+    for _rank, _n, gathered in res:
+        assert sorted(gathered) == sorted(names)
+        for name in names:
+            assert gathered[name] == (golden[name]["orient_sha256"], golden[name]["steps"]), name
