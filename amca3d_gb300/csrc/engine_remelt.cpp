@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <atomic>
 #include <cmath>
+#include <fstream>
 #include <stdexcept>
 #include <thread>
 
@@ -47,6 +48,7 @@ RemeltRealm::~RemeltRealm() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (const auto &a : allocs_) cache_give(device_, a.first, a.second);
   if (hostvel_) cudaFreeHost(hostvel_);
+  if (staging_) cudaFreeHost(staging_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -139,15 +141,56 @@ void RemeltRealm::set_scan(const amca_scan &scan, ThermalModel *model, double t_
   frames_src_ = 3;
 }
 
-// Frames avail_ .. upto - 1 into the ring (source 3).
+// Frames avail_ .. upto - 1 into the ring: generated on the GPU (scan or
+// model frames) or read from the text file (streamed text frames), with
+// their times in the ring of times.
 void RemeltRealm::fill_frames(int upto) {
   upto = std::min<int>(upto, (int)nframes_);
   if (upto <= avail_) return;
-  fill_scan_frames(&scan_, model_, t_liq_, band_, thresh_, avail_, upto - avail_, ring_, slots_, fcount_, stream_);
+  const int64_t nn = dev_.nnodes;
+  if (text_stream_) {
+    int f = avail_;
+    double t = 0;
+    while (f < upto) {
+      double *dst = staging_ + (size_t)(f - avail_) * nn;
+      if (!reader_->next(dst, t)) {  // end of the file, or a malformed frame: the frame count is known now
+        nframes_ = f;
+        dev_.nframes = f;
+        if (reader_->bad()) dev_.bad_frame = f;
+        break;
+      }
+      times_read_.push_back(t);
+      ++f;
+    }
+    for (int g = avail_; g < f; ++g) {
+      RCK(cudaMemcpyAsync(ring_ + (size_t)(g % slots_) * nn, staging_ + (size_t)(g - avail_) * nn, (size_t)nn * 8,
+                          cudaMemcpyHostToDevice, stream_));
+      RCK(cudaMemcpyAsync(ftime_ + g % slots_, &times_read_[g], 8, cudaMemcpyHostToDevice, stream_));
+    }
+    RCK(cudaStreamSynchronize(stream_));
+    h2d_bytes_ += (int64_t)(f - avail_) * nn * 8;
+    upto = f;
+  } else {
+    fill_scan_frames(&scan_, model_, t_liq_, band_, thresh_, avail_, upto - avail_, ring_, slots_, fcount_, stream_);
+    for (int g = avail_; g < upto; ++g)
+      RCK(cudaMemcpyAsync(ftime_ + g % slots_, &frames_.times[g], 8, cudaMemcpyHostToDevice, stream_));
+    RCK(cudaStreamSynchronize(stream_));
+  }
   produced_ += upto - avail_;
   ++fills_;
   avail_ = upto;
   dev_.frames_avail = avail_;
+}
+
+// A fresh reader at the start of the text frames (frame 0 and the grid).
+void RemeltRealm::open_text_frames() {
+  reader_.reset(new FrameReader(path(cfg_.fe.mesh), cfg_.fe));
+  times_read_.assign(1, reader_->head().times[0]);
+  nframes_ = 1 << 30;  // unknown until the reader reaches the end of the file
+  dev_.nframes = (int)nframes_;
+  dev_.bad_frame = -1;
+  avail_ = 0;
+  dev_.frames_avail = 0;
 }
 
 void RemeltRealm::frame_stats(int64_t out[5]) {
@@ -336,8 +379,21 @@ void RemeltRealm::initialize() {
   RCK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   RCK(cudaEventCreate(&ev0_));
   RCK(cudaEventCreate(&ev1_));
-  if (frames_src_ == 0) frames_ = read_fe_frames(path(cfg_.fe.mesh), cfg_.fe);
-  nframes_ = frames_src_ == 2 ? ros_nframes_ : frames_.nframes;
+  if (frames_src_ == 0) {
+    // text frames are read whole, or (files over 4 GiB, or AMCA_FRAME_STREAM=1) a window at a time
+    const std::string fpath = path(cfg_.fe.mesh);
+    std::ifstream probe(fpath.c_str(), std::ios::binary | std::ios::ate);
+    const long long bytes = probe ? (long long)probe.tellg() : 0;
+    const char *se = getenv("AMCA_FRAME_STREAM");
+    text_stream_ = se ? atoi(se) != 0 : bytes > (4ll << 30);
+    if (text_stream_) {
+      reader_.reset(new FrameReader(fpath, cfg_.fe));
+      frames_ = reader_->head();
+    } else {
+      frames_ = read_fe_frames(fpath, cfg_.fe);
+    }
+  }
+  nframes_ = frames_src_ == 2 ? ros_nframes_ : (text_stream_ ? (1 << 30) : frames_.nframes);
   Grid g{};
   g.nx = c.nx;
   g.ny = c.ny;
@@ -503,26 +559,47 @@ void RemeltRealm::initialize() {
     d.ecell = el;
   }
   // --- frames ---
-  double *ftime = alloc<double>(nframes_);
-  h2d(ftime, frames_.times.data(), nframes_ * 8);
-  d.frame_time = ftime;
   d.nframes = (int)nframes_;
+  d.bad_frame = (int)frames_.bad_frame;
   d.dt_cap = INFINITY;
   d.t_stop = INFINITY;
   d.external = 0;
-  if (frames_src_ == 3) {
-    // a ring of window + 4 slots, refilled a window at a time as the run reaches its end
+  if (frames_src_ == 3 || text_stream_) {
+    // a ring of window + 4 frame slots (and their times), refilled a window at a
+    // time as the run reaches its end
     window_ = 32;
     if (const char *e = getenv("AMCA_FRAME_WINDOW")) window_ = std::max(2, atoi(e));
     slots_ = (int)std::min<int64_t>(nframes_, window_ + 4);
     ring_ = alloc<double>((size_t)slots_ * d.nnodes);
-    fcount_ = alloc<unsigned long long>(4);
-    RCK(cudaMemsetAsync(fcount_, 0, 4 * sizeof(unsigned long long), stream_));
+    ftime_ = alloc<double>((size_t)slots_);
     d.frames = ring_;
+    d.frame_time = ftime_;
     d.frame_slots = slots_;
-    avail_ = 0;
+    if (text_stream_) {
+      void *st = nullptr;
+      RCK(cudaHostAlloc(&st, (size_t)(window_ + 2) * d.nnodes * 8, cudaHostAllocDefault));
+      staging_ = (double *)st;
+      // frame 0 came with the grid; the reader continues from frame 1
+      times_read_.assign(1, frames_.times[0]);
+      RCK(cudaMemcpyAsync(ring_, frames_.theta.data(), (size_t)d.nnodes * 8, cudaMemcpyHostToDevice, stream_));
+      RCK(cudaMemcpyAsync(ftime_, &times_read_[0], 8, cudaMemcpyHostToDevice, stream_));
+      RCK(cudaStreamSynchronize(stream_));
+      avail_ = 1;
+      d.frames_avail = 1;
+    } else {
+      fcount_ = alloc<unsigned long long>(4);
+      RCK(cudaMemsetAsync(fcount_, 0, 4 * sizeof(unsigned long long), stream_));
+      avail_ = 0;
+    }
     fill_frames(window_ + 2);  // sets d.frames_avail (d is dev_)
+    if (avail_ < 2) throw std::runtime_error(dev_.bad_frame == 1 ? std::string(
+        "fail to read next step temperature file, please check title of line!!") :
+        std::string("the temperature file holds fewer than two frames"));
+    if (text_stream_) frames_.times = times_read_;  // the first window's times (ts0, ts1 below)
   } else {
+    double *ftime = alloc<double>(nframes_);
+    h2d(ftime, frames_.times.data(), nframes_ * 8);
+    d.frame_time = ftime;
     double *frames = alloc<double>((size_t)nframes_ * d.nnodes);
     if (frames_src_ == 2) {
       RCK(remelt_rosenthal_frames(ros_, (int)nframes_, frames, stream_));
@@ -533,7 +610,6 @@ void RemeltRealm::initialize() {
     d.frame_slots = (int)nframes_;
     d.frames_avail = (int)nframes_;
   }
-  d.bad_frame = (int)frames_.bad_frame;
   for (int i = 0; i < 3; ++i) {
     d.theta[i] = alloc<double>(d.nnodes);
     d.theta32[i] = alloc<float>(d.nnodes);
@@ -629,7 +705,16 @@ void RemeltRealm::initialize() {
 
 void RemeltRealm::reset() {
   if (!initialized_) throw StateError("amca_reset before amca_initialize");
-  if (frames_src_ == 3 && avail_ > window_ + 2) {  // the ring has moved on: produce the first window again
+  if (text_stream_) {  // read the file again from its start
+    open_text_frames();
+    RCK(cudaMemcpyAsync(ring_, reader_->head().theta.data(), (size_t)dev_.nnodes * 8, cudaMemcpyHostToDevice,
+                        stream_));
+    RCK(cudaMemcpyAsync(ftime_, &times_read_[0], 8, cudaMemcpyHostToDevice, stream_));
+    RCK(cudaStreamSynchronize(stream_));
+    avail_ = 1;
+    dev_.frames_avail = 1;
+    fill_frames(window_ + 2);
+  } else if (frames_src_ == 3 && avail_ > window_ + 2) {  // the ring has moved on: produce the first window again
     avail_ = 0;
     dev_.frames_avail = 0;
     fill_frames(window_ + 2);

@@ -117,6 +117,13 @@ class RemeltRealm {
                       double time_offset);
   void fill_frames(int upto);
   double *ext_theta_ = nullptr;  // device copy of the host's node temperatures
+  // text frames read while the run goes on (large files, or AMCA_FRAME_STREAM=1)
+  std::unique_ptr<FrameReader> reader_;
+  bool text_stream_ = false;
+  double *ftime_ = nullptr;        // device: frame times, slot f % slots_ on a ring
+  double *staging_ = nullptr;      // page-locked: one window of text frames
+  std::vector<double> times_read_;  // host: times of the text frames read so far
+  void open_text_frames();
   bool ext_ready_ = false;       // node temperatures handed in for the next step
   std::unique_ptr<RestartData> micro_;  // set_microstructure
   // host tables

@@ -13,50 +13,76 @@ namespace amca {
 
 namespace {
 
-// std::getline over the file's bytes with the stream's eof flag: eof is
-// raised when a read reaches the end of the data (no newline, or nothing left).
+// std::getline over a file's bytes with the stream's eof flag: eof is raised
+// when a read reaches the end of the data (no newline, or nothing left). The
+// file is read in chunks, so a frame file of any size streams.
 class LineReader {
  public:
-  explicit LineReader(std::string buf) : buf_(std::move(buf)) {}
+  explicit LineReader(const std::string &path) : f_(path.c_str(), std::ios::in | std::ios::binary) {
+    if (!f_) throw std::runtime_error("fail to open the specified file " + path);
+  }
   bool eof() const { return eof_; }
   void getline(std::string &line) {
     line.clear();
-    if (pos_ >= buf_.size()) {
-      eof_ = true;
-      return;
-    }
-    const size_t nl = buf_.find('\n', pos_);
-    if (nl == std::string::npos) {
-      line.assign(buf_, pos_, std::string::npos);
-      pos_ = buf_.size();
-      eof_ = true;
-    } else {
-      line.assign(buf_, pos_, nl - pos_);
+    for (;;) {
+      if (pos_ >= buf_.size() && !refill()) {
+        if (line.empty() && !partial_) eof_ = true;  // nothing left at all
+        else eof_ = true;                             // the last line had no newline
+        partial_ = false;
+        return;
+      }
+      const size_t nl = buf_.find('\n', pos_);
+      if (nl == std::string::npos) {
+        line.append(buf_, pos_, std::string::npos);
+        pos_ = buf_.size();
+        partial_ = true;
+        continue;
+      }
+      line.append(buf_, pos_, nl - pos_);
       pos_ = nl + 1;
+      partial_ = false;
+      if (pos_ >= buf_.size()) refill_at_end();
+      return;
     }
   }
 
  private:
+  bool refill() {
+    buf_.resize(kChunk);
+    f_.read(&buf_[0], (std::streamsize)kChunk);
+    buf_.resize((size_t)f_.gcount());
+    pos_ = 0;
+    return !buf_.empty();
+  }
+  // after a line that ended exactly at the end of the buffer: fetch the next
+  // chunk now, so that "nothing left" is known at the next call
+  void refill_at_end() {
+    if (!refill()) buf_.clear();
+  }
+  static constexpr size_t kChunk = size_t(16) << 20;
+  std::ifstream f_;
   std::string buf_;
   size_t pos_ = 0;
-  bool eof_ = false;
+  bool eof_ = false, partial_ = false;
 };
-
-std::string slurp(const std::string &path) {
-  std::ifstream f(path.c_str(), std::ios::in | std::ios::binary);
-  if (!f) throw std::runtime_error("fail to open the specified file " + path);
-  std::ostringstream ss;
-  ss << f.rdbuf();
-  return ss.str();
-}
 
 }  // namespace
 
-FeFrames read_fe_frames(const std::string &path, const FeConfig &fe) {
-  LineReader L(slurp(path));
-  FeFrames fr;
+struct FrameReader::Impl {
+  LineReader L;
+  FeConfig fe;
+  double toff = 0.0;
+  std::vector<double> cur;
+  explicit Impl(const std::string &path, const FeConfig &c) : L(path), fe(c) {}
+};
+
+FrameReader::~FrameReader() = default;
+
+// load_mesh_and_first_two_steps_results_from_txt_file: title, the first
+// subtitle (node ranges, time) and the first frame with the coordinates.
+FrameReader::FrameReader(const std::string &path, const FeConfig &fe) : impl_(new Impl(path, fe)) {
+  LineReader &L = impl_->L;
   std::string line;
-  // load_mesh_and_first_two_steps_results_from_txt_file
   int dummy[2] = {0, 0};
   double time[2] = {0, 0};
   int range[6] = {0, 0, 0, 0, 0, 0};
@@ -69,13 +95,15 @@ FeFrames read_fe_frames(const std::string &path, const FeConfig &fe) {
       for (int i = 0; i < 6; i++) iss >> range[i];
     }
   }
-  const double toff = time[0];
+  impl_->toff = time[0];
+  FeFrames &fr = head_;
   for (int i = 0; i < 3; i++) fr.nn[i] = range[2 * i + 1] - range[2 * i] + 1;
   fr.nnodes = (int64_t)fr.nn[0] * fr.nn[1] * fr.nn[2];
   if (fr.nnodes == 1 || fr.nn[0] < 2 || fr.nn[1] < 2 || fr.nn[2] < 2)
     throw std::runtime_error("fail to read temperature file, please check the file type and the lines of title!!");
   fr.coord.resize(3 * (size_t)fr.nnodes);
-  std::vector<double> cur((size_t)fr.nnodes);
+  std::vector<double> &cur = impl_->cur;
+  cur.assign((size_t)fr.nnodes, 0.0);
   for (int64_t n = 0; n < fr.nnodes; ++n) {
     L.getline(line);
     std::istringstream iss(line);
@@ -91,45 +119,69 @@ FeFrames read_fe_frames(const std::string &path, const FeConfig &fe) {
     cur[n] = t;
   }
   fr.times.push_back(0.0);
-  fr.theta.insert(fr.theta.end(), cur.begin(), cur.end());
+  fr.theta = cur;
   fr.nframes = 1;
-  // load_next_step_nodal_data, until the end of the file
-  for (;;) {
-    int64_t count = 0;
-    double tnew = 0;
-    double result = 0;  // keeps the previous line's value when a line lacks it
-    bool ok = true;
-    while (count < fe.subtitle_lines + fr.nnodes) {
-      if (L.eof()) {
-        ok = false;
-        break;
-      }
-      L.getline(line);
-      if (count == 0 && line != "\r" && line != "") {
-        fr.bad_frame = fr.nframes;
-        fr.bad_msg = "fail to read next step temperature file, please check title of line!!";
-        ok = false;
-        break;
-      }
-      if (count == 3) {
-        std::istringstream iss(line);
-        int d0 = 0, d1 = 0;
-        double t0 = 0, t1 = 0;
-        iss >> d0 >> d1 >> t0 >> t1;
-        tnew = t0;
-      }
-      if (count >= fe.subtitle_lines) {
-        std::istringstream iss(line);
-        double c0, c1, c2;
-        iss >> c0 >> c1 >> c2 >> result;
-        cur[count - fe.subtitle_lines] = result;
-      }
-      count++;
+  read_ = 1;
+}
+
+// load_next_step_nodal_data: one more frame, or false at the end of the file
+// or at a malformed frame (bad() tells which).
+bool FrameReader::next(double *out, double &t) {
+  if (done_) return false;
+  LineReader &L = impl_->L;
+  const FeConfig &fe = impl_->fe;
+  std::vector<double> &cur = impl_->cur;  // keeps the previous frame's values where a line lacks one
+  const int64_t nnodes = head_.nnodes;
+  std::string line;
+  int64_t count = 0;
+  double tnew = 0;
+  double result = 0;  // keeps the previous line's value when a line lacks it
+  while (count < fe.subtitle_lines + nnodes) {
+    if (L.eof()) {
+      done_ = true;
+      return false;
     }
-    if (!ok) break;
-    fr.times.push_back((tnew - toff) * fe.time_scale);
+    L.getline(line);
+    if (count == 0 && line != "\r" && line != "") {
+      bad_ = true;
+      bad_msg_ = "fail to read next step temperature file, please check title of line!!";
+      done_ = true;
+      return false;
+    }
+    if (count == 3) {
+      std::istringstream iss(line);
+      int d0 = 0, d1 = 0;
+      double t0 = 0, t1 = 0;
+      iss >> d0 >> d1 >> t0 >> t1;
+      tnew = t0;
+    }
+    if (count >= fe.subtitle_lines) {
+      std::istringstream iss(line);
+      double c0, c1, c2;
+      iss >> c0 >> c1 >> c2 >> result;
+      cur[count - fe.subtitle_lines] = result;
+    }
+    count++;
+  }
+  t = (tnew - impl_->toff) * fe.time_scale;
+  memcpy(out, cur.data(), (size_t)nnodes * sizeof(double));
+  ++read_;
+  return true;
+}
+
+FeFrames read_fe_frames(const std::string &path, const FeConfig &fe) {
+  FrameReader rd(path, fe);
+  FeFrames fr = rd.head();
+  std::vector<double> cur((size_t)fr.nnodes);
+  double t = 0;
+  while (rd.next(cur.data(), t)) {
+    fr.times.push_back(t);
     fr.theta.insert(fr.theta.end(), cur.begin(), cur.end());
     fr.nframes++;
+  }
+  if (rd.bad()) {
+    fr.bad_frame = fr.nframes;
+    fr.bad_msg = rd.bad_msg();
   }
   if (fr.nframes < 2) {
     if (fr.bad_frame == 1) throw std::runtime_error(fr.bad_msg);

@@ -11,6 +11,7 @@
 
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -40,6 +41,31 @@ struct FeFrames {
 // Read the whole frame file. Throws std::runtime_error when the first two
 // frames cannot be read (the reference fails in load()).
 FeFrames read_fe_frames(const std::string &path, const FeConfig &fe);
+
+// The same reader a frame at a time, for files read while the run goes on:
+// the constructor reads the title, the node grid and frame 0 (head()); next()
+// reads the following frame (load_next_step_nodal_data,
+// CA/src/LoadDataFromFile.cpp:143-191) into out (nnodes values) with its
+// scaled time, and returns false at the end of the file or at a malformed
+// frame (then bad() is true and bad_msg() has the reference's message).
+class FrameReader {
+ public:
+  FrameReader(const std::string &path, const FeConfig &fe);
+  ~FrameReader();
+  const FeFrames &head() const { return head_; }
+  bool next(double *out, double &t);
+  bool bad() const { return bad_; }
+  const std::string &bad_msg() const { return bad_msg_; }
+  int64_t frames_read() const { return read_; }
+
+ private:
+  struct Impl;
+  std::unique_ptr<Impl> impl_;
+  FeFrames head_;
+  int64_t read_ = 0;
+  bool done_ = false, bad_ = false;
+  std::string bad_msg_;
+};
 
 // Frames from memory, in file units (same transformation as the reader).
 FeFrames fe_frames_from_arrays(const int32_t nodes[3], const double *coords, int64_t nframes, const double *times,

@@ -1448,7 +1448,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
           break;
         }
         ts1 = ts0;
-        ts0 = d.frame_time[f_next];
+        ts0 = d.frame_time[f_next % d.frame_slots];
         f_new = f_next;
         f_next++;
       }

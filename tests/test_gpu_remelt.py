@@ -243,3 +243,51 @@ def test_remelt_gpu_frames_streamed_through_a_ring(amca, tmp_path, monkeypatch, 
     r.run()
     assert np.array_equal(r.field("orientation_id"), g["orient"])
     r.close()
+
+
+@pytest.mark.parametrize("name", sorted(FIX))
+def test_remelt_gpu_text_frames_streamed(amca, tmp_path, monkeypatch, name):
+    """Text frames read a window at a time while the run goes on (the
+    reader of load_next_step_nodal_data, 3 frames per window) give the
+    reference's run at every step, and again after a reset (the file is read
+    again from its start)."""
+    monkeypatch.setenv("AMCA_FRAME_STREAM", "1")
+    monkeypatch.setenv("AMCA_FRAME_WINDOW", "3")
+    fx = FIX[name]
+    r = make_realm(amca, fx, str(tmp_path))
+    g = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    fields = [str(f) for f in g["fields"]]
+    n = len(g["digests"])
+    for i in range(n):
+        dt = r.single_integration_step()
+        st = r.stats()
+        assert st["time"] == g["time"][i] and dt == g["dt"][i], f"step {i + 1}: time/dt"
+        d = digests(r)
+        bad = [k for k in STATE if d[k] != g["digests"][i][fields.index(k)]]
+        assert not bad, f"step {i + 1}: {bad}"
+    r.single_integration_step()  # the reference stopped at the end of its frames
+    assert r.stats()["step"] == n and r.stats()["done"] == 1
+    fs = r.frame_stats()
+    assert fs["fills"] > 3
+    r.reset()
+    r.run()
+    assert np.array_equal(r.field("orientation_id"), g["orient"])
+    r.close()
+
+
+def test_remelt_gpu_streamed_bad_frame_stops_like_the_reference(amca, tmp_path, monkeypatch):
+    monkeypatch.setenv("AMCA_FRAME_STREAM", "1")
+    monkeypatch.setenv("AMCA_FRAME_WINDOW", "2")
+    fx = FIX["remelt_random"]
+    r = make_realm(amca, fx, str(tmp_path))
+    r.close()
+    path = tmp_path / "frames.txt"
+    text = path.read_text().split("\n")
+    fourth = [i for i, line in enumerate(text) if line == "Subtitle"][3]
+    text[fourth - 1] = "not blank"
+    path.write_text("\n".join(text))
+    r = amca.CellularAutomataRealm(fx.case.to_yaml(), seed=fx.case.seed, workdir=str(tmp_path))
+    r.initialize()
+    with pytest.raises(amca.AmcaError, match="check title of line"):
+        r.run()
+    r.close()
