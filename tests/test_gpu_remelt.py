@@ -291,3 +291,50 @@ def test_remelt_gpu_streamed_bad_frame_stops_like_the_reference(amca, tmp_path, 
     with pytest.raises(amca.AmcaError, match="check title of line"):
         r.run()
     r.close()
+
+
+def test_remelt_gpu_pbf_500_full_size(amca):
+    """pbf_500, the benchmarked FE-coupled workload (500 x 250 x 100 cells,
+    1,550 Rosenthal frames, 2,000-grain baseplate), at full size against the
+    unmodified reference's run of the same deck (tests/golden/make_pbf_golden.py):
+    the step count, time and dt, the orientation / grain-id / melted field
+    digests, grain and orientation counts and the Euler angles at every
+    checkpoint the reference recorded and at the end."""
+    import hashlib
+    import json
+
+    from amca3d_gb300 import decks
+
+    path = os.path.join(HERE, "golden", "pbf_500_golden.json")
+    if not os.path.exists(path):
+        pytest.skip("no reference run recorded for pbf_500")
+    golden = json.load(open(path))
+    ref = golden.get("reference") or golden.get("oracle")
+    case, frames, m = decks.config_pbf_500()
+    r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
+    r.set_microstructure(m["grain"], m["orient"], m["euler"], m["grain_cell"], m["grain_orient"],
+                         expected=m["expected"])
+    r.set_rosenthal_frames(**frames.rosenthal_kwargs())
+    r.initialize()
+
+    def sha(a, dt):
+        return hashlib.sha256(np.ascontiguousarray(a, dt).tobytes()).hexdigest()
+
+    def check(rec, where):
+        st = r.stats()
+        assert st["step"] == rec["step"], where
+        assert st["time"] == float.fromhex(rec["time"]) and st["dt"] == float.fromhex(rec["dt"]), where
+        assert sha(r.field("orientation_id"), "<i4") == rec["orient"], where
+        assert sha(r.field("grain_id"), "<i4") == rec["grain"], where
+        assert sha(r.field("melted"), "u1") == rec["melted"], where
+        assert st["grains"] == rec["ngrains"] and st["orientations"] == rec["norient"], where
+        if "euler" in rec:
+            assert sha(r.orientations(), "<f8") == rec["euler"], where
+
+    for cp in sorted(ref.get("checkpoints", []), key=lambda c: c["step"]):
+        r.run(cp["step"] - r.stats()["step"])
+        check(cp, f"step {cp['step']}")
+    r.run()
+    assert r.stats()["done"] == 1
+    check(ref["final"], "end of the frames")
+    r.close()
