@@ -48,7 +48,8 @@ constexpr int kErrWait = 1;
 
 enum { kEpiFwd = 0, kEpiHead = 1, kEpiBwd = 2, kEpiPartial = 3 };
 
-__device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// fast reciprocal (MUFU) on an argument kept below 2^126 (z >= -80)
+__device__ __forceinline__ float sigmoid(float z) { return __fdividef(1.0f, 1.0f + __expf(-fmaxf(z, -80.0f))); }
 __device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = sigmoid(z);
@@ -580,7 +581,10 @@ __device__ __forceinline__ int64_t frame_query(const FrameJob &j, int64_t q, int
 // Fused inference: the whole network on 128-query tiles, persistent.
 // Shared memory: activations H (128 x 256 bf16, four 64-column blocks of
 // 16 KB) and one layer's weights (256 x 256 bf16, four blocks of 32 KB).
+// 512 threads: warp w reads TMEM lanes 32 (w % 4) (its rows) and handles the
+// 64-column group w / 4 of every layer's epilogue.
 // ---------------------------------------------------------------------------
+constexpr int kInferThreads = 512, kInferGroups = 4, kGroupCols = kSurHid / kInferGroups;
 enum { kSrcArray = 0, kSrcFrames = 1 };
 
 struct InferArgs {
@@ -594,7 +598,7 @@ struct InferArgs {
 constexpr uint32_t kInferSmem = 64u * 1024u + 128u * 1024u + 1024u;
 
 template <int SRC>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(kInferThreads, 1)
     mlp_infer_kernel(const __grid_constant__ CUtensorMap tW0, const __grid_constant__ CUtensorMap tW1,
                      const __grid_constant__ CUtensorMap tW2, const __grid_constant__ CUtensorMap tW3, SurModelDev md,
                      InferArgs a) {
@@ -604,12 +608,14 @@ __global__ void __launch_bounds__(256, 1)
   __shared__ __align__(8) uint64_t wbar, mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_abort;
-  __shared__ float s_bias[kSurLayers][kSurHid], s_wh[kSurOut][kSurHid], s_bh[kSurOut];
-  __shared__ float s_head[2][128][2];
+  __shared__ __align__(16) float s_bias[kSurLayers][kSurHid];
+  __shared__ __align__(16) float s_wh[kSurOut][kSurHid];
+  __shared__ float s_bh[kSurOut];
+  __shared__ float s_head[kInferGroups][128][2];
   const CUtensorMap *tW[4] = {&tW0, &tW1, &tW2, &tW3};
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q4 = warp & 3, half = warp >> 2, row = q4 * 32 + lane;
+  const int q4 = warp & 3, grp = warp >> 2, row = q4 * 32 + lane;
   const int64_t ntiles = (a.nq + 127) / 128;
   const SurParamLayout L;
 
@@ -663,8 +669,8 @@ __global__ void __launch_bounds__(256, 1)
         scan_inputs(a.job.src, nx, ny, nz, frame_time(a.job, f), raw);
       }
     }
-    // Fourier features: this half's 32 phases, sines at column j, cosines at 64 + j
-    for (int j0 = half * 32; j0 < half * 32 + 32; j0 += 8) {
+    // Fourier features: this group's 16 phases, sines at column j, cosines at 64 + j
+    for (int j0 = grp * (kSurFreq / kInferGroups); j0 < (grp + 1) * (kSurFreq / kInferGroups); j0 += 8) {
       __align__(16) bf16 sb[8], cb[8];
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
@@ -706,23 +712,34 @@ __global__ void __launch_bounds__(256, 1)
       umma::tc_fence_after();
       // the weights are free again: stream in the next layer's (or the next tile's first) while the epilogue runs
       if (threadIdx.x == 0 && (l < kSurLayers - 1 || tile + gridDim.x < ntiles)) load_w((l + 1) % kSurLayers);
-      for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
+      for (int c0 = grp * kGroupCols; c0 < (grp + 1) * kGroupCols; c0 += 32) {
         float v[32];
         umma::tmem_ld32(trow + c0, v);
+        const float4 *b4 = reinterpret_cast<const float4 *>(&s_bias[l][c0]);
         if (l < kSurLayers - 1) {
 #pragma unroll
           for (int j = 0; j < 32; j += 8) {
+            const float4 ba = b4[j / 4], bb = b4[j / 4 + 1];
+            const float b[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
             __align__(16) bf16 hb[8];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) hb[t] = __float2bfloat16_rn(silu(v[j + t] + s_bias[l][c0 + j + t]));
+            for (int t = 0; t < 8; ++t) hb[t] = __float2bfloat16_rn(silu(v[j + t] + b[t]));
             *(uint4 *)(H + umma::sw128_offset(row, c0 + j, 128)) = *(const uint4 *)hb;
           }
         } else {
+          const float4 *w0 = reinterpret_cast<const float4 *>(&s_wh[0][c0]);
+          const float4 *w1 = reinterpret_cast<const float4 *>(&s_wh[1][c0]);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float h = silu(v[j] + s_bias[l][c0 + j]);
-            mu = fmaf(h, s_wh[0][c0 + j], mu);
-            sl = fmaf(h, s_wh[1][c0 + j], sl);
+          for (int j = 0; j < 32; j += 4) {
+            const float4 bq = b4[j / 4], m0 = w0[j / 4], m1 = w1[j / 4];
+            const float b[4] = {bq.x, bq.y, bq.z, bq.w}, x0[4] = {m0.x, m0.y, m0.z, m0.w},
+                        x1[4] = {m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const float h = silu(v[j + t] + b[t]);
+              mu = fmaf(h, x0[t], mu);
+              sl = fmaf(h, x1[t], sl);
+            }
           }
         }
       }
@@ -731,12 +748,17 @@ __global__ void __launch_bounds__(256, 1)
       __syncthreads();
     }
     if (!ok) break;
-    s_head[half][row][0] = mu;
-    s_head[half][row][1] = sl;
+    s_head[grp][row][0] = mu;
+    s_head[grp][row][1] = sl;
     __syncthreads();
-    if (half == 0) {  // whole warps
-      const float m = s_head[0][row][0] + s_head[1][row][0] + s_bh[0];
-      const float s = fminf(fmaxf(s_head[0][row][1] + s_head[1][row][1] + s_bh[1], -12.0f), 4.0f);
+    if (grp == 0) {  // whole warps
+      float m = s_bh[0], s = s_bh[1];
+#pragma unroll
+      for (int k = 0; k < kInferGroups; ++k) {
+        m += s_head[k][row][0];
+        s += s_head[k][row][1];
+      }
+      s = fminf(fmaxf(s, -12.0f), 4.0f);
       const float T = md.log_out ? md.t_shift + md.t_scale * expf(m) : md.t_shift + md.t_scale * m;
       const float e = md.log_out ? 2.0f * (T - md.t_shift) * expf(s) : 2.0f * md.t_scale * expf(s);
       if (SRC == kSrcArray) {
@@ -1207,7 +1229,7 @@ void produce_frames(ThermalModel *model, sur::FrameJob job, cudaStream_t s) {
   SCK(cudaFuncSetAttribute(mlp_infer_kernel<kSrcFrames>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
   const int64_t tiles = (ia.nq + 127) / 128;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, sms));
-  mlp_infer_kernel<kSrcFrames><<<grid, 256, kInferSmem, s>>>(tw[0], tw[1], tw[2], tw[3], model->dev(), ia);
+  mlp_infer_kernel<kSrcFrames><<<grid, kInferThreads, kInferSmem, s>>>(tw[0], tw[1], tw[2], tw[3], model->dev(), ia);
   SCK(cudaGetLastError());
 }
 
@@ -1389,7 +1411,7 @@ int amca_thermal_eval(amca_thermal *h, const float *raw, int64_t n, float *T, fl
                              (int)kInferSmem));
     const int64_t tiles = (n + 127) / 128;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, sms));
-    mlp_infer_kernel<kSrcArray><<<grid, 256, kInferSmem, m.stream>>>(tw[0], tw[1], tw[2], tw[3], m.dev(), ia);
+    mlp_infer_kernel<kSrcArray><<<grid, kInferThreads, kInferSmem, m.stream>>>(tw[0], tw[1], tw[2], tw[3], m.dev(), ia);
     SCK(cudaGetLastError());
     SCK(cudaMemcpyAsync(T, d_T, (size_t)n * 4, cudaMemcpyDeviceToHost, m.stream));
     SCK(cudaMemcpyAsync(err, d_e, (size_t)n * 4, cudaMemcpyDeviceToHost, m.stream));
