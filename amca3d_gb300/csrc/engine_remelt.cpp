@@ -781,11 +781,13 @@ static double reference_velocity(const PlainConfig &c, double T) {
 }
 
 // Runs beside a kernel launch: answers the kernel's velocity requests.
-void RemeltRealm::serve_velocities(const volatile int *stop, int w, int workers, VelocityJob *job) {
+void RemeltRealm::serve_velocities(const volatile int *stop, int w, int workers, VelocityJob *job, unsigned last) {
   HostVelocity *hv = hostvel_;
   // worker 0 watches the device's request word and hands each request to all
-  // workers; every worker spins (yielding when idle for long) on the job word
-  unsigned last = w == 0 ? __atomic_load_n(&hv->seq_done, __ATOMIC_ACQUIRE) : job->seq.load(std::memory_order_acquire);
+  // workers; every worker spins (yielding when idle for long) on the job word.
+  // `last` is what each has served before the launch (read before any thread
+  // starts: a worker that started after the first request was posted would
+  // otherwise take that request as served and never count it off)
   unsigned idle = 0;
   while (!*stop) {
     unsigned r;
@@ -910,9 +912,10 @@ void RemeltRealm::launch(long long limit) {
     const int hw = (int)std::thread::hardware_concurrency();
     const int workers = std::max(1, std::min(8, hw / 2));
     VelocityJob job;
+    const unsigned done0 = __atomic_load_n(&hostvel_->seq_done, __ATOMIC_ACQUIRE);
     std::vector<std::thread> servers;
     for (int w = 0; w < workers; ++w)
-      servers.emplace_back([&, w] { serve_velocities(&stop, w, workers, &job); });
+      servers.emplace_back([&, w] { serve_velocities(&stop, w, workers, &job, w == 0 ? done0 : 0u); });
     RCK(cudaEventRecord(ev0_, stream_));
     cudaError_t le = remelt_run_steps(dev_, limit, blocks_, stream_);
     if (le == cudaSuccess) le = cudaEventRecord(ev1_, stream_);

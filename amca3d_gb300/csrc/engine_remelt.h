@@ -80,7 +80,7 @@ class RemeltRealm {
     std::atomic<unsigned> n{0};     // its entry count
     std::atomic<unsigned> left{0};  // workers still evaluating it
   };
-  void serve_velocities(const volatile int *stop, int w, int workers, VelocityJob *job);
+  void serve_velocities(const volatile int *stop, int w, int workers, VelocityJob *job, unsigned last);
   void launch(long long limit);
   void write_snapshot();
   // host copies of the output fields of the current state
