@@ -100,16 +100,25 @@ AMCA_HD bool is_captured_f64(const double *l2g, double gcx, double gcy, double g
 // and the final sum of three absolute values adds 2*u*(its magnitude). The
 // margin used is 2^-14 relative plus 8*err per component — orders of
 // magnitude above that bound and the FP64 evaluation's own error.
-AMCA_HD int captured_f32(const float *m32, float gx, float gy, float gz, float err, float length) {
+//
+// *lower receives a lower bound of the FP64 |c'|_1 (the same FP32 estimate
+// less the margin's terms for the estimate itself, plus 2^-14 of it): an
+// envelope whose half-diagonal stays below it cannot contain the cell.
+AMCA_HD int captured_f32_lb(const float *m32, float gx, float gy, float gz, float err, float length, float *lower) {
   float cx = gx * m32[0] + gy * m32[3] + gz * m32[6];
   float cy = gx * m32[1] + gy * m32[4] + gz * m32[7];
   float cz = gx * m32[2] + gy * m32[5] + gz * m32[8];
   float s = fabsf(cx) + fabsf(cy) + fabsf(cz);
   float scale = fabsf(gx) + fabsf(gy) + fabsf(gz);
   float margin = 6.103515625e-05f * (3.0f * scale + length) + 24.0f * err;  // 2^-14
+  *lower = s - (6.103515625e-05f * (3.0f * scale + s) + 24.0f * err);
   if (s < length - margin) return 1;
   if (s > length + margin) return 0;
   return -1;
+}
+AMCA_HD int captured_f32(const float *m32, float gx, float gy, float gz, float err, float length) {
+  float lower;
+  return captured_f32_lb(m32, gx, gy, gz, err, length, &lower);
 }
 
 // CA/src/Octahedron.cpp:27-84 tables

@@ -8,9 +8,26 @@
 //   its octahedron, appending the new envelope to the list it is walking.
 //
 // Parallel equivalent, per step:
-//   generation 0 = the active list after nucleation; generation g+1 = the
-//   envelopes created while walking generation g (a contiguous id range,
-//   because ids are handed out in walk order).
+//   The envelope list lives in one array in walk order: nucleation and
+//   captures append to it, dead entries stay as tombstones until an
+//   occasional compaction. Only what changes is touched:
+//   wake    : growth is uniform, so each entry keeps a wake key, the
+//             cumulative growth at which its half-diagonal may reach a lower
+//             bound of |c'|_1 over its liquid neighbours. A scan of the keys
+//             (4 B per entry) picks, in walk order, the entries that may
+//             capture this step; the others are not read. Their half-diagonal
+//             is brought up to date when they wake, by replaying the step
+//             increments from a ring, the same FP64 sums in the same order.
+//   deaths  : each entry keeps the count of its liquid neighbours; nucleation
+//             and captures decrement the counts of the entries around the
+//             cell. A sleeping entry whose count reaches zero leaves the list
+//             in this step if every capture that emptied it came from an
+//             earlier rank of generation 0, else in the next step (at its
+//             turn a neighbour was still liquid), exactly as the reference's
+//             walk deactivates it.
+//   generation 0 = the woken entries, then this step's nuclei; generation
+//   g+1 = the envelopes created while walking generation g (a contiguous id
+//   range, because ids are handed out in walk order, appended to the list).
 //   claim   : every envelope of the generation tests its liquid neighbours
 //             (FP32 pre-test with a proven error margin, exact FP64 when the
 //             margin is not enough) and atomicMin's a claim word
@@ -19,13 +36,13 @@
 //             that reaches the cell first in the reference. An envelope of
 //             generation g+1 first builds itself: the decentred octahedron of
 //             its parent (FP64), and writes its orientation into its cell.
+//             Each sets its liquid count and its next wake key.
 //   resolve : an envelope captures the cells whose final claim is its own;
 //             it stays active iff some neighbour was liquid at its turn and
 //             not captured by it (unclaimed, or claimed by a later rank).
 //             One decoupled look-back per block over (captures, survives)
-//             gives the new envelope ids (walk order), the child records
-//             (parent id, neighbour index) and the order-preserving
-//             compaction of survivors into the next active list.
+//             gives the new envelope ids (walk order) and the child records
+//             (parent rank, neighbour index); the others become tombstones.
 // The resolve pass gives each block one contiguous chunk of the generation
 // (its look-back runs once per block); claims and a separate marking pass
 // need no order and hand out rank pieces dynamically (RankSched); nucleation
@@ -426,10 +443,90 @@ __device__ __forceinline__ uint32_t liquid_neighbours(const uint32_t *solid, con
   return ~neighbour_bits(solid, g, cell) & 0x03ffffffu;
 }
 
+// ---------------------------------------------------------------------------
+// The envelope list: wake keys, grown half-diagonals, liquid counts.
+// ---------------------------------------------------------------------------
+// Whether an entry with wake key k is processed in a step whose cumulative
+// growth is `grown` (all: every live entry, to bring its record up to date).
+// Dead entries (NaN) never are.
+__device__ __forceinline__ bool woken(float k, double grown, bool all) { return all ? !isnan(k) : (double)k <= grown; }
+
+// Wake key: the cumulative growth at which the half-diagonal L (grown up to
+// `grown`) may reach t_lb, rounded down, less a relative 2^-30 that covers
+// the rounding of the step sums between now and then (an entry is woken at
+// least every kWakeAll steps). +inf when no liquid neighbour is left.
+__device__ __forceinline__ float wake_key(float t_lb, double L, double grown) {
+  if (!(t_lb < INFINITY)) return INFINITY;
+  const double k = (double)t_lb - L + grown;
+  const double slack = 9.313225746154785e-10 * (fabs((double)t_lb) + fabs(L) + fabs(grown));
+  return __double2float_rd(k - slack);
+}
+
+// Grain::grow (Grain.h:27) of the steps (from, to]: the same FP64 additions
+// of each step's dt * vel, in order.
+__device__ __forceinline__ double replay_growth(const double *dvh, double L, long long from, long long to) {
+  for (long long t = from + 1; t <= to; ++t) L += dvh[t & (kDvRing - 1)];
+  return L;
+}
+
+// A dead entry: never woken, and no longer found from its cell.
+__device__ __forceinline__ void tombstone(const PlainDevice &d, int cur, long long q, int cell) {
+  d.key[cur][q] = __int_as_float(0x7fc00000);
+  d.pos[cell] = -1;
+}
+
+// The list positions of a generation's ranks: generation 0 is the woken
+// entries (wlist, in walk order) followed by the step's nuclei from `base`;
+// a later generation is the contiguous run from `base`.
+struct GenList {
+  const int32_t *w;
+  long long nw;
+  long long base;
+  __device__ __forceinline__ long long at(long long r) const { return r < nw ? (long long)w[r] : base + (r - nw); }
+};
+
+// Cell `cell` has just turned solid: one liquid neighbour fewer for every
+// entry around it. A decrement by a capture of a later rank (position `pc`
+// beyond the entry's) is recorded in late[]; a count reaching zero goes to
+// the zero list of this generation (parity zpar). Nucleation passes pc = -1
+// and no list: it handles a zero itself (returned as the count of entries
+// gone at their turn).
+__device__ __noinline__ unsigned neighbour_solid(const PlainDevice &d, int cur, int cell, long long pc, long long step,
+                                                 int zpar, double grown, bool all, unsigned long long *stat_dec) {
+  const Grid &g = d.grid;
+  unsigned gone = 0;
+  int32_t *nliq = d.nliq[cur];
+#pragma unroll 1
+  for (int nb = 0; nb < 26; ++nb) {
+    int di, dj, dk;
+    const int m = cell + nbr_delta(g, nb, di, dj, dk);
+    const int q = d.pos[m];
+    if (q < 0) continue;
+    ++*stat_dec;
+    if (pc > q) d.late[q] = (int32_t)step;
+    const int old = atomicSub(nliq + q, 1);
+    if (old != 1) continue;
+    if (zpar >= 0) {
+      const unsigned long long i = atomicAdd(&d.ctrl->zn[zpar], 1ull);
+      d.zlist[zpar][i] = q;
+    } else if (!woken(d.key[cur][q], grown, all)) {
+      // nucleation precedes the walk: a sleeping entry left without a liquid
+      // neighbour is deactivated at its turn (a woken one decides itself)
+      tombstone(d, cur, q, m);
+      ++gone;
+    }
+  }
+  return gone;
+}
+
 // Nucleus number r (in site order) of this step on `cell`: orientation,
-// envelope table entry and active-list record (CellularAutomataManager.cpp:262-290).
-__device__ __forceinline__ void place_nucleus(const PlainDevice &d, EnvRec *act, long long base_act,
-                                              long long base_orient, long long base_grain, long long r, int cell) {
+// envelope table entry and list record at position base_pos + r, grown from
+// the previous step on (CellularAutomataManager.cpp:262-290). Returns the
+// entries around it that leave the list at their turn.
+__device__ __forceinline__ unsigned place_nucleus(const PlainDevice &d, int cur, long long base_pos,
+                                                  long long base_orient, long long base_grain, long long r, int cell,
+                                                  long long step, double grown, bool all,
+                                                  unsigned long long *stat_dec) {
   const int oid = (int)(base_orient + r);
   const long long gid = base_grain + r;
   int I, J, K;
@@ -447,7 +544,9 @@ __device__ __forceinline__ void place_nucleus(const PlainDevice &d, EnvRec *act,
   en.cell = cell;
   en.ori = oid;
   en.id = (int32_t)gid;
-  act[base_act + r] = en;
+  d.act[cur][base_pos + r] = en;
+  d.lstep[cur][base_pos + r] = (int32_t)(step - 1);
+  return neighbour_solid(d, cur, cell, -1, step, -1, grown, all, stat_dec);
 }
 
 // Sites are held as tiles of kBlock, one per block, when they fit: tile t =
@@ -466,9 +565,29 @@ __device__ __forceinline__ bool site_tiles(const PlainDevice &d) { return d.nsit
 // count in the step's parity slot (a step without envelopes has no barrier
 // before the next nucleation), which every block reads after the barrier.
 // ---------------------------------------------------------------------------
-__device__ bool nucleation_phase(const PlainDevice &d, double time, long long step, long long base_act,
-                                 long long base_orient, long long base_grain, EnvRec *act, int *s_cell,
-                                 double *s_dtc, unsigned long long *smem, unsigned long long *stat_live) {
+// calculate_time_step (CellularAutomataManager_3D.cpp:449-507): one velocity
+// for the uniform field; dt for "some active envelope" (da) and for "none"
+// (dn: maxVelocity stays 1e-10), picked after nucleation. Every block
+// evaluates it itself (the same FP64 operations, so the same values).
+__device__ __forceinline__ void step_rates(const PlainDevice &d, double time, double &vel, double &da, double &dn) {
+  const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
+  vel = kgt_velocity(d.Tm, T, d.a1, d.a2, d.a3);
+  const double maxV = vel > 1e-10 ? vel : 1e-10;
+  const double a = d.tsf * d.grid.h / maxV, b = d.tsf * d.grid.h / 1e-10;
+  da = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
+  dn = (d.max_dt < b) ? d.max_dt : b;
+  if (d.dt_cap > 0) {  // setup_time_step_for_coupling of an external solver
+    da = (d.dt_cap < da) ? d.dt_cap : da;
+    dn = (d.dt_cap < dn) ? d.dt_cap : dn;
+  }
+}
+
+// Nuclei go to the list from position base_pos on; `gone` counts the
+// entries around them that leave the list at their turn.
+__device__ __noinline__ bool nucleation_phase(const PlainDevice &d, int cur, double time, long long step, long long base_pos,
+                                 long long base_orient, long long base_grain, double grown, bool all, int *s_cell,
+                                 double *s_dtc, unsigned long long *smem, unsigned long long *stat_live,
+                                 unsigned long long *stat_dec, unsigned *gone) {
   PlainCtrl *c = d.ctrl;
   unsigned long long *scan = d.scanA + (step & 1) * kStatusWords;
   const double T = d.T0 + d.Tdot * time;  // compute_cell_temperature (ProblemPhysics.cpp:164-169)
@@ -477,28 +596,10 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
   // previous step's nucleation, which every block finished before that
   // phase's barrier
   if (threadIdx.x == 0) d.scanA[((step + 1) & 1) * kStatusWords + t_b] = 0ull;
-  if (t_b == 0 && threadIdx.x == 0) {
-    // calculate_time_step (CellularAutomataManager_3D.cpp:449-507): one
-    // velocity for the uniform field; dt for "some active envelope" and for
-    // "none" (maxVelocity stays 1e-10), picked after nucleation. Slots by step
-    // parity: a slow block may still read last step's values.
-    const double vel = kgt_velocity(d.Tm, T, d.a1, d.a2, d.a3);
-    const double maxV = vel > 1e-10 ? vel : 1e-10;
-    const double a = d.tsf * d.grid.h / maxV, b = d.tsf * d.grid.h / 1e-10;
-    c->vel[step & 1] = vel;
-    double da = (d.max_dt < a) ? d.max_dt : a;  // std::min (:507)
-    double dn = (d.max_dt < b) ? d.max_dt : b;
-    if (d.dt_cap > 0) {  // setup_time_step_for_coupling of an external solver
-      da = (d.dt_cap < da) ? d.dt_cap : da;
-      dn = (d.dt_cap < dn) ? d.dt_cap : dn;
-    }
-    c->dt_active[step & 1] = da;
-    c->dt_none[step & 1] = dn;
-  }
   if (site_tiles(d)) {
     const long long ntiles = (d.nsites + kBlock - 1) / kBlock;
     if (t_b >= ntiles) {  // no sites in this block
-      if (ntiles == 0 && t_b == 0 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_act;
+      if (ntiles == 0 && t_b == 0 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_pos;
       return true;
     }
     const int cell = s_cell[threadIdx.x];
@@ -516,8 +617,10 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
     const unsigned long long ex = block_exclusive_scan(nuc, smem, &agg);
     const unsigned long long pre = block_prefix(scan, agg, smem, c);
     if (pre == ~0ull) return false;
-    if (nuc) place_nucleus(d, act, base_act, base_orient, base_grain, (long long)(pre + ex), cell);
-    if (t_b == ntiles - 1 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_act + (long long)(pre + agg);
+    if (nuc)
+      *gone += place_nucleus(d, cur, base_pos, base_orient, base_grain, (long long)(pre + ex), cell, step, grown, all,
+                             stat_dec);
+    if (t_b == ntiles - 1 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_pos + (long long)(pre + agg);
     return true;
   }
   long long b, e;
@@ -547,22 +650,162 @@ __device__ bool nucleation_phase(const PlainDevice &d, double time, long long st
     }
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan(nuc, smem, &tot);
-    if (nuc) place_nucleus(d, act, base_act, base_orient, base_grain, (long long)(run + ex), cell);
+    if (nuc)
+      *gone += place_nucleus(d, cur, base_pos, base_orient, base_grain, (long long)(run + ex), cell, step, grown, all,
+                             stat_dec);
     run += tot;
   }
-  if (t_b == t_nb - 1 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_act + (long long)(pre + agg);
+  if (t_b == t_nb - 1 && threadIdx.x == 0) c->n_active_nuc[step & 1] = base_pos + (long long)(pre + agg);
   return true;
 }
 
 // ---------------------------------------------------------------------------
-// Claim: growth (generation 0) or self-construction (generation >= 1),
-// neighbour tests, atomicMin claims.
+// Ordered selections over the list: the wake scan and the compaction. The
+// block takes a contiguous chunk of positions, each warp a contiguous piece
+// of it: pass 1 counts (ballots), one block scan over the warps and one
+// look-back over the blocks place the block, pass 2 writes in order.
 // ---------------------------------------------------------------------------
-__device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long long n, unsigned par, bool grow,
-                            double dv, EnvRec *cur, const EnvRec *prev, unsigned long long *stat_tests,
-                            unsigned long long *stat_tests64) {
+struct WarpPiece {
+  long long b, e;
+  __device__ WarpPiece(long long n) {
+    long long cb, ce;
+    block_chunk(n, cb, ce);
+    const long long per = ((((ce - cb) + kWarps - 1) / kWarps) + 31) & ~31ll;
+    const long long w = threadIdx.x >> 5;
+    b = cb + w * per < ce ? cb + w * per : ce;
+    e = b + per < ce ? b + per : ce;
+  }
+};
+
+// Offset of this warp's first selected position among all selected ones,
+// given the warp's count (lane 0's value counts); ~0 on a look-back failure.
+__device__ __forceinline__ unsigned long long warp_offset(unsigned cnt, unsigned long long *status,
+                                                        unsigned long long *smem, unsigned long long *total,
+                                                        PlainCtrl *c) {
+  unsigned long long agg;
+  const unsigned long long ex = block_exclusive_scan((threadIdx.x & 31) == 0 ? cnt : 0u, smem, &agg);
+  const unsigned long long pre = block_prefix(status, agg, smem, c);
+  if (pre == ~0ull) return ~0ull;
+  *total = pre + agg;
+  return pre + __shfl_sync(0xffffffffu, ex, 0);
+}
+
+// The entries among positions [0, n) that this step processes, in walk
+// order, into wlist; the count goes to n_woken[step & 1].
+__device__ __noinline__ bool wake_scan(const PlainDevice &d, int cur, long long n, long long step, double grown, bool all,
+                          unsigned long long *smem) {
+  PlainCtrl *c = d.ctrl;
+  // the next step's words start cleared (last read in the previous step)
+  if (threadIdx.x == 0) d.scanC[((step + 1) & 1) * kStatusWords + t_b] = 0ull;
+  const float *key = d.key[cur];
+  const WarpPiece wp(n);
+  const int lane = threadIdx.x & 31;
+  unsigned cnt = 0;
+  for (long long p0 = wp.b; p0 < wp.e; p0 += 32) {
+    const long long p = p0 + lane;
+    cnt += __popc(__ballot_sync(0xffffffffu, p < wp.e && woken(key[p], grown, all)));
+  }
+  unsigned long long total = 0;
+  unsigned long long off = warp_offset(cnt, d.scanC + (step & 1) * kStatusWords, smem, &total, c);
+  if (off == ~0ull) return false;
+  // a key read again here may have turned dead since (a nucleus next to a
+  // sleeping entry), which the first pass counted as not woken all the same
+  for (long long p0 = wp.b; p0 < wp.e; p0 += 32) {
+    const long long p = p0 + lane;
+    const bool w = p < wp.e && woken(key[p], grown, all);
+    const unsigned bal = __ballot_sync(0xffffffffu, w);
+    if (w) d.wlist[off + __popc(bal & ((1u << lane) - 1u))] = (int32_t)p;
+    off += __popc(bal);
+  }
+  if (t_b == t_nb - 1 && threadIdx.x == 0) c->n_woken[step & 1] = (long long)total;
+  return true;
+}
+
+// The live entries of list `cur` among [0, n), in order, into list cur ^ 1
+// with their keys, grow steps and liquid counts; the cell map follows. The
+// new length goes to compact_len.
+__device__ __noinline__ bool compact_phase(const PlainDevice &d, int cur, long long n, unsigned par, unsigned long long *smem,
+                              unsigned long long *stat_moved) {
+  PlainCtrl *c = d.ctrl;
+  if (threadIdx.x == 0) d.scanD[(par ^ 1u) * kStatusWords + t_b] = 0ull;  // the next compaction's words
+  const float *key = d.key[cur];
+  const WarpPiece wp(n);
+  const int lane = threadIdx.x & 31;
+  unsigned cnt = 0;
+  for (long long p0 = wp.b; p0 < wp.e; p0 += 32) {
+    const long long p = p0 + lane;
+    cnt += __popc(__ballot_sync(0xffffffffu, p < wp.e && !isnan(key[p])));
+  }
+  unsigned long long total = 0;
+  unsigned long long off = warp_offset(cnt, d.scanD + par * kStatusWords, smem, &total, c);
+  if (off == ~0ull) return false;
+  const int nxt = cur ^ 1;
+  for (long long p0 = wp.b; p0 < wp.e; p0 += 32) {
+    const long long p = p0 + lane;
+    const bool live = p < wp.e && !isnan(key[p]);
+    const unsigned bal = __ballot_sync(0xffffffffu, live);
+    if (live) {
+      const long long q = (long long)off + __popc(bal & ((1u << lane) - 1u));
+      const EnvRec en = d.act[cur][p];
+      d.act[nxt][q] = en;
+      d.key[nxt][q] = key[p];
+      d.lstep[nxt][q] = d.lstep[cur][p];
+      d.nliq[nxt][q] = d.nliq[cur][p];
+      d.late[q] = -1;
+      d.pos[en.cell] = (int32_t)q;
+      ++*stat_moved;
+    }
+    off += __popc(bal);
+  }
+  if (t_b == t_nb - 1 && threadIdx.x == 0) c->compact_len = (long long)total;
+  return true;
+}
+
+// The list departures this thread decided, added to the step's slots (now:
+// step % 3, next step: (step + 1) % 3), one atomic per warp that has any.
+__device__ __forceinline__ void flush_departures(PlainCtrl *c, long long step, unsigned &now, unsigned &next) {
+  const unsigned a = __reduce_add_sync(0xffffffffu, now), b = __reduce_add_sync(0xffffffffu, next);
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd((unsigned long long *)&c->deaths[step % 3], (unsigned long long)a);
+    if (b) atomicAdd((unsigned long long *)&c->deaths[(step + 1) % 3], (unsigned long long)b);
+  }
+  now = next = 0;
+}
+
+// Entries whose liquid count reached zero in the last generation (parity
+// zpar; gen0: it was generation 0): each leaves the list now or in the next
+// step, and becomes a tombstone. One that died at its own turn in that
+// generation is one already; one processed this step outlived its turn (it
+// goes next step); a sleeping one (only in generation 0) goes now unless a
+// capture by a later rank emptied it too.
+__device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int zpar, bool gen0, long long step,
+                                            unsigned *now, unsigned *next) {
+  const unsigned long long nz = ld_volatile(&d.ctrl->zn[zpar]);
+  for (unsigned long long i = (unsigned long long)t_b * kBlock + threadIdx.x; i < nz;
+       i += (unsigned long long)t_nb * kBlock) {
+    const int q = d.zlist[zpar][i];
+    if (isnan(d.key[cur][q])) continue;
+    const bool later = d.lstep[cur][q] == (int32_t)step || !gen0 || d.late[q] == (int32_t)step;
+    tombstone(d, cur, q, d.act[cur][q].cell);
+    if (later)
+      ++*next;
+    else
+      ++*now;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Claim: growth up to this step (generation 0) or self-construction
+// (generation >= 1), neighbour tests, atomicMin claims, the entry's liquid
+// count and next wake key.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind, long long lo, long long n, unsigned par,
+                            GenList list, GenList parents, long long step, double grown,
+                            unsigned long long *stat_tests, unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
+  EnvRec *act = d.act[cur];
+  int32_t *lstep = d.lstep[cur];
   unsigned long long tests = 0, tests64 = 0;
   // Claims need no order: warps or blocks take chunks of consecutive ranks
   // from a shared counter until none is left, so those that drew cheap
@@ -576,19 +819,22 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
     double gxd = 0, gyd = 0, gzd = 0;
     bool have_centre = false;
     uint32_t liq = 0;
+    const long long p = list.at(r);
     if (kind == 0) {
-      en = cur[r];
+      en = act[p];
       liq = liquid_neighbours(d.solid, g, en.cell);
-      if (grow) {
-        en.L += dv;  // Grain::grow (Grain.h:27): L + dt * vel, the product rounded once per step
-        cur[r].L = en.L;
-      }
+      // Grain::grow (Grain.h:27) for every step since the record was last
+      // grown: L + dt * vel, the product rounded once per step
+      en.L = replay_growth(d.dvh, en.L, (long long)lstep[p], step);
+      act[p].L = en.L;
+      lstep[p] = (int32_t)step;
+      if (r >= list.nw) d.pos[en.cell] = (int32_t)p;  // a nucleus of this step
     } else {
       // CellularAutomataManager_3D::capture_cell (:677-707) for the capture
       // recorded by the parent: decentred envelope from the parent's
       // (grown) envelope, same orientation.
       const uint32_t rec = d.child[r];
-      const EnvRec pe = prev[rec >> 5];
+      const EnvRec pe = act[parents.at((long long)(rec >> 5))];
       const int pnb = (int)(rec & 31u);
       int di, dj, dk, I, J, K;
       en.cell = pe.cell + nbr_delta(g, pnb, di, dj, dk);
@@ -610,7 +856,9 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
       en.dy = (float)(gyd - ccy);
       en.dz = (float)(gzd - ccz);
       have_centre = true;
-      cur[r] = en;
+      act[p] = en;
+      lstep[p] = (int32_t)step;
+      d.pos[en.cell] = (int32_t)p;
       d.gx[en.id] = gxd;
       d.gy[en.id] = gyd;
       d.gz[en.id] = gzd;
@@ -621,8 +869,15 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
     const int cell = en.cell, ori = en.ori, id = en.id;
     const double L = en.L;
     uint32_t con = 0;
+    // lower bound of |c'|_1 over the liquid neighbours it does not contain
+    float t_lb = INFINITY;
+    // no decrement reaches this entry during the claim phase: its count is
+    // the liquid neighbours it sees now
+    d.nliq[cur][p] = __popc(liq);
     // cell_is_captured is false for a zero half-diagonal (tested on the bits:
-    // an integer compare instead of one on the narrow FP64 pipe)
+    // an integer compare instead of one on the narrow FP64 pipe); such an
+    // entry is looked at again next step
+    if (liq && (__double_as_longlong(L) << 1) == 0) t_lb = -INFINITY;
     if (liq && (__double_as_longlong(L) << 1) != 0) {
       int I, J, K;
       cell_ijk(g, cell, I, J, K);
@@ -639,8 +894,9 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
         int di, dj, dk;
         nbr_offset(nb, di, dj, dk);
         ++tests;
-        int f = captured_f32(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg,
-                             L32);
+        float lower;
+        int f = captured_f32_lb(m32, (float)di * d.h32 - dxf, (float)dj * d.h32 - dyf, (float)dk * d.h32 - dzf, errg,
+                                L32, &lower);
         if (f < 0) {
           ++tests64;
           if (!have_centre) {
@@ -655,6 +911,7 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
           f = is_captured_f64(d.omat + 9 * ori, ccx - gxd, ccy - gyd, ccz - gzd, L) ? 1 : 0;
         }
         con |= (f ? 1u : 0u) << nb;
+        if (!f) t_lb = fminf(t_lb, lower);
       }
       const uint32_t mine = claim_word(par, (uint32_t)r);
       bits = con;
@@ -667,6 +924,9 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
         atomicOr(d.claimed + (nc >> 5), 1u << (nc & 31));
       }
     }
+    // growth is uniform: the entry can contain one of the neighbours left
+    // only once the run's cumulative growth reaches this key
+    d.key[cur][p] = t_lb == -INFINITY ? __double2float_rd(grown) : wake_key(t_lb, L, grown);
     d.liq[r] = liq;
     d.con[r] = con;
   }
@@ -676,16 +936,17 @@ __device__ void claim_phase(const PlainDevice &d, int kind, long long lo, long l
 }
 
 // ---------------------------------------------------------------------------
-// Resolve: captures, deactivation, child records, survivor compaction.
+// Resolve: captures, deactivation, child records, liquid counts.
 // ---------------------------------------------------------------------------
 // Mark of one rank: the captured neighbours (final claim is its own) and
 // whether it stays active, as captures | survives << 31.
-__device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r, unsigned par, const EnvRec *cur) {
+__device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r, unsigned par, const EnvRec *act,
+                                              const GenList &list) {
   const Grid &g = d.grid;
   const uint32_t lm = d.liq[r], cm = d.con[r];
   uint32_t cap = 0, surv = 0;
   if (lm) {
-    const int cell = cur[r].cell;
+    const int cell = act[list.at(r)].cell;
     const uint32_t mine = claim_word(par, (uint32_t)r);
     // a liquid neighbour this envelope does not contain and nobody claimed
     // keeps it active without a look at the cell field
@@ -713,12 +974,12 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
 // Marking pass for large generations: dynamic chunks of ranks, as in the
 // claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
-__device__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *cur) {
+__device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *act, GenList list) {
   RankSched sched(n, &d.ctrl->mark_next, &d.ctrl->error);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e))
-    for (long long r = b + first; r < e; r += stride) d.con[r] = mark_rank(d, r, par, cur);
+    for (long long r = b + first; r < e; r += stride) d.con[r] = mark_rank(d, r, par, act, list);
 }
 
 // Whether a generation of n ranks is marked inside the resolve pass (at most
@@ -728,16 +989,18 @@ __device__ __forceinline__ bool mark_in_resolve(long long n) { return n <= (long
 
 // Each block marks its contiguous chunk of ranks (the claim words are final
 // after the claim phase's barrier), then one look-back per block over the
-// chunk's marks gives new envelope ids (walk order), child records and the
-// survivors' places in the next active list. Marking reads only claim words,
-// the claimed bitmap and its own ranks' masks, none of which another block's
-// resolve writes, so no barrier separates the two passes.
-// base_next = survivors placed by this step's earlier generations; the last
-// block publishes the generation's capture count and the new survivor count,
-// which every block reads after the barrier.
-__device__ bool resolve_phase(const PlainDevice &d, long long n, long long step, unsigned par, const EnvRec *cur,
-                              EnvRec *next_act, long long base_next, unsigned long long *smem) {
+// chunk's marks gives new envelope ids (walk order) and child records; an
+// entry that does not survive its turn becomes a tombstone. Marking reads
+// only claim words, the claimed bitmap, its own ranks' masks and cells, none
+// of which another block's resolve writes, so no barrier separates the two
+// passes. Every captured cell turns solid for the next generation and takes
+// one off the liquid counts around it (zero list of parity zpar). The last
+// block publishes the generation's capture and survivor counts, which every
+// block reads after the barrier.
+__device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long long n, long long step, unsigned par,
+                              GenList list, int zpar, unsigned long long *smem, unsigned long long *stat_dec) {
   PlainCtrl *c = d.ctrl;
+  const EnvRec *act = d.act[cur];
   long long b, e;
   block_chunk(n, b, e);
   unsigned long long acc = 0;
@@ -745,7 +1008,7 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
     uint32_t word;
     if (marking) {
-      word = mark_rank(d, r, par, cur);
+      word = mark_rank(d, r, par, act, list);
       d.con[r] = word;  // read back below by the same thread
     } else {
       word = d.con[r];  // marked by mark_phase before the last barrier
@@ -756,6 +1019,9 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   block_exclusive_scan(acc, smem, &agg);
   const unsigned long long pre = block_prefix(d.scanB, agg, smem, c);
   if (pre == ~0ull) return false;
+  // the zero list after the next generation's starts empty (it was last
+  // read in this generation's claim phase)
+  if (t_b == 0 && threadIdx.x == 0) c->zn[zpar ^ 1] = 0ull;
   unsigned long long run = pre;
   for (long long r0 = b; r0 < e; r0 += kBlock) {
     const long long r = r0 + threadIdx.x;
@@ -763,18 +1029,20 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
     const uint32_t cap = word & 0x03ffffffu, surv = word >> 31;
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
-    if (r < e && (cap | surv)) {
-      const unsigned long long off = run + ex;
-      if (surv) next_act[base_next + (long long)(off & 0xffffffffull)] = cur[r];
-      long long slot = (long long)(off >> 32);  // rank of the first child in the next generation
+    if (r < e) {
+      const long long p = list.at(r);
+      const int cell = act[p].cell;
+      if (!surv) tombstone(d, cur, p, cell);  // deactivated at its turn
+      long long slot = (long long)((run + ex) >> 32);  // rank of the first child in the next generation
       uint32_t bits = cap;
-      const int cell = bits ? cur[r].cell : 0;
       while (bits) {
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
         d.child[slot++] = ((uint32_t)r << 5) | (uint32_t)nb;  // parent's rank in this generation
         int di, dj, dk;
-        set_solid(d.solid, cell + nbr_delta(d.grid, nb, di, dj, dk));  // solid for the next generation
+        const int nc = cell + nbr_delta(d.grid, nb, di, dj, dk);
+        set_solid(d.solid, nc);  // solid for the next generation
+        neighbour_solid(d, cur, nc, p, step, zpar, 0.0, false, stat_dec);
       }
     }
     run += tot;
@@ -782,7 +1050,7 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
   if (t_b == t_nb - 1 && threadIdx.x == 0) {
     const unsigned long long total = pre + agg;
     c->gen_n = (long long)(total >> 32);
-    c->n_active_next[step & 1] = base_next + (long long)(total & 0xffffffffull);
+    c->gen_surv = (long long)(total & 0xffffffffull);
   }
   return true;
 }
@@ -792,23 +1060,27 @@ __device__ bool resolve_phase(const PlainDevice &d, long long n, long long step,
 __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned long long *smem) {
   // block 0's phase clock and step counters (its thread 0 only), added to
   // the control block once per launch
-  enum { kNuc, kClaim, kClaim0, kResolve, kClaimMax, kResolveMax, kGens, kGrown, kProc, kCaps, kNucs, kClk };
+  enum { kNuc, kClaim, kClaim0, kResolve, kClaimMax, kResolveMax, kGens, kGrown, kProc, kCaps, kNucs, kScanned, kZero,
+         kClk };
   __shared__ unsigned long long s_clk[kClk];
   // this block's tile of sites when they are tiled (cell -1: removed, or no site)
   __shared__ int s_cell[kBlock];
   __shared__ double s_dtc[kBlock];
   PlainCtrl *c = d.ctrl;
-  unsigned long long tests = 0, tests64 = 0, live = 0;
+  unsigned long long tests = 0, tests64 = 0, live = 0, dec = 0, moved = 0;
   // per-step state, identical in every thread (read once, then advanced
   // locally from the counts that the last block of a phase publishes)
   long long step = ld_volatile(&c->step);
   double time = ld_volatile(&c->time), dt = ld_volatile(&c->dt);
-  long long n_act = ld_volatile(&c->n_active);
+  long long n_act = ld_volatile(&c->n_active), a_len = ld_volatile(&c->a_len);
   long long n_orient = ld_volatile(&c->n_orient), grain = ld_volatile(&c->next_grain);
   long long liquid = ld_volatile(&c->liquid);
+  unsigned long long compactions = ld_volatile(&c->compactions);
+  double grown = ld_volatile(&c->grown);
   int cur = ld_volatile(&c->cur_list);
   bool done = ld_volatile(&c->done) != 0;
   bool ok = true;
+  unsigned gone_now = 0, gone_next = 0;  // list departures this thread decided, added once per step
   if (site_tiles(d)) {
     const long long i = (long long)t_b * kBlock + threadIdx.x;
     const bool on = i < d.nsites && d.site_live[i] != 0;
@@ -825,35 +1097,66 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   unsigned long long claim_busy = 0, resolve_busy = 0;
   const double t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
   while (!done && time < t_end && step < step_limit) {
+    // the list is compacted once it is mostly tombstones
+    if (a_len > 2 * n_act + 4096) {
+      if (!(ok = compact_phase(d, cur, a_len, (unsigned)(compactions & 1ull), smem, &moved))) break;
+      if (!(ok = grid_barrier(c))) break;
+      cur ^= 1;
+      a_len = ld_volatile(&c->compact_len);
+      ++compactions;
+    }
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
-    EnvRec *act = cur ? d.act1 : d.act0;
-    EnvRec *next_act = cur ? d.act0 : d.act1;
-    if (!(ok = nucleation_phase(d, time, step, n_act, n_orient, grain, act, s_cell, s_dtc, smem, &live))) break;
+    double vel, da, dn;
+    step_rates(d, time, vel, da, dn);
+    // growth of every envelope this step (when there is one); the wake scan
+    // compares the keys with the cumulative growth
+    const double dv = da * vel;
+    const double grown_s = grown + dv;
+    const bool all = step % kWakeAll == 0;
+    if (t_b == 0 && threadIdx.x == 0) {
+      d.dvh[step & (kDvRing - 1)] = dv;
+      c->zn[0] = 0ull;  // generation 0's zero list (last read in the previous step)
+    }
+    if (!(ok = nucleation_phase(d, cur, time, step, a_len, n_orient, grain, grown_s, all, s_cell, s_dtc, smem, &live,
+                                &dec, &gone_now)))
+      break;
+    if (!(ok = wake_scan(d, cur, a_len, step, grown_s, all, smem))) break;
+    flush_departures(c, step, gone_now, gone_next);
     if (!(ok = grid_barrier(c))) break;
     if (timer) {
       t_now = now_ns();
       s_clk[kNuc] += t_now - t_mark;
       t_mark = t_now;
+      // the slot of step + 2 (last read at the end of step - 1)
+      c->deaths[(step + 2) % 3] = 0;
     }
     const long long nA = ld_volatile(&c->n_active_nuc[step & 1]);
-    const double vel = ld_volatile(&c->vel[step & 1]);
-    dt = nA > 0 ? ld_volatile(&c->dt_active[step & 1]) : ld_volatile(&c->dt_none[step & 1]);
-    const double dv = dt * vel;  // every envelope's growth this step
-    const long long nucs = nA - n_act;  // nuclei of this step
+    const long long nucs = nA - a_len;  // nuclei of this step
+    const long long nw = ld_volatile(&c->n_woken[step & 1]);
+    dt = n_act + nucs > 0 ? da : dn;
+    grown = grown_s;
     n_orient += nucs;
     grain += nucs;
     liquid -= nucs;
-    if (timer) s_clk[kNucs] += (unsigned long long)nucs;
+    if (timer) {
+      s_clk[kNucs] += (unsigned long long)nucs;
+      s_clk[kScanned] += (unsigned long long)a_len;
+    }
 
     // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
-    long long n = nA, lo = 0, processed = 0, n_next = 0;
+    long long n = nw + nucs, lo = 0, processed = 0, gen_end = nA, caps_all = 0, died = 0;
     int kind = 0;
     unsigned gen = 0;
-    EnvRec *list = act, *parents = nullptr;  // records of this generation / of its parents
+    GenList list{d.wlist, nw, a_len}, parents{nullptr, 0, 0};  // this generation / its parents
+    if (timer) s_clk[kGrown] += (unsigned long long)n;
     while (n > 0) {
       processed += n;
       unsigned long long t_work = threadIdx.x == 0 ? now_ns() : 0ull;
-      claim_phase(d, kind, lo, n, gen & 1u, gen == 0, dv, list, parents, &tests, &tests64);
+      claim_phase(d, cur, kind, lo, n, gen & 1u, list, parents, step, grown, &tests, &tests64);
+      if (gen > 0) {
+        zero_decisions(d, cur, (int)((gen - 1) & 1u), gen == 1, step, &gone_now, &gone_next);
+        flush_departures(c, step, gone_now, gone_next);
+      }
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
@@ -865,6 +1168,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         t_now = now_ns();
         s_clk[kClaim] += t_now - t_mark;
         if (gen == 0) s_clk[kClaim0] += t_now - t_mark;
+        if (gen > 0) s_clk[kZero] += ld_volatile(&c->zn[(gen - 1) & 1u]);  // reset in this generation's resolve
         t_mark = t_now;
         if (d.phase_detail) {
           s_clk[kClaimMax] += ld_volatile(&c->phase_max_scratch[0]);
@@ -875,14 +1179,14 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       t_work = threadIdx.x == 0 ? now_ns() : 0ull;
       unsigned long long w_mark = 0;  // busy time of a separate marking pass (thread 0)
       if (!mark_in_resolve(n)) {
-        mark_phase(d, n, gen & 1u, list);
+        mark_phase(d, n, gen & 1u, d.act[cur], list);
         __syncthreads();
         if (threadIdx.x == 0) w_mark = now_ns() - t_work;
         if (!(ok = grid_barrier(c))) break;
         if (timer) c->mark_next = 0ull;  // the next marking pass is two barriers away
         t_work = threadIdx.x == 0 ? now_ns() : 0ull;
       }
-      if (!(ok = resolve_phase(d, n, step, gen & 1u, list, next_act, n_next, smem))) break;
+      if (!(ok = resolve_phase(d, cur, n, step, gen & 1u, list, (int)(gen & 1u), smem, &dec))) break;
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work + w_mark;
         resolve_busy += w;
@@ -899,28 +1203,30 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         }
       }
       const long long caps = ld_volatile(&c->gen_n);  // envelopes of the next generation
-      n_next = ld_volatile(&c->n_active_next[step & 1]);
+      died += n - ld_volatile(&c->gen_surv);          // deactivated at their turn
       lo = grain;  // their ids follow on
       grain += caps;
       liquid -= caps;
+      caps_all += caps;
       if (timer) s_clk[kCaps] += (unsigned long long)caps;
       n = caps;
       kind = 1;
       ++gen;
       parents = list;
-      list = (gen & 1u) ? d.gen1 : d.gen0;
+      list = GenList{nullptr, 0, gen_end};  // appended to the list after the previous generation
+      gen_end += caps;
     }
     if (!ok) break;
     // step end (CellularAutomataManager_3D.cpp:653-659): every block advances
-    // the same locals, so no further barrier is needed
-    n_act = n_next;
-    cur ^= 1;
+    // the same locals from counts final at the last barrier, so no further
+    // barrier is needed
+    n_act = n_act + nucs + caps_all - died - (long long)ld_volatile(&c->deaths[step % 3]);
+    a_len = gen_end;
     time = time + dt;
     ++step;
     done = liquid == 0;
     if (timer) {
       s_clk[kGens] += gen;
-      s_clk[kGrown] += (unsigned long long)nA;
       s_clk[kProc] += (unsigned long long)processed;
     }
   }
@@ -930,11 +1236,16 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     c->time = time;
     c->dt = dt;
     c->n_active = n_act;
+    c->a_len = a_len;
+    c->grown = grown;
+    c->compactions = compactions;
     c->n_orient = n_orient;
     c->next_grain = grain;
     c->liquid = liquid;
     c->cur_list = cur;
     c->done = done ? 1 : 0;
+    c->keys_scanned += s_clk[kScanned];
+    c->zero_events += s_clk[kZero];
     c->ns_nucleation += s_clk[kNuc];
     c->ns_claim += s_clk[kClaim];
     c->ns_claim_gen0 += s_clk[kClaim0];
@@ -954,6 +1265,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     tests += __shfl_down_sync(0xffffffffu, tests, o);
     tests64 += __shfl_down_sync(0xffffffffu, tests64, o);
     live += __shfl_down_sync(0xffffffffu, live, o);
+    dec += __shfl_down_sync(0xffffffffu, dec, o);
+    moved += __shfl_down_sync(0xffffffffu, moved, o);
   }
   if ((threadIdx.x & 31) == 0) {
     if (threadIdx.x == 0) {
@@ -963,6 +1276,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);
     if (live) atomicAdd(&c->sites_scanned, live);
+    if (dec) atomicAdd(&c->decrements, dec);
+    if (moved) atomicAdd(&c->compacted, moved);
   }
 }
 
@@ -978,8 +1293,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
 
 // One bitmap word (32 cells) of the initial field: cells past the grid count
 // as solid.
-__device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *solid, uint32_t *claimed, const Grid &g,
-                                                long long ncells, long long w) {
+__device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *solid, uint32_t *claimed, int32_t *pos,
+                                                const Grid &g, long long ncells, long long w) {
   uint32_t bits = 0;
   for (int b = 0; b < 32; ++b) {
     const long long i = w * 32 + b;
@@ -989,6 +1304,7 @@ __device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *soli
       cell_ijk(g, i, I, J, K);
       ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
       orient[i] = ghost ? 0u : kLiquid;
+      pos[i] = -1;
     }
     bits |= (ghost ? 1u : 0u) << b;
   }
@@ -996,10 +1312,11 @@ __device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *soli
   claimed[w] = 0u;
 }
 
-__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, Grid g, long long ncells) {
+__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, int32_t *pos, Grid g,
+                                  long long ncells) {
   const long long nwords = solid_words(ncells);
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (long long)gridDim.x * blockDim.x)
-    init_field_word(orient, solid, claimed, g, ncells, w);
+    init_field_word(orient, solid, claimed, pos, g, ncells, w);
 }
 
 // ---------------------------------------------------------------------------
@@ -1075,9 +1392,14 @@ __global__ void batch_reset_kernel(const PlainDevice *insts, int ninst, unsigned
     d.scanA[i] = 0ull;
     d.scanA[kStatusWords + i] = 0ull;
     d.scanB[i] = 0ull;
+    d.scanC[i] = 0ull;
+    d.scanC[kStatusWords + i] = 0ull;
+    d.scanD[i] = 0ull;
+    d.scanD[kStatusWords + i] = 0ull;
   }
   const long long nwords = solid_words(d.ncells);
-  for (long long w = tid; w < nwords; w += stride) init_field_word(d.orient, d.solid, d.claimed, d.grid, d.ncells, w);
+  for (long long w = tid; w < nwords; w += stride)
+    init_field_word(d.orient, d.solid, d.claimed, d.pos, d.grid, d.ncells, w);
 }
 
 // out[r] = realm r's control block.
@@ -1156,6 +1478,10 @@ __global__ void noalloc_setup_kernel(PlainDevice d, long long liquid, unsigned l
     d.scanA[i] = 0ull;
     d.scanA[kStatusWords + i] = 0ull;
     d.scanB[i] = 0ull;
+    d.scanC[i] = 0ull;
+    d.scanC[kStatusWords + i] = 0ull;
+    d.scanD[i] = 0ull;
+    d.scanD[kStatusWords + i] = 0ull;
   }
 }
 
@@ -1180,8 +1506,8 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
-  size_t ctrl, check, live, omat32, scanA, gx, gy, gz, gori, gcell, act0, act1, gen0, gen1, liq, con, child, solid,
-      claimed, scanB, total;
+  size_t ctrl, check, live, omat32, scanA, gx, gy, gz, gori, gcell, act[2], key[2], lstep[2], nliq[2], late, pos, wlist,
+      zlist[2], dvh, liq, con, child, solid, claimed, scanB, scanC, scanD, total;
   // n interior cells, s sites, `cells` ghost-inclusive cells; the caller
   // bounds all three (see kNoAllocMaxCells) so that no size below wraps
   NoAllocLayout(long long n, long long s, long long cells) {
@@ -1201,16 +1527,25 @@ struct NoAllocLayout {
     gz = take((size_t)n * 8);
     gori = take((size_t)n * 4);
     gcell = take((size_t)n * 4);
-    act0 = take((size_t)n * sizeof(EnvRec));
-    act1 = take((size_t)n * sizeof(EnvRec));
-    gen0 = take((size_t)n * sizeof(EnvRec));
-    gen1 = take((size_t)n * sizeof(EnvRec));
+    for (int b = 0; b < 2; ++b) {
+      act[b] = take((size_t)n * sizeof(EnvRec));
+      key[b] = take((size_t)n * 4);
+      lstep[b] = take((size_t)n * 4);
+      nliq[b] = take((size_t)n * 4);
+      zlist[b] = take((size_t)n * 4);
+    }
+    late = take((size_t)n * 4);
+    wlist = take((size_t)n * 4);
+    pos = take((size_t)cells * 4);
+    dvh = take((size_t)kDvRing * 8);
     liq = take((size_t)n * 4);
     con = take((size_t)n * 4);
     child = take((size_t)n * 4);
     solid = take((size_t)solid_words(cells) * 4);
     claimed = take((size_t)solid_words(cells) * 4);
     scanB = take((size_t)kStatusWords * 8);
+    scanC = take((size_t)2 * kStatusWords * 8);
+    scanD = take((size_t)2 * kStatusWords * 8);
     total = o;
   }
 };
@@ -1331,16 +1666,25 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.gz = (double *)(base + lay.gz);
   d.gori = (int32_t *)(base + lay.gori);
   d.gcell = (int32_t *)(base + lay.gcell);
-  d.act0 = (EnvRec *)(base + lay.act0);
-  d.act1 = (EnvRec *)(base + lay.act1);
-  d.gen0 = (EnvRec *)(base + lay.gen0);
-  d.gen1 = (EnvRec *)(base + lay.gen1);
+  for (int b = 0; b < 2; ++b) {
+    d.act[b] = (EnvRec *)(base + lay.act[b]);
+    d.key[b] = (float *)(base + lay.key[b]);
+    d.lstep[b] = (int32_t *)(base + lay.lstep[b]);
+    d.nliq[b] = (int32_t *)(base + lay.nliq[b]);
+    d.zlist[b] = (int32_t *)(base + lay.zlist[b]);
+  }
+  d.late = (int32_t *)(base + lay.late);
+  d.wlist = (int32_t *)(base + lay.wlist);
+  d.pos = (int32_t *)(base + lay.pos);
+  d.dvh = (double *)(base + lay.dvh);
   d.liq = (uint32_t *)(base + lay.liq);
   d.con = (uint32_t *)(base + lay.con);
   d.child = (uint32_t *)(base + lay.child);
   d.solid = (uint32_t *)(base + lay.solid);
   d.claimed = (uint32_t *)(base + lay.claimed);
   d.scanB = (unsigned long long *)(base + lay.scanB);
+  d.scanC = (unsigned long long *)(base + lay.scanC);
+  d.scanD = (unsigned long long *)(base + lay.scanD);
   // everything that must start at zero is cleared here: the array keeps the
   // previous call's contents
   unsigned long long *check = (unsigned long long *)(base + lay.check);
@@ -1428,7 +1772,7 @@ cudaError_t plain_barrier_selftest(int blocks, int parties, long long wait_ns, i
 }
 
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s) {
-  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.solid, d.claimed, d.grid, d.ncells);
+  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.solid, d.claimed, d.pos, d.grid, d.ncells);
   return cudaGetLastError();
 }
 

@@ -12,13 +12,25 @@
 //   omat/omat32 per orientation: local->global matrix, 9 x f64 and 9 x f32
 //   g*          envelope table by id (capacity = interior cells), written once per
 //               envelope: centre f64 x3, orientation i32, cell i32
-//   act[2]      active list as 32-byte records (ascending id), double-buffered per step
-//   gen[2]      records of the envelopes created in the generation being walked,
-//               double-buffered by generation parity
+//   act[2]      the envelope list: 32-byte records in walk order, appended to by
+//               nucleation and captures, dead entries left in place (tombstones)
+//               until a compaction into the other buffer; per entry beside it:
+//               key[2]   f32 wake key (cumulative growth at which the entry may
+//                        contain a liquid neighbour; NaN = dead)
+//               lstep[2] i32 step up to which the record's half-diagonal is grown
+//               nliq[2]  i32 liquid neighbours now
+//   late        i32 per entry: step of the last capture next to it by a later rank
+//   pos         i32 per ghost-inclusive cell: list position of the live envelope
+//               on the cell, -1 for none
+//   wlist       i32 per entry: positions woken this step, in walk order
+//   zlist[2]    i32 per entry: entries whose liquid count reached zero in a
+//               generation, by generation parity
+//   dvh         f64 ring of the growth increment of each step
 //   liq/con     per-rank neighbour masks of the generation being processed
 //   child       per new envelope: parent's rank in its generation << 5 | neighbour index
-//   scanA/scanB decoupled look-back status words, one per block: nucleation
-//               (two sets, by step parity) / capture
+//   scanA..D    decoupled look-back status words, one per block: nucleation and
+//               wake scan (two sets each, by step parity), capture, compaction
+//               (two sets, by compaction parity)
 //   ctrl        control block: counters, time, barrier words, error flag
 #pragma once
 
@@ -34,6 +46,10 @@ namespace amca {
 constexpr long long kStatusWords = 4096;
 // Child records pack an envelope id into 27 bits.
 constexpr long long kMaxCells = 1ll << 27;
+// Steps of the growth-increment ring; every live entry is woken (its record
+// brought up to date) at least every kWakeAll steps, well inside the ring.
+constexpr long long kDvRing = 4096;
+constexpr long long kWakeAll = 2048;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values
@@ -43,12 +59,18 @@ struct PlainCtrl {
   unsigned bar_count;
   unsigned bar_gen;
   int error;        // 0, or where a bounded wait ran out (see kErr*)
-  int cur_list;     // which act[] holds the current active list
+  int cur_list;     // which act[] holds the envelope list
   long long n_orient;
   long long next_grain;
   long long n_active;          // active envelopes between launches
-  long long n_active_next[2];  // survivors of the step, by step parity
-  long long n_active_nuc[2];   // active envelopes after the step's nucleation, by step parity
+  long long a_len;             // entries of the envelope list (live and dead) between launches
+  long long n_active_nuc[2];   // list length after the step's nucleation, by step parity
+  long long n_woken[2];        // entries of the list the wake scan picked, by step parity
+  long long compact_len;       // live entries after the last compaction
+  long long deaths[3];         // entries leaving the active list in step s, in slot s % 3
+  long long gen_surv;          // survivors of the last resolved generation
+  unsigned long long zn[2];    // zero-count events of a generation, by generation parity
+  double grown;                // growth of the envelopes since the start of the run (sum of dv)
   long long liquid;
   long long gen_n;  // captures of the last resolved generation
   long long step;
@@ -66,8 +88,13 @@ struct PlainCtrl {
   // work counters behind the algorithmic-bytes figure
   unsigned long long sites_scanned;    // live sites read by nucleation, summed over steps
   unsigned long long nucleations;      // envelopes created by nucleation
-  unsigned long long active_grown;     // generation-0 envelopes (grown), summed over steps
-  unsigned long long grains_processed; // envelopes of every generation, summed
+  unsigned long long active_grown;     // generation-0 entries processed (woken and nuclei), summed over steps
+  unsigned long long grains_processed; // entries processed in every generation, summed
+  unsigned long long keys_scanned;     // list positions the wake scan read, summed over steps
+  unsigned long long decrements;       // liquid-count decrements (pos reads that found an entry)
+  unsigned long long zero_events;      // liquid counts that reached zero in a capture generation
+  unsigned long long compactions;      // compactions of the envelope list
+  unsigned long long compacted;        // entries moved by them
   // wall time of each phase as block 0 sees it (phase start to barrier exit), ns
   unsigned long long ns_nucleation, ns_claim, ns_resolve, ns_step_end;
   unsigned long long ns_claim_gen0;                    // part of ns_claim spent on generation 0
@@ -121,11 +148,18 @@ struct PlainDevice {
   double *gx, *gy, *gz;
   int32_t *gori, *gcell;
   int64_t gcap;
-  EnvRec *act0, *act1;
-  EnvRec *gen0, *gen1;
+  EnvRec *act[2];
+  float *key[2];
+  int32_t *lstep[2];
+  int32_t *nliq[2];
+  int32_t *late;
+  int32_t *pos;
+  int32_t *wlist;
+  int32_t *zlist[2];
+  double *dvh;
   uint32_t *liq, *con;
   uint32_t *child;
-  unsigned long long *scanA, *scanB;
+  unsigned long long *scanA, *scanB, *scanC, *scanD;
   PlainCtrl *ctrl;
 };
 
@@ -156,7 +190,7 @@ cudaError_t plain_barrier_selftest(int blocks, int parties, long long wait_ns, i
 
 // Fill the orientation field: -1 interior, 0 on the ghost layer
 // (CellularAutomataManager.cpp:316-326, CellularAutomataManager_3D.cpp:736-833),
-// and the solid bitmap to match.
+// the solid bitmap to match, and the cell -> list position map with -1.
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s);
 
 // Words of the solid bitmap for `ncells` cells.

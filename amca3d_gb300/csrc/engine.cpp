@@ -202,10 +202,17 @@ struct amca_t {
       d.gz = a.take<double>(d.gcap);
       d.gori = a.take<int32_t>(d.gcap);
       d.gcell = a.take<int32_t>(d.gcap);
-      d.act0 = a.take<EnvRec>(d.gcap);
-      d.act1 = a.take<EnvRec>(d.gcap);
-      d.gen0 = a.take<EnvRec>(d.gcap);
-      d.gen1 = a.take<EnvRec>(d.gcap);
+      for (int b = 0; b < 2; ++b) {
+        d.act[b] = a.take<EnvRec>(d.gcap);
+        d.key[b] = a.take<float>(d.gcap);
+        d.lstep[b] = a.take<int32_t>(d.gcap);
+        d.nliq[b] = a.take<int32_t>(d.gcap);
+        d.zlist[b] = a.take<int32_t>(d.gcap);
+      }
+      d.late = a.take<int32_t>(d.gcap);
+      d.wlist = a.take<int32_t>(d.gcap);
+      d.pos = a.take<int32_t>(d.ncells);
+      d.dvh = a.take<double>(kDvRing);
       d.liq = a.take<uint32_t>(d.gcap);
       d.con = a.take<uint32_t>(d.gcap);
       d.child = a.take<uint32_t>(d.gcap);
@@ -213,6 +220,8 @@ struct amca_t {
       d.claimed = a.take<uint32_t>(solid_words(d.ncells));
       d.scanA = a.take<unsigned long long>(ntA);
       d.scanB = a.take<unsigned long long>(ntB);
+      d.scanC = a.take<unsigned long long>(ntA);
+      d.scanD = a.take<unsigned long long>(ntA);
       d.ctrl = a.take<PlainCtrl>(1);
     };
     Arena sizing;
@@ -269,6 +278,8 @@ struct amca_t {
     if (d.nsites) CK(cudaMemsetAsync(d.site_live, 1, d.nsites, stream));
     CK(cudaMemsetAsync(d.scanA, 0, ntA_ * sizeof(unsigned long long), stream));
     CK(cudaMemsetAsync(d.scanB, 0, ntB_ * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(d.scanC, 0, ntA_ * sizeof(unsigned long long), stream));
+    CK(cudaMemsetAsync(d.scanD, 0, ntA_ * sizeof(unsigned long long), stream));
     PlainCtrl c0{};
     c0.liquid = (long long)cfg.nx * cfg.ny * cfg.nz;
     h2d(d.ctrl, &c0, sizeof c0);
@@ -287,14 +298,18 @@ struct amca_t {
   }
 
   double algorithmic_bytes() const {
-    // per step: 12 B per live site (cell id + dTc), 48 B per nucleation
-    // (new envelope 40 B + orientation id 4 B + cell write 4 B), 16 B per grown
-    // envelope (half-diagonal read + write), 216 B per envelope and
-    // generation (40 B envelope, 26 x 4 B neighbour states, 72 B matrix),
-    // 44 B per capture (cell write + 40 B envelope), 8 B per list entry.
+    // per run: 12 B per live site (cell id + dTc), 48 B per nucleation (new
+    // envelope 40 B + orientation id 4 B + cell write 4 B), 4 B per wake key
+    // scanned, 24 B per generation-0 entry (woken list write + read,
+    // half-diagonal write, grow step read + write), 228 B per entry and
+    // generation processed (40 B envelope, 26 x 4 B neighbour states, 72 B
+    // matrix, liquid count + key + cell map), 148 B per capture (cell write,
+    // 40 B envelope, 26 x 4 B of the cell map around it), 8 B per liquid-count
+    // decrement, 48 B per entry moved by a compaction.
     const double S = (double)ctrl.sites_scanned, N = (double)ctrl.nucleations, A = (double)ctrl.active_grown;
-    const double G = (double)ctrl.grains_processed, C = (double)ctrl.captures;
-    return 12 * S + 48 * N + 16 * A + 216 * G + 44 * C + 8 * (A + C);
+    const double G = (double)ctrl.grains_processed, C = (double)ctrl.captures, K = (double)ctrl.keys_scanned;
+    const double D = (double)ctrl.decrements, M = (double)ctrl.compacted;
+    return 12 * S + 48 * N + 4 * K + 24 * A + 228 * G + 148 * C + 8 * D + 48 * M;
   }
 
   bool finished() const { return ctrl.done || !(ctrl.time < cfg.final_time); }

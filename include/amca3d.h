@@ -315,7 +315,7 @@ typedef struct {
   int64_t active;        /* active envelopes */
   int64_t sites;         /* distinct nucleation sites */
   int64_t cells;         /* interior cells */
-  int64_t tests;         /* octahedron containment tests evaluated */
+  int64_t tests;         /* octahedron containment tests evaluated (by the envelopes woken or created) */
   int64_t tests_fp64;    /* ... of which needed the exact FP64 evaluation */
   int64_t generations;   /* capture generations processed */
   int32_t done;          /* 1 when no liquid cell is left */
@@ -326,7 +326,7 @@ typedef struct {
   int64_t sites_scanned;    /* live nucleation sites read */
   int64_t nucleations;      /* envelopes created by nucleation */
   int64_t captures;         /* envelopes created by capture */
-  int64_t active_grown;     /* generation-0 (grown) envelopes */
+  int64_t active_grown;     /* generation-0 entries processed: woken envelopes and nuclei */
   int64_t grains_processed; /* envelopes processed over all generations */
   double algorithmic_bytes; /* HBM bytes the step must move by the counting rule of the design notes */
   int64_t h2d_bytes;        /* host->device bytes copied by this handle */
