@@ -485,17 +485,14 @@ struct GenList {
   __device__ __forceinline__ long long at(long long r) const { return r < nw ? (long long)w[r] : base + (r - nw); }
 };
 
-// Cell `cell` has just turned solid: one liquid neighbour fewer for every
-// entry around it. A decrement by a capture of a later rank (position `pc`
-// beyond the entry's) is recorded in late[]; a count reaching zero goes to
-// the zero list of this generation (parity zpar). Nucleation passes pc = -1
-// and no list: it handles a zero itself (returned as the count of entries
-// gone at their turn).
-__device__ __noinline__ unsigned neighbour_solid(const PlainDevice &d, int cur, int cell, long long pc, long long step,
-                                                 int zpar, double grown, bool all, unsigned long long *stat_dec) {
+// A nucleus turned `cell` solid before the walk: one liquid neighbour fewer
+// for every entry around it, and a sleeping entry left without one is
+// deactivated at its turn (a woken one decides at its turn itself). Returns
+// those entries.
+__device__ __noinline__ unsigned nucleus_neighbours(const PlainDevice &d, int cur, int cell, double grown, bool all,
+                                                    unsigned long long *stat_dec) {
   const Grid &g = d.grid;
   unsigned gone = 0;
-  int32_t *nliq = d.nliq[cur];
 #pragma unroll 1
   for (int nb = 0; nb < 26; ++nb) {
     int di, dj, dk;
@@ -503,20 +500,38 @@ __device__ __noinline__ unsigned neighbour_solid(const PlainDevice &d, int cur, 
     const int q = d.pos[m];
     if (q < 0) continue;
     ++*stat_dec;
-    if (pc > q) d.late[q] = (int32_t)step;
-    const int old = atomicSub(nliq + q, 1);
-    if (old != 1) continue;
-    if (zpar >= 0) {
-      const unsigned long long i = atomicAdd(&d.ctrl->zn[zpar], 1ull);
-      d.zlist[zpar][i] = q;
-    } else if (!woken(d.key[cur][q], grown, all)) {
-      // nucleation precedes the walk: a sleeping entry left without a liquid
-      // neighbour is deactivated at its turn (a woken one decides itself)
+    if (atomicSub(d.nliq[cur] + q, 1) == 1 && !woken(d.key[cur][q], grown, all)) {
       tombstone(d, cur, q, m);
       ++gone;
     }
   }
   return gone;
+}
+
+// Block buffers of the resolve phase: the captured cells of a tile of ranks
+// (with their capturer's position), and the zero-count events.
+constexpr int kCapBuf = 512;
+constexpr int kZeroBuf = 512;
+
+// A capture by the entry at position pc turned cell m's neighbour solid: the
+// entry on m (if any) has one liquid neighbour fewer. A decrement by a later
+// rank (pc beyond the entry) is recorded in late[]; a count reaching zero
+// goes to the block's zero buffer, or to the generation's zero list (parity
+// zpar) once the buffer is full.
+__device__ __forceinline__ void lose_neighbour(const PlainDevice &d, int cur, int m, long long pc, long long step,
+                                               int zpar, int *s_zero, unsigned *s_nz, unsigned long long *stat_dec) {
+  const int q = d.pos[m];
+  if (q < 0) return;
+  ++*stat_dec;
+  if (pc > q) d.late[q] = (int32_t)step;
+  if (atomicSub(d.nliq[cur] + q, 1) != 1) return;
+  const unsigned k = atomicAdd(s_nz, 1u);
+  if (k < (unsigned)kZeroBuf) {
+    s_zero[k] = q;
+  } else {
+    const unsigned long long i = atomicAdd(&d.ctrl->zn[zpar], 1ull);
+    d.zlist[zpar][i] = q;
+  }
 }
 
 // Nucleus number r (in site order) of this step on `cell`: orientation,
@@ -546,7 +561,7 @@ __device__ __forceinline__ unsigned place_nucleus(const PlainDevice &d, int cur,
   en.id = (int32_t)gid;
   d.act[cur][base_pos + r] = en;
   d.lstep[cur][base_pos + r] = (int32_t)(step - 1);
-  return neighbour_solid(d, cur, cell, -1, step, -1, grown, all, stat_dec);
+  return nucleus_neighbours(d, cur, cell, grown, all, stat_dec);
 }
 
 // Sites are held as tiles of kBlock, one per block, when they fit: tile t =
@@ -691,31 +706,52 @@ __device__ __forceinline__ unsigned long long warp_offset(unsigned cnt, unsigned
 }
 
 // The entries among positions [0, n) that this step processes, in walk
-// order, into wlist; the count goes to n_woken[step & 1].
+// order, into wlist; the count goes to n_woken[step & 1]. Keys are read as
+// float4, 128 positions per warp and iteration (the key arrays are padded to
+// a whole number of these tiles); the team takes contiguous runs of tiles,
+// each warp a contiguous run of its block's.
+__device__ __forceinline__ unsigned woken4(const float4 v, long long p0, long long n, double grown, bool all) {
+  return (p0 < n && woken(v.x, grown, all) ? 1u : 0u) | (p0 + 1 < n && woken(v.y, grown, all) ? 2u : 0u) |
+         (p0 + 2 < n && woken(v.z, grown, all) ? 4u : 0u) | (p0 + 3 < n && woken(v.w, grown, all) ? 8u : 0u);
+}
 __device__ __noinline__ bool wake_scan(const PlainDevice &d, int cur, long long n, long long step, double grown, bool all,
-                          unsigned long long *smem) {
+                                       unsigned long long *smem) {
   PlainCtrl *c = d.ctrl;
   // the next step's words start cleared (last read in the previous step)
   if (threadIdx.x == 0) d.scanC[((step + 1) & 1) * kStatusWords + t_b] = 0ull;
-  const float *key = d.key[cur];
-  const WarpPiece wp(n);
+  const float4 *k4 = (const float4 *)d.key[cur];
+  const long long ntiles = (n + kKeyTile - 1) / kKeyTile;
+  long long tb, te;
+  block_chunk(ntiles, tb, te);
+  const long long per = ((te - tb) + kWarps - 1) / kWarps;
+  const long long wb = tb + (threadIdx.x >> 5) * per < te ? tb + (threadIdx.x >> 5) * per : te;
+  const long long we = wb + per < te ? wb + per : te;
   const int lane = threadIdx.x & 31;
   unsigned cnt = 0;
-  for (long long p0 = wp.b; p0 < wp.e; p0 += 32) {
-    const long long p = p0 + lane;
-    cnt += __popc(__ballot_sync(0xffffffffu, p < wp.e && woken(key[p], grown, all)));
+#pragma unroll 4
+  for (long long t = wb; t < we; ++t) {
+    const long long p0 = t * kKeyTile + 4 * lane;
+    cnt += __popc(woken4(k4[t * (kKeyTile / 4) + lane], p0, n, grown, all));
   }
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
   unsigned long long total = 0;
   unsigned long long off = warp_offset(cnt, d.scanC + (step & 1) * kStatusWords, smem, &total, c);
   if (off == ~0ull) return false;
   // a key read again here may have turned dead since (a nucleus next to a
   // sleeping entry), which the first pass counted as not woken all the same
-  for (long long p0 = wp.b; p0 < wp.e; p0 += 32) {
-    const long long p = p0 + lane;
-    const bool w = p < wp.e && woken(key[p], grown, all);
-    const unsigned bal = __ballot_sync(0xffffffffu, w);
-    if (w) d.wlist[off + __popc(bal & ((1u << lane) - 1u))] = (int32_t)p;
-    off += __popc(bal);
+#pragma unroll 2
+  for (long long t = wb; t < we; ++t) {
+    const long long p0 = t * kKeyTile + 4 * lane;
+    const unsigned f = woken4(k4[t * (kKeyTile / 4) + lane], p0, n, grown, all);
+    unsigned x = __popc(f);  // inclusive warp scan of the lanes' counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    unsigned long long at = off + x - __popc(f);
+    for (unsigned bits = f; bits; bits &= bits - 1) d.wlist[at++] = (int32_t)(p0 + __ffs(bits) - 1);
+    off += __shfl_sync(0xffffffffu, x, 31);
   }
   if (t_b == t_nb - 1 && threadIdx.x == 0) c->n_woken[step & 1] = (long long)total;
   return true;
@@ -1022,6 +1058,11 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
   // the zero list after the next generation's starts empty (it was last
   // read in this generation's claim phase)
   if (t_b == 0 && threadIdx.x == 0) c->zn[zpar ^ 1] = 0ull;
+  __shared__ int s_ccell[kCapBuf], s_cpos[kCapBuf], s_zero[kZeroBuf];
+  __shared__ unsigned s_nz;
+  __shared__ unsigned long long s_zbase;
+  if (threadIdx.x == 0) s_nz = 0u;  // ordered before its first use by the scans' barriers
+  const Grid &g = d.grid;
   unsigned long long run = pre;
   for (long long r0 = b; r0 < e; r0 += kBlock) {
     const long long r = r0 + threadIdx.x;
@@ -1029,24 +1070,52 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
     const uint32_t cap = word & 0x03ffffffu, surv = word >> 31;
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
+    // the tile's captures go to the block buffer when they fit, and the
+    // block then spreads their 26 neighbours over its threads
+    const unsigned tile_caps = (unsigned)(tot >> 32);
+    const bool buffered = tile_caps <= (unsigned)kCapBuf;
     if (r < e) {
       const long long p = list.at(r);
       const int cell = act[p].cell;
       if (!surv) tombstone(d, cur, p, cell);  // deactivated at its turn
       long long slot = (long long)((run + ex) >> 32);  // rank of the first child in the next generation
+      unsigned k = (unsigned)(ex >> 32);               // its place among the tile's captures
       uint32_t bits = cap;
       while (bits) {
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
         d.child[slot++] = ((uint32_t)r << 5) | (uint32_t)nb;  // parent's rank in this generation
         int di, dj, dk;
-        const int nc = cell + nbr_delta(d.grid, nb, di, dj, dk);
+        const int nc = cell + nbr_delta(g, nb, di, dj, dk);
         set_solid(d.solid, nc);  // solid for the next generation
-        neighbour_solid(d, cur, nc, p, step, zpar, 0.0, false, stat_dec);
+        if (buffered) {
+          s_ccell[k] = nc;
+          s_cpos[k] = (int)p;
+          ++k;
+        } else {
+          for (int nb2 = 0; nb2 < 26; ++nb2)
+            lose_neighbour(d, cur, nc + nbr_delta(g, nb2, di, dj, dk), p, step, zpar, s_zero, &s_nz, stat_dec);
+        }
       }
+    }
+    if (buffered && tile_caps) {
+      __syncthreads();
+      for (unsigned i = threadIdx.x; i < tile_caps * 26u; i += kBlock) {
+        const unsigned ci = i / 26u;
+        int di, dj, dk;
+        lose_neighbour(d, cur, s_ccell[ci] + nbr_delta(g, (int)(i - ci * 26u), di, dj, dk), s_cpos[ci], step, zpar,
+                       s_zero, &s_nz, stat_dec);
+      }
+      __syncthreads();  // the buffer is refilled by the next tile
     }
     run += tot;
   }
+  // the block's zero events into the generation's list
+  __syncthreads();
+  const unsigned nz = s_nz < (unsigned)kZeroBuf ? s_nz : (unsigned)kZeroBuf;
+  if (threadIdx.x == 0 && nz) s_zbase = atomicAdd(&c->zn[zpar], (unsigned long long)nz);
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < nz; i += kBlock) d.zlist[zpar][s_zbase + i] = s_zero[i];
   if (t_b == t_nb - 1 && threadIdx.x == 0) {
     const unsigned long long total = pre + agg;
     c->gen_n = (long long)(total >> 32);
@@ -1529,7 +1598,7 @@ struct NoAllocLayout {
     gcell = take((size_t)n * 4);
     for (int b = 0; b < 2; ++b) {
       act[b] = take((size_t)n * sizeof(EnvRec));
-      key[b] = take((size_t)n * 4);
+      key[b] = take((size_t)(n + kKeyTile) * 4);  // the wake scan reads whole tiles
       lstep[b] = take((size_t)n * 4);
       nliq[b] = take((size_t)n * 4);
       zlist[b] = take((size_t)n * 4);

@@ -50,6 +50,9 @@ constexpr long long kMaxCells = 1ll << 27;
 // brought up to date) at least every kWakeAll steps, well inside the ring.
 constexpr long long kDvRing = 4096;
 constexpr long long kWakeAll = 2048;
+// The wake scan reads keys in tiles of this many positions; key arrays hold
+// that many more entries than the list can (the tail of the last tile).
+constexpr long long kKeyTile = 128;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values

@@ -204,7 +204,7 @@ struct amca_t {
       d.gcell = a.take<int32_t>(d.gcap);
       for (int b = 0; b < 2; ++b) {
         d.act[b] = a.take<EnvRec>(d.gcap);
-        d.key[b] = a.take<float>(d.gcap);
+        d.key[b] = a.take<float>(d.gcap + kKeyTile);  // the wake scan reads whole tiles
         d.lstep[b] = a.take<int32_t>(d.gcap);
         d.nliq[b] = a.take<int32_t>(d.gcap);
         d.zlist[b] = a.take<int32_t>(d.gcap);
@@ -1193,6 +1193,10 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->captures = (int64_t)c.captures;
     s->active_grown = (int64_t)c.active_grown;
     s->grains_processed = (int64_t)c.grains_processed;
+    s->keys_scanned = (int64_t)c.keys_scanned;
+    s->decrements = (int64_t)c.decrements;
+    s->zero_events = (int64_t)c.zero_events;
+    s->compactions = (int64_t)c.compactions;
     s->algorithmic_bytes = h->algorithmic_bytes();
     s->h2d_bytes = h->h2d_bytes;
     s->d2h_bytes = h->d2h_bytes;

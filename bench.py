@@ -355,6 +355,12 @@ def run_ours(args, dist: Dist):
                                                                       round(st["phase_ms"][8], 3)]}
                                    if PHASE_DETAIL else {}),
                                 "fp64_tests_per_run": st["tests_fp64"],
+                                "woken_and_nuclei_per_run": st["active_grown"],
+                                "entries_processed_per_run": st["grains_processed"],
+                                "wake_keys_scanned_per_run": st["keys_scanned"],
+                                "liquid_count_decrements_per_run": st["decrements"],
+                                "zero_count_events_per_run": st["zero_events"],
+                                "list_compactions_per_run": st["compactions"],
                                 "parallelism": f"replicas x{args.gpus}", "e2e_field_matches": same}, case),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": f"{peak_kind} burst copy",

@@ -347,6 +347,13 @@ typedef struct {
    * and nucleation [13]; the slowest block's liquid-neighbour flag pass in
    * phase B [14]. */
   double detail_ms[16];
+  /* Plain realm only (zeros otherwise), summed since the last reset: list
+   * positions read by the wake scans, liquid-count decrements, counts that
+   * reached zero in a capture generation, compactions of the envelope list. */
+  int64_t keys_scanned;
+  int64_t decrements;
+  int64_t zero_events;
+  int64_t compactions;
 } amca_stats;
 /* For the FE-coupled remelting realm the fields mean: liquid_cells -1 (not
  * tracked), grains = grain objects, active = flagged (liquid-neighbour) cells
