@@ -199,63 +199,70 @@ __device__ __forceinline__ unsigned long long from_payload(unsigned long long p)
   return ((p >> 31) << 32) | (p & 0x7fffffffull);
 }
 
-// Decoupled look-back, run by the 32 lanes of warp 0. Lane 0 publishes tile
-// t's aggregate; each round the warp reads the 32 nearest unread predecessor
-// status words at once and sums them up to the nearest inclusive prefix.
-// Returns false (error flag set) when a wait ran out.
-__device__ bool look_back_warp(unsigned long long *status, long long t, unsigned long long agg,
-                               unsigned long long *excl, PlainCtrl *c) {
-  const int lane = threadIdx.x & 31;
-  if (t == 0) {
-    if (lane == 0) atomicExch(status, kFlagPrefix | to_payload(agg));
-    *excl = 0;
-    return true;
-  }
-  if (lane == 0) atomicExch(status + t, kFlagAgg | to_payload(agg));
-  unsigned long long sum = 0;
+// Exclusive prefix of this block's aggregate over the blocks before it
+// (tile index = block index), by decoupled look-back with the whole block:
+// thread 0 publishes the aggregate; each round every thread reads one of the
+// kBlock nearest unread predecessor status words, each warp finds its nearest
+// inclusive prefix and sums the payloads up to it, and the warps' results
+// (shared memory, one barrier) give the block's answer: a round covers kBlock
+// predecessors, so a team of a few hundred blocks needs at most a few rounds
+// of one dependent load each. Returns ~0 (error flag set) when a wait ran out.
+__device__ unsigned long long block_prefix(unsigned long long *status, unsigned long long agg,
+                                           unsigned long long *smem, PlainCtrl *c) {
+  (void)smem;
+  __shared__ unsigned s_pre[kWarps], s_empty[kWarps];
+  __shared__ unsigned long long s_part[kWarps];
+  __shared__ int s_bail;
+  const long long t = t_b;
+  if (threadIdx.x == 0) atomicExch(status + t, (t == 0 ? kFlagPrefix : kFlagAgg) | to_payload(agg));
+  if (t == 0) return 0ull;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long sum = 0;  // the same in every thread
   long long p = t - 1;
   const unsigned long long t0 = now_ns();
   for (;;) {
-    const long long q = p - lane;
+    const long long q = p - threadIdx.x;
     const unsigned long long s = q >= 0 ? ld_acquire(status + q) : kFlagPrefix;  // before tile 0: prefix 0
     const unsigned long long flag = s & ~kPayload;
     const unsigned pre = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
     const unsigned empty = __ballot_sync(0xffffffffu, flag == 0);
-    const unsigned upto = pre ? (((pre & (0u - pre)) << 1) - 1u) : 0xffffffffu;  // lanes up to the nearest prefix
-    if (empty & upto) {
-      int bail = 0;
-      if (lane == 0 && (now_ns() - t0 > kWaitNs || ld_volatile(&c->error) != 0)) {
-        atomicCAS(&c->error, 0, kErrLookback);
-        bail = 1;
-      }
-      if (__shfl_sync(0xffffffffu, bail, 0)) return false;
-      continue;
-    }
+    const unsigned upto = pre ? (((pre & (0u - pre)) << 1) - 1u) : 0xffffffffu;  // lanes up to the warp's prefix
     unsigned long long v = ((upto >> lane) & 1u) ? from_payload(s & kPayload) : 0ull;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    sum += v;
-    if (pre) break;
-    p -= 32;
+    if (lane == 0) {
+      s_pre[warp] = pre;
+      s_empty[warp] = empty & upto;
+      s_part[warp] = v;
+    }
+    __syncthreads();
+    // the nearest warp holding a prefix, and whether any word up to it is unpublished
+    int wstar = kWarps;
+    bool waiting = false;
+    unsigned long long part = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      if (wstar < kWarps) break;
+      waiting = waiting || s_empty[w] != 0;
+      part += s_part[w];
+      if (s_pre[w]) wstar = w;
+    }
+    if (waiting) {
+      if (threadIdx.x == 0)
+        s_bail = (now_ns() - t0 > kWaitNs || ld_volatile(&c->error) != 0) ? (atomicCAS(&c->error, 0, kErrLookback), 1) : 0;
+      __syncthreads();
+      const int bail = s_bail;
+      __syncthreads();  // s_pre and s_bail are rewritten next round
+      if (bail) return ~0ull;
+      continue;
+    }
+    sum += part;
+    __syncthreads();  // s_pre, s_empty and s_part are rewritten next round
+    if (wstar < kWarps) break;
+    p -= kBlock;
   }
-  if (lane == 0) atomicExch(status + t, kFlagPrefix | to_payload(sum + agg));
-  *excl = sum;
-  return true;
-}
-
-// Exclusive prefix of this block's aggregate over the blocks before it
-// (tile index = block index). Returns ~0 on error.
-__device__ unsigned long long block_prefix(unsigned long long *status, unsigned long long agg,
-                                           unsigned long long *smem, PlainCtrl *c) {
-  if (threadIdx.x < 32) {
-    unsigned long long pre = 0;
-    const bool ok = look_back_warp(status, t_b, agg, &pre, c);
-    if (threadIdx.x == 0) smem[kWarps] = ok ? pre : ~0ull;
-  }
-  __syncthreads();
-  const unsigned long long pre = smem[kWarps];
-  __syncthreads();
-  return pre;
+  if (threadIdx.x == 0) atomicExch(status + t, kFlagPrefix | to_payload(sum + agg));
+  return sum;
 }
 
 // This block's contiguous share [b, e) of [0, n).
@@ -508,30 +515,75 @@ __device__ __noinline__ unsigned nucleus_neighbours(const PlainDevice &d, int cu
   return gone;
 }
 
-// Block buffers of the resolve phase: the captured cells of a tile of ranks
-// (with their capturer's position), and the zero-count events.
-constexpr int kCapBuf = 512;
+// Zero-count events a block gathers before adding them to a zero list.
 constexpr int kZeroBuf = 512;
 
-// A capture by the entry at position pc turned cell m's neighbour solid: the
-// entry on m (if any) has one liquid neighbour fewer. A decrement by a later
-// rank (pc beyond the entry) is recorded in late[]; a count reaching zero
-// goes to the block's zero buffer, or to the generation's zero list (parity
-// zpar) once the buffer is full.
-__device__ __forceinline__ void lose_neighbour(const PlainDevice &d, int cur, int m, long long pc, long long step,
-                                               int zpar, int *s_zero, unsigned *s_nz, unsigned long long *stat_dec) {
-  const int q = d.pos[m];
-  if (q < 0) return;
-  ++*stat_dec;
-  if (pc > q) d.late[q] = (int32_t)step;
-  if (atomicSub(d.nliq[cur] + q, 1) != 1) return;
-  const unsigned k = atomicAdd(s_nz, 1u);
-  if (k < (unsigned)kZeroBuf) {
-    s_zero[k] = q;
-  } else {
-    const unsigned long long i = atomicAdd(&d.ctrl->zn[zpar], 1ull);
-    d.zlist[zpar][i] = q;
+// The liquid counts around the n cells that the previous generation captured
+// (its child records, this generation's ranks; `parents` gives the
+// capturers' positions): one decrement for the entry on each neighbour cell
+// listed before this generation (position below `limit`; this generation's
+// own entries count their liquid neighbours from the bitmap, which has these
+// captures). A decrement by a later rank (capturer beyond the entry) is
+// recorded in late[]; a count reaching zero goes to the zero list of parity
+// zpar, through a block buffer. The (capture, neighbour) pairs are spread over
+// the team, four per thread and pass so that their loads overlap.
+__device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, long long n, GenList parents,
+                                                long long limit, long long step, int zpar,
+                                                unsigned long long *stat_dec) {
+  __shared__ int s_zero[kZeroBuf];
+  __shared__ unsigned s_nz;
+  __shared__ unsigned long long s_zbase;
+  if (threadIdx.x == 0) s_nz = 0u;
+  __syncthreads();
+  const Grid &g = d.grid;
+  const EnvRec *act = d.act[cur];
+  const long long items = n * 26;
+  const long long stride = (long long)t_nb * kBlock * 4;
+  for (long long i0 = ((long long)t_b * kBlock + threadIdx.x) * 4; i0 < items; i0 += stride) {
+    int m[4], q[4], old[4];
+    long long pc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const long long i = i0 + j;
+      m[j] = -1;
+      pc[j] = 0;
+      if (i < items) {
+        const long long k = i / 26;
+        const uint32_t rec = d.child[k];
+        int di, dj, dk;
+        pc[j] = parents.at((long long)(rec >> 5));
+        const int cell = act[pc[j]].cell + nbr_delta(g, (int)(rec & 31u), di, dj, dk);
+        m[j] = cell + nbr_delta(g, (int)(i - k * 26), di, dj, dk);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[j] = m[j] >= 0 ? d.pos[m[j]] : -1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      old[j] = 0;
+      if (q[j] >= 0 && q[j] < limit) {
+        ++*stat_dec;
+        if (pc[j] > q[j]) d.late[q[j]] = (int32_t)step;
+        old[j] = atomicSub(d.nliq[cur] + q[j], 1);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (old[j] != 1) continue;
+      const unsigned k = atomicAdd(&s_nz, 1u);
+      if (k < (unsigned)kZeroBuf) {
+        s_zero[k] = q[j];
+      } else {
+        const unsigned long long z = atomicAdd(&d.ctrl->zn[zpar], 1ull);
+        d.zlist[zpar][z] = q[j];
+      }
+    }
   }
+  __syncthreads();
+  const unsigned nz = s_nz < (unsigned)kZeroBuf ? s_nz : (unsigned)kZeroBuf;
+  if (threadIdx.x == 0 && nz) s_zbase = atomicAdd(&d.ctrl->zn[zpar], (unsigned long long)nz);
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < nz; i += kBlock) d.zlist[zpar][s_zbase + i] = s_zero[i];
 }
 
 // Nucleus number r (in site order) of this step on `cell`: orientation,
@@ -1029,14 +1081,19 @@ __device__ __forceinline__ bool mark_in_resolve(long long n) { return n <= (long
 // entry that does not survive its turn becomes a tombstone. Marking reads
 // only claim words, the claimed bitmap, its own ranks' masks and cells, none
 // of which another block's resolve writes, so no barrier separates the two
-// passes. Every captured cell turns solid for the next generation and takes
-// one off the liquid counts around it (zero list of parity zpar). The last
-// block publishes the generation's capture and survivor counts, which every
-// block reads after the barrier.
+// passes. Every captured cell turns solid for the next generation (whose
+// claim phase takes it off the liquid counts around it). The zero events
+// that the claim phase found (parity zdec, -1: none; zgen0: of generation
+// 0's captures) are decided here, and the list of parity zreset is emptied
+// for the next claim phase. The last block publishes the generation's
+// capture and survivor counts, which every block reads after the barrier.
 __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long long n, long long step, unsigned par,
-                              GenList list, int zpar, unsigned long long *smem, unsigned long long *stat_dec) {
+                                           GenList list, int zdec, bool zgen0, int zreset, unsigned long long *smem,
+                                           unsigned *gone_now, unsigned *gone_next) {
   PlainCtrl *c = d.ctrl;
   const EnvRec *act = d.act[cur];
+  if (zdec >= 0) zero_decisions(d, cur, zdec, zgen0, step, gone_now, gone_next);
+  if (t_b == 0 && threadIdx.x == 0) c->zn[zreset] = 0ull;  // last read in the previous resolve phase
   long long b, e;
   block_chunk(n, b, e);
   unsigned long long acc = 0;
@@ -1055,13 +1112,6 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
   block_exclusive_scan(acc, smem, &agg);
   const unsigned long long pre = block_prefix(d.scanB, agg, smem, c);
   if (pre == ~0ull) return false;
-  // the zero list after the next generation's starts empty (it was last
-  // read in this generation's claim phase)
-  if (t_b == 0 && threadIdx.x == 0) c->zn[zpar ^ 1] = 0ull;
-  __shared__ int s_ccell[kCapBuf], s_cpos[kCapBuf], s_zero[kZeroBuf];
-  __shared__ unsigned s_nz;
-  __shared__ unsigned long long s_zbase;
-  if (threadIdx.x == 0) s_nz = 0u;  // ordered before its first use by the scans' barriers
   const Grid &g = d.grid;
   unsigned long long run = pre;
   for (long long r0 = b; r0 < e; r0 += kBlock) {
@@ -1070,52 +1120,22 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
     const uint32_t cap = word & 0x03ffffffu, surv = word >> 31;
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
-    // the tile's captures go to the block buffer when they fit, and the
-    // block then spreads their 26 neighbours over its threads
-    const unsigned tile_caps = (unsigned)(tot >> 32);
-    const bool buffered = tile_caps <= (unsigned)kCapBuf;
     if (r < e) {
       const long long p = list.at(r);
       const int cell = act[p].cell;
       if (!surv) tombstone(d, cur, p, cell);  // deactivated at its turn
       long long slot = (long long)((run + ex) >> 32);  // rank of the first child in the next generation
-      unsigned k = (unsigned)(ex >> 32);               // its place among the tile's captures
       uint32_t bits = cap;
       while (bits) {
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
         d.child[slot++] = ((uint32_t)r << 5) | (uint32_t)nb;  // parent's rank in this generation
         int di, dj, dk;
-        const int nc = cell + nbr_delta(g, nb, di, dj, dk);
-        set_solid(d.solid, nc);  // solid for the next generation
-        if (buffered) {
-          s_ccell[k] = nc;
-          s_cpos[k] = (int)p;
-          ++k;
-        } else {
-          for (int nb2 = 0; nb2 < 26; ++nb2)
-            lose_neighbour(d, cur, nc + nbr_delta(g, nb2, di, dj, dk), p, step, zpar, s_zero, &s_nz, stat_dec);
-        }
+        set_solid(d.solid, cell + nbr_delta(g, nb, di, dj, dk));  // solid for the next generation
       }
-    }
-    if (buffered && tile_caps) {
-      __syncthreads();
-      for (unsigned i = threadIdx.x; i < tile_caps * 26u; i += kBlock) {
-        const unsigned ci = i / 26u;
-        int di, dj, dk;
-        lose_neighbour(d, cur, s_ccell[ci] + nbr_delta(g, (int)(i - ci * 26u), di, dj, dk), s_cpos[ci], step, zpar,
-                       s_zero, &s_nz, stat_dec);
-      }
-      __syncthreads();  // the buffer is refilled by the next tile
     }
     run += tot;
   }
-  // the block's zero events into the generation's list
-  __syncthreads();
-  const unsigned nz = s_nz < (unsigned)kZeroBuf ? s_nz : (unsigned)kZeroBuf;
-  if (threadIdx.x == 0 && nz) s_zbase = atomicAdd(&c->zn[zpar], (unsigned long long)nz);
-  __syncthreads();
-  for (unsigned i = threadIdx.x; i < nz; i += kBlock) d.zlist[zpar][s_zbase + i] = s_zero[i];
   if (t_b == t_nb - 1 && threadIdx.x == 0) {
     const unsigned long long total = pre + agg;
     c->gen_n = (long long)(total >> 32);
@@ -1182,10 +1202,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     const double dv = da * vel;
     const double grown_s = grown + dv;
     const bool all = step % kWakeAll == 0;
-    if (t_b == 0 && threadIdx.x == 0) {
-      d.dvh[step & (kDvRing - 1)] = dv;
-      c->zn[0] = 0ull;  // generation 0's zero list (last read in the previous step)
-    }
+    if (t_b == 0 && threadIdx.x == 0) d.dvh[step & (kDvRing - 1)] = dv;
     if (!(ok = nucleation_phase(d, cur, time, step, a_len, n_orient, grain, grown_s, all, s_cell, s_dtc, smem, &live,
                                 &dec, &gone_now)))
       break;
@@ -1222,10 +1239,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       processed += n;
       unsigned long long t_work = threadIdx.x == 0 ? now_ns() : 0ull;
       claim_phase(d, cur, kind, lo, n, gen & 1u, list, parents, step, grown, &tests, &tests64);
-      if (gen > 0) {
-        zero_decisions(d, cur, (int)((gen - 1) & 1u), gen == 1, step, &gone_now, &gone_next);
-        flush_departures(c, step, gone_now, gone_next);
-      }
+      // the liquid counts around the previous generation's captures
+      if (gen > 0) capture_decrements(d, cur, n, parents, list.base, step, (int)((gen - 1) & 1u), &dec);
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work;
@@ -1255,7 +1270,10 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         if (timer) c->mark_next = 0ull;  // the next marking pass is two barriers away
         t_work = threadIdx.x == 0 ? now_ns() : 0ull;
       }
-      if (!(ok = resolve_phase(d, cur, n, step, gen & 1u, list, (int)(gen & 1u), smem, &dec))) break;
+      if (!(ok = resolve_phase(d, cur, n, step, gen & 1u, list, gen > 0 ? (int)((gen - 1) & 1u) : -1, gen == 1,
+                               (int)(gen & 1u), smem, &gone_now, &gone_next)))
+        break;
+      flush_departures(c, step, gone_now, gone_next);
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - t_work + w_mark;
         resolve_busy += w;
