@@ -455,18 +455,25 @@ __device__ __forceinline__ uint32_t liquid_neighbours(const uint32_t *solid, con
 // ---------------------------------------------------------------------------
 // Whether an entry with wake key k is processed in a step whose cumulative
 // growth is `grown` (all: every live entry, to bring its record up to date).
-// Dead entries (NaN) never are.
-__device__ __forceinline__ bool woken(float k, double grown, bool all) { return all ? !isnan(k) : (double)k <= grown; }
+// Dead entries (NaN) never are. The test (double)k <= grown is made in FP32
+// (the FP64 pipe is narrow), exactly: for a float k it holds iff k is at most
+// grown rounded down to float, gf.
+__device__ __forceinline__ float wake_bound(double grown) { return __double2float_rd(grown); }
+__device__ __forceinline__ bool woken(float k, float gf, bool all) { return all ? !isnan(k) : k <= gf; }
 
 // Wake key: the cumulative growth at which the half-diagonal L (grown up to
-// `grown`) may reach t_lb, rounded down, less a relative 2^-30 that covers
-// the rounding of the step sums between now and then (an entry is woken at
-// least every kWakeAll steps). +inf when no liquid neighbour is left.
-__device__ __forceinline__ float wake_key(float t_lb, double L, double grown) {
+// `grown`, gf = grown rounded down to float) may reach t_lb: t_lb + (grown -
+// L), every rounding downwards, less 2^-30 of the magnitudes involved (L is
+// at most grown plus a few cells), which covers the rounding of the FP64 step
+// sums over the at most kWakeAll steps before the entry is looked at again
+// by a factor of thousands. One FP64 subtraction and one conversion; the rest
+// in FP32. +inf when no liquid neighbour is left. Waking early only costs a
+// test.
+__device__ __forceinline__ float wake_key(float t_lb, double L, double grown, float gf) {
   if (!(t_lb < INFINITY)) return INFINITY;
-  const double k = (double)t_lb - L + grown;
-  const double slack = 9.313225746154785e-10 * (fabs((double)t_lb) + fabs(L) + fabs(grown));
-  return __double2float_rd(k - slack);
+  const float o = __double2float_rd(grown - L);
+  const float slack = 9.313225746154785e-10f * (fabsf(t_lb) + fabsf(o) + 2.0f * gf);
+  return __fsub_rd(__fadd_rd(t_lb, o), slack);
 }
 
 // Grain::grow (Grain.h:27) of the steps (from, to]: the same FP64 additions
@@ -507,7 +514,7 @@ __device__ __noinline__ unsigned nucleus_neighbours(const PlainDevice &d, int cu
     const int q = d.pos[m];
     if (q < 0) continue;
     ++*stat_dec;
-    if (atomicSub(d.nliq[cur] + q, 1) == 1 && !woken(d.key[cur][q], grown, all)) {
+    if (atomicSub(d.nliq[cur] + q, 1) == 1 && !woken(d.key[cur][q], wake_bound(grown), all)) {
       tombstone(d, cur, q, m);
       ++gone;
     }
@@ -762,9 +769,9 @@ __device__ __forceinline__ unsigned long long warp_offset(unsigned cnt, unsigned
 // float4, 128 positions per warp and iteration (the key arrays are padded to
 // a whole number of these tiles); the team takes contiguous runs of tiles,
 // each warp a contiguous run of its block's.
-__device__ __forceinline__ unsigned woken4(const float4 v, long long p0, long long n, double grown, bool all) {
-  return (p0 < n && woken(v.x, grown, all) ? 1u : 0u) | (p0 + 1 < n && woken(v.y, grown, all) ? 2u : 0u) |
-         (p0 + 2 < n && woken(v.z, grown, all) ? 4u : 0u) | (p0 + 3 < n && woken(v.w, grown, all) ? 8u : 0u);
+__device__ __forceinline__ unsigned woken4(const float4 v, long long p0, long long n, float gf, bool all) {
+  return (p0 < n && woken(v.x, gf, all) ? 1u : 0u) | (p0 + 1 < n && woken(v.y, gf, all) ? 2u : 0u) |
+         (p0 + 2 < n && woken(v.z, gf, all) ? 4u : 0u) | (p0 + 3 < n && woken(v.w, gf, all) ? 8u : 0u);
 }
 __device__ __noinline__ bool wake_scan(const PlainDevice &d, int cur, long long n, long long step, double grown, bool all,
                                        unsigned long long *smem) {
@@ -772,6 +779,7 @@ __device__ __noinline__ bool wake_scan(const PlainDevice &d, int cur, long long 
   // the next step's words start cleared (last read in the previous step)
   if (threadIdx.x == 0) d.scanC[((step + 1) & 1) * kStatusWords + t_b] = 0ull;
   const float4 *k4 = (const float4 *)d.key[cur];
+  const float gf = wake_bound(grown);
   const long long ntiles = (n + kKeyTile - 1) / kKeyTile;
   long long tb, te;
   block_chunk(ntiles, tb, te);
@@ -783,7 +791,7 @@ __device__ __noinline__ bool wake_scan(const PlainDevice &d, int cur, long long 
 #pragma unroll 4
   for (long long t = wb; t < we; ++t) {
     const long long p0 = t * kKeyTile + 4 * lane;
-    cnt += __popc(woken4(k4[t * (kKeyTile / 4) + lane], p0, n, grown, all));
+    cnt += __popc(woken4(k4[t * (kKeyTile / 4) + lane], p0, n, gf, all));
   }
   cnt = __reduce_add_sync(0xffffffffu, cnt);
   unsigned long long total = 0;
@@ -794,7 +802,7 @@ __device__ __noinline__ bool wake_scan(const PlainDevice &d, int cur, long long 
 #pragma unroll 2
   for (long long t = wb; t < we; ++t) {
     const long long p0 = t * kKeyTile + 4 * lane;
-    const unsigned f = woken4(k4[t * (kKeyTile / 4) + lane], p0, n, grown, all);
+    const unsigned f = woken4(k4[t * (kKeyTile / 4) + lane], p0, n, gf, all);
     unsigned x = __popc(f);  // inclusive warp scan of the lanes' counts
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -894,6 +902,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
   EnvRec *act = d.act[cur];
   int32_t *lstep = d.lstep[cur];
+  const float gf = wake_bound(grown);
   unsigned long long tests = 0, tests64 = 0;
   // Claims need no order: warps or blocks take chunks of consecutive ranks
   // from a shared counter until none is left, so those that drew cheap
@@ -1014,7 +1023,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
     }
     // growth is uniform: the entry can contain one of the neighbours left
     // only once the run's cumulative growth reaches this key
-    d.key[cur][p] = t_lb == -INFINITY ? __double2float_rd(grown) : wake_key(t_lb, L, grown);
+    d.key[cur][p] = t_lb == -INFINITY ? gf : wake_key(t_lb, L, grown, gf);
     d.liq[r] = liq;
     d.con[r] = con;
   }
@@ -1183,12 +1192,14 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   // per-block busy time (thread 0), added to the control block once per
   // launch; with phase_detail the per-phase maximum is raised only by a block
   // that exceeds it (same-address atomics from every block serialise)
-  unsigned long long claim_busy = 0, resolve_busy = 0;
+  unsigned long long claim_busy = 0, resolve_busy = 0, nuc_busy = 0, wake_busy = 0, compact_busy = 0;
   const double t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
   while (!done && time < t_end && step < step_limit) {
     // the list is compacted once it is mostly tombstones
     if (a_len > 2 * n_act + 4096) {
+      const unsigned long long tc = threadIdx.x == 0 ? now_ns() : 0ull;
       if (!(ok = compact_phase(d, cur, a_len, (unsigned)(compactions & 1ull), smem, &moved))) break;
+      if (threadIdx.x == 0) compact_busy += now_ns() - tc;
       if (!(ok = grid_barrier(c))) break;
       cur ^= 1;
       a_len = ld_volatile(&c->compact_len);
@@ -1196,18 +1207,31 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     }
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
     double vel, da, dn;
-    step_rates(d, time, vel, da, dn);
+    {
+      // one evaluation per warp (the FP64 pipe is narrow), shared by its lanes
+      if ((threadIdx.x & 31) == 0) step_rates(d, time, vel, da, dn);
+      vel = __shfl_sync(0xffffffffu, vel, 0);
+      da = __shfl_sync(0xffffffffu, da, 0);
+      dn = __shfl_sync(0xffffffffu, dn, 0);
+    }
     // growth of every envelope this step (when there is one); the wake scan
     // compares the keys with the cumulative growth
     const double dv = da * vel;
     const double grown_s = grown + dv;
     const bool all = step % kWakeAll == 0;
     if (t_b == 0 && threadIdx.x == 0) d.dvh[step & (kDvRing - 1)] = dv;
+    const unsigned long long tn0 = threadIdx.x == 0 ? now_ns() : 0ull;
     if (!(ok = nucleation_phase(d, cur, time, step, a_len, n_orient, grain, grown_s, all, s_cell, s_dtc, smem, &live,
                                 &dec, &gone_now)))
       break;
+    const unsigned long long tn1 = threadIdx.x == 0 ? now_ns() : 0ull;
     if (!(ok = wake_scan(d, cur, a_len, step, grown_s, all, smem))) break;
     flush_departures(c, step, gone_now, gone_next);
+    if (threadIdx.x == 0) {
+      const unsigned long long tn2 = now_ns();
+      nuc_busy += tn1 - tn0;
+      wake_busy += tn2 - tn1;
+    }
     if (!(ok = grid_barrier(c))) break;
     if (timer) {
       t_now = now_ns();
@@ -1359,6 +1383,9 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     if (threadIdx.x == 0) {
       if (claim_busy) atomicAdd(&c->ns_claim_work_sum, claim_busy);
       if (resolve_busy) atomicAdd(&c->ns_resolve_work_sum, resolve_busy);
+      if (nuc_busy) atomicAdd(&c->ns_nuc_work_sum, nuc_busy);
+      if (wake_busy) atomicAdd(&c->ns_wake_work_sum, wake_busy);
+      if (compact_busy) atomicAdd(&c->ns_compact_work_sum, compact_busy);
     }
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);

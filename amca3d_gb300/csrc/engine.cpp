@@ -1210,6 +1210,9 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->phase_ms[6] = c.ns_claim_work_max * 1e-6;
     s->phase_ms[7] = c.ns_resolve_work_sum * 1e-6 / nb;
     s->phase_ms[8] = c.ns_resolve_work_max * 1e-6;
+    s->detail_ms[0] = c.ns_nuc_work_sum * 1e-6 / nb;
+    s->detail_ms[1] = c.ns_wake_work_sum * 1e-6 / nb;
+    s->detail_ms[2] = c.ns_compact_work_sum * 1e-6 / nb;
   });
 }
 

@@ -345,7 +345,8 @@ typedef struct {
    * block [6..11], for the work closed by the barrier after phase A, B, C,
    * D, E and after the host velocity answers; block 0's new-grain ids [12]
    * and nucleation [13]; the slowest block's liquid-neighbour flag pass in
-   * phase B [14]. */
+   * phase B [14]. Plain realm: per-block busy time, mean over blocks, of
+   * nucleation [0], the wake scan [1] and list compactions [2]. */
   double detail_ms[16];
   /* Plain realm only (zeros otherwise), summed since the last reset: list
    * positions read by the wake scans, liquid-count decrements, counts that
