@@ -1220,17 +1220,21 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     const double grown_s = grown + dv;
     const bool all = step % kWakeAll == 0;
     if (t_b == 0 && threadIdx.x == 0) d.dvh[step & (kDvRing - 1)] = dv;
+    // the wake scan first: every block publishes its part of the scan at
+    // once, while only the blocks holding sites take part in nucleation's.
+    // A nucleus may turn a sleeping entry dead after the scan passed it,
+    // which the scan's rule (dead or sleeping: not woken) already gave.
     const unsigned long long tn0 = threadIdx.x == 0 ? now_ns() : 0ull;
+    if (!(ok = wake_scan(d, cur, a_len, step, grown_s, all, smem))) break;
+    const unsigned long long tn1 = threadIdx.x == 0 ? now_ns() : 0ull;
     if (!(ok = nucleation_phase(d, cur, time, step, a_len, n_orient, grain, grown_s, all, s_cell, s_dtc, smem, &live,
                                 &dec, &gone_now)))
       break;
-    const unsigned long long tn1 = threadIdx.x == 0 ? now_ns() : 0ull;
-    if (!(ok = wake_scan(d, cur, a_len, step, grown_s, all, smem))) break;
     flush_departures(c, step, gone_now, gone_next);
     if (threadIdx.x == 0) {
       const unsigned long long tn2 = now_ns();
-      nuc_busy += tn1 - tn0;
-      wake_busy += tn2 - tn1;
+      wake_busy += tn1 - tn0;
+      nuc_busy += tn2 - tn1;
     }
     if (!(ok = grid_barrier(c))) break;
     if (timer) {
