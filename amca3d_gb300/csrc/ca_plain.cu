@@ -1155,6 +1155,27 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
 
 // Whole CA steps of one realm by the current team, until it is solid, its
 // termination time, or step_limit.
+//
+// The realm's state (step, time, counts, list length, ...) is the same in
+// every thread; it lives in shared memory, written by thread 0 right after
+// the barriers at which its inputs become final and read by all after a
+// block barrier, so that the registers stay free for the phases.
+struct RealmState {
+  long long step, n_act, a_len, n_orient, grain, liquid;
+  double time, dt, grown, t_end;
+  unsigned long long compactions;
+  int cur, done;
+  // the step in progress
+  double da, dn, dv, grown_s;
+  int all;
+  long long nucs, n, lo, processed, gen_end, caps_all, died;
+  unsigned gen;
+  GenList list, parents;  // this generation / its parents
+  // thread 0's busy time per kind of work, added to the control block once
+  // per launch; block 0's phase clock
+  unsigned long long claim_busy, resolve_busy, nuc_busy, wake_busy, compact_busy, t_mark, t_work, w_mark;
+};
+
 __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned long long *smem) {
   // block 0's phase clock and step counters (its thread 0 only), added to
   // the control block once per launch
@@ -1164,201 +1185,219 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   // this block's tile of sites when they are tiled (cell -1: removed, or no site)
   __shared__ int s_cell[kBlock];
   __shared__ double s_dtc[kBlock];
+  __shared__ RealmState S;
   PlainCtrl *c = d.ctrl;
   unsigned long long tests = 0, tests64 = 0, live = 0, dec = 0, moved = 0;
-  // per-step state, identical in every thread (read once, then advanced
-  // locally from the counts that the last block of a phase publishes)
-  long long step = ld_volatile(&c->step);
-  double time = ld_volatile(&c->time), dt = ld_volatile(&c->dt);
-  long long n_act = ld_volatile(&c->n_active), a_len = ld_volatile(&c->a_len);
-  long long n_orient = ld_volatile(&c->n_orient), grain = ld_volatile(&c->next_grain);
-  long long liquid = ld_volatile(&c->liquid);
-  unsigned long long compactions = ld_volatile(&c->compactions);
-  double grown = ld_volatile(&c->grown);
-  int cur = ld_volatile(&c->cur_list);
-  bool done = ld_volatile(&c->done) != 0;
-  bool ok = true;
-  unsigned gone_now = 0, gone_next = 0;  // list departures this thread decided, added once per step
+  unsigned gone_now = 0, gone_next = 0;  // list departures this thread decided, added once per phase
+  const bool timer = t_b == 0 && threadIdx.x == 0;
+  if (threadIdx.x == 0) {
+    S.step = ld_volatile(&c->step);
+    S.time = ld_volatile(&c->time);
+    S.dt = ld_volatile(&c->dt);
+    S.n_act = ld_volatile(&c->n_active);
+    S.a_len = ld_volatile(&c->a_len);
+    S.n_orient = ld_volatile(&c->n_orient);
+    S.grain = ld_volatile(&c->next_grain);
+    S.liquid = ld_volatile(&c->liquid);
+    S.compactions = ld_volatile(&c->compactions);
+    S.grown = ld_volatile(&c->grown);
+    S.cur = ld_volatile(&c->cur_list);
+    S.done = ld_volatile(&c->done) != 0;
+    S.t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
+    S.claim_busy = S.resolve_busy = S.nuc_busy = S.wake_busy = S.compact_busy = 0ull;
+    S.t_mark = now_ns();
+  }
   if (site_tiles(d)) {
     const long long i = (long long)t_b * kBlock + threadIdx.x;
     const bool on = i < d.nsites && d.site_live[i] != 0;
     s_cell[threadIdx.x] = on ? d.site_cell[i] : -1;
     s_dtc[threadIdx.x] = on ? d.site_dtc[i] : 0.0;
   }
-  const bool timer = t_b == 0 && threadIdx.x == 0;
   if (timer)
     for (int k = 0; k < kClk; ++k) s_clk[k] = 0ull;
-  unsigned long long t_mark = timer ? now_ns() : 0ull, t_now;
-  // per-block busy time (thread 0), added to the control block once per
-  // launch; with phase_detail the per-phase maximum is raised only by a block
-  // that exceeds it (same-address atomics from every block serialise)
-  unsigned long long claim_busy = 0, resolve_busy = 0, nuc_busy = 0, wake_busy = 0, compact_busy = 0;
-  const double t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
-  while (!done && time < t_end && step < step_limit) {
+  __syncthreads();
+  bool ok = true;
+  while (!S.done && S.time < S.t_end && S.step < step_limit) {
     // the list is compacted once it is mostly tombstones
-    if (a_len > 2 * n_act + 4096) {
+    if (S.a_len > 2 * S.n_act + 4096) {
       const unsigned long long tc = threadIdx.x == 0 ? now_ns() : 0ull;
-      if (!(ok = compact_phase(d, cur, a_len, (unsigned)(compactions & 1ull), smem, &moved))) break;
-      if (threadIdx.x == 0) compact_busy += now_ns() - tc;
+      if (!(ok = compact_phase(d, S.cur, S.a_len, (unsigned)(S.compactions & 1ull), smem, &moved))) break;
+      if (threadIdx.x == 0) S.compact_busy += now_ns() - tc;
       if (!(ok = grid_barrier(c))) break;
-      cur ^= 1;
-      a_len = ld_volatile(&c->compact_len);
-      ++compactions;
+      if (threadIdx.x == 0) {
+        S.cur ^= 1;
+        S.a_len = ld_volatile(&c->compact_len);
+        ++S.compactions;
+      }
+      __syncthreads();
     }
     // --- calculate_time_step (CellularAutomataManager_3D.cpp:441-511) ---
-    double vel, da, dn;
-    {
-      // one evaluation per warp (the FP64 pipe is narrow), shared by its lanes
-      if ((threadIdx.x & 31) == 0) step_rates(d, time, vel, da, dn);
-      vel = __shfl_sync(0xffffffffu, vel, 0);
-      da = __shfl_sync(0xffffffffu, da, 0);
-      dn = __shfl_sync(0xffffffffu, dn, 0);
+    if (threadIdx.x == 0) {
+      double vel;
+      step_rates(d, S.time, vel, S.da, S.dn);
+      // growth of every envelope this step (when there is one); the wake
+      // scan compares the keys with the cumulative growth
+      S.dv = S.da * vel;
+      S.grown_s = S.grown + S.dv;
+      S.all = S.step % kWakeAll == 0;
+      if (t_b == 0) d.dvh[S.step & (kDvRing - 1)] = S.dv;
     }
-    // growth of every envelope this step (when there is one); the wake scan
-    // compares the keys with the cumulative growth
-    const double dv = da * vel;
-    const double grown_s = grown + dv;
-    const bool all = step % kWakeAll == 0;
-    if (t_b == 0 && threadIdx.x == 0) d.dvh[step & (kDvRing - 1)] = dv;
+    __syncthreads();
     // the wake scan first: every block publishes its part of the scan at
     // once, while only the blocks holding sites take part in nucleation's.
     // A nucleus may turn a sleeping entry dead after the scan passed it,
     // which the scan's rule (dead or sleeping: not woken) already gave.
     const unsigned long long tn0 = threadIdx.x == 0 ? now_ns() : 0ull;
-    if (!(ok = wake_scan(d, cur, a_len, step, grown_s, all, smem))) break;
+    if (!(ok = wake_scan(d, S.cur, S.a_len, S.step, S.grown_s, S.all != 0, smem))) break;
     const unsigned long long tn1 = threadIdx.x == 0 ? now_ns() : 0ull;
-    if (!(ok = nucleation_phase(d, cur, time, step, a_len, n_orient, grain, grown_s, all, s_cell, s_dtc, smem, &live,
-                                &dec, &gone_now)))
+    if (!(ok = nucleation_phase(d, S.cur, S.time, S.step, S.a_len, S.n_orient, S.grain, S.grown_s, S.all != 0, s_cell,
+                                s_dtc, smem, &live, &dec, &gone_now)))
       break;
-    flush_departures(c, step, gone_now, gone_next);
+    flush_departures(c, S.step, gone_now, gone_next);
     if (threadIdx.x == 0) {
       const unsigned long long tn2 = now_ns();
-      wake_busy += tn1 - tn0;
-      nuc_busy += tn2 - tn1;
+      S.wake_busy += tn1 - tn0;
+      S.nuc_busy += tn2 - tn1;
     }
     if (!(ok = grid_barrier(c))) break;
-    if (timer) {
-      t_now = now_ns();
-      s_clk[kNuc] += t_now - t_mark;
-      t_mark = t_now;
-      // the slot of step + 2 (last read at the end of step - 1)
-      c->deaths[(step + 2) % 3] = 0;
+    if (threadIdx.x == 0) {
+      const long long nA = ld_volatile(&c->n_active_nuc[S.step & 1]);
+      const long long nucs = nA - S.a_len;  // nuclei of this step
+      const long long nw = ld_volatile(&c->n_woken[S.step & 1]);
+      if (timer) {
+        const unsigned long long t_now = now_ns();
+        s_clk[kNuc] += t_now - S.t_mark;
+        S.t_mark = t_now;
+        // the slot of step + 2 (last read at the end of step - 1)
+        c->deaths[(S.step + 2) % 3] = 0;
+        s_clk[kNucs] += (unsigned long long)nucs;
+        s_clk[kScanned] += (unsigned long long)S.a_len;
+        s_clk[kGrown] += (unsigned long long)(nw + nucs);
+      }
+      S.dt = S.n_act + nucs > 0 ? S.da : S.dn;
+      S.grown = S.grown_s;
+      S.n_orient += nucs;
+      S.grain += nucs;
+      S.liquid -= nucs;
+      // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
+      S.nucs = nucs;
+      S.n = nw + nucs;
+      S.lo = 0;
+      S.processed = 0;
+      S.gen_end = nA;
+      S.caps_all = 0;
+      S.died = 0;
+      S.gen = 0;
+      S.list = GenList{d.wlist, nw, S.a_len};
+      S.parents = GenList{nullptr, 0, 0};
     }
-    const long long nA = ld_volatile(&c->n_active_nuc[step & 1]);
-    const long long nucs = nA - a_len;  // nuclei of this step
-    const long long nw = ld_volatile(&c->n_woken[step & 1]);
-    dt = n_act + nucs > 0 ? da : dn;
-    grown = grown_s;
-    n_orient += nucs;
-    grain += nucs;
-    liquid -= nucs;
-    if (timer) {
-      s_clk[kNucs] += (unsigned long long)nucs;
-      s_clk[kScanned] += (unsigned long long)a_len;
-    }
-
-    // --- single_integration_step (CellularAutomataManager_3D.cpp:516-669) ---
-    long long n = nw + nucs, lo = 0, processed = 0, gen_end = nA, caps_all = 0, died = 0;
-    int kind = 0;
-    unsigned gen = 0;
-    GenList list{d.wlist, nw, a_len}, parents{nullptr, 0, 0};  // this generation / its parents
-    if (timer) s_clk[kGrown] += (unsigned long long)n;
-    while (n > 0) {
-      processed += n;
-      unsigned long long t_work = threadIdx.x == 0 ? now_ns() : 0ull;
-      claim_phase(d, cur, kind, lo, n, gen & 1u, list, parents, step, grown, &tests, &tests64);
+    __syncthreads();
+    while (S.n > 0) {
+      if (threadIdx.x == 0) {
+        S.processed += S.n;
+        S.t_work = now_ns();
+      }
+      claim_phase(d, S.cur, S.gen ? 1 : 0, S.lo, S.n, S.gen & 1u, S.list, S.parents, S.step, S.grown, &tests, &tests64);
       // the liquid counts around the previous generation's captures
-      if (gen > 0) capture_decrements(d, cur, n, parents, list.base, step, (int)((gen - 1) & 1u), &dec);
+      if (S.gen > 0) capture_decrements(d, S.cur, S.n, S.parents, S.list.base, S.step, (int)((S.gen - 1) & 1u), &dec);
       __syncthreads();
       if (threadIdx.x == 0) {
-        const unsigned long long w = now_ns() - t_work;
-        claim_busy += w;
+        const unsigned long long w = now_ns() - S.t_work;
+        S.claim_busy += w;
         if (d.phase_detail && w > ld_volatile(&c->phase_max_scratch[0])) atomicMax(&c->phase_max_scratch[0], w);
       }
       if (!(ok = grid_barrier(c))) break;
-      if (timer) {
-        t_now = now_ns();
-        s_clk[kClaim] += t_now - t_mark;
-        if (gen == 0) s_clk[kClaim0] += t_now - t_mark;
-        if (gen > 0) s_clk[kZero] += ld_volatile(&c->zn[(gen - 1) & 1u]);  // reset in this generation's resolve
-        t_mark = t_now;
-        if (d.phase_detail) {
-          s_clk[kClaimMax] += ld_volatile(&c->phase_max_scratch[0]);
-          c->phase_max_scratch[0] = 0ull;
+      if (threadIdx.x == 0) {
+        if (timer) {
+          const unsigned long long t_now = now_ns();
+          s_clk[kClaim] += t_now - S.t_mark;
+          if (S.gen == 0) s_clk[kClaim0] += t_now - S.t_mark;
+          if (S.gen > 0) s_clk[kZero] += ld_volatile(&c->zn[(S.gen - 1) & 1u]);  // reset in this generation's resolve
+          S.t_mark = t_now;
+          if (d.phase_detail) {
+            s_clk[kClaimMax] += ld_volatile(&c->phase_max_scratch[0]);
+            c->phase_max_scratch[0] = 0ull;
+          }
+          c->claim_next = 0ull;  // the next claim phase is two barriers away
         }
-        c->claim_next = 0ull;  // the next claim phase is two barriers away
+        S.t_work = now_ns();
+        S.w_mark = 0;  // busy time of a separate marking pass
       }
-      t_work = threadIdx.x == 0 ? now_ns() : 0ull;
-      unsigned long long w_mark = 0;  // busy time of a separate marking pass (thread 0)
-      if (!mark_in_resolve(n)) {
-        mark_phase(d, n, gen & 1u, d.act[cur], list);
+      __syncthreads();
+      if (!mark_in_resolve(S.n)) {
+        mark_phase(d, S.n, S.gen & 1u, d.act[S.cur], S.list);
         __syncthreads();
-        if (threadIdx.x == 0) w_mark = now_ns() - t_work;
+        if (threadIdx.x == 0) S.w_mark = now_ns() - S.t_work;
         if (!(ok = grid_barrier(c))) break;
         if (timer) c->mark_next = 0ull;  // the next marking pass is two barriers away
-        t_work = threadIdx.x == 0 ? now_ns() : 0ull;
+        if (threadIdx.x == 0) S.t_work = now_ns();
+        __syncthreads();
       }
-      if (!(ok = resolve_phase(d, cur, n, step, gen & 1u, list, gen > 0 ? (int)((gen - 1) & 1u) : -1, gen == 1,
-                               (int)(gen & 1u), smem, &gone_now, &gone_next)))
+      if (!(ok = resolve_phase(d, S.cur, S.n, S.step, S.gen & 1u, S.list, S.gen > 0 ? (int)((S.gen - 1) & 1u) : -1,
+                               S.gen == 1, (int)(S.gen & 1u), smem, &gone_now, &gone_next)))
         break;
-      flush_departures(c, step, gone_now, gone_next);
+      flush_departures(c, S.step, gone_now, gone_next);
       if (threadIdx.x == 0) {
-        const unsigned long long w = now_ns() - t_work + w_mark;
-        resolve_busy += w;
+        const unsigned long long w = now_ns() - S.t_work + S.w_mark;
+        S.resolve_busy += w;
         if (d.phase_detail && w > ld_volatile(&c->phase_max_scratch[1])) atomicMax(&c->phase_max_scratch[1], w);
       }
       if (!(ok = grid_barrier(c))) break;
-      if (timer) {
-        t_now = now_ns();
-        s_clk[kResolve] += t_now - t_mark;
-        t_mark = t_now;
-        if (d.phase_detail) {
-          s_clk[kResolveMax] += ld_volatile(&c->phase_max_scratch[1]);
-          c->phase_max_scratch[1] = 0ull;
+      if (threadIdx.x == 0) {
+        if (timer) {
+          const unsigned long long t_now = now_ns();
+          s_clk[kResolve] += t_now - S.t_mark;
+          S.t_mark = t_now;
+          if (d.phase_detail) {
+            s_clk[kResolveMax] += ld_volatile(&c->phase_max_scratch[1]);
+            c->phase_max_scratch[1] = 0ull;
+          }
         }
+        const long long caps = ld_volatile(&c->gen_n);  // envelopes of the next generation
+        S.died += S.n - ld_volatile(&c->gen_surv);      // deactivated at their turn
+        S.lo = S.grain;  // their ids follow on
+        S.grain += caps;
+        S.liquid -= caps;
+        S.caps_all += caps;
+        if (timer) s_clk[kCaps] += (unsigned long long)caps;
+        S.n = caps;
+        ++S.gen;
+        S.parents = S.list;
+        S.list = GenList{nullptr, 0, S.gen_end};  // appended to the list after the previous generation
+        S.gen_end += caps;
       }
-      const long long caps = ld_volatile(&c->gen_n);  // envelopes of the next generation
-      died += n - ld_volatile(&c->gen_surv);          // deactivated at their turn
-      lo = grain;  // their ids follow on
-      grain += caps;
-      liquid -= caps;
-      caps_all += caps;
-      if (timer) s_clk[kCaps] += (unsigned long long)caps;
-      n = caps;
-      kind = 1;
-      ++gen;
-      parents = list;
-      list = GenList{nullptr, 0, gen_end};  // appended to the list after the previous generation
-      gen_end += caps;
+      __syncthreads();
     }
     if (!ok) break;
-    // step end (CellularAutomataManager_3D.cpp:653-659): every block advances
-    // the same locals from counts final at the last barrier, so no further
-    // barrier is needed
-    n_act = n_act + nucs + caps_all - died - (long long)ld_volatile(&c->deaths[step % 3]);
-    a_len = gen_end;
-    time = time + dt;
-    ++step;
-    done = liquid == 0;
-    if (timer) {
-      s_clk[kGens] += gen;
-      s_clk[kProc] += (unsigned long long)processed;
+    // step end (CellularAutomataManager_3D.cpp:653-659), from counts final
+    // at the last barrier
+    if (threadIdx.x == 0) {
+      S.n_act = S.n_act + S.nucs + S.caps_all - S.died - (long long)ld_volatile(&c->deaths[S.step % 3]);
+      S.a_len = S.gen_end;
+      S.time = S.time + S.dt;
+      ++S.step;
+      S.done = S.liquid == 0;
+      if (timer) {
+        s_clk[kGens] += S.gen;
+        s_clk[kProc] += (unsigned long long)S.processed;
+      }
     }
+    __syncthreads();
   }
   if (ok && timer) {
     // the realm's state for the host and the next launch
-    c->step = step;
-    c->time = time;
-    c->dt = dt;
-    c->n_active = n_act;
-    c->a_len = a_len;
-    c->grown = grown;
-    c->compactions = compactions;
-    c->n_orient = n_orient;
-    c->next_grain = grain;
-    c->liquid = liquid;
-    c->cur_list = cur;
-    c->done = done ? 1 : 0;
+    c->step = S.step;
+    c->time = S.time;
+    c->dt = S.dt;
+    c->n_active = S.n_act;
+    c->a_len = S.a_len;
+    c->grown = S.grown;
+    c->compactions = S.compactions;
+    c->n_orient = S.n_orient;
+    c->next_grain = S.grain;
+    c->liquid = S.liquid;
+    c->cur_list = S.cur;
+    c->done = S.done ? 1 : 0;
     c->keys_scanned += s_clk[kScanned];
     c->zero_events += s_clk[kZero];
     c->ns_nucleation += s_clk[kNuc];
@@ -1372,7 +1411,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     c->grains_processed += s_clk[kProc];
     c->captures += s_clk[kCaps];
     c->nucleations += s_clk[kNucs];
-    c->ns_step_end += now_ns() - t_mark;
+    c->ns_step_end += now_ns() - S.t_mark;
   }
   // statistics: one atomic per warp
 #pragma unroll
@@ -1385,11 +1424,11 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   }
   if ((threadIdx.x & 31) == 0) {
     if (threadIdx.x == 0) {
-      if (claim_busy) atomicAdd(&c->ns_claim_work_sum, claim_busy);
-      if (resolve_busy) atomicAdd(&c->ns_resolve_work_sum, resolve_busy);
-      if (nuc_busy) atomicAdd(&c->ns_nuc_work_sum, nuc_busy);
-      if (wake_busy) atomicAdd(&c->ns_wake_work_sum, wake_busy);
-      if (compact_busy) atomicAdd(&c->ns_compact_work_sum, compact_busy);
+      if (S.claim_busy) atomicAdd(&c->ns_claim_work_sum, S.claim_busy);
+      if (S.resolve_busy) atomicAdd(&c->ns_resolve_work_sum, S.resolve_busy);
+      if (S.nuc_busy) atomicAdd(&c->ns_nuc_work_sum, S.nuc_busy);
+      if (S.wake_busy) atomicAdd(&c->ns_wake_work_sum, S.wake_busy);
+      if (S.compact_busy) atomicAdd(&c->ns_compact_work_sum, S.compact_busy);
     }
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);
@@ -1401,12 +1440,19 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
 
 __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(PlainDevice d, long long step_limit) {
   __shared__ unsigned long long smem[kWarps + 2];
+  // the descriptor in shared memory: the phases take it by reference, and a
+  // reference to the kernel parameter would make every thread keep a copy of
+  // it on its stack (local memory)
+  __shared__ PlainDevice sd;
   if (threadIdx.x == 0) {
     t_nb = gridDim.x;
     t_b = blockIdx.x;
   }
+  const int *src = (const int *)&d;
+  int *dst = (int *)&sd;
+  for (int w = threadIdx.x; w < (int)(sizeof(PlainDevice) / 4); w += blockDim.x) dst[w] = src[w];
   __syncthreads();
-  run_realm(d, step_limit, smem);
+  run_realm(sd, step_limit, smem);
 }
 
 // One bitmap word (32 cells) of the initial field: cells past the grid count
