@@ -160,8 +160,14 @@ __device__ __forceinline__ bool team_barrier(unsigned *count, unsigned *gen_word
   return s_bar_ok != 0;
 }
 
-// Barrier over the blocks that run the realm; false when it failed.
-__device__ __forceinline__ bool grid_barrier(PlainCtrl *c) { return team_barrier(&c->bar_count, &c->bar_gen, &c->error); }
+// Barrier over the blocks that run the realm; false when it failed. Block 0
+// adds its time inside the barrier to ns_barrier_block0.
+__device__ __forceinline__ bool grid_barrier(PlainCtrl *c) {
+  const unsigned long long t0 = (t_b == 0 && threadIdx.x == 0) ? now_ns() : 0ull;
+  const bool ok = team_barrier(&c->bar_count, &c->bar_gen, &c->error);
+  if (t_b == 0 && threadIdx.x == 0) c->ns_barrier_block0 += now_ns() - t0;
+  return ok;
+}
 
 // Exclusive scan of one u64 per thread over the block; *total = block sum.
 __device__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long *smem,
@@ -361,8 +367,8 @@ struct RankSched {
   int *error;
   bool warp;
   bool own_chunk = true;  // warp mode: the first chunk is the warp's own
-  __device__ RankSched(long long n_, unsigned long long *c, int *err)
-      : n(n_), counter(c), error(err), warp(t_nb <= 64 || n_ <= 1024ll * t_nb) {
+  __device__ RankSched(long long n_, unsigned long long *c, int *err, int warp_sched)
+      : n(n_), counter(c), error(err), warp(t_nb <= 64 || n_ <= (long long)warp_sched * t_nb) {
     if (!warp) {
       if (threadIdx.x == 0) {
         set_block_chunks(n);
@@ -907,7 +913,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
   // Claims need no order: warps or blocks take chunks of consecutive ranks
   // from a shared counter until none is left, so those that drew cheap
   // envelopes (few liquid neighbours) take more chunks.
-  RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error);
+  RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error, d.warp_sched);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e)) {
@@ -1072,7 +1078,7 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
 // claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
 __device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *act, GenList list) {
-  RankSched sched(n, &d.ctrl->mark_next, &d.ctrl->error);
+  RankSched sched(n, &d.ctrl->mark_next, &d.ctrl->error, d.warp_sched);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e))
@@ -1173,7 +1179,7 @@ struct RealmState {
   GenList list, parents;  // this generation / its parents
   // thread 0's busy time per kind of work, added to the control block once
   // per launch; block 0's phase clock
-  unsigned long long claim_busy, resolve_busy, nuc_busy, wake_busy, compact_busy, t_mark, t_work, w_mark;
+  unsigned long long claim_busy, resolve_busy, nuc_busy, wake_busy, compact_busy, dec_busy, t_mark, t_work, w_mark;
 };
 
 __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned long long *smem) {
@@ -1204,7 +1210,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     S.cur = ld_volatile(&c->cur_list);
     S.done = ld_volatile(&c->done) != 0;
     S.t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
-    S.claim_busy = S.resolve_busy = S.nuc_busy = S.wake_busy = S.compact_busy = 0ull;
+    S.claim_busy = S.resolve_busy = S.nuc_busy = S.wake_busy = S.compact_busy = S.dec_busy = 0ull;
     S.t_mark = now_ns();
   }
   if (site_tiles(d)) {
@@ -1299,7 +1305,11 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       }
       claim_phase(d, S.cur, S.gen ? 1 : 0, S.lo, S.n, S.gen & 1u, S.list, S.parents, S.step, S.grown, &tests, &tests64);
       // the liquid counts around the previous generation's captures
-      if (S.gen > 0) capture_decrements(d, S.cur, S.n, S.parents, S.list.base, S.step, (int)((S.gen - 1) & 1u), &dec);
+      if (S.gen > 0) {
+        const unsigned long long td = threadIdx.x == 0 ? now_ns() : 0ull;
+        capture_decrements(d, S.cur, S.n, S.parents, S.list.base, S.step, (int)((S.gen - 1) & 1u), &dec);
+        if (threadIdx.x == 0) S.dec_busy += now_ns() - td;
+      }
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - S.t_work;
@@ -1429,6 +1439,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       if (S.nuc_busy) atomicAdd(&c->ns_nuc_work_sum, S.nuc_busy);
       if (S.wake_busy) atomicAdd(&c->ns_wake_work_sum, S.wake_busy);
       if (S.compact_busy) atomicAdd(&c->ns_compact_work_sum, S.compact_busy);
+      if (S.dec_busy) atomicAdd(&c->ns_dec_work_sum, S.dec_busy);
     }
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);
@@ -1817,6 +1828,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.ncells = (int64_t)g.nxyg * g.nzg;
   d.nsites = nsites;
   d.gcap = n;
+  d.warp_sched = kWarpSched;
   d.orient = (uint32_t *)orient;
   d.site_cell = site_cell;
   d.site_dtc = site_dtc;

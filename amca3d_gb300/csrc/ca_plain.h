@@ -53,6 +53,8 @@ constexpr long long kWakeAll = 2048;
 // The wake scan reads keys in tiles of this many positions; key arrays hold
 // that many more entries than the list can (the tail of the last tile).
 constexpr long long kKeyTile = 128;
+// Default of PlainDevice::warp_sched.
+constexpr int kWarpSched = 1024;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values
@@ -104,6 +106,8 @@ struct PlainCtrl {
   unsigned long long ns_claim_work_sum, ns_claim_work_max;  // per-block busy time in claim phases
   unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
   unsigned long long ns_nuc_work_sum, ns_wake_work_sum, ns_compact_work_sum;  // per-block busy time, summed
+  unsigned long long ns_dec_work_sum;    // per-block busy time of the liquid-count decrement passes, summed
+  unsigned long long ns_barrier_block0;  // block 0's time inside grid barriers (arrival to release)
   unsigned long long phase_max_scratch[2];             // running max of the current phase
   unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase
   unsigned long long mark_next;                        // next rank batch of a separate marking pass
@@ -138,6 +142,7 @@ struct PlainDevice {
   float h32;
   float coord_err;  // bound on FP64 cell-centre rounding, per component
   int phase_detail; // nonzero: also gather the slowest block's busy time per phase
+  int warp_sched;   // ranks per block of the team up to which claims are handed out warp by warp (else block by block)
   // arrays
   uint32_t *orient;
   uint32_t *solid;    // 1 bit per cell: solid at the start of the current generation (ghosts included)

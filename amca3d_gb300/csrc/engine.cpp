@@ -183,6 +183,10 @@ struct amca_t {
     // and phase, so it is gathered only on request
     const char *detail = getenv("AMCA_PHASE_DETAIL");
     d.phase_detail = detail && detail[0] && detail[0] != '0' ? 1 : 0;
+    // claims are handed out warp by warp for generations up to this many
+    // ranks per block of the team, block by block above (AMCA_WARP_SCHED)
+    d.warp_sched = kWarpSched;
+    if (const char *w = getenv("AMCA_WARP_SCHED")) d.warp_sched = std::max(1, atoi(w));
     d.ncells = (int64_t)g.nxyg * g.nzg;
     d.nsites = nsites;
     d.gcap = (int64_t)c.nx * c.ny * c.nz;
@@ -1213,6 +1217,8 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->detail_ms[0] = c.ns_nuc_work_sum * 1e-6 / nb;
     s->detail_ms[1] = c.ns_wake_work_sum * 1e-6 / nb;
     s->detail_ms[2] = c.ns_compact_work_sum * 1e-6 / nb;
+    s->detail_ms[3] = c.ns_dec_work_sum * 1e-6 / nb;
+    s->detail_ms[4] = c.ns_barrier_block0 * 1e-6;
   });
 }
 
