@@ -538,9 +538,10 @@ constexpr int kZeroBuf = 512;
 // own entries count their liquid neighbours from the bitmap, which has these
 // captures). A decrement by a later rank (capturer beyond the entry) is
 // recorded in late[]; a count reaching zero goes to the zero list of parity
-// zpar, through a block buffer. The (capture, neighbour) pairs are spread over
-// the team, four per thread and pass so that their loads overlap.
-__device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, long long n, GenList parents,
+// zpar, through a block buffer. The captures are spread over the team, one
+// per thread and pass (positions fit 31 bits: the list holds at most one
+// entry per interior cell).
+__device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, long long n, const GenList &parents,
                                                 long long limit, long long step, int zpar,
                                                 unsigned long long *stat_dec) {
   __shared__ int s_zero[kZeroBuf];
@@ -550,45 +551,37 @@ __device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, l
   __syncthreads();
   const Grid &g = d.grid;
   const EnvRec *act = d.act[cur];
-  const long long items = n * 26;
-  const long long stride = (long long)t_nb * kBlock * 4;
-  for (long long i0 = ((long long)t_b * kBlock + threadIdx.x) * 4; i0 < items; i0 += stride) {
-    int m[4], q[4], old[4];
-    long long pc[4];
+  int32_t *nliq = d.nliq[cur];
+  const int lim = (int)limit;
+  for (long long k = (long long)t_b * kBlock + threadIdx.x; k < n; k += (long long)t_nb * kBlock) {
+    // one capture per thread: its cell, then the 26 map entries around it
+    // at once, then the decrements (independent atomics; the zero tests
+    // after all of them)
+    const uint32_t rec = d.child[k];
+    const int pc = (int)parents.at((long long)(rec >> 5));
+    int di, dj, dk;
+    const int cell = act[pc].cell + nbr_delta(g, (int)(rec & 31u), di, dj, dk);
+    int q[26];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const long long i = i0 + j;
-      m[j] = -1;
-      pc[j] = 0;
-      if (i < items) {
-        const long long k = i / 26;
-        const uint32_t rec = d.child[k];
-        int di, dj, dk;
-        pc[j] = parents.at((long long)(rec >> 5));
-        const int cell = act[pc[j]].cell + nbr_delta(g, (int)(rec & 31u), di, dj, dk);
-        m[j] = cell + nbr_delta(g, (int)(i - k * 26), di, dj, dk);
-      }
-    }
+    for (int nb = 0; nb < 26; ++nb) q[nb] = d.pos[cell + nbr_delta(g, nb, di, dj, dk)];
+    uint32_t zero = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) q[j] = m[j] >= 0 ? d.pos[m[j]] : -1;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      old[j] = 0;
-      if (q[j] >= 0 && q[j] < limit) {
+    for (int nb = 0; nb < 26; ++nb) {
+      if (q[nb] >= 0 && q[nb] < lim) {
         ++*stat_dec;
-        if (pc[j] > q[j]) d.late[q[j]] = (int32_t)step;
-        old[j] = atomicSub(d.nliq[cur] + q[j], 1);
+        if (pc > q[nb]) d.late[q[nb]] = (int32_t)step;
+        zero |= (atomicSub(nliq + q[nb], 1) == 1 ? 1u : 0u) << nb;
       }
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (old[j] != 1) continue;
-      const unsigned k = atomicAdd(&s_nz, 1u);
-      if (k < (unsigned)kZeroBuf) {
-        s_zero[k] = q[j];
+    for (int nb = 0; nb < 26; ++nb) {
+      if (!((zero >> nb) & 1u)) continue;
+      const unsigned z = atomicAdd(&s_nz, 1u);
+      if (z < (unsigned)kZeroBuf) {
+        s_zero[z] = q[nb];
       } else {
-        const unsigned long long z = atomicAdd(&d.ctrl->zn[zpar], 1ull);
-        d.zlist[zpar][z] = q[j];
+        const unsigned long long zi = atomicAdd(&d.ctrl->zn[zpar], 1ull);
+        d.zlist[zpar][zi] = q[nb];
       }
     }
   }
@@ -902,7 +895,7 @@ __device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int z
 // count and next wake key.
 // ---------------------------------------------------------------------------
 __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind, long long lo, long long n, unsigned par,
-                            GenList list, GenList parents, long long step, double grown,
+                            const GenList &list, const GenList &parents, long long step, double grown,
                             unsigned long long *stat_tests, unsigned long long *stat_tests64) {
   const Grid &g = d.grid;
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
@@ -1077,7 +1070,8 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
 // Marking pass for large generations: dynamic chunks of ranks, as in the
 // claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
-__device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *act, GenList list) {
+__device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *act,
+                                       const GenList &list) {
   RankSched sched(n, &d.ctrl->mark_next, &d.ctrl->error, d.warp_sched);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
@@ -1103,7 +1097,8 @@ __device__ __forceinline__ bool mark_in_resolve(long long n) { return n <= (long
 // for the next claim phase. The last block publishes the generation's
 // capture and survivor counts, which every block reads after the barrier.
 __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long long n, long long step, unsigned par,
-                                           GenList list, int zdec, bool zgen0, int zreset, unsigned long long *smem,
+                                           const GenList &list, int zdec, bool zgen0, int zreset,
+                                           unsigned long long *smem,
                                            unsigned *gone_now, unsigned *gone_next) {
   PlainCtrl *c = d.ctrl;
   const EnvRec *act = d.act[cur];
