@@ -54,7 +54,7 @@ constexpr long long kWakeAll = 2048;
 // that many more entries than the list can (the tail of the last tile).
 constexpr long long kKeyTile = 128;
 // Default of PlainDevice::warp_sched.
-constexpr int kWarpSched = 32;
+constexpr int kWarpSched = 128;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values
