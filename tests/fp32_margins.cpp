@@ -12,6 +12,9 @@
 //                lies within a few ulps of the half-diagonal L: tiny, unit
 //                and huge L, grids far from the origin, every octant and
 //                every neighbour direction.
+//   lower        the lower bound of |c'|_1 that captured_f32_lb returns with
+//                the same inputs (the plain kernel's wake keys) must never
+//                exceed the FP64 |c'|_1 of is_captured_f64, on the same pairs.
 //   interp       the FP32 interpolation of the remelting kernel and its bound
 //                must decide T < thr exactly as the FP64 interpolation does,
 //                or be undecided, for node values whose FP64 interpolation
@@ -71,7 +74,7 @@ double l1_local(const double *m, double gx, double gy, double gz) {
 }
 
 void containment(long n, int tier) {
-  long undecided = 0, wrong = 0;
+  long undecided = 0, wrong = 0, lower_wrong = 0;
   const double origins[4] = {0.0, 1.0e-2, -0.37, 2.5};
   const double hs[2] = {2.0e-6, 5.0e-4};
   const double lscale[4] = {1.0e-9, 0.7, 1.5, 1.0e3};  // L relative to h: tiny, unit, unit, huge
@@ -120,8 +123,10 @@ void containment(long n, int tier) {
     const float dxf = (float)(c[0] - own[0]), dyf = (float)(c[1] - own[1]), dzf = (float)(c[2] - own[2]);
     const float h32 = (float)h;
     const float errg = 4.76837158203125e-07f * (h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + coord_err;
-    const int f = amca::captured_f32(m32, (float)di * h32 - dxf, (float)dj * h32 - dyf, (float)dk * h32 - dzf, errg,
-                                     (float)L);
+    float lower;
+    const int f = amca::captured_f32_lb(m32, (float)di * h32 - dxf, (float)dj * h32 - dyf, (float)dk * h32 - dzf,
+                                        errg, (float)L, &lower);
+    if ((double)lower > s) ++lower_wrong;
     const bool exact = amca::is_captured_f64(m, ccx - c[0], ccy - c[1], ccz - c[2], L);
     if (f < 0)
       ++undecided;
@@ -129,6 +134,7 @@ void containment(long n, int tier) {
       ++wrong;
   }
   printf("containment%d %ld %ld %ld\n", tier, n, undecided, wrong);
+  printf("lower%d %ld 0 %ld\n", tier, n, lower_wrong);
 }
 
 void interp(long n, int tier) {

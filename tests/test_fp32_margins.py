@@ -6,6 +6,8 @@ compiled for the host without contraction; tests/fp32_margins.cpp):
   test of Octahedron::cell_is_captured on (envelope, neighbour) pairs with
   |c'|_1 within a few ulps of L, and at 2^-30..2^-6 relative distances: tiny,
   unit and huge half-diagonals, grids far from the origin, every neighbour;
+  and the lower bound of |c'|_1 behind the wake keys (never above the FP64
+  |c'|_1);
 * the remelting kernel's FP32 interpolation bound against the FP64
   interpolation (MapVoxelManager::evaluate_temperature) at the liquidus,
   nullMatTemp_ and nullMatTemp_ + 0.01;
@@ -40,7 +42,8 @@ def test_fp32_shortcuts_never_decide_wrongly():
     for line in out.strip().splitlines():
         name, n, und, wrong = line.split()
         res[name] = (int(n), int(und), int(wrong))
-    assert set(res) == {"containment0", "containment1", "containment2", "interp0", "interp1", "interp2", "capture"}
+    assert set(res) == {"containment0", "containment1", "containment2", "lower0", "lower1", "lower2", "interp0",
+                        "interp1", "interp2", "capture"}
     for name, (n, und, wrong) in res.items():
         assert wrong == 0, (name, res[name])
         assert n > 0
