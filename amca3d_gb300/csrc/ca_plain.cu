@@ -492,7 +492,7 @@ __device__ __forceinline__ double replay_growth(const double *dvh, double L, lon
 // A dead entry: never woken, and no longer found from its cell.
 __device__ __forceinline__ void tombstone(const PlainDevice &d, int cur, long long q, int cell) {
   d.key[cur][q] = __int_as_float(0x7fc00000);
-  d.pos[cell] = -1;
+  d.cellw[cell] = kNoEntry;
 }
 
 // The list positions of a generation's ranks: generation 0 is the woken
@@ -517,10 +517,11 @@ __device__ __noinline__ unsigned nucleus_neighbours(const PlainDevice &d, int cu
   for (int nb = 0; nb < 26; ++nb) {
     int di, dj, dk;
     const int m = cell + nbr_delta(g, nb, di, dj, dk);
-    const int q = d.pos[m];
-    if (q < 0) continue;
+    const uint32_t w = atomicSub(d.cellw + m, 1u);
+    if (!has_entry(w)) continue;
     ++*stat_dec;
-    if (atomicSub(d.nliq[cur] + q, 1) == 1 && !woken(d.key[cur][q], wake_bound(grown), all)) {
+    const int q = (int)(w >> 5);
+    if ((w & 31u) == 1u && !woken(d.key[cur][q], wake_bound(grown), all)) {
       tombstone(d, cur, q, m);
       ++gone;
     }
@@ -533,17 +534,17 @@ constexpr int kZeroBuf = 512;
 
 // The liquid counts around the n cells that the previous generation captured
 // (its child records, this generation's ranks; `parents` gives the
-// capturers' positions): one decrement for the entry on each neighbour cell
-// listed before this generation (position below `limit`; this generation's
-// own entries count their liquid neighbours from the bitmap, which has these
-// captures). A decrement by a later rank (capturer beyond the entry) is
-// recorded in late[]; a count reaching zero goes to the zero list of parity
-// zpar, through a block buffer. The captures are spread over the team, one
-// per thread and pass (positions fit 31 bits: the list holds at most one
-// entry per interior cell).
+// capturers' positions): one atomic decrement of the cell word of each
+// neighbour cell, whose old value says which entry (if any) lives there and
+// its count before. This generation's own entries still hold no-entry words
+// (they set theirs in the resolve phase, from the bitmap, which has these
+// captures), and a no-entry word never reaches a zero count. A decrement by
+// a later rank (capturer beyond the entry) is recorded in late[]; a count
+// reaching zero goes to the zero list of parity zpar, through a block buffer.
+// The captures are spread over the team, one per thread and pass, the 26
+// atomics issued before any result is used.
 __device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, long long n, const GenList &parents,
-                                                long long limit, long long step, int zpar,
-                                                unsigned long long *stat_dec) {
+                                                long long step, int zpar, unsigned long long *stat_dec) {
   __shared__ int s_zero[kZeroBuf];
   __shared__ unsigned s_nz;
   __shared__ unsigned long long s_zbase;
@@ -551,37 +552,27 @@ __device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, l
   __syncthreads();
   const Grid &g = d.grid;
   const EnvRec *act = d.act[cur];
-  int32_t *nliq = d.nliq[cur];
-  const int lim = (int)limit;
   for (long long k = (long long)t_b * kBlock + threadIdx.x; k < n; k += (long long)t_nb * kBlock) {
-    // one capture per thread: its cell, then the 26 map entries around it
-    // at once, then the decrements (independent atomics; the zero tests
-    // after all of them)
     const uint32_t rec = d.child[k];
     const int pc = (int)parents.at((long long)(rec >> 5));
     int di, dj, dk;
     const int cell = act[pc].cell + nbr_delta(g, (int)(rec & 31u), di, dj, dk);
-    int q[26];
+    uint32_t w[26];
 #pragma unroll
-    for (int nb = 0; nb < 26; ++nb) q[nb] = d.pos[cell + nbr_delta(g, nb, di, dj, dk)];
-    uint32_t zero = 0;
-#pragma unroll
-    for (int nb = 0; nb < 26; ++nb) {
-      if (q[nb] >= 0 && q[nb] < lim) {
-        ++*stat_dec;
-        if (pc > q[nb]) d.late[q[nb]] = (int32_t)step;
-        zero |= (atomicSub(nliq + q[nb], 1) == 1 ? 1u : 0u) << nb;
-      }
-    }
+    for (int nb = 0; nb < 26; ++nb) w[nb] = atomicSub(d.cellw + cell + nbr_delta(g, nb, di, dj, dk), 1u);
 #pragma unroll
     for (int nb = 0; nb < 26; ++nb) {
-      if (!((zero >> nb) & 1u)) continue;
+      if (!has_entry(w[nb])) continue;
+      ++*stat_dec;
+      const int q = (int)(w[nb] >> 5);
+      if (pc > q) d.late[q] = (int32_t)step;
+      if ((w[nb] & 31u) != 1u) continue;
       const unsigned z = atomicAdd(&s_nz, 1u);
       if (z < (unsigned)kZeroBuf) {
-        s_zero[z] = q[nb];
+        s_zero[z] = q;
       } else {
         const unsigned long long zi = atomicAdd(&d.ctrl->zn[zpar], 1ull);
-        d.zlist[zpar][zi] = q[nb];
+        d.zlist[zpar][zi] = q;
       }
     }
   }
@@ -845,9 +836,8 @@ __device__ __noinline__ bool compact_phase(const PlainDevice &d, int cur, long l
       d.act[nxt][q] = en;
       d.key[nxt][q] = key[p];
       d.lstep[nxt][q] = d.lstep[cur][p];
-      d.nliq[nxt][q] = d.nliq[cur][p];
       d.late[q] = -1;
-      d.pos[en.cell] = (int32_t)q;
+      d.cellw[en.cell] = ((uint32_t)q << 5) | (d.cellw[en.cell] & 31u);
       ++*stat_moved;
     }
     off += __popc(bal);
@@ -924,7 +914,6 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
       en.L = replay_growth(d.dvh, en.L, (long long)lstep[p], step);
       act[p].L = en.L;
       lstep[p] = (int32_t)step;
-      if (r >= list.nw) d.pos[en.cell] = (int32_t)p;  // a nucleus of this step
     } else {
       // CellularAutomataManager_3D::capture_cell (:677-707) for the capture
       // recorded by the parent: decentred envelope from the parent's
@@ -954,7 +943,6 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
       have_centre = true;
       act[p] = en;
       lstep[p] = (int32_t)step;
-      d.pos[en.cell] = (int32_t)p;
       d.gx[en.id] = gxd;
       d.gy[en.id] = gyd;
       d.gz[en.id] = gzd;
@@ -967,9 +955,6 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
     uint32_t con = 0;
     // lower bound of |c'|_1 over the liquid neighbours it does not contain
     float t_lb = INFINITY;
-    // no decrement reaches this entry during the claim phase: its count is
-    // the liquid neighbours it sees now
-    d.nliq[cur][p] = __popc(liq);
     // cell_is_captured is false for a zero half-diagonal (tested on the bits:
     // an integer compare instead of one on the narrow FP64 pipe); such an
     // entry is looked at again next step
@@ -1133,7 +1118,13 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
     if (r < e) {
       const long long p = list.at(r);
       const int cell = act[p].cell;
-      if (!surv) tombstone(d, cur, p, cell);  // deactivated at its turn
+      if (!surv) {
+        tombstone(d, cur, p, cell);  // deactivated at its turn
+      } else {
+        // its cell word: position and the liquid neighbours it saw in the
+        // claim phase (this generation's captures come off in the next one)
+        d.cellw[cell] = ((uint32_t)p << 5) | (uint32_t)__popc(d.liq[r]);
+      }
       long long slot = (long long)((run + ex) >> 32);  // rank of the first child in the next generation
       uint32_t bits = cap;
       while (bits) {
@@ -1302,7 +1293,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       // the liquid counts around the previous generation's captures
       if (S.gen > 0) {
         const unsigned long long td = threadIdx.x == 0 ? now_ns() : 0ull;
-        capture_decrements(d, S.cur, S.n, S.parents, S.list.base, S.step, (int)((S.gen - 1) & 1u), &dec);
+        capture_decrements(d, S.cur, S.n, S.parents, S.step, (int)((S.gen - 1) & 1u), &dec);
         if (threadIdx.x == 0) S.dec_busy += now_ns() - td;
       }
       __syncthreads();
@@ -1463,7 +1454,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) plain_persistent_kernel(Pl
 
 // One bitmap word (32 cells) of the initial field: cells past the grid count
 // as solid.
-__device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *solid, uint32_t *claimed, int32_t *pos,
+__device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *solid, uint32_t *claimed, uint32_t *cellw,
                                                 const Grid &g, long long ncells, long long w) {
   uint32_t bits = 0;
   for (int b = 0; b < 32; ++b) {
@@ -1474,7 +1465,7 @@ __device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *soli
       cell_ijk(g, i, I, J, K);
       ghost = I == 0 || J == 0 || K == 0 || I == g.nxg - 1 || J == g.nyg - 1 || K == g.nzg - 1;
       orient[i] = ghost ? 0u : kLiquid;
-      pos[i] = -1;
+      cellw[i] = kNoEntry;
     }
     bits |= (ghost ? 1u : 0u) << b;
   }
@@ -1482,11 +1473,11 @@ __device__ __forceinline__ void init_field_word(uint32_t *orient, uint32_t *soli
   claimed[w] = 0u;
 }
 
-__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, int32_t *pos, Grid g,
+__global__ void init_field_kernel(uint32_t *orient, uint32_t *solid, uint32_t *claimed, uint32_t *cellw, Grid g,
                                   long long ncells) {
   const long long nwords = solid_words(ncells);
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (long long)gridDim.x * blockDim.x)
-    init_field_word(orient, solid, claimed, pos, g, ncells, w);
+    init_field_word(orient, solid, claimed, cellw, g, ncells, w);
 }
 
 // ---------------------------------------------------------------------------
@@ -1569,7 +1560,7 @@ __global__ void batch_reset_kernel(const PlainDevice *insts, int ninst, unsigned
   }
   const long long nwords = solid_words(d.ncells);
   for (long long w = tid; w < nwords; w += stride)
-    init_field_word(d.orient, d.solid, d.claimed, d.pos, d.grid, d.ncells, w);
+    init_field_word(d.orient, d.solid, d.claimed, d.cellw, d.grid, d.ncells, w);
 }
 
 // out[r] = realm r's control block.
@@ -1676,7 +1667,7 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
-  size_t ctrl, check, live, omat32, scanA, gx, gy, gz, gori, gcell, act[2], key[2], lstep[2], nliq[2], late, pos, wlist,
+  size_t ctrl, check, live, omat32, scanA, gx, gy, gz, gori, gcell, act[2], key[2], lstep[2], late, cellw, wlist,
       zlist[2], dvh, liq, con, child, solid, claimed, scanB, scanC, scanD, total;
   // n interior cells, s sites, `cells` ghost-inclusive cells; the caller
   // bounds all three (see kNoAllocMaxCells) so that no size below wraps
@@ -1701,12 +1692,11 @@ struct NoAllocLayout {
       act[b] = take((size_t)n * sizeof(EnvRec));
       key[b] = take((size_t)(n + kKeyTile) * 4);  // the wake scan reads whole tiles
       lstep[b] = take((size_t)n * 4);
-      nliq[b] = take((size_t)n * 4);
       zlist[b] = take((size_t)n * 4);
     }
     late = take((size_t)n * 4);
     wlist = take((size_t)n * 4);
-    pos = take((size_t)cells * 4);
+    cellw = take((size_t)cells * 4);
     dvh = take((size_t)kDvRing * 8);
     liq = take((size_t)n * 4);
     con = take((size_t)n * 4);
@@ -1841,12 +1831,11 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
     d.act[b] = (EnvRec *)(base + lay.act[b]);
     d.key[b] = (float *)(base + lay.key[b]);
     d.lstep[b] = (int32_t *)(base + lay.lstep[b]);
-    d.nliq[b] = (int32_t *)(base + lay.nliq[b]);
     d.zlist[b] = (int32_t *)(base + lay.zlist[b]);
   }
   d.late = (int32_t *)(base + lay.late);
   d.wlist = (int32_t *)(base + lay.wlist);
-  d.pos = (int32_t *)(base + lay.pos);
+  d.cellw = (uint32_t *)(base + lay.cellw);
   d.dvh = (double *)(base + lay.dvh);
   d.liq = (uint32_t *)(base + lay.liq);
   d.con = (uint32_t *)(base + lay.con);
@@ -1943,7 +1932,7 @@ cudaError_t plain_barrier_selftest(int blocks, int parties, long long wait_ns, i
 }
 
 cudaError_t plain_init_field(const PlainDevice &d, cudaStream_t s) {
-  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.solid, d.claimed, d.pos, d.grid, d.ncells);
+  init_field_kernel<<<1024, 256, 0, s>>>(d.orient, d.solid, d.claimed, d.cellw, d.grid, d.ncells);
   return cudaGetLastError();
 }
 

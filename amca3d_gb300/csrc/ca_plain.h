@@ -18,10 +18,11 @@
 //               key[2]   f32 wake key (cumulative growth at which the entry may
 //                        contain a liquid neighbour; NaN = dead)
 //               lstep[2] i32 step up to which the record's half-diagonal is grown
-//               nliq[2]  i32 liquid neighbours now
 //   late        i32 per entry: step of the last capture next to it by a later rank
-//   pos         i32 per ghost-inclusive cell: list position of the live envelope
-//               on the cell, -1 for none
+//   cellw       u32 per ghost-inclusive cell: list position of the live envelope
+//               on the cell << 5 | its liquid neighbours now; kNoEntry (all
+//               ones) for none, which the at most 26 decrements a cell sees
+//               while it has no envelope never bring to a zero count
 //   wlist       i32 per entry: positions woken this step, in walk order
 //   zlist[2]    i32 per entry: entries whose liquid count reached zero in a
 //               generation, by generation parity
@@ -44,7 +45,8 @@ namespace amca {
 
 // Look-back status words per phase: an upper bound on the persistent grid.
 constexpr long long kStatusWords = 4096;
-// Child records pack an envelope id into 27 bits.
+// Child records pack an envelope rank into 27 bits, cell words a list
+// position: a realm has fewer than kMaxCells interior cells.
 constexpr long long kMaxCells = 1ll << 27;
 // Steps of the growth-increment ring; every live entry is woken (its record
 // brought up to date) at least every kWakeAll steps, well inside the ring.
@@ -53,6 +55,10 @@ constexpr long long kWakeAll = 2048;
 // The wake scan reads keys in tiles of this many positions; key arrays hold
 // that many more entries than the list can (the tail of the last tile).
 constexpr long long kKeyTile = 128;
+// Cell word of a cell without an envelope; its position field (all ones)
+// is never a list position (the list holds fewer than kMaxCells entries).
+constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
+AMCA_HD bool has_entry(uint32_t w) { return (w >> 5) != (kNoEntry >> 5); }
 // Default of PlainDevice::warp_sched.
 constexpr int kWarpSched = 128;
 
@@ -160,9 +166,8 @@ struct PlainDevice {
   EnvRec *act[2];
   float *key[2];
   int32_t *lstep[2];
-  int32_t *nliq[2];
   int32_t *late;
-  int32_t *pos;
+  uint32_t *cellw;
   int32_t *wlist;
   int32_t *zlist[2];
   double *dvh;

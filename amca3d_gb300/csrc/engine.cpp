@@ -140,8 +140,8 @@ struct amca_t {
 
   void initialize() {
     const PlainConfig &c = cfg;
-    if ((long long)c.nx * c.ny * c.nz > kMaxCells)
-      throw std::invalid_argument("grid too large: at most 2^27 interior cells per realm");
+    if ((long long)c.nx * c.ny * c.nz >= kMaxCells)
+      throw std::invalid_argument("grid too large: fewer than 2^27 interior cells per realm");
     prepare();
     CK(cudaSetDevice(device));
     const int64_t nsites = (int64_t)sites.cell.size();
@@ -210,12 +210,11 @@ struct amca_t {
         d.act[b] = a.take<EnvRec>(d.gcap);
         d.key[b] = a.take<float>(d.gcap + kKeyTile);  // the wake scan reads whole tiles
         d.lstep[b] = a.take<int32_t>(d.gcap);
-        d.nliq[b] = a.take<int32_t>(d.gcap);
         d.zlist[b] = a.take<int32_t>(d.gcap);
       }
       d.late = a.take<int32_t>(d.gcap);
       d.wlist = a.take<int32_t>(d.gcap);
-      d.pos = a.take<int32_t>(d.ncells);
+      d.cellw = a.take<uint32_t>(d.ncells);
       d.dvh = a.take<double>(kDvRing);
       d.liq = a.take<uint32_t>(d.gcap);
       d.con = a.take<uint32_t>(d.gcap);
