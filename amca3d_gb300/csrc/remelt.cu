@@ -363,6 +363,48 @@ __device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned n
   return s_ok != 0;
 }
 
+// The overlapped form of host_velocities for a request that fits the mapped
+// buffer: block 0 writes the temperatures and posts the request without
+// waiting; every block counts it (its s_host_seq names the answer it waits
+// for). Called by every block, uniformly.
+__device__ void host_post(const RemeltDevice &d, unsigned nh, bool min_hard, double minT) {
+  const unsigned total = nh + (min_hard ? 1u : 0u);
+  if (blockIdx.x == 0 && d.host != nullptr) {
+    for (unsigned k = threadIdx.x; k < total; k += blockDim.x) d.host->T[k] = k < nh ? d.hard_T[k] : minT;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      d.host->n = total;
+      __threadfence_system();
+      st_release_sys(&d.host->seq_req, s_host_seq + 1);
+      s_clk[kClkHostCalls] += 1;
+      s_clk[kClkHostVel] += total;
+    }
+  }
+  if (threadIdx.x == 0) s_host_seq += 1;
+}
+
+// Thread 0 waits (bounded) for the answer to the block's last request; the
+// block proceeds after a barrier. A wait that runs out (or no host buffer)
+// sets the error word, which the next grid barrier reports.
+__device__ void host_wait_block(const RemeltDevice &d, RemeltCtrl *c) {
+  if (threadIdx.x == 0) {
+    const unsigned long long t0 = now_ns();
+    if (d.host == nullptr) {
+      atomicCAS(&c->error, 0, kRemeltErrHost);
+    } else {
+      while (ld_acquire_sys(&d.host->seq_done) != s_host_seq) {
+        if (now_ns() - t0 > kWaitNs) {
+          atomicCAS(&c->error, 0, kRemeltErrHost);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (blockIdx.x == 0) s_clk[kClkHost] += now_ns() - t0;
+  }
+  __syncthreads();
+}
+
 __device__ __forceinline__ void elem_nodes(const int nn[3], int64_t e, int64_t nid[8]) {
   const int64_t ncx = nn[0] - 1, ncy = nn[1] - 1;
   const int64_t i = e % ncx, j = (e / ncx) % ncy, k = e / (ncx * ncy);
@@ -1267,6 +1309,9 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
               if (slot < d.list_cap) {
                 d.hard_idx[slot] = (int32_t)q;
                 d.hard_T[slot] = Targ;
+                // the host's answer, slot `slot`, is taken in phase D
+                // (velocities are never negative)
+                d.fvel[q] = -1.0 - (double)slot;
               }
             }
           }
@@ -1299,12 +1344,24 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     __syncthreads();
     const bool min_hard = s_min_hard != 0;
     double vmin = s_vmin;
-    {
-      const unsigned nh = ld_volatile(&c->n_hard);
-      if (nh > 0 || min_hard) {  // uniform: every block read the same counter and key
-        if (blockIdx.x == 0 && !host_velocities(d, c, nh, min_hard, minT)) atomicCAS(&c->error, 0, kRemeltErrHost);
-        if (!(ok = grid_barrier(d, 5))) break;
-        if (min_hard) vmin = ld_volatile(&c->vmin);
+    // The host evaluates the hard velocities while the blocks grow and claim
+    // with the others: block 0 posts the request, every block counts it, and
+    // a block waits for the answer only before its own hard cells (or before
+    // dt, when the velocity at the minimum temperature is one of them). A
+    // request larger than the mapped buffer goes in chunks, behind a barrier.
+    const unsigned nh = ld_volatile(&c->n_hard);  // uniform: every block read the same counter and key
+    const bool ask = nh > 0 || min_hard;
+    const bool overlap = ask && nh + 1u <= (unsigned)kHostVelCap;
+    if (ask && !overlap) {
+      if (blockIdx.x == 0 && !host_velocities(d, c, nh, min_hard, minT)) atomicCAS(&c->error, 0, kRemeltErrHost);
+      if (!(ok = grid_barrier(d, 5))) break;
+      if (min_hard) vmin = ld_volatile(&c->vmin);
+    }
+    if (overlap) {
+      host_post(d, nh, min_hard, minT);
+      if (min_hard) {
+        host_wait_block(d, c);
+        vmin = ld_volatile(&d.host->v[nh]);
       }
     }
     const double maxV = vmin > 0 ? vmin : 0;
@@ -1314,16 +1371,12 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     const double dT = (d.dt_cap < dT_) ? d.dt_cap : dT_;  // setup_time_step_for_coupling of an external solver
 
     // ===== D: grow and claim (Remelting.cpp:545-622) =====
-    for (int64_t q = spread_begin(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
-      const int32_t cell = d.flagged[par][q];
-      int I, J, K;
-      cell_ijk(g, cell, I, J, K);
-      if (ghost(g, I, J, K)) continue;
-      if (d.grain[cell] < 0) continue;
-      const double vel = d.fvel[q];
+    // one flagged cell: growth by dT * vel and its claims (atomicMin of the
+    // sweep position: the order cells are taken in does not matter)
+    auto grow_claim = [&](int32_t cell, int I, int J, int K, double vel) {
       const double L = d.glen[cell] + dT * vel;
       d.glen[cell] = L;
-      if (L == 0) continue;  // Octahedron::cell_is_captured: a zero half-diagonal captures nothing
+      if (L == 0) return;  // Octahedron::cell_is_captured: a zero half-diagonal captures nothing
       const int32_t ori = d.gori[cell];
       const int32_t mine = INT_MIN + sweep_pos(g, I, J, K);
       const float dxf = d.gdx[cell], dyf = d.gdy[cell], dzf = d.gdz[cell];
@@ -1369,6 +1422,32 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
             if (slot < d.list_cap) d.claimed[slot] = nb;
           }
         }
+      }
+    };
+    bool pending = false;  // a hard velocity of this thread waits for the host's answer
+    for (int64_t q = spread_begin(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
+      const int32_t cell = d.flagged[par][q];
+      int I, J, K;
+      cell_ijk(g, cell, I, J, K);
+      if (ghost(g, I, J, K)) continue;
+      if (d.grain[cell] < 0) continue;
+      const double vel = d.fvel[q];
+      if (vel < 0) {
+        pending = true;
+        continue;
+      }
+      grow_claim(cell, I, J, K, vel);
+    }
+    if (overlap && __syncthreads_or(pending)) {  // uniform within the block
+      host_wait_block(d, c);
+      for (int64_t q = spread_begin(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
+        const double vel = d.fvel[q];
+        if (!(vel < 0)) continue;
+        const int32_t cell = d.flagged[par][q];
+        int I, J, K;
+        cell_ijk(g, cell, I, J, K);
+        if (ghost(g, I, J, K) || d.grain[cell] < 0) continue;
+        grow_claim(cell, I, J, K, ld_volatile(&d.host->v[(unsigned)(-1.0 - vel)]));
       }
     }
     if (gtid == 0) {
