@@ -531,6 +531,9 @@ __device__ __noinline__ unsigned nucleus_neighbours(const PlainDevice &d, int cu
 
 // Zero-count events a block gathers before adding them to a zero list.
 constexpr int kZeroBuf = 512;
+__shared__ int s_zero[kZeroBuf];
+__shared__ unsigned s_nz;
+__shared__ unsigned long long s_zbase;
 
 // The liquid counts around the n cells that the previous generation captured
 // (its child records, this generation's ranks; `parents` gives the
@@ -540,19 +543,16 @@ constexpr int kZeroBuf = 512;
 // (they set theirs in the resolve phase, from the bitmap, which has these
 // captures), and a no-entry word never reaches a zero count. A decrement by
 // a later rank (capturer beyond the entry) is recorded in late[]; a count
-// reaching zero goes to the zero list of parity zpar, through a block buffer.
-// The captures are spread over the team, one per thread and pass, the 26
-// atomics issued before any result is used.
-__device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, long long n, const GenList &parents,
-                                                long long step, int zpar, unsigned long long *stat_dec) {
-  __shared__ int s_zero[kZeroBuf];
-  __shared__ unsigned s_nz;
-  __shared__ unsigned long long s_zbase;
-  if (threadIdx.x == 0) s_nz = 0u;
-  __syncthreads();
+// reaching zero goes to the block's zero buffer (s_nz reset before), or to
+// the zero list of parity zpar once the buffer is full. Capture k goes to
+// the thread numbered k among `threads` ones; this thread is number t0. The
+// 26 atomics of a capture are issued before any result is used.
+__device__ __noinline__ void decrement_captures(const PlainDevice &d, int cur, long long n, const GenList &parents,
+                                                long long step, int zpar, long long t0, long long threads,
+                                                unsigned long long *stat_dec) {
   const Grid &g = d.grid;
   const EnvRec *act = d.act[cur];
-  for (long long k = (long long)t_b * kBlock + threadIdx.x; k < n; k += (long long)t_nb * kBlock) {
+  for (long long k = t0; k < n; k += threads) {
     const uint32_t rec = d.child[k];
     const int pc = (int)parents.at((long long)(rec >> 5));
     int di, dj, dk;
@@ -576,6 +576,11 @@ __device__ __noinline__ void capture_decrements(const PlainDevice &d, int cur, l
       }
     }
   }
+}
+
+// The block's buffered zero events into the zero list of parity zpar (every
+// thread of the block).
+__device__ __noinline__ void flush_zero_buffer(const PlainDevice &d, int zpar) {
   __syncthreads();
   const unsigned nz = s_nz < (unsigned)kZeroBuf ? s_nz : (unsigned)kZeroBuf;
   if (threadIdx.x == 0 && nz) s_zbase = atomicAdd(&d.ctrl->zn[zpar], (unsigned long long)nz);
@@ -884,9 +889,16 @@ __device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int z
 // (generation >= 1), neighbour tests, atomicMin claims, the entry's liquid
 // count and next wake key.
 // ---------------------------------------------------------------------------
+// With `dec` (generations after the first) the liquid counts around the
+// previous generation's captures are decremented in the same phase: the
+// first kDecWarps warps of every block do that first and then join the
+// claims, whose dynamic hand-out balances the difference, so the memory
+// latency of the decrements overlaps the FP64 decentring of the claims.
+constexpr int kDecWarps = 4;
 __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind, long long lo, long long n, unsigned par,
-                            const GenList &list, const GenList &parents, long long step, double grown,
-                            unsigned long long *stat_tests, unsigned long long *stat_tests64) {
+                            const GenList &list, const GenList &parents, long long step, double grown, bool dec,
+                            int zpar, unsigned long long *stat_tests, unsigned long long *stat_tests64,
+                            unsigned long long *stat_dec) {
   const Grid &g = d.grid;
   if (threadIdx.x == 0) d.scanB[t_b] = 0ull;  // this block's look-back word of the resolve phase
   EnvRec *act = d.act[cur];
@@ -896,7 +908,15 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
   // Claims need no order: warps or blocks take chunks of consecutive ranks
   // from a shared counter until none is left, so those that drew cheap
   // envelopes (few liquid neighbours) take more chunks.
+  if (dec) {
+    if (threadIdx.x == 0) s_nz = 0u;
+    __syncthreads();
+  }
   RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error, d.warp_sched);
+  if (dec && (int)(threadIdx.x >> 5) < kDecWarps)
+    decrement_captures(d, cur, n, parents, step, zpar,
+                       ((long long)t_b * kDecWarps + (threadIdx.x >> 5)) * 32 + (threadIdx.x & 31),
+                       (long long)t_nb * kDecWarps * 32, stat_dec);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e)) {
@@ -1014,6 +1034,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
   }
   *stat_tests += tests;
   *stat_tests64 += tests64;
+  if (dec) flush_zero_buffer(d, zpar);
 }
 
 // ---------------------------------------------------------------------------
@@ -1165,7 +1186,7 @@ struct RealmState {
   GenList list, parents;  // this generation / its parents
   // thread 0's busy time per kind of work, added to the control block once
   // per launch; block 0's phase clock
-  unsigned long long claim_busy, resolve_busy, nuc_busy, wake_busy, compact_busy, dec_busy, t_mark, t_work, w_mark;
+  unsigned long long claim_busy, resolve_busy, nuc_busy, wake_busy, compact_busy, t_mark, t_work, w_mark;
 };
 
 __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned long long *smem) {
@@ -1196,7 +1217,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     S.cur = ld_volatile(&c->cur_list);
     S.done = ld_volatile(&c->done) != 0;
     S.t_end = (d.t_stop > 0 && d.t_stop < d.final_time) ? d.t_stop : d.final_time;
-    S.claim_busy = S.resolve_busy = S.nuc_busy = S.wake_busy = S.compact_busy = S.dec_busy = 0ull;
+    S.claim_busy = S.resolve_busy = S.nuc_busy = S.wake_busy = S.compact_busy = 0ull;
     S.t_mark = now_ns();
   }
   if (site_tiles(d)) {
@@ -1289,13 +1310,9 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         S.processed += S.n;
         S.t_work = now_ns();
       }
-      claim_phase(d, S.cur, S.gen ? 1 : 0, S.lo, S.n, S.gen & 1u, S.list, S.parents, S.step, S.grown, &tests, &tests64);
-      // the liquid counts around the previous generation's captures
-      if (S.gen > 0) {
-        const unsigned long long td = threadIdx.x == 0 ? now_ns() : 0ull;
-        capture_decrements(d, S.cur, S.n, S.parents, S.step, (int)((S.gen - 1) & 1u), &dec);
-        if (threadIdx.x == 0) S.dec_busy += now_ns() - td;
-      }
+      // (and the liquid counts around the previous generation's captures)
+      claim_phase(d, S.cur, S.gen ? 1 : 0, S.lo, S.n, S.gen & 1u, S.list, S.parents, S.step, S.grown, S.gen > 0,
+                  (int)((S.gen - 1) & 1u), &tests, &tests64, &dec);
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long w = now_ns() - S.t_work;
@@ -1425,7 +1442,6 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       if (S.nuc_busy) atomicAdd(&c->ns_nuc_work_sum, S.nuc_busy);
       if (S.wake_busy) atomicAdd(&c->ns_wake_work_sum, S.wake_busy);
       if (S.compact_busy) atomicAdd(&c->ns_compact_work_sum, S.compact_busy);
-      if (S.dec_busy) atomicAdd(&c->ns_dec_work_sum, S.dec_busy);
     }
     if (tests) atomicAdd(&c->tests, tests);
     if (tests64) atomicAdd(&c->tests64, tests64);

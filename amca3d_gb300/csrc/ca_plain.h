@@ -112,7 +112,6 @@ struct PlainCtrl {
   unsigned long long ns_claim_work_sum, ns_claim_work_max;  // per-block busy time in claim phases
   unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
   unsigned long long ns_nuc_work_sum, ns_wake_work_sum, ns_compact_work_sum;  // per-block busy time, summed
-  unsigned long long ns_dec_work_sum;    // per-block busy time of the liquid-count decrement passes, summed
   unsigned long long ns_barrier_block0;  // block 0's time inside grid barriers (arrival to release)
   unsigned long long phase_max_scratch[2];             // running max of the current phase
   unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase

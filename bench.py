@@ -355,8 +355,7 @@ def run_ours(args, dist: Dist):
                                                                       round(st["phase_ms"][8], 3)]}
                                    if PHASE_DETAIL else {}),
                                 "fp64_tests_per_run": st["tests_fp64"],
-                                "busy_ms_mean_nucleation_wake_compaction_decrements": [round(x, 3)
-                                                                                       for x in st["detail_ms"][:4]],
+                                "busy_ms_mean_nucleation_wake_compaction": [round(x, 3) for x in st["detail_ms"][:3]],
                                 "barrier_ms_block0": round(st["detail_ms"][4], 3),
                                 "woken_and_nuclei_per_run": st["active_grown"],
                                 "entries_processed_per_run": st["grains_processed"],
