@@ -57,7 +57,8 @@ class Stats(ctypes.Structure):
                 ("grains_processed", ctypes.c_int64), ("algorithmic_bytes", ctypes.c_double),
                 ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("phase_ms", ctypes.c_double * 9),
                 ("detail_ms", ctypes.c_double * 16), ("keys_scanned", ctypes.c_int64),
-                ("decrements", ctypes.c_int64), ("zero_events", ctypes.c_int64), ("compactions", ctypes.c_int64)]
+                ("decrements", ctypes.c_int64), ("zero_events", ctypes.c_int64), ("compactions", ctypes.c_int64),
+                ("reference_walked", ctypes.c_int64), ("step_bytes", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -1193,7 +1193,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   // block 0's phase clock and step counters (its thread 0 only), added to
   // the control block once per launch
   enum { kNuc, kClaim, kClaim0, kResolve, kClaimMax, kResolveMax, kGens, kGrown, kProc, kCaps, kNucs, kScanned, kZero,
-         kClk };
+         kWalked, kClk };
   __shared__ unsigned long long s_clk[kClk];
   // this block's tile of sites when they are tiled (cell -1: removed, or no site)
   __shared__ int s_cell[kBlock];
@@ -1286,6 +1286,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         s_clk[kNucs] += (unsigned long long)nucs;
         s_clk[kScanned] += (unsigned long long)S.a_len;
         s_clk[kGrown] += (unsigned long long)(nw + nucs);
+        s_clk[kWalked] += (unsigned long long)(S.n_act + nucs);
       }
       S.dt = S.n_act + nucs > 0 ? S.da : S.dn;
       S.grown = S.grown_s;
@@ -1413,6 +1414,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     c->done = S.done ? 1 : 0;
     c->keys_scanned += s_clk[kScanned];
     c->zero_events += s_clk[kZero];
+    c->ref_walked += s_clk[kWalked];
     c->ns_nucleation += s_clk[kNuc];
     c->ns_claim += s_clk[kClaim];
     c->ns_claim_gen0 += s_clk[kClaim0];

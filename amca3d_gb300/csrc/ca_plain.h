@@ -99,6 +99,7 @@ struct PlainCtrl {
   // work counters behind the algorithmic-bytes figure
   unsigned long long sites_scanned;    // live sites read by nucleation, summed over steps
   unsigned long long nucleations;      // envelopes created by nucleation
+  unsigned long long ref_walked;       // the reference walk's generation 0 (active envelopes after nucleation), summed over steps
   unsigned long long active_grown;     // generation-0 entries processed (woken and nuclei), summed over steps
   unsigned long long grains_processed; // entries processed in every generation, summed
   unsigned long long keys_scanned;     // list positions the wake scan read, summed over steps

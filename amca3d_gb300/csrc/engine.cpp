@@ -301,18 +301,33 @@ struct amca_t {
   }
 
   double algorithmic_bytes() const {
-    // per run: 12 B per live site (cell id + dTc), 48 B per nucleation (new
-    // envelope 40 B + orientation id 4 B + cell write 4 B), 4 B per wake key
-    // scanned, 24 B per generation-0 entry (woken list write + read,
-    // half-diagonal write, grow step read + write), 228 B per entry and
-    // generation processed (40 B envelope, 26 x 4 B neighbour states, 72 B
-    // matrix, liquid count + key + cell map), 148 B per capture (cell write,
-    // 40 B envelope, 26 x 4 B of the cell map around it), 8 B per liquid-count
-    // decrement, 48 B per entry moved by a compaction.
-    const double S = (double)ctrl.sites_scanned, N = (double)ctrl.nucleations, A = (double)ctrl.active_grown;
+    // The byte model of the reference's step (one figure for every
+    // implementation of it): per step 12 B per live site (cell id + dTc),
+    // 48 B per nucleation (new envelope 40 B + orientation id 4 B + cell write
+    // 4 B), 16 B per active envelope (half-diagonal read + write), 216 B per
+    // envelope and generation of the reference's walk (40 B envelope, 26 x 4 B
+    // neighbour states, 72 B matrix), 44 B per capture (cell write + 40 B
+    // envelope), 8 B per list entry. The walk's generation 0 is every active
+    // envelope after nucleation, its later generations the captures; this
+    // step processes only the envelopes that may change, so A counts the
+    // reference's active envelopes, not the ones processed here.
+    const double S = (double)ctrl.sites_scanned, N = (double)ctrl.nucleations, A = (double)ctrl.ref_walked;
+    const double C = (double)ctrl.captures;
+    return 12 * S + 48 * N + 16 * A + 216 * (A + C) + 44 * C + 8 * (A + C);
+  }
+
+  // Bytes this step moves by its own accounting: 4 B per wake key scanned,
+  // 24 B per generation-0 entry processed (woken list write + read,
+  // half-diagonal write, grow step read + write), 228 B per entry and
+  // generation processed (40 B envelope, 26 x 4 B neighbour states, 72 B
+  // matrix, key + cell word), 148 B per capture (cell write, 40 B envelope,
+  // the 26 cell words around it), 8 B per liquid-count decrement, 48 B per
+  // entry moved by a compaction, and the sites and nucleations as above.
+  double step_bytes() const {
+    const double S = (double)ctrl.sites_scanned, N = (double)ctrl.nucleations, A0 = (double)ctrl.active_grown;
     const double G = (double)ctrl.grains_processed, C = (double)ctrl.captures, K = (double)ctrl.keys_scanned;
     const double D = (double)ctrl.decrements, M = (double)ctrl.compacted;
-    return 12 * S + 48 * N + 4 * K + 24 * A + 228 * G + 148 * C + 8 * D + 48 * M;
+    return 12 * S + 48 * N + 4 * K + 24 * A0 + 228 * G + 148 * C + 8 * D + 48 * M;
   }
 
   bool finished() const { return ctrl.done || !(ctrl.time < cfg.final_time); }
@@ -1200,6 +1215,8 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->decrements = (int64_t)c.decrements;
     s->zero_events = (int64_t)c.zero_events;
     s->compactions = (int64_t)c.compactions;
+    s->reference_walked = (int64_t)c.ref_walked;
+    s->step_bytes = h->step_bytes();
     s->algorithmic_bytes = h->algorithmic_bytes();
     s->h2d_bytes = h->h2d_bytes;
     s->d2h_bytes = h->d2h_bytes;

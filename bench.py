@@ -357,6 +357,8 @@ def run_ours(args, dist: Dist):
                                 "fp64_tests_per_run": st["tests_fp64"],
                                 "busy_ms_mean_nucleation_wake_compaction": [round(x, 3) for x in st["detail_ms"][:3]],
                                 "barrier_ms_block0": round(st["detail_ms"][4], 3),
+                                "reference_walk_envelopes_per_run": st["reference_walked"],
+                                "own_step_bytes_per_run": st["step_bytes"],
                                 "woken_and_nuclei_per_run": st["active_grown"],
                                 "entries_processed_per_run": st["grains_processed"],
                                 "wake_keys_scanned_per_run": st["keys_scanned"],

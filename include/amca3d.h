@@ -356,6 +356,12 @@ typedef struct {
   int64_t decrements;
   int64_t zero_events;
   int64_t compactions;
+  /* Plain realm only: envelopes the reference's walk visits (its active
+   * envelopes after nucleation, summed over steps; algorithmic_bytes counts
+   * these), and the bytes this implementation moves by its own accounting
+   * (it processes only the envelopes that may change). */
+  int64_t reference_walked;
+  double step_bytes;
 } amca_stats;
 /* For the FE-coupled remelting realm the fields mean: liquid_cells -1 (not
  * tracked), grains = grain objects, active = flagged (liquid-neighbour) cells
