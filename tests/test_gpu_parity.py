@@ -74,6 +74,29 @@ def test_gpu_matches_oracle_step_by_step(amca, oracle, name, cuts):
         assert np.array_equal(out["euler"], ref["euler"])
 
 
+def test_gpu_long_run_wake_all_and_growth_ring(amca, oracle):
+    """A 24^3 deck with a small time step (5,005 steps): sleeping envelopes
+    are all woken every 2,048 steps and their half-diagonals replayed from a
+    ring of the last 4,096 step increments. Step by step around those
+    boundaries and at the end, the counts and fields equal the C
+    restatement's."""
+    import dataclasses
+
+    base = [c for c in cases.small_cases() if c.name == "mixed_24_s1"][0]
+    case = dataclasses.replace(base, name="long_24", time_step=2e-5)
+    for n in [2047, 2048, 2049, 4095, 4096, 4097, 4700, -1]:
+        out = run_gpu(amca, case, max_steps=n)
+        ref = oracle.run_plain(case, max_steps=n)
+        assert out["stats"]["step"] == ref["steps"], n
+        assert out["stats"]["time"] == ref["time"], n
+        assert out["stats"]["grains"] == ref["num_grains"], n
+        assert out["stats"]["active"] == ref["active_grains"], n
+        assert out["stats"]["liquid_cells"] == ref["liquid_cells"], n
+        assert np.array_equal(out["orient"], ref["orient"]), n
+        assert np.array_equal(out["grain"], ref["grain"]), n
+    assert ref["steps"] > 4096 and ref["liquid_cells"] == 0
+
+
 def test_gpu_step_api_equals_run(amca):
     case = cases.small_cases()[2]
     r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
