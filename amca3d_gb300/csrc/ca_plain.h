@@ -87,9 +87,6 @@ struct PlainCtrl {
   long long step;
   double time;
   double dt;
-  double vel[2];        // growth velocity at the step's time (uniform field), by step parity
-  double dt_active[2];  // dt when some envelope is active, by step parity
-  double dt_none[2];    // dt when none is (maxVelocity stays 1e-10), by step parity
   int done;
   int pad;
   unsigned long long tests;
