@@ -513,16 +513,19 @@ __device__ __noinline__ unsigned nucleus_neighbours(const PlainDevice &d, int cu
                                                     unsigned long long *stat_dec) {
   const Grid &g = d.grid;
   unsigned gone = 0;
-#pragma unroll 1
+  int di, dj, dk;
+  // the 26 atomics issued before any result is used
+  uint32_t w[26];
+#pragma unroll
+  for (int nb = 0; nb < 26; ++nb) w[nb] = atomicSub(d.cellw + cell + nbr_delta(g, nb, di, dj, dk), 1u);
+  const float gf = wake_bound(grown);
+#pragma unroll
   for (int nb = 0; nb < 26; ++nb) {
-    int di, dj, dk;
-    const int m = cell + nbr_delta(g, nb, di, dj, dk);
-    const uint32_t w = atomicSub(d.cellw + m, 1u);
-    if (!has_entry(w)) continue;
+    if (!has_entry(w[nb])) continue;
     ++*stat_dec;
-    const int q = (int)(w >> 5);
-    if ((w & 31u) == 1u && !woken(d.key[cur][q], wake_bound(grown), all)) {
-      tombstone(d, cur, q, m);
+    const int q = (int)(w[nb] >> 5);
+    if ((w[nb] & 31u) == 1u && !woken(d.key[cur][q], gf, all)) {
+      tombstone(d, cur, q, cell + nbr_delta(g, nb, di, dj, dk));
       ++gone;
     }
   }
@@ -1193,7 +1196,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   // block 0's phase clock and step counters (its thread 0 only), added to
   // the control block once per launch
   enum { kNuc, kClaim, kClaim0, kResolve, kClaimMax, kResolveMax, kGens, kGrown, kProc, kCaps, kNucs, kScanned, kZero,
-         kWalked, kClk };
+         kWalked, kNucMax, kClk };
   __shared__ unsigned long long s_clk[kClk];
   // this block's tile of sites when they are tiled (cell -1: removed, or no site)
   __shared__ int s_cell[kBlock];
@@ -1271,6 +1274,8 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       const unsigned long long tn2 = now_ns();
       S.wake_busy += tn1 - tn0;
       S.nuc_busy += tn2 - tn1;
+      if (d.phase_detail && tn2 - tn0 > ld_volatile(&c->phase_max_scratch[2]))
+        atomicMax(&c->phase_max_scratch[2], tn2 - tn0);
     }
     if (!(ok = grid_barrier(c))) break;
     if (threadIdx.x == 0) {
@@ -1283,6 +1288,10 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         S.t_mark = t_now;
         // the slot of step + 2 (last read at the end of step - 1)
         c->deaths[(S.step + 2) % 3] = 0;
+        if (d.phase_detail) {
+          s_clk[kNucMax] += ld_volatile(&c->phase_max_scratch[2]);
+          c->phase_max_scratch[2] = 0ull;
+        }
         s_clk[kNucs] += (unsigned long long)nucs;
         s_clk[kScanned] += (unsigned long long)S.a_len;
         s_clk[kGrown] += (unsigned long long)(nw + nucs);
@@ -1415,6 +1424,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
     c->keys_scanned += s_clk[kScanned];
     c->zero_events += s_clk[kZero];
     c->ref_walked += s_clk[kWalked];
+    c->ns_nuc_work_max += s_clk[kNucMax];
     c->ns_nucleation += s_clk[kNuc];
     c->ns_claim += s_clk[kClaim];
     c->ns_claim_gen0 += s_clk[kClaim0];

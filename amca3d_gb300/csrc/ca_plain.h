@@ -111,7 +111,8 @@ struct PlainCtrl {
   unsigned long long ns_resolve_work_sum, ns_resolve_work_max;
   unsigned long long ns_nuc_work_sum, ns_wake_work_sum, ns_compact_work_sum;  // per-block busy time, summed
   unsigned long long ns_barrier_block0;  // block 0's time inside grid barriers (arrival to release)
-  unsigned long long phase_max_scratch[2];             // running max of the current phase
+  unsigned long long ns_nuc_work_max;                  // slowest block's busy time in nucleation + wake scan (detail)
+  unsigned long long phase_max_scratch[3];             // running max of the current phase
   unsigned long long claim_next;                       // next unclaimed rank batch of the claim phase
   unsigned long long mark_next;                        // next rank batch of a separate marking pass
 };

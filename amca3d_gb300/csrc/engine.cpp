@@ -1233,6 +1233,7 @@ int amca_get_stats(amca_t *h, amca_stats *s) {
     s->detail_ms[0] = c.ns_nuc_work_sum * 1e-6 / nb;
     s->detail_ms[1] = c.ns_wake_work_sum * 1e-6 / nb;
     s->detail_ms[2] = c.ns_compact_work_sum * 1e-6 / nb;
+    s->detail_ms[3] = c.ns_nuc_work_max * 1e-6;
     s->detail_ms[4] = c.ns_barrier_block0 * 1e-6;
   });
 }

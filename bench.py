@@ -352,7 +352,8 @@ def run_ours(args, dist: Dist):
                                 "busy_ms_mean_claim_resolve": [round(st["phase_ms"][5], 3),
                                                                round(st["phase_ms"][7], 3)],
                                 **({"busy_ms_slowest_claim_resolve": [round(st["phase_ms"][6], 3),
-                                                                      round(st["phase_ms"][8], 3)]}
+                                                                      round(st["phase_ms"][8], 3)],
+                                    "busy_ms_slowest_nucleation_wake": round(st["detail_ms"][3], 3)}
                                    if PHASE_DETAIL else {}),
                                 "fp64_tests_per_run": st["tests_fp64"],
                                 "busy_ms_mean_nucleation_wake_compaction": [round(x, 3) for x in st["detail_ms"][:3]],

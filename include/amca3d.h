@@ -346,8 +346,9 @@ typedef struct {
    * D, E and after the host velocity answers; block 0's new-grain ids [12]
    * and nucleation [13]; the slowest block's liquid-neighbour flag pass in
    * phase B [14]. Plain realm: per-block busy time, mean over blocks, of
-   * nucleation [0], the wake scan [1] and list compactions [2]; block 0's
-   * time inside grid barriers [4]. */
+   * nucleation [0], the wake scan [1] and list compactions [2]; the slowest
+   * block's busy time in nucleation and wake scan [3] (AMCA_PHASE_DETAIL
+   * only); block 0's time inside grid barriers [4]. */
   double detail_ms[16];
   /* Plain realm only (zeros otherwise), summed since the last reset: list
    * positions read by the wake scans, liquid-count decrements, counts that
