@@ -557,9 +557,6 @@ void RemeltRealm::initialize() {
     RCK(cudaStreamSynchronize(stream_));
     d.ecell_start = es;
     d.ecell = el;
-    int64_t most = 0;
-    for (int64_t e = 0; e < ne; ++e) most = std::max(most, start[(size_t)e + 1] - start[(size_t)e]);
-    d.ecell_chunks = (int)std::max<int64_t>(1, (most + 31) / 32);
   }
   // --- frames ---
   d.nframes = (int)nframes_;

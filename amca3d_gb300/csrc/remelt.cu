@@ -1132,21 +1132,15 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         phase_update(d, c, (int64_t)K * g.nxyg + (int64_t)J * g.nxg + I, th, th32, S, true, exactT, melts);
       }
       visited += (M + nthr - 1 - gtid) / nthr;
-    } else {  // the cells of the active elements, 32-cell pieces of an element per warp
-      // (a warp per whole element left the warps with two elements twice as
-      // long as those with one)
+    } else {  // the cells of the active elements (a warp per element)
       const unsigned na = ld_volatile(&c->n_eact[par]);
       const int lane = tid & 31;
       const int64_t gw = gtid >> 5, nw = nthr >> 5;
-      const int64_t kc = d.ecell_chunks;
-      for (int64_t w = gw; w < (int64_t)na * kc; w += nw) {
-        const int64_t ei = w / kc;
-        const int32_t e = d.eact[par][ei];
-        const int64_t b = d.ecell_start[e] + (w - ei * kc) * 32, en = d.ecell_start[e + 1];
-        if (b >= en) continue;  // uniform in the warp: this element has fewer pieces
+      for (int64_t w = gw; w < na; w += nw) {
+        const int32_t e = d.eact[par][w];
+        const int64_t b = d.ecell_start[e], en = d.ecell_start[e + 1];
         const ElemView ev = elem_view(d, th32, e);
-        const int64_t k = b + lane;
-        if (k < en) {
+        for (int64_t k = b + lane; k < en; k += 32) {
           phase_update(d, c, d.ecell[k], th, th32, S, false, exactT, melts, &ev);
           ++visited;
         }

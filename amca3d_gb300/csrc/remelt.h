@@ -137,7 +137,6 @@ struct RemeltDevice {
   uint8_t *fnear[2];         // per element: some node of that frame near void_temperature + 1e-5 (or NaN)
   const int64_t *ecell_start;  // element -> its interior cells (CSR)
   const int32_t *ecell;
-  int ecell_chunks;            // 32-cell pieces of the largest element's cell list
   int32_t *eact[2];          // elements whose cells the next phase update visits, by step parity
   uint8_t *snuc;             // per site: nucleates this step (1), and creates a grain object (2)
   // lists
