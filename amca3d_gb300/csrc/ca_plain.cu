@@ -1091,7 +1091,9 @@ __device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsig
 // Whether a generation of n ranks is marked inside the resolve pass (at most
 // one rank per thread of the team: the barrier a separate pass needs would
 // cost more than the imbalance of static chunks).
-__device__ __forceinline__ bool mark_in_resolve(long long n) { return n <= (long long)kBlock * t_nb; }
+__device__ __forceinline__ bool mark_in_resolve(const PlainDevice &d, long long n) {
+  return n <= (long long)d.mark_split * t_nb;
+}
 
 // Each block marks its contiguous chunk of ranks (the claim words are final
 // after the claim phase's barrier), then one look-back per block over the
@@ -1116,7 +1118,7 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
   long long b, e;
   block_chunk(n, b, e);
   unsigned long long acc = 0;
-  const bool marking = mark_in_resolve(n);
+  const bool marking = mark_in_resolve(d, n);
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
     uint32_t word;
     if (marking) {
@@ -1347,7 +1349,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         S.w_mark = 0;  // busy time of a separate marking pass
       }
       __syncthreads();
-      if (!mark_in_resolve(S.n)) {
+      if (!mark_in_resolve(d, S.n)) {
         mark_phase(d, S.n, S.gen & 1u, d.act[S.cur], S.list);
         __syncthreads();
         if (threadIdx.x == 0) S.w_mark = now_ns() - S.t_work;
@@ -1842,6 +1844,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.nsites = nsites;
   d.gcap = n;
   d.warp_sched = kWarpSched;
+  d.mark_split = kMarkSplit;
   d.orient = (uint32_t *)orient;
   d.site_cell = site_cell;
   d.site_dtc = site_dtc;

@@ -59,8 +59,9 @@ constexpr long long kKeyTile = 128;
 // is never a list position (the list holds fewer than kMaxCells entries).
 constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
 AMCA_HD bool has_entry(uint32_t w) { return (w >> 5) != (kNoEntry >> 5); }
-// Default of PlainDevice::warp_sched.
+// Defaults of PlainDevice::warp_sched and PlainDevice::mark_split.
 constexpr int kWarpSched = 128;
+constexpr int kMarkSplit = 1024;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values
@@ -147,6 +148,7 @@ struct PlainDevice {
   float coord_err;  // bound on FP64 cell-centre rounding, per component
   int phase_detail; // nonzero: also gather the slowest block's busy time per phase
   int warp_sched;   // ranks per block of the team up to which claims are handed out warp by warp (else block by block)
+  int mark_split;   // ranks per block of the team up to which a generation is marked inside the resolve pass
   // arrays
   uint32_t *orient;
   uint32_t *solid;    // 1 bit per cell: solid at the start of the current generation (ghosts included)

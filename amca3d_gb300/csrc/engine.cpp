@@ -187,6 +187,10 @@ struct amca_t {
     // ranks per block of the team, block by block above (AMCA_WARP_SCHED)
     d.warp_sched = kWarpSched;
     if (const char *w = getenv("AMCA_WARP_SCHED")) d.warp_sched = std::max(1, atoi(w));
+    // generations of up to this many ranks per block are marked inside the
+    // resolve pass, larger ones in a pass of their own (AMCA_MARK_SPLIT)
+    d.mark_split = kMarkSplit;
+    if (const char *m = getenv("AMCA_MARK_SPLIT")) d.mark_split = std::max(1, atoi(m));
     d.ncells = (int64_t)g.nxyg * g.nzg;
     d.nsites = nsites;
     d.gcap = (int64_t)c.nx * c.ny * c.nz;
