@@ -41,7 +41,7 @@ thread_local std::string g_create_error;
 
 // Interior cells up to which a plain realm runs 3 blocks per SM instead of
 // the kernel's full occupancy (see initialize).
-constexpr long long kSmallRealmCells = 4ll << 20;
+constexpr long long kSmallRealmCells = 8ll << 20;
 
 }  // namespace
 
@@ -255,9 +255,9 @@ struct amca_t {
     {
       // Blocks per SM of the persistent launch: a small realm's generations
       // are short, so its steps are set by barrier and look-back latency,
-      // which fall with the number of blocks (128^3 on GB300: 19.06 ms at 4
-      // blocks per SM, 18.04 at 3; 200^3 equal; 320^3 94.7 at 4, 100.1 at 3).
-      // AMCA_PLAIN_BLOCKS_PER_SM overrides the choice.
+      // which fall with the number of blocks (GB300: 128^3 20.2 ms at 3
+      // blocks per SM, 21.4 at 4; 200^3 30.0 at 3, 31.2 at 4; 320^3 69 at 4,
+      // 75.6 at 3). AMCA_PLAIN_BLOCKS_PER_SM overrides the choice.
       int per_sm = (long long)c.nx * c.ny * c.nz <= kSmallRealmCells ? 3 : 0;
       if (const char *e = getenv("AMCA_PLAIN_BLOCKS_PER_SM")) per_sm = std::max(1, atoi(e));
       if (per_sm > 0) {
