@@ -37,6 +37,13 @@ unsigned long long host_dkey(double x) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// The largest float at most t and the smallest float at least t.
+void float_bounds(double t, float &lo, float &hi) {
+  lo = hi = (float)t;
+  if ((double)lo > t) lo = std::nextafter(lo, -INFINITY);
+  if ((double)hi < t) hi = std::nextafter(hi, INFINITY);
+}
+
 }  // namespace
 
 RemeltRealm::RemeltRealm(RemeltConfig cfg, const amca_opts &opts, std::string workdir)
@@ -411,6 +418,8 @@ void RemeltRealm::initialize() {
   d.ncells = (int64_t)g.nxyg * g.nzg;
   const int64_t N = d.ncells;
   d.Tm = c.Tm;
+  float_bounds(c.Tm, d.tm_lo, d.tm_hi);
+  float_bounds(-1.0 + 0.01, d.np_lo, d.np_hi);  // nullMatTemp_ + 0.01
   d.Ts = c.Ts;
   d.Tnuc = c.Tmin_nuc;
   d.a1 = c.a1;

@@ -987,10 +987,14 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   bool have32 = false;
   double T = -1.0;  // nullMatTemp_ (Remelting.cpp:29)
   bool exact = !withMat;
-  auto below = [&](double thr) -> int {  // 1: T < thr, 0: T >= thr, -1: undecided
+  // In FP32 (the FP64 pipe is narrow): T lies in [T32 - err, T32 + err], so
+  // with those ends rounded outwards and the threshold rounded inwards
+  // (thr_lo <= thr <= thr_hi, floats) every decided comparison holds for T;
+  // within a float ulp of the threshold it stays undecided.
+  auto below = [&](double thr, float thr_lo, float thr_hi) -> int {  // 1: T < thr, 0: T >= thr, -1: undecided
     if (exact) return T < thr ? 1 : 0;
-    if ((double)T32 + (double)err < thr) return 1;
-    if ((double)T32 - (double)err >= thr) return 0;
+    if (__fadd_ru(T32, err) < thr_lo) return 1;
+    if (__fsub_rd(T32, err) >= thr_hi) return 0;
     return -1;
   };
   auto make_exact = [&]() {
@@ -1006,16 +1010,16 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
       if (ev ? ev->quiet : (d.emax[e] < d.Tm && d.emin[e] >= np)) return;
       T32 = ev ? eval_T32_view(d, cell, *ev, err) : eval_T32(d, th32, cell, e, err);
       have32 = true;
-      int b = below(d.Tm);
+      int b = below(d.Tm, d.tm_lo, d.tm_hi);
       if (b < 0) {
         make_exact();
-        b = below(d.Tm);
+        b = below(d.Tm, d.tm_lo, d.tm_hi);
       }
       if (b == 1) {  // stays solid; the liquid-neighbour pass clears melted below nullMatTemp_ + 0.01
-        int bn = below(np);
+        int bn = below(np, d.np_lo, d.np_hi);
         if (bn < 0) {
           make_exact();
-          bn = below(np);
+          bn = below(np, d.np_lo, d.np_hi);
         }
         if (bn == 1 && d.melted[cell]) d.melted[cell] = 0;
         return;
@@ -1036,13 +1040,16 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   bool decided = false;
   if (!exact) {
     if (!have32) T32 = ev ? eval_T32_view(d, cell, *ev, err) : eval_T32(d, th32, cell, e, err);
-    const double lo = (double)T32 - (double)err, hi = (double)T32 + (double)err;
-    const bool ok_np = hi < np || lo >= np, ok_tm = hi < d.Tm || lo > d.Tm, ok_nl = hi <= -1.0 || lo > -1.0;
+    // the bounds of T rounded outwards, the thresholds inwards (see below());
+    // -1 is a float
+    const float lo = __fsub_rd(T32, err), hi = __fadd_ru(T32, err);
+    const bool ok_np = hi < d.np_lo || lo >= d.np_hi, ok_tm = hi < d.tm_lo || lo > d.tm_hi,
+               ok_nl = hi <= -1.0f || lo > -1.0f;
     if (ok_np && ok_tm && ok_nl && T32 == T32) {
-      wm2 = lo >= np;
-      flags = hi < d.Tm;
-      le = hi < d.Tm;
-      gtn = lo > -1.0;
+      wm2 = lo >= d.np_hi;
+      flags = hi < d.tm_lo;
+      le = flags;
+      gtn = lo > -1.0f;
       decided = true;
     } else {
       make_exact();

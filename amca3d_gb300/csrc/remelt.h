@@ -92,6 +92,9 @@ struct RemeltDevice {
   int b1, b2, b3;
   double tsf_ca, h, trunc, cutoff, final_time, void_t;
   float h32, coord_err;
+  // the liquidus and nullMatTemp_ + 0.01 rounded down and up to float: the
+  // FP32 temperature bounds are compared with these (float_bounds)
+  float tm_lo, tm_hi, np_lo, np_hi;
   // cells (ghost-inclusive)
   int32_t *orient;     // cellOrientationID_ (claims during a step: INT_MIN + sweep position)
   int32_t *grain;      // cellGrainID_

@@ -16,9 +16,10 @@
 //                the same inputs (the plain kernel's wake keys) must never
 //                exceed the FP64 |c'|_1 of is_captured_f64, on the same pairs.
 //   interp       the FP32 interpolation of the remelting kernel and its bound
-//                must decide T < thr exactly as the FP64 interpolation does,
-//                or be undecided, for node values whose FP64 interpolation
-//                lies within a few ulps of the liquidus, nullMatTemp_ (-1) and
+//                (ends rounded outwards, thresholds inwards to float) must
+//                decide T < thr exactly as the FP64 interpolation does, or be
+//                undecided, for node values whose FP64 interpolation lies
+//                within a few ulps of the liquidus, nullMatTemp_ (-1) and
 //                nullMatTemp_ + 0.01.
 //   capture      capture_f64 (ca_math.h) against amca_oracle_capture, bit for
 //                bit, on random captured pairs.
@@ -137,6 +138,21 @@ void containment(long n, int tier) {
   printf("lower%d %ld 0 %ld\n", tier, n, lower_wrong);
 }
 
+// float rounding of a double downwards / upwards (a sum of two floats is
+// exact in double, so this is the FP32 addition with that rounding)
+float round_down(double x) {
+  float f = (float)x;
+  if ((double)f > x) f = nextafterf(f, -INFINITY);
+  return f;
+}
+float round_up(double x) {
+  float f = (float)x;
+  if ((double)f < x) f = nextafterf(f, INFINITY);
+  return f;
+}
+float below_of(double t) { return round_down(t); }
+float above_of(double t) { return round_up(t); }
+
 void interp(long n, int tier) {
   long undecided = 0, wrong = 0;
   const double thr[3] = {1700.0, -1.0, -1.0 + 0.01};
@@ -173,10 +189,11 @@ void interp(long n, int tier) {
     for (int q = 0; q < 8; ++q) t32[q] = (float)t[q];
     const float v = amca::hex8_interp32(t32, (float)pc[0], (float)pc[1], (float)pc[2]);
     const float err = amca::hex8_err32(t32);
-    // the kernel's decision rule (phase_update's `below`)
+    // the kernel's decision rule (phase_update's `below`): the ends of the
+    // bound rounded outwards to float, the threshold inwards
     int b = -1;
-    if ((double)v + (double)err < T0) b = 1;
-    else if ((double)v - (double)err >= T0) b = 0;
+    if (round_up((double)v + (double)err) < below_of(T0)) b = 1;
+    else if (round_down((double)v - (double)err) >= above_of(T0)) b = 0;
     if (b < 0)
       ++undecided;
     else if ((b == 1) != (T < T0))
