@@ -65,8 +65,9 @@ constexpr int kMarkSplit = 1024;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values
-// as identical locals; the fields written by one block in a phase are read
-// by all only after the barrier that closes that phase.
+// in shared memory (identical in every block); the fields written by one
+// block in a phase are read by all only after the barrier that closes that
+// phase.
 struct PlainCtrl {
   unsigned bar_count;
   unsigned bar_gen;
@@ -101,7 +102,7 @@ struct PlainCtrl {
   unsigned long long active_grown;     // generation-0 entries processed (woken and nuclei), summed over steps
   unsigned long long grains_processed; // entries processed in every generation, summed
   unsigned long long keys_scanned;     // list positions the wake scan read, summed over steps
-  unsigned long long decrements;       // liquid-count decrements (pos reads that found an entry)
+  unsigned long long decrements;       // liquid-count decrements that reached an envelope's cell word
   unsigned long long zero_events;      // liquid counts that reached zero in a capture generation
   unsigned long long compactions;      // compactions of the envelope list
   unsigned long long compacted;        // entries moved by them
@@ -125,8 +126,8 @@ static_assert(offsetof(PlainCtrl, bar_count) == 0 && offsetof(PlainCtrl, bar_gen
 
 enum { kErrBarrier = 1, kErrLookback = 2 };
 
-// One envelope as the generation lists carry it: everything the neighbour
-// tests need in one 32-byte, coalesced record.
+// One envelope as the envelope list carries it: everything the neighbour
+// tests need in one 32-byte record.
 struct alignas(16) EnvRec {
   double L;            // half-diagonal length
   float dx, dy, dz;    // centre minus own-cell centre, rounded to float
