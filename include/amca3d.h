@@ -454,8 +454,9 @@ typedef struct {
  * ((nx+2)(ny+2)(nz+2) cells, filled by this call). The run's other state
  * lives in one static device array of 32 MiB, which every GPU that loads the
  * library holds until the process exits; grids that need more (about
- * 172 bytes per interior cell plus 37 per site and 100 KB, i.e. roughly
- * 225,000 interior cells, a 61^3 cube) are rejected with AMCA_ERR_ARG and a message.
+ * 148 bytes per interior cell plus 37 per site and 300 KB, i.e. roughly
+ * 225,000 interior cells, a 61^3 cube) are rejected with AMCA_ERR_ARG and a
+ * message.
  *
  * The site list is checked on the GPU before the run (every site cell an
  * interior cell, ids strictly ascending, at most one site per interior cell);
