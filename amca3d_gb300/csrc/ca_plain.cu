@@ -88,11 +88,6 @@ __device__ __forceinline__ unsigned long long now_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
   unsigned long long v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -1033,6 +1028,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
     d.key[cur][p] = t_lb == -INFINITY ? gf : wake_key(t_lb, L, grown, gf);
     d.liq[r] = liq;
     d.con[r] = con;
+    d.cellr[r] = cell;
   }
   }
   *stat_tests += tests;
@@ -1045,13 +1041,12 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
 // ---------------------------------------------------------------------------
 // Mark of one rank: the captured neighbours (final claim is its own) and
 // whether it stays active, as captures | survives << 31.
-__device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r, unsigned par, const EnvRec *act,
-                                              const GenList &list) {
+__device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r, unsigned par) {
   const Grid &g = d.grid;
   const uint32_t lm = d.liq[r], cm = d.con[r];
   uint32_t cap = 0, surv = 0;
   if (lm) {
-    const int cell = act[list.at(r)].cell;
+    const int cell = d.cellr[r];
     const uint32_t mine = claim_word(par, (uint32_t)r);
     // a liquid neighbour this envelope does not contain and nobody claimed
     // keeps it active without a look at the cell field
@@ -1079,13 +1074,12 @@ __device__ __forceinline__ uint32_t mark_rank(const PlainDevice &d, long long r,
 // Marking pass for large generations: dynamic chunks of ranks, as in the
 // claim phase, and write each rank's mark over its containment
 // mask; a grid barrier then opens the scan.
-__device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsigned par, const EnvRec *act,
-                                       const GenList &list) {
+__device__ __noinline__ void mark_phase(const PlainDevice &d, long long n, unsigned par) {
   RankSched sched(n, &d.ctrl->mark_next, &d.ctrl->error, d.warp_sched);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e))
-    for (long long r = b + first; r < e; r += stride) d.con[r] = mark_rank(d, r, par, act, list);
+    for (long long r = b + first; r < e; r += stride) d.con[r] = mark_rank(d, r, par);
 }
 
 // Whether a generation of n ranks is marked inside the resolve pass (at most
@@ -1112,7 +1106,6 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
                                            unsigned long long *smem,
                                            unsigned *gone_now, unsigned *gone_next) {
   PlainCtrl *c = d.ctrl;
-  const EnvRec *act = d.act[cur];
   if (zdec >= 0) zero_decisions(d, cur, zdec, zgen0, step, gone_now, gone_next);
   if (t_b == 0 && threadIdx.x == 0) c->zn[zreset] = 0ull;  // last read in the previous resolve phase
   long long b, e;
@@ -1122,7 +1115,7 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
   for (long long r = b + threadIdx.x; r < e; r += kBlock) {
     uint32_t word;
     if (marking) {
-      word = mark_rank(d, r, par, act, list);
+      word = mark_rank(d, r, par);
       d.con[r] = word;  // read back below by the same thread
     } else {
       word = d.con[r];  // marked by mark_phase before the last barrier
@@ -1143,7 +1136,7 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
     const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
     if (r < e) {
       const long long p = list.at(r);
-      const int cell = act[p].cell;
+      const int cell = d.cellr[r];
       if (!surv) {
         tombstone(d, cur, p, cell);  // deactivated at its turn
       } else {
@@ -1350,7 +1343,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       }
       __syncthreads();
       if (!mark_in_resolve(d, S.n)) {
-        mark_phase(d, S.n, S.gen & 1u, d.act[S.cur], S.list);
+        mark_phase(d, S.n, S.gen & 1u);
         __syncthreads();
         if (threadIdx.x == 0) S.w_mark = now_ns() - S.t_work;
         if (!(ok = grid_barrier(c))) break;
@@ -1698,7 +1691,7 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // Byte offsets of every scratch buffer for a grid of n interior cells and s sites.
 struct NoAllocLayout {
   size_t ctrl, check, live, omat32, scanA, gx, gy, gz, gori, gcell, act[2], key[2], lstep[2], late, cellw, wlist,
-      zlist[2], dvh, liq, con, child, solid, claimed, scanB, scanC, scanD, total;
+      zlist[2], dvh, liq, con, cellr, child, solid, claimed, scanB, scanC, scanD, total;
   // n interior cells, s sites, `cells` ghost-inclusive cells; the caller
   // bounds all three (see kNoAllocMaxCells) so that no size below wraps
   NoAllocLayout(long long n, long long s, long long cells) {
@@ -1729,6 +1722,7 @@ struct NoAllocLayout {
     cellw = take((size_t)cells * 4);
     dvh = take((size_t)kDvRing * 8);
     liq = take((size_t)n * 4);
+    cellr = take((size_t)n * 4);
     con = take((size_t)n * 4);
     child = take((size_t)n * 4);
     solid = take((size_t)solid_words(cells) * 4);
@@ -1869,6 +1863,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.cellw = (uint32_t *)(base + lay.cellw);
   d.dvh = (double *)(base + lay.dvh);
   d.liq = (uint32_t *)(base + lay.liq);
+  d.cellr = (int32_t *)(base + lay.cellr);
   d.con = (uint32_t *)(base + lay.con);
   d.child = (uint32_t *)(base + lay.child);
   d.solid = (uint32_t *)(base + lay.solid);

@@ -28,6 +28,7 @@
 //               generation, by generation parity
 //   dvh         f64 ring of the growth increment of each step
 //   liq/con     per-rank neighbour masks of the generation being processed
+//   cellr       per-rank cell of the generation being processed
 //   child       per new envelope: parent's rank in its generation << 5 | neighbour index
 //   scanA..D    decoupled look-back status words, one per block: nucleation and
 //               wake scan (two sets each, by step parity), capture, compaction
@@ -173,6 +174,7 @@ struct PlainDevice {
   int32_t *zlist[2];
   double *dvh;
   uint32_t *liq, *con;
+  int32_t *cellr;
   uint32_t *child;
   unsigned long long *scanA, *scanB, *scanC, *scanD;
   PlainCtrl *ctrl;

@@ -221,6 +221,7 @@ struct amca_t {
       d.cellw = a.take<uint32_t>(d.ncells);
       d.dvh = a.take<double>(kDvRing);
       d.liq = a.take<uint32_t>(d.gcap);
+      d.cellr = a.take<int32_t>(d.gcap);
       d.con = a.take<uint32_t>(d.gcap);
       d.child = a.take<uint32_t>(d.gcap);
       d.solid = a.take<uint32_t>(solid_words(d.ncells));
