@@ -534,8 +534,8 @@ __shared__ unsigned s_nz;
 __shared__ unsigned long long s_zbase;
 
 // The liquid counts around the n cells that the previous generation captured
-// (its child records, this generation's ranks; `parents` gives the
-// capturers' positions): one atomic decrement of the cell word of each
+// (its child records, this generation's ranks, which name the capturers'
+// list positions): one atomic decrement of the cell word of each
 // neighbour cell, whose old value says which entry (if any) lives there and
 // its count before. This generation's own entries still hold no-entry words
 // (they set theirs in the resolve phase, from the bitmap, which has these
@@ -545,14 +545,14 @@ __shared__ unsigned long long s_zbase;
 // the zero list of parity zpar once the buffer is full. Capture k goes to
 // the thread numbered k among `threads` ones; this thread is number t0. The
 // 26 atomics of a capture are issued before any result is used.
-__device__ __noinline__ void decrement_captures(const PlainDevice &d, int cur, long long n, const GenList &parents,
+__device__ __noinline__ void decrement_captures(const PlainDevice &d, int cur, long long n,
                                                 long long step, int zpar, long long t0, long long threads,
                                                 unsigned long long *stat_dec) {
   const Grid &g = d.grid;
   const EnvRec *act = d.act[cur];
   for (long long k = t0; k < n; k += threads) {
     const uint32_t rec = d.child[k];
-    const int pc = (int)parents.at((long long)(rec >> 5));
+    const int pc = (int)(rec >> 5);  // the capturer's list position
     int di, dj, dk;
     const int cell = act[pc].cell + nbr_delta(g, (int)(rec & 31u), di, dj, dk);
     uint32_t w[26];
@@ -894,7 +894,7 @@ __device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int z
 // latency of the decrements overlaps the FP64 decentring of the claims.
 constexpr int kDecWarps = 4;
 __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind, long long lo, long long n, unsigned par,
-                            const GenList &list, const GenList &parents, long long step, double grown, bool dec,
+                            const GenList &list, long long step, double grown, bool dec,
                             int zpar, unsigned long long *stat_tests, unsigned long long *stat_tests64,
                             unsigned long long *stat_dec) {
   const Grid &g = d.grid;
@@ -912,7 +912,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
   }
   RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error, d.warp_sched);
   if (dec && (int)(threadIdx.x >> 5) < kDecWarps)
-    decrement_captures(d, cur, n, parents, step, zpar,
+    decrement_captures(d, cur, n, step, zpar,
                        ((long long)t_b * kDecWarps + (threadIdx.x >> 5)) * 32 + (threadIdx.x & 31),
                        (long long)t_nb * kDecWarps * 32, stat_dec);
   const int first = sched.first(), stride = sched.stride();
@@ -937,7 +937,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
       // recorded by the parent: decentred envelope from the parent's
       // (grown) envelope, same orientation.
       const uint32_t rec = d.child[r];
-      const EnvRec pe = act[parents.at((long long)(rec >> 5))];
+      const EnvRec pe = act[rec >> 5];  // the parent, by its list position
       const int pnb = (int)(rec & 31u);
       int di, dj, dk, I, J, K;
       en.cell = pe.cell + nbr_delta(g, pnb, di, dj, dk);
@@ -1149,7 +1149,7 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
       while (bits) {
         const int nb = __ffs(bits) - 1;
         bits &= bits - 1;
-        d.child[slot++] = ((uint32_t)r << 5) | (uint32_t)nb;  // parent's rank in this generation
+        d.child[slot++] = ((uint32_t)p << 5) | (uint32_t)nb;  // parent's list position
         int di, dj, dk;
         set_solid(d.solid, cell + nbr_delta(g, nb, di, dj, dk));  // solid for the next generation
       }
@@ -1181,7 +1181,7 @@ struct RealmState {
   int all;
   long long nucs, n, lo, processed, gen_end, caps_all, died;
   unsigned gen;
-  GenList list, parents;  // this generation / its parents
+  GenList list;  // this generation's list positions
   // thread 0's busy time per kind of work, added to the control block once
   // per launch; block 0's phase clock
   unsigned long long claim_busy, resolve_busy, nuc_busy, wake_busy, compact_busy, t_mark, t_work, w_mark;
@@ -1307,7 +1307,6 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
       S.died = 0;
       S.gen = 0;
       S.list = GenList{d.wlist, nw, S.a_len};
-      S.parents = GenList{nullptr, 0, 0};
     }
     __syncthreads();
     while (S.n > 0) {
@@ -1316,7 +1315,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         S.t_work = now_ns();
       }
       // (and the liquid counts around the previous generation's captures)
-      claim_phase(d, S.cur, S.gen ? 1 : 0, S.lo, S.n, S.gen & 1u, S.list, S.parents, S.step, S.grown, S.gen > 0,
+      claim_phase(d, S.cur, S.gen ? 1 : 0, S.lo, S.n, S.gen & 1u, S.list, S.step, S.grown, S.gen > 0,
                   (int)((S.gen - 1) & 1u), &tests, &tests64, &dec);
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -1380,7 +1379,6 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
         if (timer) s_clk[kCaps] += (unsigned long long)caps;
         S.n = caps;
         ++S.gen;
-        S.parents = S.list;
         S.list = GenList{nullptr, 0, S.gen_end};  // appended to the list after the previous generation
         S.gen_end += caps;
       }

@@ -29,7 +29,7 @@
 //   dvh         f64 ring of the growth increment of each step
 //   liq/con     per-rank neighbour masks of the generation being processed
 //   cellr       per-rank cell of the generation being processed
-//   child       per new envelope: parent's rank in its generation << 5 | neighbour index
+//   child       per new envelope: parent's list position << 5 | neighbour index
 //   scanA..D    decoupled look-back status words, one per block: nucleation and
 //               wake scan (two sets each, by step parity), capture, compaction
 //               (two sets, by compaction parity)
@@ -46,8 +46,8 @@ namespace amca {
 
 // Look-back status words per phase: an upper bound on the persistent grid.
 constexpr long long kStatusWords = 4096;
-// Child records pack an envelope rank into 27 bits, cell words a list
-// position: a realm has fewer than kMaxCells interior cells.
+// Child records and cell words pack a list position into 27 bits: a realm
+// has fewer than kMaxCells interior cells.
 constexpr long long kMaxCells = 1ll << 27;
 // Steps of the growth-increment ring; every live entry is woken (its record
 // brought up to date) at least every kWakeAll steps, well inside the ring.
