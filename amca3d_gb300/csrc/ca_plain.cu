@@ -889,10 +889,9 @@ __device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int z
 // ---------------------------------------------------------------------------
 // With `dec` (generations after the first) the liquid counts around the
 // previous generation's captures are decremented in the same phase: the
-// first kDecWarps warps of every block do that first and then join the
+// first dec_warps warps of every block do that first and then join the
 // claims, whose dynamic hand-out balances the difference, so the memory
 // latency of the decrements overlaps the FP64 decentring of the claims.
-constexpr int kDecWarps = 4;
 __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind, long long lo, long long n, unsigned par,
                             const GenList &list, long long step, double grown, bool dec,
                             int zpar, unsigned long long *stat_tests, unsigned long long *stat_tests64,
@@ -911,10 +910,10 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
     __syncthreads();
   }
   RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error, d.warp_sched);
-  if (dec && (int)(threadIdx.x >> 5) < kDecWarps)
+  if (dec && (int)(threadIdx.x >> 5) < d.dec_warps)
     decrement_captures(d, cur, n, step, zpar,
-                       ((long long)t_b * kDecWarps + (threadIdx.x >> 5)) * 32 + (threadIdx.x & 31),
-                       (long long)t_nb * kDecWarps * 32, stat_dec);
+                       ((long long)t_b * d.dec_warps + (threadIdx.x >> 5)) * 32 + (threadIdx.x & 31),
+                       (long long)t_nb * d.dec_warps * 32, stat_dec);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e)) {
@@ -1837,6 +1836,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.gcap = n;
   d.warp_sched = kWarpSched;
   d.mark_split = kMarkSplit;
+  d.dec_warps = kDecWarps;
   d.orient = (uint32_t *)orient;
   d.site_cell = site_cell;
   d.site_dtc = site_dtc;

@@ -63,6 +63,7 @@ AMCA_HD bool has_entry(uint32_t w) { return (w >> 5) != (kNoEntry >> 5); }
 // Defaults of PlainDevice::warp_sched and PlainDevice::mark_split.
 constexpr int kWarpSched = 128;
 constexpr int kMarkSplit = 1024;
+constexpr int kDecWarps = 2;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values
@@ -151,6 +152,7 @@ struct PlainDevice {
   int phase_detail; // nonzero: also gather the slowest block's busy time per phase
   int warp_sched;   // ranks per block of the team up to which claims are handed out warp by warp (else block by block)
   int mark_split;   // ranks per block of the team up to which a generation is marked inside the resolve pass
+  int dec_warps;    // warps per block that start a claim phase with the liquid-count decrements (1..kWarps)
   // arrays
   uint32_t *orient;
   uint32_t *solid;    // 1 bit per cell: solid at the start of the current generation (ghosts included)
