@@ -910,10 +910,13 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
     __syncthreads();
   }
   RankSched sched(n, &d.ctrl->claim_next, &d.ctrl->error, d.warp_sched);
-  if (dec && (int)(threadIdx.x >> 5) < d.dec_warps)
-    decrement_captures(d, cur, n, step, zpar,
-                       ((long long)t_b * d.dec_warps + (threadIdx.x >> 5)) * 32 + (threadIdx.x & 31),
-                       (long long)t_nb * d.dec_warps * 32, stat_dec);
+  // teams of the batched launch (at most 64 blocks) give the decrements more
+  // of their warps (batched_64: 77 ms at four, 81 at two; the whole GPU on
+  // one realm: 64.7 ms at two, 69 at four)
+  const int dw = t_nb <= 64 ? kDecWarpsTeam : d.dec_warps;
+  if (dec && (int)(threadIdx.x >> 5) < dw)
+    decrement_captures(d, cur, n, step, zpar, ((long long)t_b * dw + (threadIdx.x >> 5)) * 32 + (threadIdx.x & 31),
+                       (long long)t_nb * dw * 32, stat_dec);
   const int first = sched.first(), stride = sched.stride();
   long long b, e;
   while (sched.next(b, e)) {

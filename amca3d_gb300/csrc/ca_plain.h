@@ -64,6 +64,9 @@ AMCA_HD bool has_entry(uint32_t w) { return (w >> 5) != (kNoEntry >> 5); }
 constexpr int kWarpSched = 128;
 constexpr int kMarkSplit = 1024;
 constexpr int kDecWarps = 2;
+// Warps per block that start a claim phase with the decrements on teams of
+// at most 64 blocks (the batched launch).
+constexpr int kDecWarpsTeam = 4;
 
 // Control block. Between launches it holds the realm's state (step, time,
 // active count, ...). Inside a launch every block keeps the per-step values

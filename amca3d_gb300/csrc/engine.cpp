@@ -191,7 +191,8 @@ struct amca_t {
     // resolve pass, larger ones in a pass of their own (AMCA_MARK_SPLIT)
     d.mark_split = kMarkSplit;
     if (const char *m = getenv("AMCA_MARK_SPLIT")) d.mark_split = std::max(1, atoi(m));
-    // warps per block that start a claim phase with the decrements (AMCA_DEC_WARPS, 1..8)
+    // warps per block that start a claim phase with the decrements on a
+    // realm run by the whole GPU (AMCA_DEC_WARPS, 1..8)
     d.dec_warps = kDecWarps;
     if (const char *w = getenv("AMCA_DEC_WARPS")) d.dec_warps = std::min(8, std::max(1, atoi(w)));
     d.ncells = (int64_t)g.nxyg * g.nzg;
