@@ -860,12 +860,12 @@ __device__ __forceinline__ void flush_departures(PlainCtrl *c, long long step, u
   now = next = 0;
 }
 
-// Entries whose liquid count reached zero in the last generation (parity
-// zpar; gen0: it was generation 0): each leaves the list now or in the next
-// step, and becomes a tombstone. One that died at its own turn in that
-// generation is one already; one processed this step outlived its turn (it
-// goes next step); a sleeping one (only in generation 0) goes now unless a
-// capture by a later rank emptied it too.
+// Entries whose liquid count reached zero through the previous generation's
+// captures (zero list of parity zpar; gen0: those were generation 0's): each
+// leaves the list now or in the next step, and becomes a tombstone. One that
+// died at its own turn is one already; one processed this step outlived its
+// turn (it goes next step); a sleeping one (emptied only by generation 0)
+// goes now unless a capture by a later rank emptied it too.
 __device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int zpar, bool gen0, long long step,
                                             unsigned *now, unsigned *next) {
   const unsigned long long nz = ld_volatile(&d.ctrl->zn[zpar]);
@@ -884,8 +884,8 @@ __device__ __noinline__ void zero_decisions(const PlainDevice &d, int cur, int z
 
 // ---------------------------------------------------------------------------
 // Claim: growth up to this step (generation 0) or self-construction
-// (generation >= 1), neighbour tests, atomicMin claims, the entry's liquid
-// count and next wake key.
+// (generation >= 1), neighbour tests, atomicMin claims and the entry's next
+// wake key (its liquid count is set in the resolve phase).
 // ---------------------------------------------------------------------------
 // With `dec` (generations after the first) the liquid counts around the
 // previous generation's captures are decremented in the same phase: the
