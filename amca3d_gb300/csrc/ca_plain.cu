@@ -1094,7 +1094,9 @@ __device__ __forceinline__ bool mark_in_resolve(const PlainDevice &d, long long 
 // Each block marks its contiguous chunk of ranks (the claim words are final
 // after the claim phase's barrier), then one look-back per block over the
 // chunk's marks gives new envelope ids (walk order) and child records; an
-// entry that does not survive its turn becomes a tombstone. Marking reads
+// entry that does not survive its turn becomes a tombstone, one that does
+// gets its cell word (its position and the liquid neighbours it saw in the
+// claim phase). Marking reads
 // only claim words, the claimed bitmap, its own ranks' masks and cells, none
 // of which another block's resolve writes, so no barrier separates the two
 // passes. Every captured cell turns solid for the next generation (whose
