@@ -61,7 +61,7 @@ constexpr long long kKeyTile = 128;
 constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
 AMCA_HD bool has_entry(uint32_t w) { return (w >> 5) != (kNoEntry >> 5); }
 // Defaults of PlainDevice::warp_sched and PlainDevice::mark_split.
-constexpr int kWarpSched = 128;
+constexpr int kWarpSched = 32;
 constexpr int kMarkSplit = 1024;
 constexpr int kDecWarps = 2;
 // Warps per block that start a claim phase with the decrements on teams of
