@@ -901,7 +901,7 @@ __device__ __noinline__ void claim_phase(const PlainDevice &d, int cur, int kind
   EnvRec *act = d.act[cur];
   int32_t *lstep = d.lstep[cur];
   const float gf = wake_bound(grown);
-  unsigned long long tests = 0, tests64 = 0;
+  unsigned tests = 0, tests64 = 0;  // this phase's, added to the launch totals at its end
   // Claims need no order: warps or blocks take chunks of consecutive ranks
   // from a shared counter until none is left, so those that drew cheap
   // envelopes (few liquid neighbours) take more chunks.
