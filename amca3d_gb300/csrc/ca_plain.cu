@@ -1234,7 +1234,7 @@ __device__ void run_realm(const PlainDevice &d, long long step_limit, unsigned l
   bool ok = true;
   while (!S.done && S.time < S.t_end && S.step < step_limit) {
     // the list is compacted once it is mostly tombstones
-    if (S.a_len > 2 * S.n_act + 4096) {
+    if (S.a_len > 2 * S.n_act + d.compact_slack) {
       const unsigned long long tc = threadIdx.x == 0 ? now_ns() : 0ull;
       if (!(ok = compact_phase(d, S.cur, S.a_len, (unsigned)(S.compactions & 1ull), smem, &moved))) break;
       if (threadIdx.x == 0) S.compact_busy += now_ns() - tc;
@@ -1842,6 +1842,7 @@ extern "C" int amca_plain_run_noalloc(int device, const amca_plain_params *p, co
   d.warp_sched = kWarpSched;
   d.mark_split = kMarkSplit;
   d.dec_warps = kDecWarps;
+  d.compact_slack = kCompactSlack;
   d.orient = (uint32_t *)orient;
   d.site_cell = site_cell;
   d.site_dtc = site_dtc;

@@ -64,6 +64,7 @@ AMCA_HD bool has_entry(uint32_t w) { return (w >> 5) != (kNoEntry >> 5); }
 constexpr int kWarpSched = 32;
 constexpr int kMarkSplit = 1024;
 constexpr int kDecWarps = 2;
+constexpr int kCompactSlack = 4096;
 // Warps per block that start a claim phase with the decrements on teams of
 // at most 64 blocks (the batched launch).
 constexpr int kDecWarpsTeam = 4;
@@ -156,6 +157,7 @@ struct PlainDevice {
   int warp_sched;   // ranks per block of the team up to which claims are handed out warp by warp (else block by block)
   int mark_split;   // ranks per block of the team up to which a generation is marked inside the resolve pass
   int dec_warps;    // warps per block that start a claim phase with the liquid-count decrements (1..kWarps)
+  int compact_slack;  // the list is compacted when it holds more than 2 x active + this many entries
   // arrays
   uint32_t *orient;
   uint32_t *solid;    // 1 bit per cell: solid at the start of the current generation (ghosts included)

@@ -195,6 +195,9 @@ struct amca_t {
     // realm run by the whole GPU (AMCA_DEC_WARPS, 1..8)
     d.dec_warps = kDecWarps;
     if (const char *w = getenv("AMCA_DEC_WARPS")) d.dec_warps = std::min(8, std::max(1, atoi(w)));
+    // the list is compacted above 2 x active + this many entries (AMCA_COMPACT_SLACK)
+    d.compact_slack = kCompactSlack;
+    if (const char *cs = getenv("AMCA_COMPACT_SLACK")) d.compact_slack = std::max(0, atoi(cs));
     d.ncells = (int64_t)g.nxyg * g.nzg;
     d.nsites = nsites;
     d.gcap = (int64_t)c.nx * c.ny * c.nz;

@@ -97,6 +97,29 @@ def test_gpu_long_run_wake_all_and_growth_ring(amca, oracle):
     assert ref["steps"] > 4096 and ref["liquid_cells"] == 0
 
 
+def test_gpu_compaction_every_step_matches_oracle(amca, oracle, monkeypatch):
+    """With no compaction slack the envelope list is compacted whenever it
+    holds more than twice as many entries as active envelopes (nearly every
+    step on a small deck): records, keys, grow steps and cell words move
+    while the run stays the reference's step by step."""
+    monkeypatch.setenv("AMCA_COMPACT_SLACK", "0")
+    case = [c for c in cases.small_cases() if c.name == "mixed_24_s1"][0]
+    compactions = 0
+    for n in [5, 30, 61, -1]:
+        r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
+        r.initialize()
+        r.run(n)
+        st = r.stats()
+        orient, grain = r.field("orientation_id"), r.field("grain_id")
+        r.close()
+        ref = oracle.run_plain(case, max_steps=n)
+        assert st["step"] == ref["steps"] and st["active"] == ref["active_grains"], n
+        assert st["grains"] == ref["num_grains"] and st["liquid_cells"] == ref["liquid_cells"], n
+        assert np.array_equal(orient, ref["orient"]) and np.array_equal(grain, ref["grain"]), n
+        compactions = st["compactions"]
+    assert compactions > 10
+
+
 def test_gpu_step_api_equals_run(amca):
     case = cases.small_cases()[2]
     r = amca.CellularAutomataRealm(case.to_yaml(), seed=case.seed)
