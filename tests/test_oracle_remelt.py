@@ -74,3 +74,21 @@ def test_remelt_oracle_rejects_bad_frame_file(oracle, tmp_path):
     path.write_text("\n".join(text))
     with pytest.raises(RuntimeError, match="check title of line"):
         oracle.run_remelt(fx.case, str(tmp_path), fields=False)
+
+
+def test_pbf_500_oracle_equals_reference_at_full_size():
+    """The full-size pbf_500 record (tests/golden/make_pbf_golden.py): the
+    unmodified reference's run and the C restatement's run of the same deck,
+    frames and baseplate end at the same step, time and dt with the same
+    orientation / grain-id / melted field digests and counts, and the
+    reference's record carries its checkpoints."""
+    g = json.load(open(os.path.join(HERE, "golden", "pbf_500_golden.json")))
+    assert g["cells"] == [500, 250, 100] and g["frames"] == 1550
+    ref, ora = g["reference"], g["oracle"]
+    assert "unmodified reference" in ref["source"]
+    # the restatement's record has no grain-table or Euler digest
+    assert set(ora["final"]) >= {"step", "time", "dt", "orient", "grain", "melted", "ngrains", "norient"}
+    assert all(ref["final"][k] == v for k, v in ora["final"].items())
+    assert ref["final"]["step"] == 7659 and ref["final"]["norient"] == 2036
+    steps = [c["step"] for c in ref["checkpoints"]]
+    assert steps == sorted(steps) and steps[-1] < ref["final"]["step"] and len(steps) >= 5
