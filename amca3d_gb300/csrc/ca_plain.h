@@ -75,7 +75,7 @@ constexpr int kDecWarpsTeam = 4;
 // block in a phase are read by all only after the barrier that closes that
 // phase.
 struct PlainCtrl {
-  unsigned bar_count;
+  unsigned bar_count;  // with bar_gen: one 64-bit arrival counter of the grid barrier, zero at every launch
   unsigned bar_gen;
   int error;        // 0, or where a bounded wait ran out (see kErr*)
   int cur_list;     // which act[] holds the envelope list
@@ -190,7 +190,7 @@ struct PlainDevice {
 // One team of the batched launch: its barrier words and the realm it runs in
 // the current round, by round parity (-1: none left).
 struct alignas(8) BatchTeam {
-  unsigned count;  // barrier arrivals; with gen one 64-bit word (gen in the high half)
+  unsigned count;  // with gen: one 64-bit arrival counter of the team barrier, zero at every launch
   unsigned gen;
   int slot[2];
 };

@@ -63,6 +63,11 @@ __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long l
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned long long atom_add_acq_rel64(unsigned long long *p, unsigned long long x) {
+  unsigned long long old;
+  asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(x) : "memory");
+  return old;
+}
 template <typename T>
 __device__ __forceinline__ T ld_volatile(const T *p) {
   return *(const volatile T *)p;
@@ -110,33 +115,37 @@ __device__ bool grid_barrier(const RemeltDevice &d, int p) {
     const unsigned long long w = tb - s_left;
     s_busy[p] += w;
     if (d.detail && w > ld_volatile(&c->work_scratch[p])) atomicMax(&c->work_scratch[p], w);
-    // (bar_count, bar_gen) as one 64-bit word, generation in the high half:
-    // an arrival is one atomicAdd; the last one resets the count and opens
-    // the next generation with one more
+    // (bar_count, bar_gen) as one 64-bit arrival counter that only grows:
+    // zero when the launch starts (host reset), one acquire-release atomic
+    // per arrival (the block's writes, ordered before it by the block
+    // barrier, are released with it; the last arrival acquires the others'
+    // through it), and barrier k of the launch ends when it reaches k x
+    // gridDim.x; the others wait with acquire loads. No arrival has to open
+    // the next barrier with a second atomic.
     unsigned long long *bw = (unsigned long long *)&c->bar_count;
-    __threadfence();
     const int seen = ld_volatile(&c->error);
-    const unsigned long long old = atomicAdd(bw, 1ull);
-    const unsigned gen = (unsigned)(old >> 32);
+    const unsigned long long old = atom_add_acq_rel64(bw, 1ull);
+    const unsigned long long nb = gridDim.x;
+    const unsigned long long target = (old / nb + 1ull) * nb;
     bool ok = true;
-    if ((unsigned)old == gridDim.x - 1) {
-      atomicAdd(bw, (1ull << 32) - (unsigned long long)gridDim.x);
-    } else {
+    if (old + 1ull != target) {
       const unsigned long long t0 = now_ns();
-      while ((unsigned)(ld_acquire64(bw) >> 32) == gen) {
-        if (ld_volatile(&c->error) != 0) {
-          ok = false;
-          break;
-        }
-        if (now_ns() - t0 > kWaitNs) {
-          atomicCAS(&c->error, 0, kRemeltErrBarrier);
-          ok = false;
-          break;
+      unsigned it = 0;
+      while (ld_acquire64(bw) < target) {
+        if ((++it & 7u) == 0u) {
+          if (ld_volatile(&c->error) != 0) {
+            ok = false;
+            break;
+          }
+          if (now_ns() - t0 > kWaitNs) {
+            atomicCAS(&c->error, 0, kRemeltErrBarrier);
+            ok = false;
+            break;
+          }
         }
         __nanosleep(32);
       }
     }
-    __threadfence();
     s_left = now_ns();
     s_bar_ok = ok && seen == 0;
     if (blockIdx.x == 0) {
@@ -1671,6 +1680,9 @@ int remelt_persistent_grid(int device, int per_sm) {
 
 cudaError_t remelt_run_steps(const RemeltDevice &d, long long limit, int blocks, cudaStream_t s) {
   void *args[] = {(void *)&d, (void *)&limit};
+  // the barrier's arrival counter starts every launch at zero
+  const cudaError_t e = cudaMemsetAsync(d.ctrl, 0, 2 * sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
   return cudaLaunchCooperativeKernel((const void *)remelt_kernel, dim3(blocks), dim3(kBlock), args, 0, s);
 }
 

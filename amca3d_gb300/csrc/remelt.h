@@ -41,7 +41,7 @@ struct HostVelocity {
 constexpr uint8_t kTlt = 1, kTle = 2, kTgtNull = 4, kTgeNullPlus = 8;
 
 struct RemeltCtrl {
-  unsigned int bar_count, bar_gen;  // one 64-bit word for the grid barrier, generation in the high half
+  unsigned int bar_count, bar_gen;  // one 64-bit arrival counter of the grid barrier, zero at every launch
   int error;
   int status;
   // coupling scalars, published by block 0 at the end of every step
