@@ -51,6 +51,7 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
+constexpr int kCellPre = 4;  // cells per lane whose phase-update loads are issued together
 constexpr unsigned long long kWaitNs = 5000000000ull;  // 5 s bound on any spin
 
 __device__ __forceinline__ unsigned long long now_ns() {
@@ -974,19 +975,33 @@ __device__ __forceinline__ ElemView elem_view(const RemeltDevice &d, const float
   return v;
 }
 
+// What the phase update reads of one cell, loaded for several cells of an
+// element at once (their load chains overlap instead of running one after
+// another): orientation id, melted flag and FP32 parametric coordinates.
+struct CellPre {
+  int32_t o;
+  uint8_t m;
+  float xi, eta, zeta;
+};
+
 // eval_T32 with the element's nodal values already at hand (same operands,
 // same operation order, same result).
-__device__ __forceinline__ float eval_T32_view(const RemeltDevice &d, int64_t c, const ElemView &v, float &err) {
+__device__ __forceinline__ float eval_T32_view(const RemeltDevice &d, int64_t c, const ElemView &v, float &err,
+                                               const CellPre *pre) {
   err = v.err;
+  if (pre) return hex8_interp32(v.t, pre->xi, pre->eta, pre->zeta);
   return hex8_interp32(v.t, d.pc32[3 * c], d.pc32[3 * c + 1], d.pc32[3 * c + 2]);
 }
 
 // `ev`: the cell's element view when the caller walks an element's cells
-// (the cell's tag is then ev->e), or nullptr.
-__device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell, const double *th,
-                             const float *th32, const StepScalars &S, bool count_all, unsigned long long &exactT,
-                             unsigned long long &melts, const ElemView *ev = nullptr) {
-  int32_t o = d.orient[cell];
+// (the cell's tag is then ev->e), or nullptr; `pre`: the cell's values
+// loaded by the caller, or nullptr.
+__device__ __forceinline__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell, const double *th,
+                                             const float *th32, const StepScalars &S, bool count_all,
+                                             unsigned long long &exactT, unsigned long long &melts,
+                                             const ElemView *ev = nullptr, const CellPre *pre = nullptr) {
+  int32_t o = pre ? pre->o : d.orient[cell];
+  uint8_t mel = pre ? pre->m : 0;  // the cell's melted flag as this pass leaves it (with pre)
   const int32_t e = ev ? ev->e : d.tag[cell];
   const bool withMat = e >= 0 && !(ev ? ev->void_ : d.evoid[e] != 0);
   const double np = null_plus();
@@ -1017,7 +1032,7 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
     if (withMat) {
       // certainly below the liquidus and above nullMatTemp_ + 0.01: nothing changes
       if (ev ? ev->quiet : (d.emax[e] < d.Tm && d.emin[e] >= np)) return;
-      T32 = ev ? eval_T32_view(d, cell, *ev, err) : eval_T32(d, th32, cell, e, err);
+      T32 = ev ? eval_T32_view(d, cell, *ev, err, pre) : eval_T32(d, th32, cell, e, err);
       have32 = true;
       int b = below(d.Tm, d.tm_lo, d.tm_hi);
       if (b < 0) {
@@ -1030,12 +1045,13 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
           make_exact();
           bn = below(np, d.np_lo, d.np_hi);
         }
-        if (bn == 1 && d.melted[cell]) d.melted[cell] = 0;
+        if (bn == 1 && (pre ? mel : d.melted[cell])) d.melted[cell] = 0;
         return;
       }
     }
     d.orient[cell] = -1;  // melt
     d.melted[cell] = withMat ? 1 : 0;
+    mel = withMat ? 1 : 0;
     o = -1;
     ++melts;
     if (e >= 0 && !count_all) atomicAdd(&d.eliq[e], 1);
@@ -1048,7 +1064,7 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
   bool wm2, flags, le, gtn;
   bool decided = false;
   if (!exact) {
-    if (!have32) T32 = ev ? eval_T32_view(d, cell, *ev, err) : eval_T32(d, th32, cell, e, err);
+    if (!have32) T32 = ev ? eval_T32_view(d, cell, *ev, err, pre) : eval_T32(d, th32, cell, e, err);
     // the bounds of T rounded outwards, the thresholds inwards (see below());
     // -1 is a float
     const float lo = __fsub_rd(T32, err), hi = __fadd_ru(T32, err);
@@ -1070,7 +1086,7 @@ __device__ void phase_update(const RemeltDevice &d, RemeltCtrl *c, int64_t cell,
     le = !(T > d.Tm);
     gtn = T > -1.0;
   }
-  const uint8_t m0 = d.melted[cell];
+  const uint8_t m0 = pre ? mel : d.melted[cell];
   uint8_t m1 = m0;
   if (wm2 && S.time >= S.max_ts) m1 = 1;
   if (!wm2) m1 = 0;
@@ -1156,9 +1172,28 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         const int32_t e = d.eact[par][w];
         const int64_t b = d.ecell_start[e], en = d.ecell_start[e + 1];
         const ElemView ev = elem_view(d, th32, e);
-        for (int64_t k = b + lane; k < en; k += 32) {
-          phase_update(d, c, d.ecell[k], th, th32, S, false, exactT, melts, &ev);
-          ++visited;
+        // kCellPre cells per lane at a time: their ids, then everything the
+        // update reads of them, each set of loads in flight together
+        for (int64_t k0 = b + lane; k0 < en; k0 += 32 * kCellPre) {
+          int64_t cl[kCellPre];
+          CellPre pre[kCellPre];
+#pragma unroll
+          for (int j = 0; j < kCellPre; ++j) cl[j] = k0 + 32 * j < en ? d.ecell[k0 + 32 * j] : -1;
+#pragma unroll
+          for (int j = 0; j < kCellPre; ++j) {
+            if (cl[j] < 0) continue;
+            pre[j].o = d.orient[cl[j]];
+            pre[j].m = d.melted[cl[j]];
+            pre[j].xi = d.pc32[3 * cl[j]];
+            pre[j].eta = d.pc32[3 * cl[j] + 1];
+            pre[j].zeta = d.pc32[3 * cl[j] + 2];
+          }
+#pragma unroll
+          for (int j = 0; j < kCellPre; ++j) {
+            if (cl[j] < 0) continue;
+            phase_update(d, c, cl[j], th, th32, S, false, exactT, melts, &ev, &pre[j]);
+            ++visited;
+          }
         }
       }
     }
@@ -1246,6 +1281,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         }
       }
       d.snuc[sidx] = f;
+      if (f) atomicAdd(&c->n_nuc_sites[par], 1u);
     }
     if (gtid == 0) {
       const unsigned long long t1 = now_ns();
@@ -1259,7 +1295,9 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     if (nf > d.list_cap) {
       if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
     }
-    if (blockIdx.x == 0 && d.nsites > 0) {
+    if (blockIdx.x == 0 && tid == 0) c->n_nuc_sites[par ^ 1] = 0u;  // counted again in the next step's phase B
+    // (in most steps no site nucleates and the scan over the sites is skipped)
+    if (blockIdx.x == 0 && d.nsites > 0 && ld_volatile(&c->n_nuc_sites[par]) > 0u) {
       const unsigned long long tn = tid == 0 ? now_ns() : 0ull;
       // nucleate_at_nucleation_sites (Remelting.cpp:936-999): ascending sites,
       // orientation id = count so far, a grain object created where the cell has none

@@ -79,6 +79,7 @@ struct RemeltCtrl {
   unsigned long long ns_flags_max, flags_scratch;  // slowest block's liquid-neighbour flag pass (phase B)
   int fstat_frame[2];          // frame whose per-element extrema each slot holds (-1: none)
   int any_near;                // some element met a frame near the void threshold: rebuild every step
+  unsigned int n_nuc_sites[2];  // sites that nucleate in the step, by step parity (phase B counts, C reads)
 };
 
 static_assert(offsetof(RemeltCtrl, bar_count) == 0 && offsetof(RemeltCtrl, bar_gen) == 4,
