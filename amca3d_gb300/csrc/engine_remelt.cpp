@@ -666,6 +666,10 @@ void RemeltRealm::initialize() {
     void *dv = nullptr;
     RCK(cudaHostGetDevicePointer(&dv, hv, 0));
     d.host = (HostVelocity *)dv;
+    // entries one request may use; AMCA_HOST_VEL_CAP (tests) makes it small
+    // so that steps take the chunked path
+    d.host_cap = kHostVelCap;
+    if (const char *e = getenv("AMCA_HOST_VEL_CAP")) d.host_cap = std::min(kHostVelCap, std::max(2, atoi(e)));
   }
   // --- orientations and sites ---
   orient_cap_ = (int64_t)otab_.euler.size() / 3;

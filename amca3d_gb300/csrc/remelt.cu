@@ -324,14 +324,16 @@ __device__ __forceinline__ void st_release_sys(unsigned *p, unsigned v) {
 
 // Block 0: have the host evaluate the velocities flagged `hard` this step
 // (and the velocity at the minimum temperature when `min_hard`), in chunks
-// of the mapped buffer. Every wait is bounded; false on a timeout.
+// of host_cap entries, one request each (the other blocks count them after
+// the barrier that follows). Every wait is bounded; false on a timeout.
 __device__ bool host_velocities(const RemeltDevice &d, RemeltCtrl *c, unsigned nh, bool min_hard, double minT) {
   __shared__ int s_ok;
   const unsigned total = nh + (min_hard ? 1u : 0u);
+  const unsigned cap = (unsigned)d.host_cap;
   if (threadIdx.x == 0) s_ok = d.host != nullptr;
   __syncthreads();
-  for (unsigned base = 0; base < total && s_ok; base += kHostVelCap) {
-    const unsigned cnt = min(total - base, (unsigned)kHostVelCap);
+  for (unsigned base = 0; base < total && s_ok; base += cap) {
+    const unsigned cnt = min(total - base, cap);
     for (unsigned k = threadIdx.x; k < cnt; k += blockDim.x) {
       const unsigned i = base + k;
       d.host->T[k] = i < nh ? d.hard_T[i] : minT;
@@ -1405,10 +1407,12 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     // request larger than the mapped buffer goes in chunks, behind a barrier.
     const unsigned nh = ld_volatile(&c->n_hard);  // uniform: every block read the same counter and key
     const bool ask = nh > 0 || min_hard;
-    const bool overlap = ask && nh + 1u <= (unsigned)kHostVelCap;
+    const bool overlap = ask && nh + 1u <= (unsigned)d.host_cap;
     if (ask && !overlap) {
       if (blockIdx.x == 0 && !host_velocities(d, c, nh, min_hard, minT)) atomicCAS(&c->error, 0, kRemeltErrHost);
       if (!(ok = grid_barrier(d, 5))) break;
+      // block 0's requests, one per chunk, counted by the others
+      if (tid == 0 && blockIdx.x != 0) s_host_seq += (nh + (min_hard ? 1u : 0u) + d.host_cap - 1u) / d.host_cap;
       if (min_hard) vmin = ld_volatile(&c->vmin);
     }
     if (overlap) {

@@ -153,6 +153,7 @@ struct RemeltDevice {
   int32_t *hard_idx;         // flagged-list entries whose velocity the host evaluates
   double *hard_T;
   HostVelocity *host;        // device view of the mapped host buffer
+  int host_cap;              // entries of `host` one request may use (kHostVelCap; smaller in tests)
   int64_t list_cap;
   RemeltCtrl *ctrl;
 };

@@ -75,6 +75,33 @@ def test_remelt_gpu_matches_reference_every_step(amca, tmp_path, name):
     r.close()
 
 
+@pytest.mark.parametrize("name", ["remelt_random", "remelt_scaled", "remelt_new_grains"])
+def test_remelt_gpu_host_velocities_in_chunks(amca, tmp_path, monkeypatch, name):
+    """The hard glibc-pow velocities of a step normally go to the host in one
+    request that overlaps the growth of the other cells. With room for 3
+    entries a step with 3 or more of them sends them in chunks of 3, one
+    request each, before the growth: the run still matches the reference
+    step by step, with more host requests than the normal run."""
+    fx = FIX[name]
+    for sub in ("a", "b"):
+        (tmp_path / sub).mkdir()
+    r = make_realm(amca, fx, str(tmp_path / "a"))
+    r.run()
+    calls = r.stats()["reserved"]
+    r.close()
+    monkeypatch.setenv("AMCA_HOST_VEL_CAP", "3")
+    r = make_realm(amca, fx, str(tmp_path / "b"))
+    g = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    fields = [str(f) for f in g["fields"]]
+    for i in range(len(g["digests"])):
+        dt = r.single_integration_step()
+        assert r.stats()["time"] == g["time"][i] and dt == g["dt"][i], f"step {i + 1}: time/dt"
+        d = digests(r)
+        assert not [k for k in STATE if d[k] != g["digests"][i][fields.index(k)]], f"step {i + 1}"
+    assert r.stats()["reserved"] > calls > 0
+    r.close()
+
+
 @pytest.mark.parametrize("frames", ["file", "rosenthal", "arrays"])
 @pytest.mark.parametrize("name", ["remelt_nucleation", "remelt_scaled", "remelt_new_grains"])
 def test_remelt_gpu_full_run(amca, tmp_path, name, frames):
