@@ -1127,15 +1127,24 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
   block_chunk(n, b, e);
   unsigned long long acc = 0;
   const bool marking = mark_in_resolve(d, n);
-  for (long long r = b + threadIdx.x; r < e; r += kBlock) {
-    uint32_t word;
-    if (marking) {
-      word = mark_rank(d, r, par);
-      d.con[r] = word;  // read back below by the same thread
-    } else {
-      word = d.con[r];  // marked by mark_phase before the last barrier
+  // kMarkBatch ranks per thread marked before any mark is stored: a store
+  // through one array could alias the next rank's loads, so storing each
+  // mark at once would run the ranks' load chains one after another
+  for (long long r0 = b + threadIdx.x; r0 < e; r0 += (long long)kBlock * kMarkBatch) {
+    uint32_t word[kMarkBatch];
+#pragma unroll
+    for (int j = 0; j < kMarkBatch; ++j) {
+      const long long r = r0 + (long long)j * kBlock;
+      // marked here, or by mark_phase before the last barrier
+      word[j] = r < e ? (marking ? mark_rank(d, r, par) : d.con[r]) : 0u;
     }
-    acc += ((unsigned long long)__popc(word & 0x03ffffffu) << 32) | (word >> 31);
+#pragma unroll
+    for (int j = 0; j < kMarkBatch; ++j) {
+      const long long r = r0 + (long long)j * kBlock;
+      if (r >= e) continue;
+      if (marking) d.con[r] = word[j];  // read back below by the same thread
+      acc += ((unsigned long long)__popc(word[j] & 0x03ffffffu) << 32) | (word[j] >> 31);
+    }
   }
   unsigned long long agg;
   block_exclusive_scan(acc, smem, &agg);
@@ -1147,17 +1156,19 @@ __device__ __noinline__ bool resolve_phase(const PlainDevice &d, int cur, long l
     const long long r = r0 + threadIdx.x;
     const uint32_t word = r < e ? d.con[r] : 0u;
     const uint32_t cap = word & 0x03ffffffu, surv = word >> 31;
+    // what the rank's entry needs, loaded before the scan (independent of it)
+    const long long p = r < e ? list.at(r) : 0;
+    const int cell = r < e ? d.cellr[r] : 0;
+    const uint32_t lq = r < e ? d.liq[r] : 0u;
     unsigned long long tot;
     const unsigned long long ex = block_exclusive_scan(((unsigned long long)__popc(cap) << 32) | surv, smem, &tot);
     if (r < e) {
-      const long long p = list.at(r);
-      const int cell = d.cellr[r];
       if (!surv) {
         tombstone(d, cur, p, cell);  // deactivated at its turn
       } else {
         // its cell word: position and the liquid neighbours it saw in the
         // claim phase (this generation's captures come off in the next one)
-        d.cellw[cell] = ((uint32_t)p << 5) | (uint32_t)__popc(d.liq[r]);
+        d.cellw[cell] = ((uint32_t)p << 5) | (uint32_t)__popc(lq);
       }
       long long slot = (long long)((run + ex) >> 32);  // rank of the first child in the next generation
       uint32_t bits = cap;

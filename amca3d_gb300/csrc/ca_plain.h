@@ -65,6 +65,7 @@ constexpr int kWarpSched = 32;
 constexpr int kMarkSplit = 1024;
 constexpr int kDecWarps = 2;
 constexpr int kCompactSlack = 4096;
+constexpr int kMarkBatch = 4;  // ranks per thread whose marks are computed before any is stored
 // Warps per block that start a claim phase with the decrements on teams of
 // at most 64 blocks (the batched launch).
 constexpr int kDecWarpsTeam = 4;
