@@ -39,8 +39,10 @@ namespace {
 
 thread_local std::string g_create_error;
 
-// Interior cells up to which a plain realm runs 3 blocks per SM instead of
-// the kernel's full occupancy (see initialize).
+// Interior cells up to which a plain realm runs 2 (kTinyRealmCells) or 3
+// (kSmallRealmCells) blocks per SM instead of the kernel's full occupancy
+// (see initialize).
+constexpr long long kTinyRealmCells = 4200000ll;
 constexpr long long kSmallRealmCells = 8ll << 20;
 
 }  // namespace
@@ -263,10 +265,12 @@ struct amca_t {
     {
       // Blocks per SM of the persistent launch: a small realm's generations
       // are short, so its steps are set by barrier and look-back latency,
-      // which fall with the number of blocks (GB300: 128^3 20.2 ms at 3
-      // blocks per SM, 21.4 at 4; 200^3 30.0 at 3, 31.2 at 4; 320^3 69 at 4,
-      // 75.6 at 3). AMCA_PLAIN_BLOCKS_PER_SM overrides the choice.
-      int per_sm = (long long)c.nx * c.ny * c.nz <= kSmallRealmCells ? 3 : 0;
+      // which fall with the number of blocks (GB300, blocks per SM 2 / 3 /
+      // 4: 128^3 17.2 / 17.9 / 19.0 ms, 160^3 21.4 / 21.8, 200^3 29.0 /
+      // 27.8, 256^3 44.6 / 42.4 / 41.9, 320^3 70.8 / 64.6 / 63.0).
+      // AMCA_PLAIN_BLOCKS_PER_SM overrides the choice.
+      const long long interior = (long long)c.nx * c.ny * c.nz;
+      int per_sm = interior <= kTinyRealmCells ? 2 : interior <= kSmallRealmCells ? 3 : 0;
       if (const char *e = getenv("AMCA_PLAIN_BLOCKS_PER_SM")) per_sm = std::max(1, atoi(e));
       if (per_sm > 0) {
         int sms = 0;
