@@ -95,10 +95,10 @@ enum {
   kClkN = kClkWorkMax + 6
 };
 __shared__ unsigned long long s_clk[kClkN];
-__shared__ unsigned s_host_seq;  // block 0: requests posted to the host so far
+__shared__ unsigned s_host_seq;  // requests posted to the host so far (every block counts them)
 __shared__ int s_bar_ok;         // thread 0's verdict on the block's last barrier
 
-// Sense-counting grid barrier bounded in time; false when a wait ran out or
+// Counting grid barrier bounded in time; false when a wait ran out or
 // thread 0 saw the error word set: sampled as it arrives (the load's latency
 // hides behind the arrival) and while it waits. An error raised in this
 // block before the barrier is always seen; one raised elsewhere at the latest
