@@ -1233,15 +1233,44 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
             nbr_offset(n, di, dj, dk);
             solid |= (d.orient[cell + dk * g.nxyg + dj * g.nxg + di] > -1 ? 1u : 0u) << n;
           }
+          // the three neighbours of a (dj, dk) row are consecutive cells:
+          // one atomicOr per flag word the row touches (one, or two where
+          // it crosses a word) sets all of its solid ones, so a cell takes
+          // 9 to 18 atomics instead of one per solid neighbour, and fewer
+          // of them meet on the same words
           uint32_t fresh = 0;
+          unsigned lo_old[9], hi_old[9];
 #pragma unroll
-          for (int n = 0; n < 26; ++n) {
-            if (!((solid >> n) & 1u)) continue;
-            int di, dj, dk;
-            nbr_offset(n, di, dj, dk);
-            const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
-            const unsigned bit = 1u << (nb & 31);
-            if (!(atomicOr(&d.flagbits[nb >> 5], bit) & bit)) fresh |= 1u << n;
+          for (int r = 0; r < 9; ++r) {
+            const int dj = r % 3 - 1, dk = r / 3 - 1;
+            // neighbour index of di = -1, 0, +1 in this row (-1: the centre cell)
+            const int nm = r <= 4 ? 3 * r : 3 * r - 1;
+            const int nc = r <= 3 ? 3 * r + 1 : (r == 4 ? -1 : 3 * r);
+            const int np_ = r <= 3 ? 3 * r + 2 : (r == 4 ? 13 : 3 * r + 1);
+            const unsigned pat = ((solid >> nm) & 1u) | (nc >= 0 ? ((solid >> nc) & 1u) << 1 : 0u) |
+                                 (((solid >> np_) & 1u) << 2);
+            const int32_t rb = cell + dk * g.nxyg + dj * g.nxg - 1;
+            const unsigned long long m64 = (unsigned long long)pat << (rb & 31);
+            const unsigned lo = (unsigned)m64, hi = (unsigned)(m64 >> 32);
+            lo_old[r] = lo ? atomicOr(&d.flagbits[rb >> 5], lo) : 0xffffffffu;
+            hi_old[r] = hi ? atomicOr(&d.flagbits[(rb >> 5) + 1], hi) : 0xffffffffu;
+          }
+#pragma unroll
+          for (int r = 0; r < 9; ++r) {
+            const int dj = r % 3 - 1, dk = r / 3 - 1;
+            const int nm = r <= 4 ? 3 * r : 3 * r - 1;
+            const int nc = r <= 3 ? 3 * r + 1 : (r == 4 ? -1 : 3 * r);
+            const int np_ = r <= 3 ? 3 * r + 2 : (r == 4 ? 13 : 3 * r + 1);
+            const int32_t rb = cell + dk * g.nxyg + dj * g.nxg - 1;
+            // bits of this row set here for the first time, by di
+            const unsigned long long old64 = (unsigned long long)lo_old[r] | ((unsigned long long)hi_old[r] << 32);
+            const unsigned newbits = (unsigned)((~old64) >> (rb & 31)) & 7u;
+            const unsigned pat = ((solid >> nm) & 1u) | (nc >= 0 ? ((solid >> nc) & 1u) << 1 : 0u) |
+                                 (((solid >> np_) & 1u) << 2);
+            const unsigned f = newbits & pat;
+            fresh |= (f & 1u) << nm;
+            if (nc >= 0) fresh |= ((f >> 1) & 1u) << nc;
+            fresh |= ((f >> 2) & 1u) << np_;
           }
           unsigned slot = append_slots(&c->n_flag[par], (unsigned)__popc(fresh));
           while (fresh) {
