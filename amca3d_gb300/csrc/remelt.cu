@@ -1150,13 +1150,12 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         c->n_eact[par ^ 1] = 0;  // built in phase E for the next step; its last reader was the previous phase A
       }
     }
-    {  // clear the previous step's liquid-neighbour flags
-      const unsigned nprev = ld_volatile(&c->n_flag[par ^ 1]);
+    {  // clear the previous step's liquid-neighbour flags: every bit set in
+       // the bitmap is one of them (phase B sets them, this pass clears them
+       // all), so each listed cell's word is zeroed with a plain store
+      const int64_t nprev = min((int64_t)ld_volatile(&c->n_flag[par ^ 1]), d.list_cap);
       const int32_t *fl = d.flagged[par ^ 1];
-      for (int64_t q = gtid; q < nprev; q += nthr) {
-        const int32_t x = fl[q];
-        atomicAnd(&d.flagbits[x >> 5], ~(1u << (x & 31)));
-      }
+      for (int64_t q = gtid; q < nprev; q += nthr) d.flagbits[fl[q] >> 5] = 0u;
     }
     if (S.step == 0) {  // every interior cell; the liquid count per element starts here
       for (int64_t q = gtid; q < M; q += nthr) {
