@@ -986,6 +986,17 @@ struct CellPre {
   float xi, eta, zeta;
 };
 
+// A flagged cell's growth inputs other than dt and its velocity (phase D).
+struct GrowPre {
+  int32_t cell;
+  int I, J, K;
+  double glen;
+  int32_t ori;
+  float dx, dy, dz;
+  float m32[9];
+  uint32_t cand;
+};
+
 // eval_T32 with the element's nodal values already at hand (same operands,
 // same operation order, same result).
 __device__ __forceinline__ float eval_T32_view(const RemeltDevice &d, int64_t c, const ElemView &v, float &err,
@@ -1415,6 +1426,52 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     }
     if (!(ok = grid_barrier(d, 2))) break;
 
+    // What the growth of a flagged cell reads besides dt and its velocity:
+    // its state, orientation matrix and candidate neighbours (non-ghost
+    // liquid neighbours with material at or below Tm, from all 26 neighbour
+    // states loaded at once). Neither the dt phase nor another cell's growth
+    // changes any of it (a claim leaves a candidate a candidate), so this
+    // thread's first flagged cell is loaded while dt is found.
+    auto grow_load = [&](int32_t cell, int I, int J, int K) {
+      GrowPre p;
+      p.cell = cell;
+      p.I = I;
+      p.J = J;
+      p.K = K;
+      p.glen = d.glen[cell];
+      p.ori = d.gori[cell];
+      p.dx = d.gdx[cell];
+      p.dy = d.gdy[cell];
+      p.dz = d.gdz[cell];
+#pragma unroll
+      for (int qq = 0; qq < 9; ++qq) p.m32[qq] = d.omat32[9 * (int64_t)p.ori + qq];
+      uint32_t cand = 0;
+#pragma unroll
+      for (int n = 0; n < 26; ++n) {
+        int di, dj, dk;
+        nbr_offset(n, di, dj, dk);
+        const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
+        const bool in = !ghost(g, I + di, J + dj, K + dk);
+        const int32_t o = in ? d.orient[nb] : 0;
+        const uint8_t cls = in ? d.tcls[nb] : 0;  // a liquid neighbour's classes are this step's
+        cand |= (in && o <= -1 && (cls & kTle) && (cls & kTgtNull) ? 1u : 0u) << n;
+      }
+      p.cand = cand;
+      return p;
+    };
+    const int64_t q0 = spread_begin(0);
+    GrowPre pre0{};
+    bool use0 = false;
+    if (q0 < nf && nf <= d.list_cap) {
+      const int32_t cell = d.flagged[par][q0];
+      int I, J, K;
+      cell_ijk(g, cell, I, J, K);
+      if (!ghost(g, I, J, K) && d.grain[cell] >= 0) {
+        pre0 = grow_load(cell, I, J, K);
+        use0 = true;
+      }
+    }
+
     // ===== dt (Remelting.cpp:706-726, CafeSolver.cpp:195-199) =====
     const double minT = dkey_inv(ld_volatile(&c->minT_key));
     // the same FP64 velocity for every thread: one thread per block computes it
@@ -1459,31 +1516,19 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
     // ===== D: grow and claim (Remelting.cpp:545-622) =====
     // one flagged cell: growth by dT * vel and its claims (atomicMin of the
     // sweep position: the order cells are taken in does not matter)
-    auto grow_claim = [&](int32_t cell, int I, int J, int K, double vel) {
-      const double L = d.glen[cell] + dT * vel;
+    auto grow_finish = [&](const GrowPre &p, double vel) {
+      const int32_t cell = p.cell;
+      const int I = p.I, J = p.J, K = p.K;
+      const double L = p.glen + dT * vel;
       d.glen[cell] = L;
       if (L == 0) return;  // Octahedron::cell_is_captured: a zero half-diagonal captures nothing
-      const int32_t ori = d.gori[cell];
+      const int32_t ori = p.ori;
       const int32_t mine = INT_MIN + sweep_pos(g, I, J, K);
-      const float dxf = d.gdx[cell], dyf = d.gdy[cell], dzf = d.gdz[cell];
+      const float dxf = p.dx, dyf = p.dy, dzf = p.dz;
       const float errg = 4.76837158203125e-07f * (d.h32 + fabsf(dxf) + fabsf(dyf) + fabsf(dzf)) + d.coord_err;
       const float L32 = (float)L;
-      float m32[9];
-#pragma unroll
-      for (int qq = 0; qq < 9; ++qq) m32[qq] = d.omat32[9 * (int64_t)ori + qq];
-      // candidates: non-ghost liquid neighbours with material at or below Tm,
-      // from all 26 neighbour states loaded at once
-      uint32_t cand = 0;
-#pragma unroll
-      for (int n = 0; n < 26; ++n) {
-        int di, dj, dk;
-        nbr_offset(n, di, dj, dk);
-        const int32_t nb = cell + dk * g.nxyg + dj * g.nxg + di;
-        const bool in = !ghost(g, I + di, J + dj, K + dk);
-        const int32_t o = in ? d.orient[nb] : 0;
-        const uint8_t cls = in ? d.tcls[nb] : 0;  // a liquid neighbour's classes are this step's
-        cand |= (in && o <= -1 && (cls & kTle) && (cls & kTgtNull) ? 1u : 0u) << n;
-      }
+      const float *m32 = p.m32;
+      uint32_t cand = p.cand;
       while (cand) {
         const int n = __ffs(cand) - 1;
         cand &= cand - 1;
@@ -1510,8 +1555,18 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         }
       }
     };
+    auto grow_claim = [&](int32_t cell, int I, int J, int K, double vel) {
+      grow_finish(grow_load(cell, I, J, K), vel);
+    };
     bool pending = false;  // a hard velocity of this thread waits for the host's answer
-    for (int64_t q = spread_begin(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
+    if (use0) {
+      const double vel = d.fvel[q0];  // (the chunked host path rewrites it in the dt phase)
+      if (vel < 0)
+        pending = true;
+      else
+        grow_finish(pre0, vel);
+    }
+    for (int64_t q = q0 + spread_stride(0); q < nf && nf <= d.list_cap; q += spread_stride(0)) {
       const int32_t cell = d.flagged[par][q];
       int I, J, K;
       cell_ijk(g, cell, I, J, K);
