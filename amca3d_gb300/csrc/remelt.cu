@@ -1588,7 +1588,11 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         int I, J, K;
         cell_ijk(g, cell, I, J, K);
         if (ghost(g, I, J, K) || d.grain[cell] < 0) continue;
-        grow_claim(cell, I, J, K, ld_volatile(&d.host->v[(unsigned)(-1.0 - vel)]));
+        const double v = ld_volatile(&d.host->v[(unsigned)(-1.0 - vel)]);
+        if (q == q0 && use0)
+          grow_finish(pre0, v);  // loaded ahead, still current (only this thread grows the cell)
+        else
+          grow_claim(cell, I, J, K, v);
       }
     }
     if (gtid == 0) {
