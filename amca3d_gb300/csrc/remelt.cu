@@ -1683,10 +1683,25 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
         const double *f1 = d.frames + (int64_t)((f_new - 1) % d.frame_slots) * d.nnodes;
         double *tn = d.theta[(S.step + 1) % 3];
         float *tn32 = d.theta32[(S.step + 1) % 3];
-        for (int64_t n = gtid; n < d.nnodes; n += nthr) {
-          const double v = lerp_node(f0[n], f1[n], ratio, d.void_t);
-          tn[n] = v;
-          tn32[n] = (float)v;
+        // four nodes per thread at a time: their frame values are loaded
+        // before any interpolated value is stored (a store could alias the
+        // next node's loads and would keep them one after another)
+        for (int64_t n0 = gtid; n0 < d.nnodes; n0 += 4 * nthr) {
+          double a[4], b[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int64_t n = n0 + j * nthr;
+            a[j] = n < d.nnodes ? f0[n] : 0.0;
+            b[j] = n < d.nnodes ? f1[n] : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int64_t n = n0 + j * nthr;
+            if (n >= d.nnodes) continue;
+            const double v = lerp_node(a[j], b[j], ratio, d.void_t);
+            tn[n] = v;
+            tn32[n] = (float)v;
+          }
         }
         // Element bounds depend on the frame pair only (every interpolated node value lies between
         // its two frame values), so the active list is rebuilt when the pair changes; elements near
