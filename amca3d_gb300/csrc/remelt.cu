@@ -254,6 +254,12 @@ __device__ __forceinline__ int64_t spread_begin(int first_block) {
 __device__ __forceinline__ int64_t spread_stride(int first_block) {
   return (int64_t)(gridDim.x - first_block) * blockDim.x;
 }
+// The same spread over all blocks, last block first: for short lists whose
+// items are heavy, so that they meet the blocks with the least other work in
+// the phase (those past the ends of the thread-ordered loops).
+__device__ __forceinline__ int64_t spread_begin_last() {
+  return (int64_t)threadIdx.x * gridDim.x + (gridDim.x - 1 - blockIdx.x);
+}
 
 // Order-preserving key of a double (for atomicMin); NaN never reaches it.
 __device__ __forceinline__ unsigned long long dkey(double x) {
@@ -1166,7 +1172,9 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
        // all), so each listed cell's word is zeroed with a plain store
       const int64_t nprev = min((int64_t)ld_volatile(&c->n_flag[par ^ 1]), d.list_cap);
       const int32_t *fl = d.flagged[par ^ 1];
-      for (int64_t q = gtid; q < nprev; q += nthr) d.flagbits[fl[q] >> 5] = 0u;
+      // (from the last thread down: the first blocks' warps walk two active
+      // elements in the update below)
+      for (int64_t q = nthr - 1 - gtid; q < nprev; q += nthr) d.flagbits[fl[q] >> 5] = 0u;
     }
     if (S.step == 0) {  // every interior cell; the liquid count per element starts here
       for (int64_t q = gtid; q < M; q += nthr) {
@@ -1608,7 +1616,7 @@ __global__ void __launch_bounds__(kBlock, 2) remelt_kernel(RemeltDevice d, long 
       if (nc > d.list_cap) {
         if (gtid == 0) atomicCAS(&c->error, 0, kRemeltErrList);
       } else {
-        for (int64_t q = spread_begin(0); q < nc; q += spread_stride(0)) {
+        for (int64_t q = spread_begin_last(); q < nc; q += spread_stride(0)) {
           const int32_t nb = d.claimed[q];
           const int32_t w = d.orient[nb] - INT_MIN;
           const int wi = (int)(w / nyzg), wj = (int)((w / g.nzg) % g.nyg), wk = (int)(w % g.nzg);
