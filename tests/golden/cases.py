@@ -39,6 +39,10 @@ def small_cases() -> list:
         dataclasses.replace(_mixed("nosite_6x5x4", (6, 5, 4), 0, 0, 0), termination_time=0.0105),
         _mixed("single_cell", (1, 1, 1), 0, 0, 1),
         _mixed("shuffle_16_s8", (16, 16, 16), 8, 30, 40, shuffle_vtr=True),
+        # one cell thick: every cell is a surface cell, listed once per face
+        # it lies on, and the x-end rule of the surface list meets nx == 1
+        _mixed("slab_1x20x24_s9", (1, 20, 24), 9, 40, 20),
+        _mixed("plate_24x20x1_s10", (24, 20, 1), 10, 40, 20),
     ]
 
 
