@@ -43,6 +43,9 @@ def small_cases() -> list:
         # it lies on, and the x-end rule of the surface list meets nx == 1
         _mixed("slab_1x20x24_s9", (1, 20, 24), 9, 40, 20),
         _mixed("plate_24x20x1_s10", (24, 20, 1), 10, 40, 20),
+        # one cell thick in two directions: a line of cells along x, and along z
+        _mixed("line_40x1x1_s11", (40, 1, 1), 11, 12, 6),
+        _mixed("column_1x1x30_s12", (1, 1, 30), 12, 10, 5),
     ]
 
 
