@@ -86,6 +86,16 @@ def fixtures() -> list:
         RemeltCase(name="remelt_void", void_temperature=293.0001, has_been_melted=True,
                    cutoff_factor=None, time_step_factor_ca=0.3, **base),
         _small_frames(src=dict(void_above=-0.3e-5, power=36.0))))
+    # two cells thick, the source on its top surface: the pool melts through
+    thin = dict(base)
+    thin["cells"] = (40, 20, 2)
+    out.append(RemeltFixture(
+        RemeltCase(name="remelt_thin", seed=6, nucleation=True, bulk=(4.0e14, 20.0, 5.0), **thin),
+        _small_frames(src=dict(z_top=4.0e-6))))
+    # the track along the domain's y = 0 face: half the pool lies over the ghost layer
+    out.append(RemeltFixture(
+        RemeltCase(name="remelt_edge", seed=8, nucleation=True, bulk=(4.0e14, 20.0, 5.0), **base),
+        _small_frames(src=dict(y_line=0.0))))
     mm = dict(base)
     mm["origin"] = (1.0e-3, 2.0e-3, 0.0)
     out.append(RemeltFixture(
